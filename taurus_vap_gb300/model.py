@@ -1,0 +1,285 @@
+"""Model-space setup: HO basis, two-body interaction, operators, seeds.
+
+Thin ctypes layer over ``libtvap_setup.so`` (``include/tvap_setup.h``), which
+restates the reference's initialisation (set_basis, set_hamiltonian,
+set_multipoles).  The arrays it returns are exactly the module globals the
+hot path reads in the reference (``hamil_abcd``, ``hamil_H2``,
+``hamil_trperm``, ``hamil_H1``, ``HOsp_*``), with the reference's values
+(1-based indices) and column-major complex matrices.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _build
+
+_lib = None
+
+
+def _setup_lib():
+    global _lib
+    if _lib is None:
+        path = _build.SETUP_LIB
+        if not os.path.exists(path):
+            _build.build_setup()
+        L = ctypes.CDLL(path)
+        vp = ctypes.c_void_p
+        L.tvs_load_antoine.restype = vp
+        L.tvs_load_antoine.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double]
+        L.tvs_synthetic.restype = vp
+        L.tvs_synthetic.argtypes = [
+            ctypes.c_int, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+            ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double,
+        ]
+        L.tvs_error.restype = ctypes.c_char_p
+        L.tvs_error.argtypes = [vp]
+        L.tvs_free.argtypes = [vp]
+        for name in ("tvs_dim", "tvs_nshells"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = ctypes.c_int
+        L.tvs_nelements.argtypes = [vp]
+        L.tvs_nelements.restype = ctypes.c_longlong
+        for name in ("tvs_hw", "tvs_oscillator_length"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = ctypes.c_double
+        L.tvs_get_basis.argtypes = [vp] * 8
+        L.tvs_get_shells.argtypes = [vp, vp]
+        L.tvs_get_hamiltonian.argtypes = [vp] * 6
+        L.tvs_multipoles.argtypes = [vp, vp]
+        L.tvs_coeff_betalm.argtypes = [vp, vp]
+        L.tvs_write_red.argtypes = [vp, ctypes.c_char_p]
+        L.tvs_write_red.restype = ctypes.c_int
+        L.tvs_read_red.argtypes = [vp, ctypes.c_char_p]
+        L.tvs_read_red.restype = ctypes.c_int
+        L.tvs_clebsch.restype = ctypes.c_double
+        L.tvs_clebsch.argtypes = [ctypes.c_int] * 6
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+@dataclass
+class Basis:
+    """Spherical HO single-particle basis (module_basis.f90:73-245)."""
+
+    shells: np.ndarray  # HOsh_na labels (ANTOINE: 1000 n + 100 l + 2 j)
+    sp_n: np.ndarray
+    sp_l: np.ndarray
+    sp_2j: np.ndarray
+    sp_2mj: np.ndarray
+    sp_2mt: np.ndarray
+    sp_sh: np.ndarray  # 1-based shell index
+    sp_tr: np.ndarray  # 1-based time-reversal partner
+    hw: float
+    b: float
+
+    @property
+    def n(self) -> int:
+        return int(self.sp_n.size)
+
+
+@dataclass
+class Hamiltonian:
+    """m-scheme Hamiltonian arrays (module_hamiltonian.f90:53-58)."""
+
+    H0: complex
+    H1: np.ndarray  # complex128 (n, n), Fortran order
+    abcd: np.ndarray  # int16 [4 S], 1-based
+    h2: np.ndarray  # float32 [S]
+    trperm: np.ndarray  # int8 [S]
+
+    @property
+    def S(self) -> int:
+        return int(self.h2.size)
+
+
+@dataclass
+class Model:
+    basis: Basis
+    ham: Hamiltonian
+    valence_Z: float
+    valence_N: float
+    core_Z: float = 0.0
+    core_N: float = 0.0
+    _handle: int | None = field(default=None, repr=False)
+
+    @property
+    def n(self) -> int:
+        return self.basis.n
+
+    def multipoles(self) -> np.ndarray:
+        """Q_lm operators, shape (4 lambda, 2 isospin, 5 |mu|, n*n) in the
+        reference's vectorised layout (set_multipoles)."""
+        n = self.n
+        q = np.zeros((4, 2, 5, n * n), dtype=np.float64)
+        _setup_lib().tvs_multipoles(self._handle, _ptr(q))
+        return q
+
+    def coeff_betalm(self) -> np.ndarray:
+        c = np.zeros((4, 4), dtype=np.float64)
+        _setup_lib().tvs_coeff_betalm(self._handle, _ptr(c))
+        return c
+
+    def write_red(self, path: str) -> None:
+        rc = _setup_lib().tvs_write_red(self._handle, path.encode())
+        if rc:
+            raise IOError(f"cannot write {path}")
+
+    def __del__(self):
+        if self._handle is not None and _lib is not None:
+            _lib.tvs_free(self._handle)
+            self._handle = None
+
+
+def _extract(handle, valence_Z, valence_N, core_Z=0.0, core_N=0.0) -> Model:
+    L = _setup_lib()
+    err = L.tvs_error(handle)
+    if err:
+        L.tvs_free(handle)
+        raise ValueError(err.decode())
+    n = L.tvs_dim(handle)
+    nsh = L.tvs_nshells(handle)
+    arrs = [np.zeros(n, dtype=np.int32) for _ in range(7)]
+    L.tvs_get_basis(handle, *[_ptr(a) for a in arrs])
+    shells = np.zeros(nsh, dtype=np.int32)
+    L.tvs_get_shells(handle, _ptr(shells))
+    basis = Basis(shells, *arrs, hw=L.tvs_hw(handle), b=L.tvs_oscillator_length(handle))
+    S = L.tvs_nelements(handle)
+    H0 = np.zeros(2)
+    H1 = np.zeros((n, n), dtype=np.complex128, order="F")
+    abcd = np.zeros(4 * S, dtype=np.int16)
+    h2 = np.zeros(S, dtype=np.float32)
+    tr = np.zeros(S, dtype=np.int8)
+    L.tvs_get_hamiltonian(handle, _ptr(H0), _ptr(H1), _ptr(abcd), _ptr(h2), _ptr(tr))
+    ham = Hamiltonian(complex(H0[0], H0[1]), H1, abcd, h2, tr)
+    return Model(basis, ham, valence_Z, valence_N, core_Z, core_N, _handle=handle)
+
+
+def load_antoine(path: str, valence_Z: float, valence_N: float) -> Model:
+    """Basis + interaction from an ANTOINE (hamil_type 1/2) ``.sho`` file."""
+    h = _setup_lib().tvs_load_antoine(path.encode(), float(valence_Z), float(valence_N))
+    return _extract(h, valence_Z, valence_N)
+
+
+# Shells up to major quantum number e = 2n + l, ordered by e then by the
+# ANTOINE label of the shell (n, l, j).
+def shells_up_to(emax: int) -> list[int]:
+    out = []
+    for e in range(emax + 1):
+        for l in range(e, -1, -2):
+            nr = (e - l) // 2
+            for twoj in ((2 * l + 1, 2 * l - 1) if l > 0 else (1,)):
+                out.append(1000 * nr + 100 * l + twoj)
+    return out
+
+
+SD_SHELLS = [205, 1001, 203]
+SD_SPE = [-3.9, -3.2, 2.1]
+
+
+def synthetic(shells, spe, hw: float, valence_Z: float, valence_N: float, seed: int,
+              core_Z: float = 0.0, core_N: float = 0.0, scale: float = 1.0, damp: float = 0.0) -> Model:
+    """Seeded rotation- and isospin-invariant JT interaction on ``shells``."""
+    sh = np.asarray(shells, dtype=np.int32)
+    sp = np.asarray(spe, dtype=np.float64)
+    h = _setup_lib().tvs_synthetic(len(sh), _ptr(sh), _ptr(sp), _ptr(sp), float(hw), float(core_Z),
+                                   float(core_N), float(valence_Z), float(valence_N), int(seed),
+                                   float(scale), float(damp))
+    return _extract(h, valence_Z, valence_N, core_Z, core_N)
+
+
+def sd_model(seed: int = 1, valence_Z: float = 4, valence_N: float = 4) -> Model:
+    """sd valence space (0d5/2, 1s1/2, 0d3/2; n = 24), spe -3.9/-3.2/+2.1 MeV."""
+    return synthetic(SD_SHELLS, SD_SPE, hw=0.0, valence_Z=valence_Z, valence_N=valence_N, seed=seed,
+                     core_Z=8, core_N=8)
+
+
+def noncore_model(emax: int, seed: int = 1, hw: float = 20.0, valence_Z: float = 8,
+                  valence_N: float = 8) -> Model:
+    """No-core SHO basis up to emax with V ~ N(0,1) exp(-(e_a+e_b+e_c+e_d)/8);
+    single-particle energies hw (e + 3/2) / 2 (the HO kinetic expectation)."""
+    shells = shells_up_to(emax)
+    spe = [hw * ((2 * (s // 1000) + (s % 1000) // 100) + 1.5) / 2.0 for s in shells]
+    return synthetic(shells, spe, hw=hw, valence_Z=valence_Z, valence_N=valence_N, seed=seed,
+                     scale=1.0, damp=8.0)
+
+
+# ---------------------------------------------------------------------------
+# Wave functions
+# ---------------------------------------------------------------------------
+
+def read_wavefunction_text(path: str, n: int):
+    """initial_wf.txt text format (module_wavefunctions.f90:568-655)."""
+    vals = [float(x.replace("D", "E").replace("d", "E")) for x in open(path).read().split()]
+    nsh = int(vals[0])
+    k = 1 + nsh + 1
+    U = np.array(vals[k:k + n * n]).reshape(n, n).T.copy(order="F")
+    V = np.array(vals[k + n * n:k + 2 * n * n]).reshape(n, n).T.copy(order="F")
+    return U, V
+
+
+def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: int,
+                      block: int = 0):
+    """Random real Bogoliubov seed in the spirit of seed_type 0
+    (module_wavefunctions.f90:134-204,250-354,442-547): BCS occupations drawn
+    until the particle numbers are reached, then two random orthogonal
+    transformations D (left) and C (right).  ``block`` > 0 exchanges the
+    columns of U and V for that quasiparticle (block_quasiparticle,
+    :959-984).  The random stream is NumPy's, not the Fortran processor's."""
+    rng = np.random.default_rng(seed)
+    n = basis.n
+    v2c = np.zeros(n // 2)
+
+    def fill(lo, hi, target):
+        num = -1.0
+        while num < 0.98 * target:
+            num = 0.0
+            for i in range(lo, hi):
+                v2c[i] = min(0.99, v2c[i] + rng.random())
+                num += 2.0 * v2c[i]
+        if num > target and target > 0:
+            v2c[lo:hi] /= num / target
+
+    fill(0, n // 4, valence_Z)
+    fill(n // 4, n // 2, valence_N)
+    U = np.zeros((n, n))
+    V = np.zeros((n, n))
+    ipos = 0
+    k = 0
+    shells2j = [s % 100 for s in basis.shells]
+    for j in shells2j:
+        for m in range(1, (j + 1) // 2 + 1):
+            p1 = ipos + m - 1
+            p2 = ipos + j + 2 - m - 1
+            p3, p4 = p1 + n // 2, p2 + n // 2
+            U[p1, p1] = np.sqrt(1 - v2c[k])
+            U[p2, p2] = U[p1, p1]
+            U[p3, p3] = np.sqrt(1 - v2c[k + n // 4])
+            U[p4, p4] = U[p3, p3]
+            V[p1, p2] = np.sqrt(v2c[k])
+            V[p2, p1] = -V[p1, p2]
+            V[p3, p4] = np.sqrt(v2c[k + n // 4])
+            V[p4, p3] = -V[p3, p4]
+            k += 1
+        ipos += j + 1
+
+    def unitary():
+        B = rng.random((n, n))
+        B = np.triu(B) + np.triu(B, 1).T
+        return np.linalg.eigh(B)[1]
+
+    D = unitary()
+    U, V = D @ U, D @ V
+    C = unitary()
+    U, V = U @ C, V @ C
+    if block > 0:
+        U[:, block - 1], V[:, block - 1] = V[:, block - 1].copy(), U[:, block - 1].copy()
+    return np.asfortranarray(U), np.asfortranarray(V)
