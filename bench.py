@@ -1,0 +1,403 @@
+#!/usr/bin/env python
+"""PNVAP gradient iterations per second on GB300.
+
+Workload: the emax=4 no-core SHO basis (70 m-states per isospin, n = 140,
+hbar*omega = 20 MeV) with a seeded synthetic rotation- and isospin-invariant
+JT interaction V ~ N(0,1) exp(-(e_a+e_b+e_c+e_d)/8), Z = N = 8, 15 gauge
+angles per species (225 angle pairs), a random real Bogoliubov seed, FP64.
+One step = one gradient iteration of the reference's loop
+(taurus_vap.f90:77-123) without constraints (PNVAP lifts the N/Z ones):
+project_wavefunction + calculate_projected_H20, calculate_gradient
+(gradient_type 0), cholesky_factorization + evolve_wavefunction.
+
+  --impl ours       (default) device path; `value` with the state resident in
+                    HBM, `e2e` through the C ABI with host buffers.
+  --impl reference  the CPU restatement of the reference path (oracle/) on the
+                    host cores, on a bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+EMAX, ZV, NV, MPHI = 4, 8.0, 8.0, 15
+ETA, MU = 0.005, 0.3
+METRIC = "PNVAP gradient iters/s, emax=4, 15 gauge angles: batched+adjoint vs plain GPU (FP64)"
+WORKLOAD = ("PNVAP gradient iteration, emax=4 no-core SHO basis (n=140), Z=N=8, 15x15 gauge angles, "
+            "synthetic JT interaction (seed 1), random real Bogoliubov seed (seed 2), FP64")
+
+
+def build_workload():
+    from taurus_vap_gb300 import model as M
+
+    mdl = M.noncore_model(EMAX, seed=1, valence_Z=ZV, valence_N=NV)
+    U, V = M.random_bogoliubov(mdl.basis, ZV, NV, seed=2)
+    return mdl, U, V
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            w = [x.strip() for x in line.split(",")]
+            if len(w) < 6:
+                continue
+            try:
+                sm.append(float(w[0]))
+                mx = float(w[1])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if w[2 + k].lower().startswith("active"):
+                    reasons.add(name)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# device arm
+# --------------------------------------------------------------------------
+class DeviceIteration:
+    """One gradient iteration with the state resident on the device."""
+
+    def __init__(self, ctx, U, V, mode, torch):
+        import ctypes
+
+        from taurus_vap_gb300 import native as N
+
+        self.N = N
+        self.ctx = ctx
+        self.torch = torch
+        n = ctx.n
+        dev = torch.device("cuda")
+        f = lambda a: torch.tensor(a.reshape(-1, order="F"), dtype=torch.float64, device=dev)
+        self.U, self.V = f(U), f(V)
+        self.U1 = torch.empty_like(self.U)
+        self.V1 = torch.empty_like(self.V)
+        self.H = torch.zeros(n * n, dtype=torch.float64, device=dev)
+        self.Zi = torch.zeros_like(self.H)
+        self.Zim1 = torch.zeros_like(self.H)
+        self.opts = N.TvapProjOpts(MPHI, MPHI, 2 * math.pi, ZV, NV, 1.0, 0.0, 0, mode)
+        self.pnp = N.TvapPnp()
+        self.norm = ctypes.c_double()
+        self.launches = 0
+        self.energy = None
+
+    def step(self):
+        N, L, h = self.N, self.N.lib(), self.ctx.h
+        import ctypes
+
+        p = lambda t: ctypes.c_void_p(t.data_ptr())
+        N._check(L.tvap_project(h, p(self.U), p(self.V), ctypes.byref(self.opts), ctypes.byref(self.pnp), p(self.H)),
+                 "tvap_project")
+        k = L.tvap_kernel_launches(h)
+        N._check(L.tvap_calculate_gradient(h, p(self.H), 0, None, None, p(self.Zim1), ETA, MU, p(self.Zi),
+                                           ctypes.byref(self.norm)), "tvap_calculate_gradient")
+        k += L.tvap_kernel_launches(h)
+        N._check(L.tvap_evolve(h, p(self.U), p(self.V), p(self.Zi), p(self.U1), p(self.V1)), "tvap_evolve")
+        k += L.tvap_kernel_launches(h)
+        self.U, self.U1 = self.U1, self.U
+        self.V, self.V1 = self.V1, self.V
+        self.Zim1.copy_(self.Zi)
+        self.launches += k + 1  # + the Zim1 copy
+        self.energy = (self.pnp.c("ener") / self.pnp.c("over")).real
+
+
+def host_iteration(ctx, state, mode):
+    """Same iteration through the C ABI with host buffers (copies inside)."""
+    U, V, Zim1 = state
+    pnp, H20v = ctx.project(U, V, MPHI, MPHI, 2 * math.pi, ZV, NV, mode=mode)
+    Zi, norm = ctx.calculate_gradient(H20v, None, None, Zim1, ETA, MU)
+    U1, V1 = ctx.evolve(U, V, Zi)
+    return (U1, V1, Zi), (pnp.c("ener") / pnp.c("over")).real
+
+
+def fp64_flops_per_iteration(n, G):
+    """Algorithmic FP64 flops of the reduced per-angle formulation."""
+    return G * (10.7 + 8 + 12 + 40 + 4 + 1.4) * n ** 3
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from taurus_vap_gb300 import native as N
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    mdl, U, V = build_workload()
+    n = mdl.n
+    ctx = N.Context(mdl.basis, mdl.ham, device=local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    # ---- device-resident value (batched form)
+    it = DeviceIteration(ctx, U, V, 0, torch)
+    for _ in range(args.warmup):
+        it.step()
+    torch.cuda.synchronize()
+    barrier()
+    ctx.set_timing(True)
+    it.launches = 0
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for _ in range(args.steps):
+        it.step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = t0.elapsed_time(t1)
+    sections = ctx.get_timing()
+    ctx.set_timing(False)
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_per_step = ms / args.steps
+    value = world * args.steps / (ms / 1000.0)
+    launches = it.launches
+
+    # ---- plain form (one angle per launch sequence), same state
+    plain = None
+    if args.plain_steps > 0:
+        itp = DeviceIteration(ctx, U, V, 1, torch)
+        itp.step()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.plain_steps):
+            itp.step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        pms = a.elapsed_time(b) / args.plain_steps
+        plain = {"value": 1000.0 / pms, "unit": "iters/s", "ms_per_step": pms, "steps": args.plain_steps,
+                 "batched_over_plain": (1000.0 / ms_per_step) / (1000.0 / pms)}
+
+    # ---- end to end through the C ABI with host buffers
+    state = (np.asfortranarray(U), np.asfortranarray(V), np.zeros(n * n))
+    state, _ = host_iteration(ctx, state, 0)
+    torch.cuda.synchronize()
+    e_steps = max(1, min(args.steps, 3))
+    tw = time.perf_counter()
+    for _ in range(e_steps):
+        state, _ = host_iteration(ctx, state, 0)
+    torch.cuda.synchronize()
+    e_ms = (time.perf_counter() - tw) * 1000.0 / e_steps
+    h2d = 8 * n * n * (2 + 2 + 3)
+    d2h = 8 * n * n * (1 + 1 + 2)
+    e2e = {"value": world * 1000.0 / e_ms, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    # ---- roofline of the dominant kernel, from the live section timings
+    G_total = MPHI * MPHI
+    G = (G_total + 1) // 2  # folded angle pairs computed
+    S = mdl.ham.S
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    fp64_peak = 1.25  # TFLOP/s nominal; see profiles/fp64_peak.md for the measured figure
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "fp64_peak.md")):
+            if line.startswith("measured_fp64_tflops:"):
+                fp64_peak = float(line.split(":")[1])
+    except OSError:
+        pass
+    steps = args.steps
+    fld_ms = (sections["fields_gamma"][0] + sections["fields_delta"][0]) / steps
+    fld_bytes = 13 * S + 16 * n * n * 7 * G
+    dom = max(sections.items(), key=lambda kv: kv[1][0])
+    roofline = {
+        "kernel": "fields (calculate_fields gather, Gamma + Delta, all angles)",
+        "bound": "hbm",
+        "achieved": fld_bytes / (fld_ms / 1000.0) / 1e9,
+        "peak": hbm_peak,
+        "unit": "GB/s",
+        "frac": (fld_bytes / (fld_ms / 1000.0) / 1e9) / hbm_peak,
+        "traffic": None,
+        "algorithmic_bytes_per_launch": fld_bytes,
+        "ms_per_launch": fld_ms,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+    }
+    sec_ms = {k: v[0] / steps for k, v in sections.items()}
+    total_sec = sum(sec_ms.values())
+    fp64 = fp64_flops_per_iteration(n, G) + 4 * 8 * (S * 1.65) * G  # dense + fields (48 flops x passes)
+    roofline_fp64 = {
+        "scope": "whole iteration",
+        "bound": "fp64",
+        "achieved": fp64 / (ms_per_step / 1000.0) / 1e12,
+        "peak": fp64_peak,
+        "unit": "TFLOP/s",
+        "frac": fp64 / (ms_per_step / 1000.0) / 1e12 / fp64_peak,
+        "algorithmic_fp64_flops_per_step": fp64,
+    }
+
+    # ---- CPU baseline: the oracle on a bounded sample, rank 0 only
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(mdl, U, V, args)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "elements": S, "angle_pairs": G_total, "angle_pairs_computed": G,
+                   "form": "batched (all angles per launch, conjugate folding)",
+                   "parallelism": f"replicas x{world}", "l2": "working set > L2 (per-angle arrays ~0.7 GB)",
+                   "eta": ETA, "mu": MU},
+        "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "roofline_fp64": roofline_fp64,
+        "sections_ms_per_step": {k: round(v, 4) for k, v in sec_ms.items()},
+        "dominant_section": dom[0], "plain_gpu": plain, "cpu_baseline": cpu, "final_energy": it.energy,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# CPU legs (oracle)
+# --------------------------------------------------------------------------
+def _oracle_iteration_time(mdl, U, V, Mp, Mn, nthreads, reps=1):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle as O
+
+    om = O.OracleModel(mdl)
+    vap = O.OracleVAP(om, U, V, Mp, Mn, 2 * math.pi, ZV, NV, ETA, MU, 0.0, np.zeros((0, mdl.n * mdl.n)),
+                      np.zeros(0), nthreads=nthreads)
+    best = None
+    for _ in range(reps):
+        t = time.perf_counter()
+        vap.iterate()
+        dt = time.perf_counter() - t
+        best = dt if best is None else min(best, dt)
+    return best
+
+
+def cpu_baseline(mdl, U, V, args):
+    cores = os.cpu_count() or 1
+    t2 = _oracle_iteration_time(mdl, U, V, 1, 2, cores)
+    t9 = _oracle_iteration_time(mdl, U, V, 3, 3, cores)
+    per_angle = max((t9 - t2) / 7.0, 1e-9)
+    t225 = t2 + (MPHI * MPHI - 2) * per_angle
+    return {"value": 1.0 / t225, "unit": "iters/s", "cores": cores, "kind": "port",
+            "sample": f"oracle iterations with 1x2 and 3x3 angle grids ({t2:.2f} s, {t9:.2f} s), "
+                      f"extrapolated linearly in the angle count to 15x15 ({t225:.1f} s/iteration)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mdl, U, V = build_workload()
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        pass
+    samples = []
+    t_start = time.perf_counter()
+    base = cpu_baseline(mdl, U, V, args)
+    for _ in range(max(1, args.steps)):
+        t9 = _oracle_iteration_time(mdl, U, V, 3, 3, cores)
+        samples.append(t9)
+    elapsed = time.perf_counter() - t_start
+    value = base["value"]
+    ms = 1000.0 / value
+    out = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "form": "CPU restatement of the reference path (oracle/), OpenMP fields + "
+                                                 "threaded BLAS/LAPACK"},
+        "cpu_baseline": {"value": value, "unit": "iters/s", "cores": cores, "kind": "port", "sample": base["sample"]},
+        "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": elapsed,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,147 @@
+/*
+ * tvap.h -- C ABI of the GB300 (sm_103a) PNVAP hot path.
+ *
+ * Drop-in for the three Fortran call sites of TAURUS_vap's gradient loop:
+ *
+ *   call calculate_fields(rhoLR,kappaLR,kappaRL,gammaLR,hspLR,deltaLR,deltaRL,ndim)
+ *        src/module_fields.f90:99-105           -> tvap_calculate_fields
+ *   call project_wavefunction(0,iprint,Mphip,Mphin,ndim)
+ *        src/module_projection.f90:201-203      -> tvap_project
+ *   call calculate_gradient(ndim)
+ *        src/module_gradient.f90:79-81          -> tvap_calculate_gradient
+ *
+ * plus the Thouless evolution used by adjust_constraints
+ * (cholesky_factorization + evolve_wavefunction,
+ * src/module_constraints.f90:497-590 -> tvap_evolve) and the adjoint of the
+ * projected energy with respect to the Thouless matrix (tvap_energy_adjoint,
+ * no counterpart in the reference).
+ *
+ * Conventions
+ *   - all matrices are column-major (Fortran order); complex(r64) arguments
+ *     are arrays of interleaved (re, im) doubles, exactly the memory layout of
+ *     a Fortran complex(r64) array;
+ *   - pointers may be host or device memory; the library detects which;
+ *   - the module globals the Fortran routines read implicitly (HOsp_2mj,
+ *     HOsp_tr, HOsp_l, hamil_abcd, hamil_H2, hamil_trperm, hamil_H1,
+ *     hamil_H0, src/module_basis.f90:33-41, src/module_hamiltonian.f90:53-58)
+ *     are handed over once through tvap_init / tvap_set_hamiltonian;
+ *   - every call returns a status code; the Fortran shim turns a non-zero
+ *     code into the reference's `stop` (the reference has no status codes).
+ *   - one context per host thread; a context is not re-entrant.
+ */
+#ifndef TVAP_H
+#define TVAP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tvap_ctx tvap_ctx;
+
+enum {
+  TVAP_OK = 0,
+  TVAP_ERR_ARG = 1,           /* bad argument or size */
+  TVAP_ERR_CUDA = 2,          /* CUDA runtime error (tvap_last_error has text) */
+  TVAP_ERR_NOT_READY = 3,     /* tvap_set_hamiltonian not called */
+  TVAP_ERR_SINGULAR_UPHI = 10,/* U_phi singular (calculate_thouless) */
+  TVAP_ERR_SINGULAR_RN = 11,  /* canonical overlap matrix singular: the reference
+                                 stops with 'got info from zgetrf'
+                                 (module_projection.f90:860-864) */
+  TVAP_ERR_IMAG_GRADIENT = 13,/* Im(gradient) > 1e-8 (module_projection.f90:751-755) */
+  TVAP_ERR_CHOLESKY = 14,     /* dpbtrf failed (module_constraints.f90:528-531) */
+  TVAP_ERR_TRTRI = 15,        /* dtrtri failed (module_constraints.f90:568-571) */
+  TVAP_ERR_CANONICAL = 16,    /* canonical basis: eigen solver did not converge or a
+                                 degenerate block larger than 2 (DGEES case) */
+  TVAP_ERR_NUMBER_DRIFT = 18  /* particle numbers wrong 3 times in 5 iterations
+                                 (module_gradient.f90:528-545) */
+};
+
+/* Projected sums of one call of the gauge-angle loop: pnp_over, pnp_ener,
+ * pnp_prot, pnp_neut, pnp_prot2, pnp_neut2 (module_projection.f90:58-66) and
+ * the canonical-basis counts nocc/nemp of the projected state. */
+typedef struct {
+  double over[2], ener[2], prot[2], neut[2], prot2[2], neut2[2];
+  int nocc, nemp;
+} tvap_pnp;
+
+/* Options of the projection that the reference reads from module globals. */
+typedef struct {
+  int Mphip, Mphin;      /* proj_Mphip, proj_Mphin */
+  double facpi;          /* proj_facpi (2 pi, or pi for separate N/Z) */
+  double valence_Z, valence_N;
+  double factor_delta;   /* factor_delta (module_fields.f90:40) */
+  double seed_occeps;    /* cutoff of occupied states (0 -> 1e-8) */
+  int seed_allemp;       /* include all empty sp states in the overlap */
+  int mode;              /* 0: batched (all angles per launch, conjugate
+                            folding), 1: plain (one angle per launch sequence) */
+} tvap_proj_opts;
+
+/* Context: basis size n = HOsp_dim and the single-particle tables
+ * (src/module_basis.f90:209-238).  device < 0 selects the current device. */
+int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* sp_tr, const int32_t* sp_l,
+              int device);
+void tvap_destroy(tvap_ctx* ctx);
+int tvap_set_stream(tvap_ctx* ctx, void* cuda_stream);
+const char* tvap_last_error(void);
+/* Number of kernels the last top-level call launched. */
+int tvap_kernel_launches(const tvap_ctx* ctx);
+/* Optional per-section timing with CUDA events on the context's stream
+ * (sections: canonical basis, angle-independent blocks, Thouless solve,
+ * U~/V~, densities, Gamma gather, Delta gather, traces, H20, overlap,
+ * Pfaffian, sums, gradient, evolve).  tvap_set_timing resets the totals;
+ * tvap_get_timing returns milliseconds and call counts per section. */
+int tvap_set_timing(tvap_ctx* ctx, int on);
+int tvap_get_timing(tvap_ctx* ctx, double* ms, long long* calls, int nsec);
+
+/* One upload of the reduced two-body list and the one-body part:
+ * hamil_H2dim, hamil_abcd (i16, 1-based, 4 per element), hamil_H2 (f32),
+ * hamil_trperm (i8), hamil_H1 (complex n x n), hamil_H0 (complex).
+ * (src/module_hamiltonian.f90:53-58; read_hamiltonian_reduced :533-599)
+ * The list is decoded on the device -- time-reversal pass included -- into
+ * the gather form used by tvap_calculate_fields. */
+int tvap_set_hamiltonian(tvap_ctx* ctx, int64_t S, const int16_t* abcd, const float* h2, const int8_t* trperm,
+                         const double* H1, const double* H0);
+
+/* calculate_fields (src/module_fields.f90:99-189), same arguments and
+ * semantics: rho, kappaLR, kappaRL in; gamma, h = gamma + H1, deltaLR,
+ * deltaRL out (complex n x n each). */
+int tvap_calculate_fields(tvap_ctx* ctx, const double* rhoLR, const double* kappaLR, const double* kappaRL,
+                          double* gammaLR, double* hspLR, double* deltaLR, double* deltaRL);
+
+/* calculate_fields for `ncol` independent density sets stored one after the
+ * other (matrix c at offset c*n*n complex elements). */
+int tvap_calculate_fields_batched(tvap_ctx* ctx, int ncol, const double* rhoLR, const double* kappaLR,
+                                  const double* kappaRL, double* gammaLR, double* hspLR, double* deltaLR,
+                                  double* deltaRL);
+
+/* project_wavefunction(iopt=0) + calculate_projected_H20
+ * (src/module_projection.f90:201-373,729-759): from the real Bogoliubov
+ * matrices U0, V0 (n x n) computes the projected sums and
+ * field_H20v (n*n reals, may be NULL). */
+int tvap_project(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts, tvap_pnp* out,
+                 double* H20v);
+
+/* calculate_gradient with gradient_type 0 (src/module_gradient.f90:79-143):
+ * Zi = -eta (H20v - sum_j lambda_j C20_j) + mu Zim1, and
+ * gradient_norm = |Zi|_F / eta.  C20 holds cdim operators of n*n reals. */
+int tvap_calculate_gradient(tvap_ctx* ctx, const double* H20v, int cdim, const double* lambda, const double* C20,
+                            const double* Zim1, double eta, double mu, double* Zi, double* gradient_norm);
+
+/* Thouless evolution (cholesky_factorization + evolve_wavefunction,
+ * src/module_constraints.f90:497-590): U1 = (U0 + V0 Z) L^-T,
+ * V1 = (V0 + U0 Z) L^-T with L L^T = 1 + Z^T Z. */
+int tvap_evolve(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z, double* U1, double* V1);
+
+/* Adjoint of the projected energy E(Z) = <Phi(Z)|H P|Phi(Z)>/<Phi(Z)|P|Phi(Z)>
+ * of the state Phi(Z) = evolve(U0, V0, Z) with respect to the real Thouless
+ * matrix Z: writes E and dE/dZ (n*n reals).  The per-angle densities are
+ * recomputed, not stored.  No counterpart in the reference. */
+int tvap_energy_adjoint(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z,
+                        const tvap_proj_opts* opts, double* energy, double* dEdZ);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

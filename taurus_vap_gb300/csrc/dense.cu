@@ -1,0 +1,571 @@
+// Dense FP64 building blocks of the per-angle algebra, batched over gauge
+// angles: strided batched GEMM (complex/real operands specialised so that no
+// FP64 operation is spent on zero imaginary parts), the Thouless solve, the
+// Parlett-Reid Pfaffian, the Jacobi eigen-decomposition and the Cholesky
+// factorisation with triangular inverse.
+//
+// On GB300 the FP64 pipe (about 1.25 TFLOP/s for the whole chip) bounds every
+// kernel in this file, so each kernel is written to issue the minimum number
+// of DFMAs; memory traffic is secondary.
+
+#include <algorithm>
+
+#include "tvap_internal.cuh"
+
+namespace tvap {
+
+namespace {
+
+// multiply-accumulate specialised on operand types
+__device__ __forceinline__ void mac(double2& c, double2 a, double2 b) { cfma(c, a, b); }
+__device__ __forceinline__ void mac(double2& c, double a, double2 b) {
+  c.x = fma(a, b.x, c.x);
+  c.y = fma(a, b.y, c.y);
+}
+__device__ __forceinline__ void mac(double2& c, double2 a, double b) {
+  c.x = fma(a.x, b, c.x);
+  c.y = fma(a.y, b, c.y);
+}
+__device__ __forceinline__ void mac(double& c, double a, double b) { c = fma(a, b, c); }
+
+template <typename T>
+__device__ __forceinline__ T load_el(const View& v, long long i, long long j, long long b, bool cj);
+template <>
+__device__ __forceinline__ double load_el<double>(const View& v, long long i, long long j, long long b, bool) {
+  return static_cast<const double*>(v.p)[i * v.rs + j * v.cs + b * v.bs];
+}
+template <>
+__device__ __forceinline__ double2 load_el<double2>(const View& v, long long i, long long j, long long b, bool cj) {
+  double2 x = static_cast<const double2*>(v.p)[i * v.rs + j * v.cs + b * v.bs];
+  if (cj) x.y = -x.y;
+  return x;
+}
+template <typename T>
+__device__ __forceinline__ T zero_of();
+template <>
+__device__ __forceinline__ double zero_of<double>() {
+  return 0.0;
+}
+template <>
+__device__ __forceinline__ double2 zero_of<double2>() {
+  return make_double2(0.0, 0.0);
+}
+
+template <typename TA, typename TB>
+struct AccT {
+  typedef double2 type;
+};
+template <>
+struct AccT<double, double> {
+  typedef double type;
+};
+
+__device__ __forceinline__ void store_out(const GemmArgs& g, long long idx, double acc, double2 alpha) {
+  double* C = static_cast<double*>(g.C);
+  double v = alpha.x * acc;
+  if (g.beta.x != 0.0) v = fma(g.beta.x, C[idx], v);
+  C[idx] = v;
+}
+__device__ __forceinline__ void store_out(const GemmArgs& g, long long idx, double2 acc, double2 alpha) {
+  double2* C = static_cast<double2*>(g.C);
+  double2 v = cmul(alpha, acc);
+  if (g.beta.x != 0.0 || g.beta.y != 0.0) v = cadd(v, cmul(g.beta, C[idx]));
+  C[idx] = v;
+}
+__device__ __forceinline__ void store_out_real_from_complex(const GemmArgs& g, long long idx, double2 acc,
+                                                            double2 alpha) {
+  double* C = static_cast<double*>(g.C);
+  double v = (cmul(alpha, acc)).x;
+  if (g.beta.x != 0.0) v = fma(g.beta.x, C[idx], v);
+  C[idx] = v;
+}
+
+// TM x TN output tile per CTA, 2 x 2 outputs per thread (strided by half the
+// tile so that neighbouring threads read neighbouring shared-memory words).
+template <int TM, int TN, typename TA, typename TB>
+__global__ void __launch_bounds__((TM / 2) * (TN / 2)) gemm_kernel(GemmArgs g) {
+  typedef typename AccT<TA, TB>::type TC;
+  constexpr int BK = 16;
+  constexpr int HM = TM / 2, HN = TN / 2;
+  constexpr int NT = HM * HN;
+  __shared__ TA As[BK][TM + 1];
+  __shared__ TB Bs[BK][TN + 1];
+  const long long b = blockIdx.z;
+  const int i0 = blockIdx.y * TM, j0 = blockIdx.x * TN;
+  const int tid = threadIdx.x;
+  const int ty = tid / HN, tx = tid % HN;
+  TC acc[2][2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) acc[r][c] = zero_of<TC>();
+  const bool live = (i0 + ty < g.M) && (j0 + tx < g.N);
+  for (int k0 = 0; k0 < g.K; k0 += BK) {
+    const int kt = min(BK, g.K - k0);
+    for (int idx = tid; idx < TM * BK; idx += NT) {
+      const int ii = idx % TM, kk = idx / TM;
+      TA v = zero_of<TA>();
+      if (i0 + ii < g.M && kk < kt) v = load_el<TA>(g.A, i0 + ii, k0 + kk, b, g.conj_a);
+      As[kk][ii] = v;
+    }
+    for (int idx = tid; idx < TN * BK; idx += NT) {
+      const int jj = idx % TN, kk = idx / TN;
+      TB v = zero_of<TB>();
+      if (j0 + jj < g.N && kk < kt) v = load_el<TB>(g.B, k0 + kk, j0 + jj, b, g.conj_b);
+      Bs[kk][jj] = v;
+    }
+    __syncthreads();
+    if (live) {
+      for (int kk = 0; kk < kt; ++kk) {
+        const TA a0 = As[kk][ty], a1 = As[kk][ty + HM];
+        const TB b0 = Bs[kk][tx], b1 = Bs[kk][tx + HN];
+        mac(acc[0][0], a0, b0);
+        mac(acc[0][1], a0, b1);
+        mac(acc[1][0], a1, b0);
+        mac(acc[1][1], a1, b1);
+      }
+    }
+    __syncthreads();
+  }
+  double2 alpha = g.alpha;
+  if (g.alpha_vec) alpha = cmul(alpha, g.alpha_vec[b]);
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int i = i0 + ty + r * HM, j = j0 + tx + c * HN;
+      if (i < g.M && j < g.N) {
+        const long long idx = i * g.crs + j * g.ccs + b * g.cbs;
+        if constexpr (sizeof(TC) == sizeof(double)) {
+          store_out(g, idx, acc[r][c], alpha);
+        } else {
+          if (g.c_real)
+            store_out_real_from_complex(g, idx, acc[r][c], alpha);
+          else
+            store_out(g, idx, acc[r][c], alpha);
+        }
+      }
+    }
+}
+
+template <int T, typename TA, typename TB>
+void launch_gemm_t(const GemmArgs& g, cudaStream_t s) {
+  dim3 grid((g.N + T - 1) / T, (g.M + T - 1) / T, g.batch);
+  gemm_kernel<T, T, TA, TB><<<grid, (T / 2) * (T / 2), 0, s>>>(g);
+}
+
+template <int T>
+void launch_gemm_tile(const GemmArgs& g, cudaStream_t s) {
+  if (g.a_real && g.b_real)
+    launch_gemm_t<T, double, double>(g, s);
+  else if (g.a_real)
+    launch_gemm_t<T, double, double2>(g, s);
+  else if (g.b_real)
+    launch_gemm_t<T, double2, double>(g, s);
+  else
+    launch_gemm_t<T, double2, double2>(g, s);
+}
+
+// Tile choice: minimise padded FP64 work (the pipe is the bound), then prefer
+// larger tiles.  Candidates are compiled instantiations.
+const int kTiles[] = {16, 24, 28, 32, 40, 48, 56};
+
+int pick_tile(int M, int N) {
+  int best = 32;
+  double best_w = 1e30;
+  for (int t : kTiles) {
+    const double w = double((M + t - 1) / t) * ((N + t - 1) / t) * t * t / (double(M) * N);
+    if (w < best_w - 1e-9 || (std::fabs(w - best_w) < 1e-9 && t > best)) {
+      best_w = w;
+      best = t;
+    }
+  }
+  return best;
+}
+
+}  // namespace
+
+int gemm(const GemmArgs& g, cudaStream_t s) {
+  if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return TVAP_OK;
+  switch (pick_tile(g.M, g.N)) {
+    case 16: launch_gemm_tile<16>(g, s); break;
+    case 24: launch_gemm_tile<24>(g, s); break;
+    case 28: launch_gemm_tile<28>(g, s); break;
+    case 40: launch_gemm_tile<40>(g, s); break;
+    case 48: launch_gemm_tile<48>(g, s); break;
+    case 56: launch_gemm_tile<56>(g, s); break;
+    default: launch_gemm_tile<32>(g, s); break;
+  }
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
+namespace {
+
+__device__ void block_argmax(double v, int idx, double* sv, int* si, int& out_idx, double& out_v) {
+  // first index of the maximum, like IZAMAX
+  const int tid = threadIdx.x;
+  sv[tid] = v;
+  si[tid] = idx;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (tid < s) {
+      const double a = sv[tid], b = sv[tid + s];
+      const int ia = si[tid], ib = si[tid + s];
+      if (b > a || (b == a && ib < ia)) {
+        sv[tid] = b;
+        si[tid] = ib;
+      }
+    }
+    __syncthreads();
+  }
+  out_idx = si[0];
+  out_v = sv[0];
+  __syncthreads();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Pfaffian: PFAPACK ZSKTF2 (UPLO='U', MODE='P') restated for one CTA per
+// matrix (subroutines_pfaffian.f:1694-2017 with the ZSKR2 update :2387-2630):
+// pivot = first maximum of |Re|+|Im| over A(1:K-1,K) (IZAMAX), row/column
+// exchange, skew rank-2 update of the leading block, and
+// Pf = prod A(K-1,K) * (-1)^(#exchanges) (ZSKPFA :193-203).  The product is
+// returned as (log|Pf|, phase) to stay finite for large n.
+// Output per matrix: pf[b] = (log|Pf|, 0), phase in pf[batch + b]; a zero
+// pivot yields log|Pf| = -inf.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kPfThreads = 512;
+
+__global__ void __launch_bounds__(kPfThreads) pfaffian_kernel(int N, double2* Aall, double2* pf, int batch,
+                                                              int* flags) {
+  __shared__ double sv[kPfThreads];
+  __shared__ int si[kPfThreads];
+  __shared__ double2 xcol[512], ycol[512];
+  const int b = blockIdx.x;
+  double2* A = Aall + size_t(b) * N * N;
+  auto a = [A, N](int i, int j) -> double2& { return A[size_t(i - 1) + size_t(j - 1) * N]; };
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double logmag = 0.0;
+  double2 phase = make_double2(1.0, 0.0);
+  bool zero = false;
+  for (int K = N; K >= 2; K -= 2) {
+    double best = -1.0;
+    int bi = N + 1;
+    for (int i = 1 + tid; i <= K - 1; i += nt) {
+      const double v = cabs1(a(i, K));
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+    int KP;
+    double pv;
+    block_argmax(best, bi, sv, si, KP, pv);
+    const int KK = K - 1;
+    if (pv == 0.0) {
+      zero = true;
+      KP = KK;
+    }
+    if (KP != KK) {
+      for (int i = 1 + tid; i <= KP - 1; i += nt) {
+        const double2 t = a(i, KK);
+        a(i, KK) = a(i, KP);
+        a(i, KP) = t;
+      }
+      for (int t = tid; t < KK - KP - 1; t += nt) {
+        const double2 u = a(KP + 1 + t, KK);
+        a(KP + 1 + t, KK) = a(KP, KP + 1 + t);
+        a(KP, KP + 1 + t) = u;
+      }
+      for (int j = K + tid; j <= N; j += nt) {
+        const double2 u = a(KK, j);
+        a(KK, j) = a(KP, j);
+        a(KP, j) = u;
+      }
+      __syncthreads();
+      for (int i = KP + tid; i <= KK - 1; i += nt) a(i, KK) = cneg(a(i, KK));
+      for (int j = KP + 1 + tid; j <= KK - 1; j += nt) a(KP, j) = cneg(a(KP, j));
+      __syncthreads();
+    }
+    const double2 piv = a(K - 1, K);
+    if (!zero) {
+      const double m = hypot(piv.x, piv.y);
+      logmag += log(m);
+      phase = cmul(phase, make_double2(piv.x / m, piv.y / m));
+      if (KP != KK) phase = cneg(phase);
+      const double2 alpha = crcp(piv);
+      const int nn = K - 2;
+      for (int i = 1 + tid; i <= nn; i += nt) {
+        xcol[i] = a(i, K);
+        ycol[i] = a(i, K - 1);
+      }
+      __syncthreads();
+      // A(I,J) += X(I) * (alpha Y(J)) - Y(I) * (alpha X(J)),  I < J <= nn
+      // (ZSKR2 skips a column J whose X(J) and Y(J) are both zero)
+      for (long long idx = tid; idx < (long long)nn * nn; idx += nt) {
+        const int I = 1 + int(idx % nn), J = 1 + int(idx / nn);
+        if (I >= J) continue;
+        const double2 xj = xcol[J], yj = ycol[J];
+        if (xj.x == 0.0 && xj.y == 0.0 && yj.x == 0.0 && yj.y == 0.0) continue;
+        const double2 t1 = cmul(alpha, yj), t2 = cmul(alpha, xj);
+        double2 v = a(I, J);
+        cfma(v, xcol[I], t1);
+        cfma(v, cneg(ycol[I]), t2);
+        a(I, J) = v;
+      }
+      __syncthreads();
+      for (int i = 1 + tid; i <= nn; i += nt) a(i, K) = cmul(alpha, a(i, K));
+      __syncthreads();
+    }
+  }
+  if (tid == 0) {
+    pf[b] = make_double2(zero ? -INFINITY : logmag, 0.0);
+    pf[batch + b] = zero ? make_double2(0.0, 0.0) : phase;
+    if (zero) atomicOr(flags, DEV_PFAFF_ZERO);
+  }
+}
+
+}  // namespace
+
+int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s) {
+  if (n > 512 || (n & 1)) return TVAP_ERR_ARG;
+  pfaffian_kernel<<<batch, kPfThreads, 0, s>>>(n, A, pf, batch, flags);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Symmetric eigen-decomposition by parallel cyclic Jacobi (round-robin pair
+// ordering, n/2 disjoint rotations per round), one CTA, FP64.  A (n x n,
+// column-major) is destroyed; W receives the eigenvectors as columns and
+// evals the eigenvalues, both sorted ascending (the DSYEV convention).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kJacThreads = 1024;
+
+__global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, double* W, double* evals,
+                                                             double* work, int* flags) {
+  extern __shared__ double jsh[];
+  const int m = (n + 1) & ~1;  // even count incl. a dummy index
+  double* cs = jsh;                                    // m/2 cosines
+  double* sn = cs + m / 2;                             // m/2 sines
+  int* pairs = reinterpret_cast<int*>(sn + m / 2);     // m round-robin slots
+  int* pp = pairs + m;                                 // m/2 p indices
+  int* qq = pp + m / 2;                                // m/2 q indices
+  __shared__ double red[kJacThreads];
+  __shared__ int done;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  auto Ael = [A, n](int i, int j) -> double& { return A[i + size_t(j) * n]; };
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) W[idx] = ((idx % n) == (idx / n)) ? 1.0 : 0.0;
+  for (int i = tid; i < m; i += nt) pairs[i] = i;
+  double anorm = 0.0;
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) anorm += A[idx] * A[idx];
+  red[tid] = anorm;
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s) red[tid] += red[tid + s];
+    __syncthreads();
+  }
+  const double fro2 = red[0];
+  __syncthreads();
+  const double tol2 = fro2 * 1.0e-30;  // converged when off-diagonal <= 1e-15 ||A||_F
+  int sweep = 0;
+  for (sweep = 0; sweep < 60; ++sweep) {
+    // off-diagonal norm
+    double off = 0.0;
+    for (size_t idx = tid; idx < size_t(n) * n; idx += nt) {
+      const int i = int(idx % n), j = int(idx / n);
+      if (i != j) off += A[idx] * A[idx];
+    }
+    red[tid] = off;
+    __syncthreads();
+    for (int s = nt / 2; s > 0; s >>= 1) {
+      if (tid < s) red[tid] += red[tid + s];
+      __syncthreads();
+    }
+    if (tid == 0) done = (red[0] <= tol2) ? 1 : 0;
+    __syncthreads();
+    if (done) break;
+    for (int round = 0; round < m - 1; ++round) {
+      // pairs (pairs[k], pairs[m-1-k]) for k < m/2
+      for (int k = tid; k < m / 2; k += nt) {
+        int p = pairs[k], q = pairs[m - 1 - k];
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        double c = 1.0, s = 0.0;
+        if (q < n) {
+          const double apq = Ael(p, q);
+          if (apq != 0.0) {
+            const double app = Ael(p, p), aqq = Ael(q, q);
+            const double theta = (aqq - app) / (2.0 * apq);
+            const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            s = t * c;
+          }
+        }
+        pp[k] = p;
+        qq[k] = q;
+        cs[k] = c;
+        sn[k] = s;
+      }
+      __syncthreads();
+      // columns: A <- A J, W <- W J
+      for (long long idx = tid; idx < (long long)n * (m / 2); idx += nt) {
+        const int r = int(idx % n), k = int(idx / n);
+        const int p = pp[k], q = qq[k];
+        if (q >= n || sn[k] == 0.0) continue;
+        const double c = cs[k], s = sn[k];
+        const double ap = Ael(r, p), aq = Ael(r, q);
+        Ael(r, p) = c * ap - s * aq;
+        Ael(r, q) = s * ap + c * aq;
+        const double wp = W[r + size_t(p) * n], wq = W[r + size_t(q) * n];
+        W[r + size_t(p) * n] = c * wp - s * wq;
+        W[r + size_t(q) * n] = s * wp + c * wq;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (long long idx = tid; idx < (long long)n * (m / 2); idx += nt) {
+        const int col = int(idx % n), k = int(idx / n);
+        const int p = pp[k], q = qq[k];
+        if (q >= n || sn[k] == 0.0) continue;
+        const double c = cs[k], s = sn[k];
+        const double ap = Ael(p, col), aq = Ael(q, col);
+        Ael(p, col) = c * ap - s * aq;
+        Ael(q, col) = s * ap + c * aq;
+      }
+      __syncthreads();
+      // rotate the round-robin schedule (slot 0 fixed)
+      if (tid == 0) {
+        const int last = pairs[m - 1];
+        for (int i = m - 1; i > 1; --i) pairs[i] = pairs[i - 1];
+        pairs[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  if (sweep >= 60 && tid == 0) atomicOr(flags, DEV_EIGEN_NOCONV);
+  // sort ascending (selection by rank; ties broken by index)
+  for (int i = tid; i < n; i += nt) work[i] = Ael(i, i);
+  __syncthreads();
+  for (int i = tid; i < n; i += nt) {
+    const double v = work[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const double u = work[j];
+      rank += (u < v || (u == v && j < i)) ? 1 : 0;
+    }
+    evals[rank] = v;
+    reinterpret_cast<int*>(work + n)[i] = rank;
+  }
+  __syncthreads();
+  // permute eigenvector columns into A (as scratch) then copy back
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) {
+    const int r = int(idx % n), j = int(idx / n);
+    const int dst = reinterpret_cast<int*>(work + n)[j];
+    A[r + size_t(dst) * n] = W[idx];
+  }
+  __syncthreads();
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) W[idx] = A[idx];
+}
+
+}  // namespace
+
+int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s) {
+  const int m = (n + 1) & ~1;
+  const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
+  jacobi_kernel<<<1, kJacThreads, shm, s>>>(n, A, W, evals, work, flags);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky L L^T = A (lower, right-looking) followed by L^{-1} in place
+// (DPBTRF + DTRTRI of cholesky_factorization / evolve_wavefunction,
+// module_constraints.f90:497-590).  One CTA.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void __launch_bounds__(1024) cholesky_inverse_kernel(int n, double* A, int* flags) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  auto a = [A, n](int i, int j) -> double& { return A[i + size_t(j) * n]; };
+  __shared__ double dkk;
+  __shared__ int bad;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      const double d = a(k, k);
+      if (!(d > 0.0)) bad = 1;
+      dkk = sqrt(fmax(d, 0.0));
+      a(k, k) = dkk;
+    }
+    __syncthreads();
+    if (bad) break;
+    for (int i = k + 1 + tid; i < n; i += nt) a(i, k) = a(i, k) / dkk;
+    __syncthreads();
+    const int rows = n - k - 1;
+    for (long long idx = tid; idx < (long long)rows * rows; idx += nt) {
+      const int i = k + 1 + int(idx % rows), j = k + 1 + int(idx / rows);
+      if (j <= i) a(i, j) = fma(-a(i, k), a(j, k), a(i, j));
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (tid == 0) atomicOr(flags, DEV_CHOLESKY);
+    return;
+  }
+  // zero the strict upper triangle
+  for (long long idx = tid; idx < (long long)n * n; idx += nt) {
+    const int i = int(idx % n), j = int(idx / n);
+    if (i < j) a(i, j) = 0.0;
+  }
+  __syncthreads();
+  // inverse of lower-triangular L, column by column from the right:
+  // for j = n-1..0: L^{-1}(j,j) = 1/L(j,j); L^{-1}(i,j) = -(sum_{k=j+1..i} L^{-1}(i,k) L(k,j)) / L(j,j)
+  // done in place with the standard DTRTI2-style update.
+  for (int j = n - 1; j >= 0; --j) {
+    __shared__ double ajj;
+    if (tid == 0) {
+      if (a(j, j) == 0.0) bad = 1;
+      a(j, j) = 1.0 / a(j, j);
+      ajj = -a(j, j);
+    }
+    __syncthreads();
+    if (bad) break;
+    // x = A(j+1:n, j); A(j+1:n, j) = T * x with T = A(j+1:n, j+1:n) (already inverted, lower)
+    // computed row by row: y_i = sum_{k=j+1..i} T(i,k) x_k
+    const int len = n - j - 1;
+    for (int r = tid; r < len; r += nt) {
+      const int i = j + 1 + r;
+      double y = 0.0;
+      for (int k = j + 1; k <= i; ++k) y = fma(a(i, k), a(k, j), y);
+      A[size_t(n) * n + i] = y;  // scratch row after the matrix
+    }
+    __syncthreads();
+    for (int r = tid; r < len; r += nt) {
+      const int i = j + 1 + r;
+      a(i, j) = A[size_t(n) * n + i] * ajj;
+    }
+    __syncthreads();
+  }
+  if (bad && tid == 0) atomicOr(flags, DEV_TRTRI);
+}
+
+}  // namespace
+
+// A must have room for n*n + n doubles (scratch row).
+int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s) {
+  cholesky_inverse_kernel<<<1, 1024, 0, s>>>(n, A, flags);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
+}  // namespace tvap

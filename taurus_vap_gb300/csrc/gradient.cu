@@ -1,0 +1,227 @@
+// Gradient step, Thouless evolution and the adjoint of the projected energy.
+//
+//   calculate_gradient (module_gradient.f90:79-143), gradient_type 0
+//   cholesky_factorization + evolve_wavefunction (module_constraints.f90:497-590)
+//   dE/dZ for E(Z) = projected energy of evolve(U0, V0, Z): with
+//     L L^T = 1 + Z^T Z and Phi1 = evolve(U0, V0, Z), a change dZ moves Phi1
+//     by the Thouless matrix L^{-1} dZ L^{-T} in Phi1's quasiparticle basis,
+//     and the gradient there is field_H20v(Phi1) (the projected H20 of
+//     calculate_projected_H20).  Hence dE/dZ = L^{-T} H20v(Phi1) L^{-1}.
+//     The per-angle densities are recomputed by the projection at Phi1.
+
+#include <cmath>
+
+#include "tvap_internal.cuh"
+
+namespace tvap {
+
+int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
+int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
+int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out);
+int ensure_workspace(tvap_ctx* c, int G);
+int angle_count(const tvap_proj_opts& o);
+int check_flags(tvap_ctx* c);
+
+namespace {
+
+__global__ void gradient_kernel(size_t nn, int cdim, const double* __restrict__ H20v,
+                                const double* __restrict__ lambda, const double* __restrict__ C20,
+                                const double* __restrict__ Zim1, double eta, double mu, double* __restrict__ Zi,
+                                double* __restrict__ partial) {
+  __shared__ double red[256];
+  const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  double z2 = 0.0;
+  if (i < nn) {
+    double sg = 0.0;
+    for (int j = 0; j < cdim; ++j) sg += lambda[j] * C20[size_t(j) * nn + i];
+    const double z = -eta * (H20v[i] - sg) + mu * Zim1[i];
+    Zi[i] = z;
+    z2 = z * z;
+  }
+  red[threadIdx.x] = z2;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void sum_partials_kernel(int m, const double* __restrict__ partial, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < m; ++i) s += partial[i];
+    out[0] = s;
+  }
+}
+
+__global__ void add_identity_kernel(int n, double* A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) A[i + size_t(i) * n] += 1.0;
+}
+
+int rgemm(int M, int N, int K, View A, View B, double* C, int ldc, double alpha, double beta, cudaStream_t s) {
+  GemmArgs g{};
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.batch = 1;
+  g.A = A;
+  g.B = B;
+  g.C = C;
+  g.crs = 1;
+  g.ccs = ldc;
+  g.alpha = make_double2(alpha, 0.0);
+  g.beta = make_double2(beta, 0.0);
+  g.a_real = g.b_real = g.c_real = true;
+  return gemm(g, s);
+}
+
+struct EvolveBuf {
+  double *Z = nullptr, *L = nullptr, *A1 = nullptr, *A2 = nullptr, *U0 = nullptr, *V0 = nullptr;
+};
+
+// U1 = (U0 + V0 Z) L^{-T}, V1 = (V0 + U0 Z) L^{-T}; L^{-1} left in b.L
+int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1) {
+  cudaStream_t s = c->stream;
+  const size_t nn = size_t(n) * n;
+  int rc;
+  const View Zv = view_cm(b.Z, n, 0);
+  sec_begin(c, SEC_EVOLVE);
+  if ((rc = rgemm(n, n, n, view_t(Zv), Zv, b.L, n, 1.0, 0.0, s))) return rc;
+  add_identity_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, b.L);
+  if ((rc = cholesky_inverse(n, b.L, c->d_flags, s))) return rc;
+  TVAP_CUDA(cudaMemcpyAsync(b.A1, b.U0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+  TVAP_CUDA(cudaMemcpyAsync(b.A2, b.V0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+  if ((rc = rgemm(n, n, n, view_cm(b.V0, n, 0), Zv, b.A1, n, 1.0, 1.0, s))) return rc;
+  if ((rc = rgemm(n, n, n, view_cm(b.U0, n, 0), Zv, b.A2, n, 1.0, 1.0, s))) return rc;
+  const View LinvT = view_t(view_cm(b.L, n, 0));
+  if ((rc = rgemm(n, n, n, view_cm(b.A1, n, 0), LinvT, U1, n, 1.0, 0.0, s))) return rc;
+  if ((rc = rgemm(n, n, n, view_cm(b.A2, n, 0), LinvT, V1, n, 1.0, 0.0, s))) return rc;
+  sec_end(c, SEC_EVOLVE);
+  c->kernel_launches += 8;
+  return TVAP_OK;
+}
+
+}  // namespace
+
+double* ws_U(tvap_ctx* c);
+double* ws_V(tvap_ctx* c);
+double* ws_H20v(tvap_ctx* c);
+
+}  // namespace tvap
+
+using namespace tvap;
+
+extern "C" {
+
+int tvap_calculate_gradient(tvap_ctx* c, const double* H20v, int cdim, const double* lambda, const double* C20,
+                            const double* Zim1, double eta, double mu, double* Zi, double* gradient_norm) {
+  if (!c || !H20v || !Zim1 || !Zi || !gradient_norm || cdim < 0 || (cdim > 0 && (!lambda || !C20)) || eta == 0.0)
+    return TVAP_ERR_ARG;
+  c->kernel_launches = 0;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  const int tb = 256;
+  const int nblocks = int((nn + tb - 1) / tb);
+  double* buf = nullptr;
+  const size_t tot = nn * (3 + size_t(cdim)) + cdim + nblocks + 1;
+  TVAP_CUDA(cudaMalloc(&buf, sizeof(double) * tot));
+  double *dH = buf, *dZm = buf + nn, *dZ = buf + 2 * nn, *dC = buf + 3 * nn, *dl = dC + nn * cdim,
+         *part = dl + cdim, *sum = part + nblocks;
+  int rc = upload_matrix(H20v, dH, sizeof(double) * nn, s);
+  if (!rc) rc = upload_matrix(Zim1, dZm, sizeof(double) * nn, s);
+  if (!rc && cdim > 0) rc = upload_matrix(C20, dC, sizeof(double) * nn * cdim, s);
+  if (!rc && cdim > 0) rc = upload_matrix(lambda, dl, sizeof(double) * cdim, s);
+  if (!rc) {
+    sec_begin(c, SEC_GRADIENT);
+    gradient_kernel<<<nblocks, tb, 0, s>>>(nn, cdim, dH, dl, dC, dZm, eta, mu, dZ, part);
+    sum_partials_kernel<<<1, 32, 0, s>>>(nblocks, part, sum);
+    sec_end(c, SEC_GRADIENT);
+    c->kernel_launches += 2;
+    double h = 0.0;
+    rc = download_matrix(dZ, Zi, sizeof(double) * nn, s);
+    if (!rc) {
+      cudaMemcpyAsync(&h, sum, sizeof(double), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) rc = TVAP_ERR_CUDA;
+      *gradient_norm = std::sqrt(h) / eta;
+    }
+  }
+  cudaFree(buf);
+  return rc;
+}
+
+int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z, double* U1, double* V1) {
+  if (!c || !U0 || !V0 || !Z || !U1 || !V1) return TVAP_ERR_ARG;
+  c->kernel_launches = 0;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  double* buf = nullptr;
+  TVAP_CUDA(cudaMalloc(&buf, sizeof(double) * (8 * nn + n)));
+  EvolveBuf b;
+  b.Z = buf;
+  b.U0 = buf + nn;
+  b.V0 = buf + 2 * nn;
+  b.A1 = buf + 3 * nn;
+  b.A2 = buf + 4 * nn;
+  double* dU1 = buf + 5 * nn;
+  double* dV1 = buf + 6 * nn;
+  b.L = buf + 7 * nn;  // n*n + n (scratch row)
+  int rc = upload_matrix(Z, b.Z, sizeof(double) * nn, s);
+  if (!rc) rc = upload_matrix(U0, b.U0, sizeof(double) * nn, s);
+  if (!rc) rc = upload_matrix(V0, b.V0, sizeof(double) * nn, s);
+  if (!rc) rc = evolve_device(c, b, n, dU1, dV1);
+  if (!rc) rc = download_matrix(dU1, U1, sizeof(double) * nn, s);
+  if (!rc) rc = download_matrix(dV1, V1, sizeof(double) * nn, s);
+  if (!rc) rc = check_flags(c);
+  cudaFree(buf);
+  return rc;
+}
+
+int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const double* Z,
+                        const tvap_proj_opts* opts, double* energy, double* dEdZ) {
+  if (!c || !U0 || !V0 || !Z || !opts || !energy || !dEdZ) return TVAP_ERR_ARG;
+  if (!c->have_ham) return TVAP_ERR_NOT_READY;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  int rc;
+  if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
+  c->kernel_launches = 0;
+  double* buf = nullptr;
+  TVAP_CUDA(cudaMalloc(&buf, sizeof(double) * (7 * nn + n)));
+  EvolveBuf b;
+  b.Z = buf;
+  b.U0 = buf + nn;
+  b.V0 = buf + 2 * nn;
+  b.A1 = buf + 3 * nn;
+  b.A2 = buf + 4 * nn;
+  double* G = buf + 5 * nn;
+  b.L = buf + 6 * nn;
+  rc = upload_matrix(Z, b.Z, sizeof(double) * nn, s);
+  if (!rc) rc = upload_matrix(U0, b.U0, sizeof(double) * nn, s);
+  if (!rc) rc = upload_matrix(V0, b.V0, sizeof(double) * nn, s);
+  if (!rc) rc = evolve_device(c, b, n, ws_U(c), ws_V(c));
+  if (!rc) rc = check_flags(c);
+  tvap_pnp p{};
+  if (!rc) rc = project_device(c, *opts, &p);
+  if (!rc) {
+    // dE/dZ = L^{-T} H20v L^{-1}
+    const View Li = view_cm(b.L, n, 0);
+    rc = rgemm(n, n, n, view_cm(ws_H20v(c), n, 0), Li, G, n, 1.0, 0.0, s);
+    if (!rc) rc = rgemm(n, n, n, view_t(Li), view_cm(G, n, 0), b.A1, n, 1.0, 0.0, s);
+    if (!rc) rc = download_matrix(b.A1, dEdZ, sizeof(double) * nn, s);
+    if (!rc) {
+      if (cudaStreamSynchronize(s) != cudaSuccess) rc = TVAP_ERR_CUDA;
+      const double ore = p.over[0], oim = p.over[1], ere = p.ener[0], eim = p.ener[1];
+      const double d = ore * ore + oim * oim;
+      *energy = (ere * ore + eim * oim) / d;
+    }
+  }
+  cudaFree(buf);
+  return rc;
+}
+
+}  // extern "C"

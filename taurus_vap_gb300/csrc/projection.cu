@@ -1,0 +1,1010 @@
+// The gauge-angle loop of project_wavefunction (module_projection.f90:201-373)
+// for all angles at once, followed by calculate_projected_H20 (:729-759).
+//
+// Per call (state U0, V0 real n x n):
+//   canonical basis (construct_canonical_basis, module_wavefunctions.f90:777-945)
+//   angle-independent real blocks:  V_t^T V_t, U_t^T U_t, V_t^T U_t, U_t^T V_t,
+//       D_t^T D_t  for t = protons, neutrons, so that for every angle
+//       U_phi = sum_t e^{-i phi_t} V_t^T V_t + e^{i phi_t} U_t^T U_t,
+//       V_phi = sum_t e^{i phi_t} V_t^T U_t + e^{-i phi_t} U_t^T V_t,
+//       R_n   = sum_t e^{i phi_t} D_t^T D_t
+//     replace the rotation and Thouless ZGEMMs (:641-653, :695-700, :847-848)
+//     by O(n^2) combinations;
+//   per angle, batched:  A_phi (Thouless solve), U~ = U + V A, V~ = V + U A,
+//     rho = V~ V^T, kappaLR = V~ U^T, kappaRL = V U~^T, the fields, particle
+//     number and energy traces, H20 and the Pfaffian overlap;
+//   sum_gauge over angles and the projected gradient.
+//
+// Angle folding: for proj_facpi = 2 pi and integer particle numbers the angle
+// pairs (phi_p, phi_n) and (-phi_p, -phi_n) carry complex-conjugate weights and
+// complex-conjugate rotated quantities (U0, V0 are real), so only one member of
+// each pair is computed and it enters the sums as 2 Re(w o X).
+//
+// Overlap: the reference evaluates Pf(M) for the 2 n2 x 2 n2 matrix
+//   M = [[A1, -P], [P^T, C0]],  P = leading block of R_n2^{-1}
+// after an LU and an inverse of R_n2 (:840-933).  Here the Schur-complement
+// identities Pf([[A, B], [-B^T, C]]) = Pf(A) Pf(C + B^T A^{-1} B) and
+// Pf(X^T Y X) = det(X) Pf(Y) give the same number as
+//   overlap = signfac det(R22) Pf(A1) Pf(A1^{-1} + S^T C0 S) exp(ovac),
+//   S = R11 - R12 R22^{-1} R21  (R22: the nocc occupied states),
+// which needs one Pfaffian of size n2 - nocc and no inverse of R_n2.
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "tvap_internal.cuh"
+
+namespace tvap {
+
+// ---------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------
+struct Workspace {
+  int n = 0, G = 0;
+  // real n x n
+  double *U = nullptr, *V = nullptr, *rho = nullptr, *kap = nullptr, *jac = nullptr, *D = nullptr,
+         *evals = nullptr, *jwork = nullptr, *rhoc = nullptr, *kapc = nullptr, *tmp = nullptr, *blocks = nullptr;
+  // canonical summary (device): ints [nocc, nemp, bad], doubles [ovac, logPfA1, signPfA1], voveru[n]
+  int* canon_i = nullptr;
+  double* canon_d = nullptr;
+  // per angle complex n x n (batch G)
+  double2 *Uphi = nullptr, *Vphi = nullptr, *W = nullptr, *A = nullptr, *Ut = nullptr, *Vt = nullptr,
+          *X = nullptr, *Y = nullptr, *T = nullptr, *Rn = nullptr, *K = nullptr, *SZ = nullptr;
+  // angle-innermost (n*n*G)
+  double2 *rhoL = nullptr, *kLR = nullptr, *kRL = nullptr, *gam = nullptr, *hsp = nullptr, *dLR = nullptr,
+          *dRL = nullptr;
+  // per angle scalars
+  double2 *ephase = nullptr;  // [G][2] e^{i phi_p}, e^{i phi_n}
+  double2 *weight = nullptr;  // [G] w_p w_n
+  double* mult = nullptr;     // [G] 1 or 2 (folded)
+  double2 *obs = nullptr;     // [G][8]: over, ener, prot, neut, prot2, neut2, logdet terms
+  double2 *pf = nullptr;      // [2G] (log|Pf|, phase)
+  double2 *detR22 = nullptr;  // [2G] (log|det|, phase)
+  double2 *coefA = nullptr;   // [G] c_b (multiplicity-weighted w*o)
+  double2 *coefAE = nullptr;  // [G] c_b E_b
+  // sums
+  double2 *pA = nullptr, *pH = nullptr, *pAH = nullptr, *pscal = nullptr;
+  double* H20v = nullptr;
+  size_t bytes = 0;
+};
+
+namespace {
+
+template <typename T>
+int dalloc(T** p, size_t count, size_t& total) {
+  if (count == 0) count = 1;
+  TVAP_CUDA(cudaMalloc(p, sizeof(T) * count));
+  total += sizeof(T) * count;
+  return TVAP_OK;
+}
+
+void ws_free(Workspace* w) {
+  void* ptrs[] = {w->U,   w->V,     w->rho,    w->kap,   w->jac,    w->D,     w->evals,  w->jwork, w->rhoc,
+                  w->kapc, w->tmp,  w->blocks, w->canon_i, w->canon_d, w->Uphi, w->Vphi,   w->W,     w->A,
+                  w->Ut,  w->Vt,    w->X,      w->Y,     w->T,      w->Rn,    w->K,      w->SZ,    w->rhoL,
+                  w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
+                  w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
+                  w->H20v};
+  for (void* p : ptrs) cudaFree(p);
+  *w = Workspace();
+}
+
+int ws_ensure(tvap_ctx* c, int G) {
+  Workspace* w = c->ws;
+  const int n = c->n;
+  if (w && w->n == n && w->G >= G) return TVAP_OK;
+  if (!w) {
+    w = new Workspace();
+    c->ws = w;
+  } else {
+    ws_free(w);
+  }
+  w->n = n;
+  w->G = G;
+  const size_t nn = size_t(n) * n, nG = nn * G;
+  size_t& t = w->bytes;
+  int rc = TVAP_OK;
+#define A_(p, cnt) \
+  if ((rc = dalloc(&w->p, (cnt), t)) != TVAP_OK) return rc;
+  A_(U, nn) A_(V, nn) A_(rho, nn) A_(kap, nn) A_(jac, nn) A_(D, nn) A_(evals, n) A_(jwork, 2 * n + 2)
+  A_(rhoc, nn) A_(kapc, nn) A_(tmp, nn + n) A_(blocks, 10 * nn) A_(canon_i, 8) A_(canon_d, 8 + n)
+  A_(Uphi, nG) A_(Vphi, nG) A_(W, 2 * nG) A_(A, nG) A_(Ut, nG) A_(Vt, nG) A_(X, nG) A_(Y, nG) A_(T, nG)
+  A_(Rn, nG) A_(K, nG) A_(SZ, nG) A_(rhoL, nG) A_(kLR, nG) A_(kRL, nG) A_(gam, nG) A_(hsp, nG) A_(dLR, nG)
+  A_(dRL, nG) A_(ephase, 2 * G) A_(weight, G) A_(mult, G) A_(obs, 8 * G) A_(pf, 2 * G) A_(detR22, 2 * G)
+  A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
+#undef A_
+  return TVAP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// small kernels
+// ---------------------------------------------------------------------------
+
+// canonical-basis bookkeeping (construct_canonical_basis after the
+// diagonalisation, module_wavefunctions.f90:818-945, and the v/u extraction
+// of project_wavefunction, module_projection.f90:219-234).  One CTA.
+__global__ void canon_kernel(int n, const double* __restrict__ rhoc, const double* __restrict__ kapc, double eps,
+                             int allemp, int* canon_i, double* canon_d) {
+  __shared__ int submax[1024];
+  __shared__ int s_nocc, s_nemp;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) {
+    int nocc = 0, nemp = 0;
+    double ovac = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double v2 = fabs(rhoc[i + size_t(i) * n]);
+      const double u = sqrt(fabs(1.0 - v2));
+      if (v2 >= 1.0 - eps)
+        ++nocc;
+      else if (v2 <= eps && allemp == 0)
+        ++nemp;
+      else
+        ovac += log(u);
+    }
+    if (n - nocc - nemp == 0) ovac = 0.0;
+    s_nocc = nocc;
+    s_nemp = nemp;
+    canon_d[0] = ovac;
+  }
+  __syncthreads();
+  const int nocc = s_nocc, nemp = s_nemp;
+  // submax (1-based indices as in the reference)
+  for (int i = 1 + nemp + tid; i <= n - nocc; i += nt) {
+    int sm = i;
+    for (int j = i + 1; j <= n - nocc; ++j)
+      if (fabs(kapc[(j - 1) + size_t(i - 1) * n]) > sqrt(eps) * 1.0e-2) sm = j;
+    submax[i] = sm;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int bad = 0;
+    // subspace dimensions (the reference merges overlapping ranges)
+    int k = 1 + nemp;
+    while (k < n - nocc) {
+      const int j = submax[k];
+      int mx = 0;
+      for (int t = k; t <= j; ++t) mx = max(mx, submax[t]);
+      for (int t = k; t <= j; ++t) submax[t] = mx;
+      if (mx == j) k = j + 1;
+    }
+    k = 1 + nemp;
+    while (k < n - nocc) {
+      int d = submax[k] - k + 1;
+      if (d > 2 && (d % 2) != 0) d = 2;
+      if (d > 2) bad = 1;  // the reference would Schur-reduce this block (DGEES)
+      k += d;
+    }
+    // v/u with the sign of kappa in the canonical basis
+    double* vu = canon_d + 8;
+    for (int i = 0; i < n; ++i) vu[i] = 0.0;
+    int kk = 0, j = 1;
+    for (int i = 1; i <= n; ++i) {
+      const double v2 = fabs(rhoc[(i - 1) + size_t(i - 1) * n]);
+      const double v = sqrt(v2), u = sqrt(fabs(1.0 - v2));
+      double vc = 0.0;  // zVc(i, i+1) or zVc(i, i-1)
+      const bool paired = !(v2 > 1.0 - eps) && !(v2 <= eps);
+      if (paired) {
+        if (kk % 2 == 0)
+          vc = (i < n) ? copysign(v, kapc[(i - 1) + size_t(i) * n]) : 0.0;
+        else
+          vc = copysign(v, kapc[(i - 1) + size_t(i - 2) * n]);
+        ++kk;
+      }
+      if (i >= 1 + nemp && i <= n - nocc) {
+        // the reference reads zVc(i,i+1) for odd j and zVc(i,i-1) for even j
+        vu[i - 1] = paired ? vc / u : 0.0;
+        ++j;
+      }
+    }
+    const int nbloc = n - nocc - nemp;
+    if (nbloc % 2 != 0) bad = 1;
+    // Pf(A1) = prod over odd i of vu(i + nemp), as (log|.|, sign)
+    double lp = 0.0, sg = 1.0;
+    for (int i = 1; i <= nbloc - 1; i += 2) {
+      const double a = vu[i + nemp - 1];
+      if (a == 0.0) bad = 1;
+      lp += log(fabs(a));
+      if (a < 0.0) sg = -sg;
+    }
+    canon_d[1] = lp;
+    canon_d[2] = sg;
+    canon_i[0] = nocc;
+    canon_i[1] = nemp;
+    canon_i[2] = bad;
+  }
+}
+
+// per angle: U_phi, V_phi and the trailing n2 block of R_n
+__global__ void build_angle_kernel(int n, int G, const double* __restrict__ blk, const double2* __restrict__ eph,
+                                   const int* __restrict__ canon_i, double2* __restrict__ Uphi,
+                                   double2* __restrict__ Vphi, double2* __restrict__ Rn) {
+  const size_t nn = size_t(n) * n;
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= nn * G) return;
+  const int b = int(idx / nn);
+  const size_t e = idx % nn;
+  const double2 pp = eph[2 * b], pn = eph[2 * b + 1];  // e^{i phi_p}, e^{i phi_n}
+  // blocks: 0 VpVp 1 VnVn 2 UpUp 3 UnUn 4 VpUp 5 VnUn 6 UpVp 7 UnVn 8 DpDp 9 DnDn
+  const double vvp = blk[0 * nn + e], vvn = blk[1 * nn + e], uup = blk[2 * nn + e], uun = blk[3 * nn + e];
+  const double vup = blk[4 * nn + e], vun = blk[5 * nn + e], uvp = blk[6 * nn + e], uvn = blk[7 * nn + e];
+  double2 up;
+  up.x = (vvp + uup) * pp.x + (vvn + uun) * pn.x;
+  up.y = (uup - vvp) * pp.y + (uun - vvn) * pn.y;
+  double2 vp;
+  vp.x = (vup + uvp) * pp.x + (vun + uvn) * pn.x;
+  vp.y = (vup - uvp) * pp.y + (vun - uvn) * pn.y;
+  Uphi[idx] = up;
+  Vphi[idx] = vp;
+  const int nemp = canon_i[1];
+  const int n2 = n - nemp;
+  const int i = int(e % n), j = int(e / n);
+  if (i >= nemp && j >= nemp) {
+    const double dp = blk[8 * nn + e], dn = blk[9 * nn + e];
+    Rn[size_t(b) * n2 * n2 + (i - nemp) + size_t(j - nemp) * n2] =
+        make_double2(dp * pp.x + dn * pn.x, dp * pp.y + dn * pn.y);
+  }
+}
+
+// broadcast a real n x n matrix into a complex batch
+__global__ void broadcast_real_kernel(size_t nn, int G, const double* __restrict__ src, double2* __restrict__ dst) {
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= nn * G) return;
+  dst[idx] = make_double2(src[idx % nn], 0.0);
+}
+
+// K = A1^{-1} (nbloc x nbloc, skew 2x2 blocks) and Y = C0 S, with S the
+// (Schur-reduced) nbloc x nbloc block of R_n2 stored with leading dim ldS.
+__global__ void overlap_prep_kernel(int n, int G, const int* __restrict__ canon_i, const double* __restrict__ canon_d,
+                                    const double2* __restrict__ S, int ldS, long long bsS, double2* __restrict__ K,
+                                    double2* __restrict__ Y) {
+  const int nocc = canon_i[0], nemp = canon_i[1];
+  const int nb = n - nocc - nemp;
+  const size_t nb2 = size_t(nb) * nb;
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= nb2 * G) return;
+  const int b = int(idx / nb2);
+  const size_t e = idx % nb2;
+  const int i = int(e % nb), j = int(e / nb);  // 0-based local indices
+  const double* vu = canon_d + 8;
+  // A1u: upper entries A1(i, i+1) = vu(i + nemp) for odd 1-based i
+  double2 kv = make_double2(0.0, 0.0);
+  if ((i % 2) == 0 && j == i + 1) kv.x = -1.0 / vu[i + nemp];     // (A1^{-1})(i, i+1) = -1/a
+  if ((i % 2) == 1 && j == i - 1) kv.x = 1.0 / vu[i - 1 + nemp];  // (A1^{-1})(i+1, i) = 1/a
+  K[size_t(b) * nb2 + e] = kv;
+  // C0u upper entries C0(i, i+1) = -vu(i + nemp) for odd 1-based i (self overlap)
+  // Y(i, :) = C0(i, i+1) S(i+1, :) for even 0-based i; Y(i, :) = -C0(i-1, i) S(i-1, :) for odd
+  double2 y;
+  if ((i % 2) == 0) {
+    const double g = -vu[i + nemp];
+    const double2 s = S[b * bsS + (i + 1) + size_t(j) * ldS];
+    y = make_double2(g * s.x, g * s.y);
+  } else {
+    const double g = -vu[i - 1 + nemp];
+    const double2 s = S[b * bsS + (i - 1) + size_t(j) * ldS];
+    y = make_double2(-g * s.x, -g * s.y);
+  }
+  Y[size_t(b) * nb2 + e] = y;
+}
+
+// per-angle traces: particle numbers (calculate_particle_number io=0,
+// module_particlenumber.f90:78-143) and energy (calculate_expectval_energy,
+// module_hamiltonian.f90:1098-1126), from angle-innermost arrays.
+__global__ void traces_kernel(int n, int G, const double2* __restrict__ rho, const double2* __restrict__ kLR,
+                              const double2* __restrict__ kRL, const double2* __restrict__ gam,
+                              const double2* __restrict__ dLR, const double2* __restrict__ H1, double2 H0,
+                              double2* __restrict__ obs) {
+  const int b = blockIdx.x;
+  const int h = n / 2;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // accumulators: prot, neut, tr1, tr2, tr3, tr4, e1, e2, e3
+  double2 a[9];
+  for (int q = 0; q < 9; ++q) a[q] = make_double2(0.0, 0.0);
+  auto at = [G, n, b](const double2* X, int i, int j) { return X[(size_t(i) + size_t(j) * n) * G + b]; };
+  for (size_t e = tid; e < size_t(n) * n; e += nt) {
+    const int i = int(e % n), j = int(e / n);
+    const double2 rij = at(rho, i, j), rji = at(rho, j, i);
+    if (i == j) {
+      if (i < h)
+        a[0] = cadd(a[0], rij);
+      else
+        a[1] = cadd(a[1], rij);
+    }
+    const bool pblk = (i < h && j < h), nblk = (i >= h && j >= h);
+    if (pblk) {
+      cfma(a[2], rij, rji);
+      cfma(a[3], at(kRL, i, j), at(kLR, i, j));
+    } else if (nblk) {
+      cfma(a[4], rij, rji);
+      cfma(a[5], at(kRL, i, j), at(kLR, i, j));
+    }
+    cfma(a[6], H1[i + size_t(j) * n], rji);
+    cfma(a[7], at(gam, i, j), rji);
+    cfma(a[8], at(dLR, i, j), at(kRL, i, j));
+  }
+  __shared__ double2 red[9][256];
+  for (int q = 0; q < 9; ++q) red[q][tid] = a[q];
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s)
+      for (int q = 0; q < 9; ++q) red[q][tid] = cadd(red[q][tid], red[q][tid + s]);
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const double2 prot = red[0][0], neut = red[1][0];
+    const double2 prot2 = cadd(csub(cadd(prot, cmul(prot, prot)), red[2][0]), red[3][0]);
+    const double2 neut2 = cadd(csub(cadd(neut, cmul(neut, neut)), red[4][0]), red[5][0]);
+    const double2 ener = cadd(cadd(H0, red[6][0]), cscale(cadd(red[7][0], red[8][0]), 0.5));
+    obs[8 * b + 1] = ener;
+    obs[8 * b + 2] = prot;
+    obs[8 * b + 3] = neut;
+    obs[8 * b + 4] = prot2;
+    obs[8 * b + 5] = neut2;
+  }
+}
+
+// overlap per angle and the sum_gauge coefficients
+__global__ void overlap_finish_kernel(int n, int G, int have_overlap, const int* __restrict__ canon_i,
+                                      const double* __restrict__ canon_d, const double2* __restrict__ pf,
+                                      const double2* __restrict__ detR22, const double2* __restrict__ weight,
+                                      const double* __restrict__ mult, double2* __restrict__ obs,
+                                      double2* __restrict__ coefA, double2* __restrict__ coefAE) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= G) return;
+  double2 over = make_double2(1.0, 0.0);
+  if (have_overlap) {
+    const int nocc = canon_i[0], nemp = canon_i[1];
+    const int n2 = n - nemp;
+    const int n0 = n - nocc;
+    // signfac (module_projection.f90:813-816) with nocc0 = nocc1, nempm = nemp
+    const long long e1 = (long long)n2 * (n2 + 1) / 2;
+    const long long e2 = (long long)nocc * (nocc - 1) / 2;
+    const long long e3 = (long long)nocc * (nocc + 1) + (long long)nocc * (n0 + n2) + (long long)nocc * n0;
+    const double signfac = ((e1 + e2 + e3) & 1) ? -1.0 : 1.0;
+    const double ovac = canon_d[0];
+    const double2 pK = pf[b], phK = pf[G + b];
+    const double2 pR = detR22[b], phR = detR22[G + b];
+    if (isinf(pK.x) && pK.x < 0) {
+      over = make_double2(0.0, 0.0);
+    } else {
+      const double logm = pK.x + pR.x + canon_d[1] + ovac;
+      double2 ph = cmul(phK, phR);
+      ph = cscale(ph, canon_d[2] * signfac);
+      const double m = exp(logm);
+      over = make_double2(m * ph.x, m * ph.y);
+    }
+  }
+  obs[8 * b + 0] = over;
+  const double2 f1 = cmul(weight[b], over);
+  const double2 f2 = cmul(f1, obs[8 * b + 1]);
+  coefA[b] = cscale(f1, 1.0);
+  coefAE[b] = f2;
+}
+
+// sum_gauge of the scalars (module_projection.f90:425-458), folded pairs as 2 Re
+__global__ void sum_scalars_kernel(int G, const double2* __restrict__ obs, const double* __restrict__ mult,
+                                   const double2* __restrict__ weight, double2* __restrict__ pscal, int accumulate) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double2 s[6];
+  for (int q = 0; q < 6; ++q) s[q] = accumulate ? pscal[q] : make_double2(0.0, 0.0);
+  for (int b = 0; b < G; ++b) {
+    const double2 f1 = cmul(weight[b], obs[8 * b]);
+    const double2 terms[6] = {f1, cmul(obs[8 * b + 1], f1), cmul(obs[8 * b + 2], f1), cmul(obs[8 * b + 3], f1),
+                              cmul(obs[8 * b + 4], f1), cmul(obs[8 * b + 5], f1)};
+    for (int q = 0; q < 6; ++q) {
+      if (mult[b] == 2.0)
+        s[q].x += 2.0 * terms[q].x;
+      else
+        s[q] = cadd(s[q], terms[q]);
+    }
+  }
+  for (int q = 0; q < 6; ++q) pscal[q] = s[q];
+}
+
+// pnp_A, pnp_H20, pnp_AH20: sums over angles of c_b A_b, c_b H20_b,
+// c_b E_b A_b with H20_b = T_b - T_b^T (skew).
+__global__ void sum_matrices_kernel(int n, int G, const double2* __restrict__ A, const double2* __restrict__ T,
+                                    const double2* __restrict__ coefA, const double2* __restrict__ coefAE,
+                                    const double* __restrict__ mult, double2* __restrict__ pA, double2* __restrict__ pH,
+                                    double2* __restrict__ pAH, int accumulate) {
+  const size_t nn = size_t(n) * n;
+  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (e >= nn) return;
+  const int i = int(e % n), j = int(e / n);
+  const size_t et = j + size_t(i) * n;
+  double2 sa = accumulate ? pA[e] : make_double2(0.0, 0.0);
+  double2 sh = accumulate ? pH[e] : make_double2(0.0, 0.0);
+  double2 sah = accumulate ? pAH[e] : make_double2(0.0, 0.0);
+  for (int b = 0; b < G; ++b) {
+    const double2 a = A[size_t(b) * nn + e];
+    const double2 h = csub(T[size_t(b) * nn + e], T[size_t(b) * nn + et]);
+    const double2 t1 = cmul(a, coefA[b]), t2 = cmul(h, coefA[b]), t3 = cmul(a, coefAE[b]);
+    if (mult[b] == 2.0) {
+      sa.x += 2.0 * t1.x;
+      sh.x += 2.0 * t2.x;
+      sah.x += 2.0 * t3.x;
+    } else {
+      sa = cadd(sa, t1);
+      sh = cadd(sh, t2);
+      sah = cadd(sah, t3);
+    }
+  }
+  pA[e] = sa;
+  pH[e] = sh;
+  pAH[e] = sah;
+}
+
+// calculate_projected_H20 (module_projection.f90:729-759)
+__global__ void projected_h20_kernel(int n, const double2* __restrict__ pA, const double2* __restrict__ pH,
+                                     const double2* __restrict__ pAH, const double2* __restrict__ pscal,
+                                     double* __restrict__ H20v, int* flags) {
+  const size_t nn = size_t(n) * n;
+  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (e >= nn) return;
+  const int i = int(e % n), j = int(e / n);
+  const size_t et = j + size_t(i) * n;
+  const double2 over = pscal[0];
+  const double2 ener = cdiv(pscal[1], over);
+  const double2 rov = crcp(over);
+  const double2 A = cmul(cscale(csub(pA[e], pA[et]), 0.5), rov);
+  const double2 H = cmul(cscale(csub(pH[e], pH[et]), 0.5), rov);
+  const double2 AH = cmul(cscale(csub(pAH[e], pAH[et]), 0.5), rov);
+  H20v[e] = (cadd(csub(AH, cmul(ener, A)), H)).x;
+  const double ig = cmul(cadd(csub(pAH[e], cmul(ener, pA[e])), pH[e]), rov).y;
+  if (ig > 1.0e-8) atomicOr(flags, DEV_IMAG_GRAD);
+}
+
+// generic batched left solve X = A^{-1} B (A m x m, B m x k) by Gaussian
+// elimination with partial pivoting on [A | B]; also returns log|det A| and
+// the phase of det A.  Views give element (i,j) of batch b at p[i rs + j cs + b bs].
+constexpr int kLsThreads = 512;
+__global__ void __launch_bounds__(kLsThreads)
+    left_solve_kernel(int m, int k, View Av, View Bv, double2* __restrict__ Wall, double2* __restrict__ X,
+                      long long xrs, long long xcs, long long xbs, int conj_out, double2* __restrict__ det, int G,
+                      int* flags, int flag_bit) {
+  __shared__ double sv[kLsThreads];
+  __shared__ int si[kLsThreads];
+  __shared__ double2 prow[1024];
+  __shared__ double2 mult[512];
+  const int b = blockIdx.x;
+  const int w = m + k;
+  double2* W = Wall + size_t(b) * m * w;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const double2* Ap = static_cast<const double2*>(Av.p);
+  const double2* Bp = static_cast<const double2*>(Bv.p);
+  for (size_t idx = tid; idx < size_t(m) * w; idx += nt) {
+    const int r = int(idx % m), c = int(idx / m);
+    W[idx] = (c < m) ? Ap[r * Av.rs + c * Av.cs + b * Av.bs] : Bp[r * Bv.rs + (c - m) * Bv.cs + b * Bv.bs];
+  }
+  __syncthreads();
+  bool singular = false;
+  double logdet = 0.0;
+  double2 ph = make_double2(1.0, 0.0);
+  for (int kk = 0; kk < m; ++kk) {
+    double best = -1.0;
+    int bi = m;
+    for (int i = kk + tid; i < m; i += nt) {
+      const double v = cabs1(W[i + size_t(kk) * m]);
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+    sv[tid] = best;
+    si[tid] = bi;
+    __syncthreads();
+    for (int s = nt / 2; s > 0; s >>= 1) {
+      if (tid < s) {
+        const double a = sv[tid], bb = sv[tid + s];
+        const int ia = si[tid], ib = si[tid + s];
+        if (bb > a || (bb == a && ib < ia)) {
+          sv[tid] = bb;
+          si[tid] = ib;
+        }
+      }
+      __syncthreads();
+    }
+    int p = si[0];
+    const double pv = sv[0];
+    __syncthreads();
+    if (pv == 0.0) {
+      singular = true;
+      p = kk;
+    }
+    for (int c = kk + tid; c < w; c += nt) {
+      double2 a = W[kk + size_t(c) * m], q = W[p + size_t(c) * m];
+      if (p != kk) {
+        W[kk + size_t(c) * m] = q;
+        W[p + size_t(c) * m] = a;
+        a = q;
+      }
+      prow[c] = a;
+    }
+    __syncthreads();
+    const double2 piv = prow[kk];
+    if (!singular) {
+      const double mg = hypot(piv.x, piv.y);
+      logdet += log(mg);
+      ph = cmul(ph, make_double2(piv.x / mg, piv.y / mg));
+      if (p != kk) ph = cneg(ph);
+    }
+    const double2 rp = (pv == 0.0) ? make_double2(0.0, 0.0) : crcp(piv);
+    for (int i = kk + 1 + tid; i < m; i += nt) mult[i] = cmul(W[i + size_t(kk) * m], rp);
+    __syncthreads();
+    const int rows = m - kk - 1, cols = w - kk - 1;
+    for (long long idx = tid; idx < (long long)rows * cols; idx += nt) {
+      const int i = kk + 1 + int(idx % rows), c = kk + 1 + int(idx / rows);
+      double2 v = W[i + size_t(c) * m];
+      const double2 mu = mult[i], r = prow[c];
+      v.x = fma(-mu.x, r.x, v.x);
+      v.x = fma(mu.y, r.y, v.x);
+      v.y = fma(-mu.x, r.y, v.y);
+      v.y = fma(-mu.y, r.x, v.y);
+      W[i + size_t(c) * m] = v;
+    }
+    __syncthreads();
+  }
+  for (int kk = m - 1; kk >= 0; --kk) {
+    const double2 rk = crcp(W[kk + size_t(kk) * m]);
+    for (int c = tid; c < k; c += nt) {
+      const double2 y = cmul(W[kk + size_t(m + c) * m], rk);
+      W[kk + size_t(m + c) * m] = y;
+      prow[c] = y;
+    }
+    __syncthreads();
+    for (long long idx = tid; idx < (long long)kk * k; idx += nt) {
+      const int i = int(idx % kk), c = int(idx / kk);
+      double2 v = W[i + size_t(m + c) * m];
+      const double2 mu = W[i + size_t(kk) * m], r = prow[c];
+      v.x = fma(-mu.x, r.x, v.x);
+      v.x = fma(mu.y, r.y, v.x);
+      v.y = fma(-mu.x, r.y, v.y);
+      v.y = fma(-mu.y, r.x, v.y);
+      W[i + size_t(m + c) * m] = v;
+    }
+    __syncthreads();
+  }
+  if (X) {
+    for (size_t idx = tid; idx < size_t(m) * k; idx += nt) {
+      const int r = int(idx % m), c = int(idx / m);
+      double2 v = W[r + size_t(m + c) * m];
+      if (conj_out) v.y = -v.y;
+      X[r * xrs + c * xcs + b * xbs] = v;
+    }
+  }
+  if (tid == 0) {
+    if (det) {
+      det[b] = make_double2(singular ? -INFINITY : logdet, 0.0);
+      det[G + b] = singular ? make_double2(0.0, 0.0) : ph;
+    }
+    if (singular) atomicOr(flags, flag_bit);
+  }
+}
+
+__global__ void fill_det_one_kernel(int G, double2* det) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < G) {
+    det[b] = make_double2(0.0, 0.0);
+    det[G + b] = make_double2(1.0, 0.0);
+  }
+}
+
+// S = R11 - R12 Z with Z = R22^{-1} R21 (nb x nb, in place into SZ)
+__global__ void schur_kernel(int n2, int nb, int G, const double2* __restrict__ Rn, const double2* __restrict__ Z,
+                             double2* __restrict__ S) {
+  const size_t nb2 = size_t(nb) * nb;
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= nb2 * G) return;
+  const int b = int(idx / nb2);
+  const size_t e = idx % nb2;
+  const int i = int(e % nb), j = int(e / nb);
+  const int no = n2 - nb;
+  const double2* R = Rn + size_t(b) * n2 * n2;
+  double2 s = R[i + size_t(j) * n2];
+  for (int t = 0; t < no; ++t) {
+    const double2 r12 = R[i + size_t(nb + t) * n2];
+    const double2 z = Z[size_t(b) * no * nb + t + size_t(j) * no];
+    s = csub(s, cmul(r12, z));
+  }
+  S[size_t(b) * nb2 + e] = s;
+}
+
+inline unsigned nblk(size_t total, int tb) { return unsigned((total + tb - 1) / tb); }
+
+// host-side angle table (assign_angles, module_projection.f90:112-185)
+struct AngleTable {
+  std::vector<double> php, phn, mult;
+  std::vector<std::complex<double>> w;
+};
+
+AngleTable make_angles(const tvap_proj_opts& o, bool fold) {
+  AngleTable t;
+  const int Mp = o.Mphip, Mn = o.Mphin;
+  const std::complex<double> I(0.0, 1.0);
+  auto phi = [&](int M, int j) { return (M % 2 == 1) ? o.facpi * (j - 1.0) / M : o.facpi * (j - 0.5) / M; };
+  auto partner = [](int M, int j) { return (M % 2 == 1) ? ((M - (j - 1)) % M) + 1 : M + 1 - j; };
+  std::vector<char> seen(size_t(Mp) * Mn, 0);
+  for (int jp = 1; jp <= Mp; ++jp)
+    for (int jn = 1; jn <= Mn; ++jn) {
+      if (seen[size_t(jp - 1) * Mn + (jn - 1)]) continue;
+      seen[size_t(jp - 1) * Mn + (jn - 1)] = 1;
+      double mult = 1.0;
+      if (fold) {
+        const int qp = partner(Mp, jp), qn = partner(Mn, jn);
+        if (!(qp == jp && qn == jn)) {
+          seen[size_t(qp - 1) * Mn + (qn - 1)] = 1;
+          mult = 2.0;
+        }
+      }
+      const double pp = phi(Mp, jp), pn = phi(Mn, jn);
+      t.php.push_back(pp);
+      t.phn.push_back(pn);
+      t.mult.push_back(mult);
+      t.w.push_back(std::exp(-I * pp * o.valence_Z) / double(Mp) * std::exp(-I * pn * o.valence_N) / double(Mn));
+    }
+  return t;
+}
+
+bool is_integer(double x) { return std::fabs(x - std::round(x)) < 1e-12; }
+
+int real_gemm(int M, int N, int K, View A, View B, double* C, int ldc, double alpha, double beta, cudaStream_t s) {
+  GemmArgs g{};
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.batch = 1;
+  g.A = A;
+  g.B = B;
+  g.C = C;
+  g.crs = 1;
+  g.ccs = ldc;
+  g.cbs = 0;
+  g.alpha = make_double2(alpha, 0.0);
+  g.beta = make_double2(beta, 0.0);
+  g.a_real = g.b_real = g.c_real = true;
+  return gemm(g, s);
+}
+
+}  // namespace
+
+// Canonical basis + angle-independent blocks for state (w->U, w->V).
+int prepare_state(tvap_ctx* c, double occeps, double allemp_d, int* host_canon /*[3] or null*/) {
+  Workspace* w = c->ws;
+  const int n = c->n, h = n / 2;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  int rc;
+  const View Vn = view_cm(w->V, n, 0), Un = view_cm(w->U, n, 0);
+  sec_begin(c, SEC_CANONICAL);
+  // rho = V V^T, kappa = V U^T (construct_canonical_basis :826, :862)
+  if ((rc = real_gemm(n, n, n, Vn, view_t(Vn), w->rho, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, Vn, view_t(Un), w->kap, n, 1.0, 0.0, s))) return rc;
+  TVAP_CUDA(cudaMemcpyAsync(w->jac, w->rho, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+  if ((rc = jacobi_eigen(n, w->jac, w->D, w->evals, w->jwork, c->d_flags, s))) return rc;
+  const View Dn = view_cm(w->D, n, 0);
+  // rhoc = D^T rho D, kappac = D^T kappa D
+  if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->rho, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->rhoc, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->kap, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->kapc, n, 1.0, 0.0, s))) return rc;
+  const double eps = (occeps < 2.2250738585072014e-308) ? 1.0e-8 : occeps;
+  canon_kernel<<<1, 256, 0, s>>>(n, w->rhoc, w->kapc, eps, int(allemp_d), w->canon_i, w->canon_d);
+  TVAP_CUDA(cudaGetLastError());
+  sec_end(c, SEC_CANONICAL);
+  sec_begin(c, SEC_BLOCKS);
+  // angle-independent blocks (row halves p = 0..h-1, n = h..n-1)
+  const double* Xs[4][2] = {{w->V, w->V}, {w->U, w->U}, {w->V, w->U}, {w->U, w->V}};
+  for (int q = 0; q < 4; ++q)
+    for (int t = 0; t < 2; ++t) {
+      const double* L = Xs[q][0] + t * h;
+      const double* R = Xs[q][1] + t * h;
+      // (L_t)^T R_t: A(i,k) = L(k,i) -> rs = n, cs = 1; B(k,j) = R(k,j)
+      if ((rc = real_gemm(n, n, h, View{L, n, 1, 0}, View{R, 1, n, 0}, w->blocks + (2 * q + t) * nn, n, 1.0, 0.0,
+                          s)))
+        return rc;
+    }
+  for (int t = 0; t < 2; ++t) {
+    const double* L = w->D + t * h;
+    if ((rc = real_gemm(n, n, h, View{L, n, 1, 0}, View{L, 1, n, 0}, w->blocks + (8 + t) * nn, n, 1.0, 0.0, s)))
+      return rc;
+  }
+  sec_end(c, SEC_BLOCKS);
+  c->kernel_launches += 13 + 1 + 2;
+  if (host_canon) {
+    TVAP_CUDA(cudaMemcpyAsync(host_canon, w->canon_i, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+    TVAP_CUDA(cudaStreamSynchronize(s));
+  }
+  return TVAP_OK;
+}
+
+// Angles [0, G) of the table: rotated quantities and their contribution to
+// the sums (accumulate = 0 starts new sums).  nocc/nemp are the host copies
+// of the canonical counts.
+int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d_weight, const double* d_mult,
+                   bool have_overlap, int nocc, int nemp, double factor_delta, int accumulate) {
+  Workspace* w = c->ws;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  const int tb = 256;
+  int rc;
+  sec_begin(c, SEC_SOLVE);
+  build_angle_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(n, G, w->blocks, d_ephase, w->canon_i, w->Uphi, w->Vphi,
+                                                     w->Rn);
+  TVAP_CUDA(cudaGetLastError());
+  // A_phi = conj(V_phi U_phi^{-1}): solve U_phi^T Y = V_phi^T, A = conj(Y^T)
+  left_solve_kernel<<<G, kLsThreads, 0, s>>>(n, n, View{w->Uphi, (long long)n, 1, (long long)nn},
+                                             View{w->Vphi, (long long)n, 1, (long long)nn}, w->W, w->A, n, 1,
+                                             (long long)nn, 1, nullptr, G, c->d_flags, DEV_SINGULAR_UPHI);
+  TVAP_CUDA(cudaGetLastError());
+  sec_end(c, SEC_SOLVE);
+  sec_begin(c, SEC_UV);
+  // U~ = U + V A, V~ = V + U A
+  broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(nn, G, w->U, w->Ut);
+  broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(nn, G, w->V, w->Vt);
+  {
+    GemmArgs g{};
+    g.M = g.N = g.K = n;
+    g.batch = G;
+    g.A = view_cm(w->V, n, 0);
+    g.B = view_cm(w->A, n, (long long)nn);
+    g.C = w->Ut;
+    g.crs = 1;
+    g.ccs = n;
+    g.cbs = (long long)nn;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(1.0, 0.0);
+    g.a_real = true;
+    if ((rc = gemm(g, s))) return rc;
+    g.A = view_cm(w->U, n, 0);
+    g.C = w->Vt;
+    if ((rc = gemm(g, s))) return rc;
+  }
+  sec_end(c, SEC_UV);
+  sec_begin(c, SEC_DENSITIES);
+  // densities in angle-innermost layout: X[(i + j n) G + b]
+  {
+    GemmArgs g{};
+    g.M = g.N = g.K = n;
+    g.batch = G;
+    g.crs = G;
+    g.ccs = (long long)n * G;
+    g.cbs = 1;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    // rho = V~ V^T
+    g.A = view_cm(w->Vt, n, (long long)nn);
+    g.B = view_t(view_cm(w->V, n, 0));
+    g.b_real = true;
+    g.C = w->rhoL;
+    if ((rc = gemm(g, s))) return rc;
+    // kappaLR = V~ U^T
+    g.B = view_t(view_cm(w->U, n, 0));
+    g.C = w->kLR;
+    if ((rc = gemm(g, s))) return rc;
+    // kappaRL = V U~^T
+    g.A = view_cm(w->V, n, 0);
+    g.a_real = true;
+    g.b_real = false;
+    g.B = view_t(view_cm(w->Ut, n, (long long)nn));
+    g.C = w->kRL;
+    if ((rc = gemm(g, s))) return rc;
+  }
+  sec_end(c, SEC_DENSITIES);
+  if ((rc = fields_batched(c, G, G, w->rhoL, w->kLR, w->kRL, w->gam, w->hsp, w->dLR, w->dRL, s))) return rc;
+  sec_begin(c, SEC_TRACES);
+  traces_kernel<<<G, 256, 0, s>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR, c->d_H1, c->H0, w->obs);
+  TVAP_CUDA(cudaGetLastError());
+  sec_end(c, SEC_TRACES);
+  sec_begin(c, SEC_H20);
+  // H20: T = U~^T (h V~ + fd/2 DeltaLR U~) - fd/2 V~^T DeltaRL V~, H20 = T - T^T
+  {
+    const View hv{w->hsp, (long long)G, (long long)n * G, 1};
+    const View dl{w->dLR, (long long)G, (long long)n * G, 1};
+    const View dr{w->dRL, (long long)G, (long long)n * G, 1};
+    GemmArgs g{};
+    g.M = g.N = g.K = n;
+    g.batch = G;
+    g.crs = 1;
+    g.ccs = n;
+    g.cbs = (long long)nn;
+    g.A = hv;
+    g.B = view_cm(w->Vt, n, (long long)nn);
+    g.C = w->X;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    if ((rc = gemm(g, s))) return rc;
+    g.A = dl;
+    g.B = view_cm(w->Ut, n, (long long)nn);
+    g.alpha = make_double2(0.5 * factor_delta, 0.0);
+    g.beta = make_double2(1.0, 0.0);
+    if ((rc = gemm(g, s))) return rc;
+    g.A = dr;
+    g.B = view_cm(w->Vt, n, (long long)nn);
+    g.C = w->Y;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    if ((rc = gemm(g, s))) return rc;
+    g.A = view_t(view_cm(w->Ut, n, (long long)nn));
+    g.B = view_cm(w->X, n, (long long)nn);
+    g.C = w->T;
+    if ((rc = gemm(g, s))) return rc;
+    g.A = view_t(view_cm(w->Vt, n, (long long)nn));
+    g.B = view_cm(w->Y, n, (long long)nn);
+    g.alpha = make_double2(-0.5 * factor_delta, 0.0);
+    g.beta = make_double2(1.0, 0.0);
+    if ((rc = gemm(g, s))) return rc;
+  }
+  sec_end(c, SEC_H20);
+  sec_begin(c, SEC_OVERLAP);
+  // overlap
+  const int n2 = n - nemp, nb = n2 - nocc;
+  if (have_overlap) {
+    const double2* S = w->Rn;
+    int ldS = n2;
+    long long bsS = (long long)n2 * n2;
+    if (nocc > 0) {
+      // Z = R22^{-1} R21 (nocc x nb), det(R22); S = R11 - R12 Z
+      left_solve_kernel<<<G, kLsThreads, 0, s>>>(
+          nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
+          View{w->Rn + nb, 1, n2, (long long)n2 * n2}, w->W, w->X, 1, nocc, (long long)nocc * nb, 0, w->detR22, G,
+          c->d_flags, DEV_SINGULAR_RN);
+      schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s>>>(n2, nb, G, w->Rn, w->X, w->SZ);
+      TVAP_CUDA(cudaGetLastError());
+      S = w->SZ;
+      ldS = nb;
+      bsS = (long long)nb * nb;
+    } else {
+      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s>>>(G, w->detR22);
+    }
+    if (nb > 0) {
+      overlap_prep_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s>>>(n, G, w->canon_i, w->canon_d, S, ldS, bsS,
+                                                                       w->K, w->Y);
+      TVAP_CUDA(cudaGetLastError());
+      // K += S^T Y
+      GemmArgs g{};
+      g.M = g.N = g.K = nb;
+      g.batch = G;
+      g.A = View{S, (long long)ldS, 1, bsS};
+      g.B = view_cm(w->Y, nb, (long long)nb * nb);
+      g.C = w->K;
+      g.crs = 1;
+      g.ccs = nb;
+      g.cbs = (long long)nb * nb;
+      g.alpha = make_double2(1.0, 0.0);
+      g.beta = make_double2(1.0, 0.0);
+      if ((rc = gemm(g, s))) return rc;
+      sec_end(c, SEC_OVERLAP);
+      sec_begin(c, SEC_PFAFFIAN);
+      if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s))) return rc;
+      sec_end(c, SEC_PFAFFIAN);
+      sec_begin(c, SEC_OVERLAP);
+    } else {
+      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s>>>(G, w->pf);
+    }
+  }
+  sec_end(c, SEC_OVERLAP);
+  sec_begin(c, SEC_SUMS);
+  overlap_finish_kernel<<<nblk(G, tb), tb, 0, s>>>(n, G, have_overlap ? 1 : 0, w->canon_i, w->canon_d, w->pf,
+                                                    w->detR22, d_weight, d_mult, w->obs, w->coefA, w->coefAE);
+  sum_scalars_kernel<<<1, 32, 0, s>>>(G, w->obs, d_mult, d_weight, w->pscal, accumulate);
+  sum_matrices_kernel<<<nblk(nn, tb), tb, 0, s>>>(n, G, w->A, w->T, w->coefA, w->coefAE, d_mult, w->pA, w->pH,
+                                                  w->pAH, accumulate);
+  TVAP_CUDA(cudaGetLastError());
+  sec_end(c, SEC_SUMS);
+  c->kernel_launches += 1 + 1 + 2 + 2 + 3 + 1 + 5 + (have_overlap ? (nocc > 0 ? 2 : 1) + (nb > 0 ? 3 : 1) : 0) + 3;
+  return TVAP_OK;
+}
+
+int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s) {
+  cudaPointerAttributes at{};
+  cudaError_t e = cudaPointerGetAttributes(&at, src);
+  if (e != cudaSuccess) cudaGetLastError();
+  const bool dev = (e == cudaSuccess && (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged));
+  TVAP_CUDA(cudaMemcpyAsync(dst, src, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  return TVAP_OK;
+}
+
+int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s) {
+  cudaPointerAttributes at{};
+  cudaError_t e = cudaPointerGetAttributes(&at, dst);
+  if (e != cudaSuccess) cudaGetLastError();
+  const bool dev = (e == cudaSuccess && (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged));
+  TVAP_CUDA(cudaMemcpyAsync(dst, src, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  return TVAP_OK;
+}
+
+int check_flags(tvap_ctx* c) {
+  int f = 0;
+  TVAP_CUDA(cudaMemcpyAsync(&f, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  TVAP_CUDA(cudaStreamSynchronize(c->stream));
+  TVAP_CUDA(cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
+  if (f & DEV_SINGULAR_RN) return TVAP_ERR_SINGULAR_RN;
+  if (f & DEV_SINGULAR_UPHI) return TVAP_ERR_SINGULAR_UPHI;
+  if (f & (DEV_EIGEN_NOCONV | DEV_CANON_BLOCK)) return TVAP_ERR_CANONICAL;
+  if (f & DEV_CHOLESKY) return TVAP_ERR_CHOLESKY;
+  if (f & DEV_TRTRI) return TVAP_ERR_TRTRI;
+  if (f & DEV_IMAG_GRAD) return TVAP_ERR_IMAG_GRADIENT;
+  return TVAP_OK;
+}
+
+// Full projection of state (w->U, w->V) already on the device.  Leaves the
+// sums in w->pscal/pA/pH/pAH and the gradient in w->H20v.
+int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  int canon[3] = {0, 0, 0};
+  int rc;
+  if ((rc = prepare_state(c, o.seed_occeps, o.seed_allemp, canon))) return rc;
+  const bool have_overlap = std::max(o.Mphip, o.Mphin) > 1;
+  if (canon[2] && have_overlap) {
+    set_last_error("canonical basis has a degenerate block larger than 2 or an odd paired block", __FILE__,
+                   __LINE__);
+    return TVAP_ERR_CANONICAL;
+  }
+  const bool fold = (o.mode == 0) && std::fabs(o.facpi - 2.0 * M_PI) < 1e-12 && is_integer(o.valence_Z) &&
+                    is_integer(o.valence_N);
+  AngleTable t = make_angles(o, fold);
+  const int G = int(t.php.size());
+  Workspace* w = c->ws;
+  std::vector<double2> eph(2 * G), wt(G);
+  for (int b = 0; b < G; ++b) {
+    const std::complex<double> I(0.0, 1.0);
+    const std::complex<double> ep = std::exp(I * t.php[b]), en = std::exp(I * t.phn[b]);
+    eph[2 * b] = make_double2(ep.real(), ep.imag());
+    eph[2 * b + 1] = make_double2(en.real(), en.imag());
+    wt[b] = make_double2(t.w[b].real(), t.w[b].imag());
+  }
+  TVAP_CUDA(cudaMemcpyAsync(w->ephase, eph.data(), sizeof(double2) * 2 * G, cudaMemcpyHostToDevice, s));
+  TVAP_CUDA(cudaMemcpyAsync(w->weight, wt.data(), sizeof(double2) * G, cudaMemcpyHostToDevice, s));
+  TVAP_CUDA(cudaMemcpyAsync(w->mult, t.mult.data(), sizeof(double) * G, cudaMemcpyHostToDevice, s));
+  if (o.mode == 0) {
+    if ((rc = project_angles(c, G, w->ephase, w->weight, w->mult, have_overlap, canon[0], canon[1], o.factor_delta,
+                             0)))
+      return rc;
+  } else {
+    // plain form: one angle per launch sequence
+    for (int b = 0; b < G; ++b)
+      if ((rc = project_angles(c, 1, w->ephase + 2 * b, w->weight + b, w->mult + b, have_overlap, canon[0],
+                               canon[1], o.factor_delta, b > 0 ? 1 : 0)))
+        return rc;
+  }
+  projected_h20_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->pA, w->pH, w->pAH, w->pscal, w->H20v, c->d_flags);
+  TVAP_CUDA(cudaGetLastError());
+  c->kernel_launches += 1;
+  if (out) {
+    double2 sc[6];
+    TVAP_CUDA(cudaMemcpyAsync(sc, w->pscal, sizeof(double2) * 6, cudaMemcpyDeviceToHost, s));
+    TVAP_CUDA(cudaStreamSynchronize(s));
+    double* dst[6] = {out->over, out->ener, out->prot, out->neut, out->prot2, out->neut2};
+    for (int q = 0; q < 6; ++q) {
+      dst[q][0] = sc[q].x;
+      dst[q][1] = sc[q].y;
+    }
+    out->nocc = canon[0];
+    out->nemp = canon[1];
+  }
+  return check_flags(c);
+}
+
+int ensure_workspace(tvap_ctx* c, int G) { return ws_ensure(c, G); }
+double* ws_U(tvap_ctx* c) { return c->ws->U; }
+double* ws_V(tvap_ctx* c) { return c->ws->V; }
+double* ws_H20v(tvap_ctx* c) { return c->ws->H20v; }
+int angle_count(const tvap_proj_opts& o) {
+  const bool fold = (o.mode == 0) && std::fabs(o.facpi - 2.0 * M_PI) < 1e-12 && is_integer(o.valence_Z) &&
+                    is_integer(o.valence_N);
+  return int(make_angles(o, fold).php.size());
+}
+void destroy_workspace(tvap_ctx* c) {
+  if (c->ws) {
+    ws_free(c->ws);
+    delete c->ws;
+    c->ws = nullptr;
+  }
+}
+
+}  // namespace tvap

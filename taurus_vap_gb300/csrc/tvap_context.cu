@@ -1,0 +1,300 @@
+// C ABI (include/tvap.h): context, Hamiltonian upload, calculate_fields and
+// project_wavefunction entry points.
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "tvap_internal.cuh"
+
+namespace tvap {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const char* msg, const char* file, int line) {
+  g_last_error = std::string(msg) + " (" + file + ":" + std::to_string(line) + ")";
+}
+
+int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
+int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
+int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out);
+int ensure_workspace(tvap_ctx* c, int G);
+void destroy_workspace(tvap_ctx* c);
+int angle_count(const tvap_proj_opts& o);
+int check_flags(tvap_ctx* c);
+double* ws_U(tvap_ctx* c);
+double* ws_V(tvap_ctx* c);
+double* ws_H20v(tvap_ctx* c);
+
+static cudaEvent_t take_event(tvap_ctx* c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void sec_begin(tvap_ctx* c, int sec) {
+  if (!c->timing) return;
+  cudaEvent_t a = take_event(c), b = take_event(c);
+  cudaEventRecord(a, c->stream);
+  c->ev_open.push_back({sec, {a, b}});
+}
+
+void sec_end(tvap_ctx* c, int sec) {
+  if (!c->timing) return;
+  for (auto it = c->ev_open.rbegin(); it != c->ev_open.rend(); ++it)
+    if (it->first == sec && it->second.second) {
+      cudaEventRecord(it->second.second, c->stream);
+      it->first = sec + 1000;  // closed
+      return;
+    }
+}
+
+static void collect_sections(tvap_ctx* c) {
+  if (c->ev_open.empty()) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto& e : c->ev_open) {
+    if (e.first >= 1000) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e.second.first, e.second.second);
+      c->section_ms[e.first - 1000] += ms;
+      c->section_calls[e.first - 1000] += 1;
+    }
+    c->ev_pool.push_back(e.second.first);
+    c->ev_pool.push_back(e.second.second);
+  }
+  c->ev_open.clear();
+}
+
+namespace {
+
+// column-major n x n (ncol matrices) <-> angle-innermost
+__global__ void to_inner_kernel(size_t nn, int ncol, const double2* __restrict__ src, double2* __restrict__ dst) {
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= nn * ncol) return;
+  const size_t e = idx / ncol;
+  const int col = int(idx % ncol);
+  dst[idx] = src[size_t(col) * nn + e];
+}
+__global__ void from_inner_kernel(size_t nn, int ncol, const double2* __restrict__ src, double2* __restrict__ dst) {
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= nn * ncol) return;
+  const size_t e = idx % nn;
+  const int col = int(idx / nn);
+  dst[idx] = src[e * ncol + col];
+}
+
+}  // namespace
+
+}  // namespace tvap
+
+using namespace tvap;
+
+extern "C" {
+
+const char* tvap_last_error(void) { return g_last_error.c_str(); }
+
+int tvap_kernel_launches(const tvap_ctx* ctx) { return ctx ? ctx->kernel_launches : 0; }
+
+int tvap_set_timing(tvap_ctx* c, int on) {
+  if (!c) return TVAP_ERR_ARG;
+  collect_sections(c);
+  c->timing = (on != 0);
+  for (int i = 0; i < 16; ++i) {
+    c->section_ms[i] = 0.0;
+    c->section_calls[i] = 0;
+  }
+  return TVAP_OK;
+}
+
+int tvap_get_timing(tvap_ctx* c, double* ms, long long* calls, int nsec) {
+  if (!c || !ms) return TVAP_ERR_ARG;
+  collect_sections(c);
+  for (int i = 0; i < nsec && i < 16; ++i) {
+    ms[i] = c->section_ms[i];
+    if (calls) calls[i] = c->section_calls[i];
+  }
+  return TVAP_OK;
+}
+
+int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* sp_tr, const int32_t* sp_l,
+              int device) {
+  if (!ctx || n <= 0 || n > 512 || (n % 2) != 0 || !sp_2mj || !sp_tr || !sp_l) {
+    g_last_error = "tvap_init: n must be even and in 2..512, tables non-null";
+    return TVAP_ERR_ARG;
+  }
+  auto* c = new tvap_ctx();
+  c->n = int(n);
+  if (device >= 0) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      delete c;
+      return TVAP_ERR_CUDA;
+    }
+  }
+  cudaGetDevice(&c->device);
+  c->h_sp_2mj.assign(sp_2mj, sp_2mj + n);
+  c->h_sp_tr.assign(sp_tr, sp_tr + n);
+  c->h_sp_l.assign(sp_l, sp_l + n);
+  for (int i = 0; i < n; ++i)
+    if (sp_tr[i] < 1 || sp_tr[i] > n) {
+      g_last_error = "tvap_init: HOsp_tr out of range";
+      delete c;
+      return TVAP_ERR_ARG;
+    }
+  auto fail = [&](cudaError_t e) {
+    set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    tvap_destroy(c);
+    return TVAP_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  c->own_stream = true;
+  if ((e = cudaMalloc(&c->d_sp_2mj, sizeof(int) * n)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->d_sp_tr, sizeof(int) * n)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->d_sp_l, sizeof(int) * n)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->d_flags, sizeof(int))) != cudaSuccess) return fail(e);
+  cudaMemcpy(c->d_sp_2mj, sp_2mj, sizeof(int) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_sp_tr, sp_tr, sizeof(int) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_sp_l, sp_l, sizeof(int) * n, cudaMemcpyHostToDevice);
+  cudaMemset(c->d_flags, 0, sizeof(int));
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+  *ctx = c;
+  return TVAP_OK;
+}
+
+void tvap_destroy(tvap_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  destroy_workspace(c);
+  free_field_csr(c->csr);
+  cudaFree(c->d_sp_2mj);
+  cudaFree(c->d_sp_tr);
+  cudaFree(c->d_sp_l);
+  cudaFree(c->d_abcd);
+  cudaFree(c->d_h2);
+  cudaFree(c->d_trperm);
+  cudaFree(c->d_H1);
+  cudaFree(c->d_flags);
+  for (auto& e : c->ev_open) {
+    cudaEventDestroy(e.second.first);
+    cudaEventDestroy(e.second.second);
+  }
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int tvap_set_stream(tvap_ctx* c, void* stream) {
+  if (!c) return TVAP_ERR_ARG;
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  c->stream = static_cast<cudaStream_t>(stream);
+  c->own_stream = false;
+  return TVAP_OK;
+}
+
+int tvap_set_hamiltonian(tvap_ctx* c, int64_t S, const int16_t* abcd, const float* h2, const int8_t* trperm,
+                         const double* H1, const double* H0) {
+  if (!c || S < 0 || (S > 0 && (!abcd || !h2 || !trperm)) || !H1 || !H0) return TVAP_ERR_ARG;
+  if (S > (int64_t(1) << 26)) {
+    g_last_error = "tvap_set_hamiltonian: element list too long (16 slots per element must fit int32)";
+    return TVAP_ERR_ARG;
+  }
+  const int n = c->n;
+  cudaFree(c->d_abcd);
+  cudaFree(c->d_h2);
+  cudaFree(c->d_trperm);
+  cudaFree(c->d_H1);
+  c->d_abcd = nullptr;
+  c->d_h2 = nullptr;
+  c->d_trperm = nullptr;
+  c->S = S;
+  TVAP_CUDA(cudaMalloc(&c->d_abcd, sizeof(int16_t) * 4 * std::max<int64_t>(S, 1)));
+  TVAP_CUDA(cudaMalloc(&c->d_h2, sizeof(float) * std::max<int64_t>(S, 1)));
+  TVAP_CUDA(cudaMalloc(&c->d_trperm, sizeof(int8_t) * std::max<int64_t>(S, 1)));
+  TVAP_CUDA(cudaMalloc(&c->d_H1, sizeof(double2) * size_t(n) * n));
+  int rc;
+  if (S > 0) {
+    if ((rc = upload_matrix(abcd, c->d_abcd, sizeof(int16_t) * 4 * S, c->stream))) return rc;
+    if ((rc = upload_matrix(h2, c->d_h2, sizeof(float) * S, c->stream))) return rc;
+    if ((rc = upload_matrix(trperm, c->d_trperm, sizeof(int8_t) * S, c->stream))) return rc;
+  }
+  if ((rc = upload_matrix(H1, c->d_H1, sizeof(double2) * size_t(n) * n, c->stream))) return rc;
+  c->H0 = make_double2(H0[0], H0[1]);
+  TVAP_CUDA(cudaStreamSynchronize(c->stream));
+  if ((rc = build_field_csr(c))) return rc;
+  c->have_ham = true;
+  return TVAP_OK;
+}
+
+int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, const double* kLR, const double* kRL,
+                                  double* gamma, double* hsp, double* dLR, double* dRL) {
+  if (!c || ncol <= 0 || ncol > 256 || !rho || !kLR || !kRL || !gamma || !hsp || !dLR || !dRL)
+    return TVAP_ERR_ARG;
+  if (!c->have_ham) return TVAP_ERR_NOT_READY;
+  c->kernel_launches = 0;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n, tot = nn * ncol;
+  cudaStream_t s = c->stream;
+  double2* buf = nullptr;  // 7 * tot: staging (column-major) + 3 inner inputs + 4 inner outputs ... reused
+  TVAP_CUDA(cudaMalloc(&buf, sizeof(double2) * tot * 8));
+  double2* stage = buf;
+  double2* in[3] = {buf + tot, buf + 2 * tot, buf + 3 * tot};
+  double2* out[4] = {buf + 4 * tot, buf + 5 * tot, buf + 6 * tot, buf + 7 * tot};
+  const double* srcs[3] = {rho, kLR, kRL};
+  double* dsts[4] = {gamma, hsp, dLR, dRL};
+  int rc = TVAP_OK;
+  const int tb = 256;
+  const unsigned nb = unsigned((tot + tb - 1) / tb);
+  for (int q = 0; q < 3 && rc == TVAP_OK; ++q) {
+    rc = upload_matrix(srcs[q], stage, sizeof(double2) * tot, s);
+    if (rc == TVAP_OK) to_inner_kernel<<<nb, tb, 0, s>>>(nn, ncol, stage, in[q]);
+  }
+  if (rc == TVAP_OK) rc = fields_batched(c, ncol, ncol, in[0], in[1], in[2], out[0], out[1], out[2], out[3], s);
+  for (int q = 0; q < 4 && rc == TVAP_OK; ++q) {
+    from_inner_kernel<<<nb, tb, 0, s>>>(nn, ncol, out[q], stage);
+    rc = download_matrix(stage, dsts[q], sizeof(double2) * tot, s);
+    if (rc == TVAP_OK) {
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+        rc = TVAP_ERR_CUDA;
+      }
+    }
+  }
+  c->kernel_launches += 7;
+  cudaFree(buf);
+  return rc;
+}
+
+int tvap_calculate_fields(tvap_ctx* c, const double* rho, const double* kLR, const double* kRL, double* gamma,
+                          double* hsp, double* dLR, double* dRL) {
+  return tvap_calculate_fields_batched(c, 1, rho, kLR, kRL, gamma, hsp, dLR, dRL);
+}
+
+int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_proj_opts* opts, tvap_pnp* out,
+                 double* H20v) {
+  if (!c || !U0 || !V0 || !opts || opts->Mphip < 1 || opts->Mphin < 1) return TVAP_ERR_ARG;
+  if (!c->have_ham) return TVAP_ERR_NOT_READY;
+  c->kernel_launches = 0;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  int rc;
+  if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
+  if ((rc = upload_matrix(U0, ws_U(c), sizeof(double) * nn, c->stream))) return rc;
+  if ((rc = upload_matrix(V0, ws_V(c), sizeof(double) * nn, c->stream))) return rc;
+  if ((rc = project_device(c, *opts, out))) return rc;
+  if (H20v) {
+    if ((rc = download_matrix(ws_H20v(c), H20v, sizeof(double) * nn, c->stream))) return rc;
+    TVAP_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return TVAP_OK;
+}
+
+}  // extern "C"

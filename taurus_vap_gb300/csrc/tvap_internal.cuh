@@ -1,0 +1,183 @@
+// Internal declarations of the sm_103a device path (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "tvap.h"
+
+namespace tvap {
+
+// ---------------------------------------------------------------------------
+// complex helpers (double2 = re, im)
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ double2 cmk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__host__ __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
+// c += a * b
+__device__ __forceinline__ void cfma(double2& c, double2 a, double2 b) {
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+}
+// 1/z with scaling (Smith)
+__host__ __device__ __forceinline__ double2 crcp(double2 z) {
+  if (fabs(z.x) >= fabs(z.y)) {
+    const double r = z.y / z.x, d = z.x + z.y * r;
+    return make_double2(1.0 / d, -r / d);
+  } else {
+    const double r = z.x / z.y, d = z.y + z.x * r;
+    return make_double2(r / d, -1.0 / d);
+  }
+}
+__host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) { return cmul(a, crcp(b)); }
+__host__ __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
+
+// ---------------------------------------------------------------------------
+// error handling
+// ---------------------------------------------------------------------------
+#define TVAP_CUDA(call)                                                                        \
+  do {                                                                                         \
+    cudaError_t e__ = (call);                                                                  \
+    if (e__ != cudaSuccess) {                                                                  \
+      tvap::set_last_error(cudaGetErrorString(e__), __FILE__, __LINE__);                       \
+      return TVAP_ERR_CUDA;                                                                    \
+    }                                                                                          \
+  } while (0)
+
+void set_last_error(const char* msg, const char* file, int line);
+
+// device status word bits, written by kernels and read back by the host
+enum DevFlag : int {
+  DEV_SINGULAR_UPHI = 1,
+  DEV_SINGULAR_RN = 2,
+  DEV_PFAFF_ZERO = 4,
+  DEV_CANON_BLOCK = 8,
+  DEV_EIGEN_NOCONV = 16,
+  DEV_CHOLESKY = 32,
+  DEV_TRTRI = 64,
+  DEV_IMAG_GRAD = 128,
+};
+
+// ---------------------------------------------------------------------------
+// strided batched matrix view: element (i,j) of batch b at
+//   p[i*rs + j*cs + b*bs]   (units: elements)
+// ---------------------------------------------------------------------------
+struct View {
+  const void* p;
+  long long rs, cs, bs;
+};
+inline View view_cm(const void* p, int ld, long long bs) { return View{p, 1, ld, bs}; }
+inline View view_t(View v) { return View{v.p, v.cs, v.rs, v.bs}; }
+
+// Batched GEMM  C_b = alpha_b * op(A_b) op(B_b) + beta * C_b  with complex or
+// real operands (A real: ar = true).  alpha_b = alpha * (alpha_vec ? alpha_vec[b] : 1).
+// C is complex unless c_real.
+struct GemmArgs {
+  int M, N, K, batch;
+  View A, B;
+  void* C;
+  long long crs, ccs, cbs;
+  double2 alpha, beta;
+  const double2* alpha_vec;
+  bool a_real, b_real, c_real;
+  bool conj_a, conj_b;
+};
+int gemm(const GemmArgs& g, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Hamiltonian in gather form (built once from the reference's element list)
+// ---------------------------------------------------------------------------
+struct FieldCSR {
+  // Gamma: one row per output entry (x + y n), entries: src index (z + w n), coef
+  int* g_rowptr = nullptr;
+  int* g_src = nullptr;
+  double* g_coef = nullptr;
+  long long g_nnz = 0;
+  // Delta (strict lower triangle rows b > a, output index b + a n)
+  int* d_rows = nullptr;  // list of output indices with at least one entry
+  int* d_rowptr = nullptr;
+  int* d_src = nullptr;
+  double* d_coef = nullptr;
+  int d_nrows = 0;
+  long long d_nnz = 0;
+};
+
+struct Workspace;
+
+}  // namespace tvap
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct tvap_ctx {
+  int n = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int* d_sp_2mj = nullptr;
+  int* d_sp_tr = nullptr;
+  int* d_sp_l = nullptr;
+  std::vector<int> h_sp_2mj, h_sp_tr, h_sp_l;
+  // raw element list as uploaded (the reference's arrays)
+  long long S = 0;
+  int16_t* d_abcd = nullptr;
+  float* d_h2 = nullptr;
+  int8_t* d_trperm = nullptr;
+  double2* d_H1 = nullptr;
+  double2 H0 = {0.0, 0.0};
+  bool have_ham = false;
+  tvap::FieldCSR csr;
+  tvap::Workspace* ws = nullptr;
+  int* d_flags = nullptr;  // device status word
+  int kernel_launches = 0;  // launches issued by the last top-level call
+  // optional section timing with CUDA events on the context's stream
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_open;
+  double section_ms[16] = {0};
+  long long section_calls[16] = {0};
+};
+
+namespace tvap {
+enum Section : int {
+  SEC_CANONICAL = 0, SEC_BLOCKS, SEC_SOLVE, SEC_UV, SEC_DENSITIES, SEC_FIELDS_GAMMA, SEC_FIELDS_DELTA, SEC_TRACES,
+  SEC_H20, SEC_OVERLAP, SEC_PFAFFIAN, SEC_SUMS, SEC_GRADIENT, SEC_EVOLVE, SEC_COUNT
+};
+// brackets a section with events when timing is on (no-ops otherwise)
+void sec_begin(tvap_ctx* c, int sec);
+void sec_end(tvap_ctx* c, int sec);
+}  // namespace tvap
+
+namespace tvap {
+
+int build_field_csr(tvap_ctx* c);
+void free_field_csr(FieldCSR& f);
+
+// Fields for `ncol` columns (angles) in angle-innermost layout:
+// X[(i + j n) * ldc + col].  hsp/dLR/dRL outputs in the same layout.
+int fields_batched(tvap_ctx* c, int ncol, int ldc, const double2* rho, const double2* kLR, const double2* kRL,
+                   double2* gamma, double2* hsp, double2* dLR, double2* dRL, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// dense per-batch factorizations
+// ---------------------------------------------------------------------------
+// Pfaffian of `batch` skew matrices (upper triangle of column-major n x n
+// blocks, stride n*n), Parlett-Reid with the reference's pivoting.
+int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s);
+// symmetric eigen-decomposition by cyclic Jacobi (one matrix), ascending order
+int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s);
+// Cholesky L L^T = A (lower), then L^{-1} in place
+int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
+
+}  // namespace tvap

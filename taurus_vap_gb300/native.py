@@ -1,0 +1,232 @@
+"""ctypes binding of ``libtvap_gpu.so`` (include/tvap.h) with the argument
+meaning of the reference's Fortran routines.
+
+The library is the only compute path: there is no CPU fallback.  Importing
+this module on a machine without the built library, or calling it without a
+CUDA device, raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import _build
+
+TVAP_OK = 0
+ERRORS = {
+    1: "bad argument", 2: "CUDA error", 3: "hamiltonian not set",
+    10: "U_phi singular (calculate_thouless)",
+    11: "canonical overlap matrix singular (calculate_overlap: info from zgetrf)",
+    13: "the gradient has non-zero imaginary part (calculate_projected_H20)",
+    14: "Cholesky factorization has failed (cholesky_factorization)",
+    15: "error in the inverse of L (evolve_wavefunction)",
+    16: "canonical basis: eigen solver did not converge or degenerate block > 2",
+    18: "particle numbers wrong three times in the last five iterations",
+}
+
+
+class TvapError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        msg = f"{where}: status {code} ({ERRORS.get(code, 'unknown')})"
+        if detail:
+            msg += f": {detail}"
+        super().__init__(msg)
+
+
+class TvapPnp(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double * 2) for k in ("over", "ener", "prot", "neut", "prot2", "neut2")] + [
+        ("nocc", ctypes.c_int), ("nemp", ctypes.c_int)]
+
+    def c(self, k: str) -> complex:
+        v = getattr(self, k)
+        return complex(v[0], v[1])
+
+
+class TvapProjOpts(ctypes.Structure):
+    _fields_ = [("Mphip", ctypes.c_int), ("Mphin", ctypes.c_int), ("facpi", ctypes.c_double),
+                ("valence_Z", ctypes.c_double), ("valence_N", ctypes.c_double),
+                ("factor_delta", ctypes.c_double), ("seed_occeps", ctypes.c_double),
+                ("seed_allemp", ctypes.c_int), ("mode", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.GPU_LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+        L = ctypes.CDLL(path)
+        vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        L.tvap_init.argtypes = [ctypes.POINTER(vp), ctypes.c_int64, vp, vp, vp, ci]
+        L.tvap_init.restype = ci
+        L.tvap_destroy.argtypes = [vp]
+        L.tvap_last_error.restype = ctypes.c_char_p
+        L.tvap_kernel_launches.argtypes = [vp]
+        L.tvap_kernel_launches.restype = ci
+        L.tvap_set_stream.argtypes = [vp, vp]
+        L.tvap_set_timing.argtypes = [vp, ci]
+        L.tvap_set_timing.restype = ci
+        L.tvap_get_timing.argtypes = [vp, vp, vp, ci]
+        L.tvap_get_timing.restype = ci
+        L.tvap_set_hamiltonian.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp, vp]
+        L.tvap_set_hamiltonian.restype = ci
+        L.tvap_calculate_fields.argtypes = [vp] * 8
+        L.tvap_calculate_fields.restype = ci
+        L.tvap_calculate_fields_batched.argtypes = [vp, ci] + [vp] * 7
+        L.tvap_calculate_fields_batched.restype = ci
+        L.tvap_project.argtypes = [vp, vp, vp, ctypes.POINTER(TvapProjOpts), ctypes.POINTER(TvapPnp), vp]
+        L.tvap_project.restype = ci
+        L.tvap_calculate_gradient.argtypes = [vp, vp, ci, vp, vp, vp, cd, cd, vp, vp]
+        L.tvap_calculate_gradient.restype = ci
+        L.tvap_evolve.argtypes = [vp] * 6
+        L.tvap_evolve.restype = ci
+        L.tvap_energy_adjoint.argtypes = [vp, vp, vp, vp, ctypes.POINTER(TvapProjOpts), vp, vp]
+        L.tvap_energy_adjoint.restype = ci
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):  # torch tensor (host or device)
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(rc: int, where: str):
+    if rc != TVAP_OK:
+        raise TvapError(rc, where, lib().tvap_last_error().decode(errors="replace"))
+
+
+def _f(a, dtype):
+    if hasattr(a, "data_ptr"):
+        return a
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+class Context:
+    """One device context: basis tables and the uploaded Hamiltonian."""
+
+    def __init__(self, basis, ham=None, device: int = -1):
+        L = lib()
+        self.n = basis.n
+        self._tables = [np.ascontiguousarray(x, dtype=np.int32) for x in (basis.sp_2mj, basis.sp_tr, basis.sp_l)]
+        h = ctypes.c_void_p()
+        _check(L.tvap_init(ctypes.byref(h), self.n, *[_p(t) for t in self._tables], device), "tvap_init")
+        self.h = h
+        if ham is not None:
+            self.set_hamiltonian(ham)
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.tvap_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def kernel_launches(self) -> int:
+        return lib().tvap_kernel_launches(self.h)
+
+    SECTIONS = ("canonical", "blocks", "solve", "uv", "densities", "fields_gamma", "fields_delta", "traces",
+                "h20", "overlap", "pfaffian", "sums", "gradient", "evolve")
+
+    def set_timing(self, on: bool):
+        _check(lib().tvap_set_timing(self.h, 1 if on else 0), "tvap_set_timing")
+
+    def get_timing(self):
+        ms = np.zeros(16)
+        calls = np.zeros(16, dtype=np.int64)
+        _check(lib().tvap_get_timing(self.h, _p(ms), _p(calls), 16), "tvap_get_timing")
+        return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(self.SECTIONS)}
+
+    def set_stream(self, stream_handle: int):
+        lib().tvap_set_stream(self.h, ctypes.c_void_p(stream_handle))
+
+    def set_hamiltonian(self, ham):
+        abcd = np.ascontiguousarray(ham.abcd, dtype=np.int16)
+        h2 = np.ascontiguousarray(ham.h2, dtype=np.float32)
+        tr = np.ascontiguousarray(ham.trperm, dtype=np.int8)
+        H1 = np.asfortranarray(ham.H1, dtype=np.complex128)
+        H0 = np.array([ham.H0.real, ham.H0.imag])
+        _check(lib().tvap_set_hamiltonian(self.h, ham.S, _p(abcd), _p(h2), _p(tr), _p(H1), _p(H0)),
+               "tvap_set_hamiltonian")
+
+    # -- calculate_fields (module_fields.f90:99-189) --------------------------
+    def calculate_fields(self, rhoLR, kappaLR, kappaRL):
+        n = self.n
+        rho, kl, kr = (_f(x, np.complex128) for x in (rhoLR, kappaLR, kappaRL))
+        outs = [np.zeros((n, n), dtype=np.complex128, order="F") for _ in range(4)]
+        _check(lib().tvap_calculate_fields(self.h, _p(rho), _p(kl), _p(kr), *[_p(o) for o in outs]),
+               "tvap_calculate_fields")
+        return tuple(outs)  # gammaLR, hspLR, deltaLR, deltaRL
+
+    def calculate_fields_batched(self, rho, kLR, kRL):
+        """rho, kLR, kRL: arrays (ncol, n, n) of Fortran-ordered matrices."""
+        ncol = rho.shape[0]
+        n = self.n
+        conv = [np.ascontiguousarray(np.transpose(np.asarray(x, dtype=np.complex128), (0, 2, 1)))
+                for x in (rho, kLR, kRL)]
+        outs = [np.zeros((ncol, n, n), dtype=np.complex128) for _ in range(4)]
+        _check(lib().tvap_calculate_fields_batched(self.h, ncol, *[_p(x) for x in conv], *[_p(o) for o in outs]),
+               "tvap_calculate_fields_batched")
+        return tuple(np.transpose(o, (0, 2, 1)) for o in outs)
+
+    # -- project_wavefunction(0, ...) + calculate_projected_H20 ----------------
+    def project(self, U0, V0, Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta=1.0, seed_occeps=0.0,
+                seed_allemp=0, mode=0):
+        n = self.n
+        U, V = _f(U0, np.float64), _f(V0, np.float64)
+        o = TvapProjOpts(Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta, seed_occeps, seed_allemp, mode)
+        out = TvapPnp()
+        H20v = np.zeros(n * n)
+        _check(lib().tvap_project(self.h, _p(U), _p(V), ctypes.byref(o), ctypes.byref(out), _p(H20v)),
+               "tvap_project")
+        return out, H20v
+
+    # -- calculate_gradient (module_gradient.f90:79-143), gradient_type 0 -----
+    def calculate_gradient(self, H20v, lambdas, C20, Zim1, eta, mu):
+        n = self.n
+        cdim = 0 if lambdas is None else len(lambdas)
+        H = np.ascontiguousarray(H20v, dtype=np.float64)
+        Zm = np.ascontiguousarray(Zim1, dtype=np.float64).reshape(-1)
+        lam = None if cdim == 0 else np.ascontiguousarray(lambdas, dtype=np.float64)
+        C = None if cdim == 0 else np.ascontiguousarray(C20, dtype=np.float64)
+        Zi = np.zeros(n * n)
+        norm = ctypes.c_double()
+        _check(lib().tvap_calculate_gradient(self.h, _p(H), cdim, _p(lam), _p(C), _p(Zm), eta, mu, _p(Zi),
+                                             ctypes.byref(norm)), "tvap_calculate_gradient")
+        return Zi, norm.value
+
+    # -- cholesky_factorization + evolve_wavefunction --------------------------
+    def evolve(self, U0, V0, Z):
+        n = self.n
+        U, V, Zm = _f(U0, np.float64), _f(V0, np.float64), _f(np.reshape(Z, (n, n), order="F"), np.float64)
+        U1 = np.zeros((n, n), order="F")
+        V1 = np.zeros((n, n), order="F")
+        _check(lib().tvap_evolve(self.h, _p(U), _p(V), _p(Zm), _p(U1), _p(V1)), "tvap_evolve")
+        return U1, V1
+
+    # -- adjoint of E(Z) -------------------------------------------------------
+    def energy_adjoint(self, U0, V0, Z, Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta=1.0, mode=0):
+        n = self.n
+        U, V, Zm = _f(U0, np.float64), _f(V0, np.float64), _f(np.reshape(Z, (n, n), order="F"), np.float64)
+        o = TvapProjOpts(Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta, 0.0, 0, mode)
+        E = ctypes.c_double()
+        G = np.zeros((n, n), order="F")
+        _check(lib().tvap_energy_adjoint(self.h, _p(U), _p(V), _p(Zm), ctypes.byref(o), ctypes.byref(E), _p(G)),
+               "tvap_energy_adjoint")
+        return E.value, G
+
+
+TWO_PI = 2.0 * math.pi

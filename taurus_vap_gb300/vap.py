@@ -1,0 +1,174 @@
+"""Host mirror of TAURUS_vap's gradient loop (taurus_vap.f90:77-123) over the
+device entry points.
+
+Device (libtvap_gpu.so):  project_wavefunction + calculate_projected_H20,
+calculate_gradient, cholesky_factorization + evolve_wavefunction.
+Host (NumPy):  the constraint algebra -- set_operator_qpbasis, the Lagrange
+multipliers and the adjust_constraints Newton loop
+(module_constraints.f90:270-484, module_operators.f90:49-97) -- which works on
+a handful of n x n real matrices per iteration.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .native import Context, TvapError
+
+
+def set_operator_qpbasis(part: str, U, V, A):
+    """module_operators.f90:49-97 (U, V, A real, column-major n x n)."""
+    if part == "f11":
+        fac, A2, A3 = 1.0, U.T @ A @ U, V.T @ A.T @ V
+    elif part == "g11":
+        fac, A2, A3 = 1.0, U.T @ A @ V, V.T @ A @ U
+    elif part == "f20":
+        fac, A2, A3 = -1.0, U.T @ A @ V, V.T @ A.T @ U
+    else:  # g20
+        fac, A2, A3 = -1.0, U.T @ A @ U, V.T @ A @ V
+    A1 = A2 - A3
+    return 0.5 * (A1 + fac * A1.T)
+
+
+def expectval_obo(rho, B):
+    A1 = B @ rho
+    h = rho.shape[0] // 2
+    return np.trace(A1[:h, :h]) + np.trace(A1[h:, h:])
+
+
+def expectval_pair(kappa, B):
+    return np.trace(B @ kappa.T)
+
+
+@dataclass
+class Constraints:
+    """Constraint operators in the HO basis (constraint_HO, vectorised as in
+    the reference: entry k of operator j is element (i, j) with k = i + j n)."""
+
+    ops: list = field(default_factory=list)  # n*n vectors
+    values: list = field(default_factory=list)
+    npair: int = 0
+    eps: float = 1e-6
+
+    @property
+    def dim(self) -> int:
+        return len(self.values)
+
+
+class VAP:
+    """State and loop of one PNVAP minimisation."""
+
+    def __init__(self, ctx: Context, U0, V0, Mphip, Mphin, valence_Z, valence_N, eta, mu, gradient_eps=1e-4,
+                 constraints: Constraints | None = None, facpi=2 * np.pi, factor_delta=1.0, mode=0):
+        self.ctx = ctx
+        self.n = ctx.n
+        self.U0 = np.asfortranarray(U0, dtype=np.float64)
+        self.V0 = np.asfortranarray(V0, dtype=np.float64)
+        self.Mp, self.Mn, self.facpi = Mphip, Mphin, facpi
+        self.Z, self.N = valence_Z, valence_N
+        self.eta, self.mu, self.geps = eta, mu, gradient_eps
+        self.cons = constraints or Constraints()
+        self.factor_delta = factor_delta
+        self.mode = mode
+        n = self.n
+        self.Zi = np.zeros(n * n)
+        self.Zim1 = np.zeros(n * n)
+        self.lam0 = np.zeros(self.cons.dim)
+        self.lam1 = np.zeros(self.cons.dim)
+        self.C20 = np.zeros((self.cons.dim, n * n))
+        self._ops = [np.reshape(o, (n, n), order="F") for o in self.cons.ops]
+        self.control_NZ = [0] * 5
+        self.history = []
+
+    def _part(self, i):
+        return "f20" if i < self.cons.dim - self.cons.npair else "g20"
+
+    def update_constraints_qpbasis(self, U, V):
+        for i, A in enumerate(self._ops):
+            self.C20[i] = set_operator_qpbasis(self._part(i), U, V, A).reshape(-1, order="F")
+
+    def lagrange_multipliers(self, H20v):
+        c = self.cons.dim
+        if c == 0:
+            return
+        n = self.n
+        Cm = [C.reshape((n, n), order="F") for C in self.C20]
+        H = H20v.reshape((n, n), order="F")
+        A = np.array([[np.trace(Cm[i] @ Cm[j].T) for j in range(c)] for i in range(c)])
+        B = np.array([np.trace(H @ Cm[i].T) for i in range(c)])
+        try:
+            self.lam1 = np.linalg.solve(A, B)
+        except np.linalg.LinAlgError:
+            self.lam1 = self.lam0.copy()
+        self.lam0 = self.lam1.copy()
+
+    def adjust_constraints(self):
+        """module_constraints.f90:270-373; the Thouless evolution runs on the device."""
+        n, c = self.n, self.cons.dim
+        U1, V1 = self.U0, self.V0
+        for _ in range(100):
+            U1, V1 = self.ctx.evolve(self.U0, self.V0, self.Zi)
+            rho = V1 @ V1.T
+            kap = V1 @ U1.T
+            expec = np.array([expectval_obo(rho, A) if i < c - self.cons.npair else expectval_pair(kap, A)
+                              for i, A in enumerate(self._ops)])
+            B = np.asarray(self.cons.values, dtype=np.float64) - expec if c else np.zeros(0)
+            ia = int(np.sum(np.abs(B) > self.cons.eps))
+            self.update_constraints_qpbasis(U1, V1)
+            if ia == 0:
+                break
+            Cm = [C.reshape((n, n), order="F") for C in self.C20]
+            A = np.array([[np.trace(Cm[i].T @ Cm[j]) for j in range(c)] for i in range(c)])
+            B = np.linalg.solve(A, B)
+            self.Zi = self.Zi + B @ self.C20
+        self.U0, self.V0 = np.asfortranarray(U1), np.asfortranarray(V1)
+
+    def iterate(self):
+        """One gradient iteration.  Returns (status, info) with status 0
+        continue, 1 converged; info = gradient norm, E, <Z>, Var Z, <N>, Var N."""
+        self.update_constraints_qpbasis(self.U0, self.V0)
+        pnp, H20v = self.ctx.project(self.U0, self.V0, self.Mp, self.Mn, self.facpi, self.Z, self.N,
+                                     self.factor_delta, mode=self.mode)
+        self.lagrange_multipliers(H20v)
+        self.Zi, gnorm = self.ctx.calculate_gradient(H20v, self.lam1 if self.cons.dim else None,
+                                                     self.C20 if self.cons.dim else None, self.Zim1, self.eta,
+                                                     self.mu)
+        over = pnp.c("over")
+        ener = (pnp.c("ener") / over).real
+        prot = (pnp.c("prot") / over).real
+        neut = (pnp.c("neut") / over).real
+        prot2 = abs((pnp.c("prot2") / over).real - prot**2)
+        neut2 = abs((pnp.c("neut2") / over).real - neut**2)
+        info = (gnorm, ener, prot, prot2, neut, neut2)
+        self.history.append(info)
+        self.control_NZ = [1 if (abs(prot - self.Z) > 0.5 or abs(neut - self.N) > 0.5) else 0] + self.control_NZ[:4]
+        if sum(self.control_NZ) >= 3:
+            raise TvapError(18, "print_iteration")
+        if gnorm <= self.geps:
+            return 1, info
+        self.adjust_constraints()
+        self.Zim1 = self.Zi.copy()
+        return 0, info
+
+    def run(self, iter_max=3000, initial_adjust=True):
+        if initial_adjust:
+            self.adjust_constraints()
+        info = None
+        for it in range(1, iter_max + 1):
+            st, info = self.iterate()
+            if st == 1:
+                return it, info
+        return iter_max, info
+
+
+def particle_number_ops(n: int):
+    """partnumb_Z, partnumb_N (module_particlenumber.f90:30-57), vectorised."""
+    Qz = np.zeros(n * n)
+    Qn = np.zeros(n * n)
+    for i in range(n // 2):
+        Qz[i * n + i] = 1.0
+        j = i + n // 2
+        Qn[j * n + j] = 1.0
+    return Qz, Qn
