@@ -348,8 +348,9 @@ namespace {
 
 constexpr int kJacThreads = 1024;
 
-__global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, double* W, double* evals,
-                                                             double* work, int* flags) {
+template <typename T>
+__global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, double* evals, double* work,
+                                                             int* flags, double tolfac) {
   extern __shared__ double jsh[];
   const int m = (n + 1) & ~1;  // even count incl. a dummy index
   double* cs = jsh;                                    // m/2 cosines
@@ -360,11 +361,11 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, d
   __shared__ double red[kJacThreads];
   __shared__ int done;
   const int tid = threadIdx.x, nt = blockDim.x;
-  auto Ael = [A, n](int i, int j) -> double& { return A[i + size_t(j) * n]; };
-  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) W[idx] = ((idx % n) == (idx / n)) ? 1.0 : 0.0;
+  auto Ael = [A, n](int i, int j) -> T& { return A[i + size_t(j) * n]; };
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) W[idx] = ((idx % n) == (idx / n)) ? T(1) : T(0);
   for (int i = tid; i < m; i += nt) pairs[i] = i;
   double anorm = 0.0;
-  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) anorm += A[idx] * A[idx];
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) anorm += double(A[idx]) * double(A[idx]);
   red[tid] = anorm;
   __syncthreads();
   for (int s = nt / 2; s > 0; s >>= 1) {
@@ -373,14 +374,14 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, d
   }
   const double fro2 = red[0];
   __syncthreads();
-  const double tol2 = fro2 * 1.0e-30;  // converged when off-diagonal <= 1e-15 ||A||_F
+  const double tol2 = fro2 * tolfac;  // converged when off-diagonal^2 <= tolfac ||A||_F^2
   int sweep = 0;
   for (sweep = 0; sweep < 60; ++sweep) {
     // off-diagonal norm
     double off = 0.0;
     for (size_t idx = tid; idx < size_t(n) * n; idx += nt) {
       const int i = int(idx % n), j = int(idx / n);
-      if (i != j) off += A[idx] * A[idx];
+      if (i != j) off += double(A[idx]) * double(A[idx]);
     }
     red[tid] = off;
     __syncthreads();
@@ -400,14 +401,14 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, d
           p = q;
           q = t;
         }
-        double c = 1.0, s = 0.0;
+        T c = T(1), s = T(0);
         if (q < n) {
-          const double apq = Ael(p, q);
-          if (apq != 0.0) {
-            const double app = Ael(p, p), aqq = Ael(q, q);
-            const double theta = (aqq - app) / (2.0 * apq);
-            const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            c = 1.0 / sqrt(t * t + 1.0);
+          const T apq = Ael(p, q);
+          if (apq != T(0)) {
+            const T app = Ael(p, p), aqq = Ael(q, q);
+            const T theta = (aqq - app) / (T(2) * apq);
+            const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+            c = T(1) / sqrt(t * t + T(1));
             s = t * c;
           }
         }
@@ -422,11 +423,11 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, d
         const int r = int(idx % n), k = int(idx / n);
         const int p = pp[k], q = qq[k];
         if (q >= n || sn[k] == 0.0) continue;
-        const double c = cs[k], s = sn[k];
-        const double ap = Ael(r, p), aq = Ael(r, q);
+        const T c = T(cs[k]), s = T(sn[k]);
+        const T ap = Ael(r, p), aq = Ael(r, q);
         Ael(r, p) = c * ap - s * aq;
         Ael(r, q) = s * ap + c * aq;
-        const double wp = W[r + size_t(p) * n], wq = W[r + size_t(q) * n];
+        const T wp = W[r + size_t(p) * n], wq = W[r + size_t(q) * n];
         W[r + size_t(p) * n] = c * wp - s * wq;
         W[r + size_t(q) * n] = s * wp + c * wq;
       }
@@ -436,8 +437,8 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, d
         const int col = int(idx % n), k = int(idx / n);
         const int p = pp[k], q = qq[k];
         if (q >= n || sn[k] == 0.0) continue;
-        const double c = cs[k], s = sn[k];
-        const double ap = Ael(p, col), aq = Ael(q, col);
+        const T c = T(cs[k]), s = T(sn[k]);
+        const T ap = Ael(p, col), aq = Ael(q, col);
         Ael(p, col) = c * ap - s * aq;
         Ael(q, col) = s * ap + c * aq;
       }
@@ -453,7 +454,7 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, d
   }
   if (sweep >= 60 && tid == 0) atomicOr(flags, DEV_EIGEN_NOCONV);
   // sort ascending (selection by rank; ties broken by index)
-  for (int i = tid; i < n; i += nt) work[i] = Ael(i, i);
+  for (int i = tid; i < n; i += nt) work[i] = double(Ael(i, i));
   __syncthreads();
   for (int i = tid; i < n; i += nt) {
     const double v = work[i];
@@ -481,7 +482,15 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, double* A, d
 int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s) {
   const int m = (n + 1) & ~1;
   const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
-  jacobi_kernel<<<1, kJacThreads, shm, s>>>(n, A, W, evals, work, flags);
+  jacobi_kernel<double><<<1, kJacThreads, shm, s>>>(n, A, W, evals, work, flags, 1.0e-30);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
+int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s) {
+  const int m = (n + 1) & ~1;
+  const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
+  jacobi_kernel<float><<<1, kJacThreads, shm, s>>>(n, A, W, evals, work, flags, 1.0e-13);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }

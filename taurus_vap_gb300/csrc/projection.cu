@@ -68,6 +68,11 @@ struct Workspace {
   // sums
   double2 *pA = nullptr, *pH = nullptr, *pAH = nullptr, *pscal = nullptr;
   double* H20v = nullptr;
+  // eigenvector refinement (warm start from the previous canonical basis)
+  double *Xr = nullptr, *Xn = nullptr, *Rr = nullptr, *Br = nullptr, *Sr = nullptr, *Mr = nullptr,
+         *lam = nullptr, *rscal = nullptr;
+  int* rflag = nullptr;
+  bool have_basis = false;
   size_t bytes = 0;
 };
 
@@ -87,7 +92,8 @@ void ws_free(Workspace* w) {
                   w->Ut,  w->Vt,    w->X,      w->Y,     w->T,      w->Rn,    w->K,      w->SZ,    w->rhoL,
                   w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
                   w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
-                  w->H20v};
+                  w->H20v,  w->Xr,    w->Xn,     w->Rr,    w->Br,     w->Sr,    w->Mr,     w->lam,   w->rscal,
+                  w->rflag};
   for (void* p : ptrs) cudaFree(p);
   *w = Workspace();
 }
@@ -115,6 +121,7 @@ int ws_ensure(tvap_ctx* c, int G) {
   A_(Rn, nG) A_(K, nG) A_(SZ, nG) A_(rhoL, nG) A_(kLR, nG) A_(kRL, nG) A_(gam, nG) A_(hsp, nG) A_(dLR, nG)
   A_(dRL, nG) A_(ephase, 2 * G) A_(weight, G) A_(mult, G) A_(obs, 8 * G) A_(pf, 2 * G) A_(detR22, 2 * G)
   A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
+  A_(Xr, nn) A_(Xn, nn) A_(Rr, nn) A_(Br, nn) A_(Sr, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
 #undef A_
   return TVAP_OK;
 }
@@ -611,6 +618,187 @@ __global__ void schur_kernel(int n2, int nb, int G, const double2* __restrict__ 
   S[size_t(b) * nb2 + e] = s;
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric eigenvector refinement (Ogita & Aishima, Japan J. Indust. Appl.
+// Math. 35 (2018) 1007): from approximate eigenvectors X of A,
+//   R = I - X^T X,  S = X^T A X,  l_i = S_ii / (1 - R_ii),
+//   E_ij = (S_ij + l_j R_ij) / (l_j - l_i)  if |l_i - l_j| > delta,  R_ij / 2 otherwise,
+//   X <- X (I + E),  delta = 2 (||S - diag(l)|| + ||A|| ||R||),
+// converges quadratically; every step is three GEMMs on all SMs instead of
+// a serial Jacobi sweep on one SM.  Near-degenerate clusters are
+// diagonalised exactly afterwards (cluster_finish_kernel).
+// ---------------------------------------------------------------------------
+__global__ void refine_lambda_kernel(int n, const double* __restrict__ XtX, const double* __restrict__ S,
+                                     const double* __restrict__ A, double* __restrict__ lam,
+                                     double* __restrict__ rscal) {
+  __shared__ double red[3][256];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < n; i += nt) lam[i] = S[i + size_t(i) * n] / XtX[i + size_t(i) * n];
+  __syncthreads();
+  double s_off = 0.0, s_r = 0.0, s_a = 0.0;
+  for (size_t e = tid; e < size_t(n) * n; e += nt) {
+    const int i = int(e % n), j = int(e / n);
+    const double r = ((i == j) ? 1.0 : 0.0) - XtX[e];
+    const double so = S[e] - ((i == j) ? lam[i] : 0.0);
+    s_off += so * so;
+    s_r += r * r;
+    s_a += A[e] * A[e];
+  }
+  red[0][tid] = s_off;
+  red[1][tid] = s_r;
+  red[2][tid] = s_a;
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s)
+      for (int q = 0; q < 3; ++q) red[q][tid] += red[q][tid + s];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const double nS = sqrt(red[0][0]), nR = sqrt(red[1][0]), nA = sqrt(red[2][0]);
+    rscal[0] = 2.0 * (nS + nA * nR);  // delta
+    rscal[1] = nA;
+    rscal[2] = nS;
+    rscal[3] = nR;
+  }
+}
+
+__global__ void refine_update_kernel(int n, const double* __restrict__ XtX, const double* __restrict__ S,
+                                     const double* __restrict__ lam, const double* __restrict__ rscal,
+                                     double* __restrict__ M) {
+  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (e >= size_t(n) * n) return;
+  const int i = int(e % n), j = int(e / n);
+  const double r = ((i == j) ? 1.0 : 0.0) - XtX[e];
+  const double dl = lam[j] - lam[i];
+  const double E = (fabs(dl) > rscal[0]) ? (S[e] + lam[j] * r) / dl : 0.5 * r;
+  M[e] = ((i == j) ? 1.0 : 0.0) + E;
+}
+
+// Sort by eigenvalue, diagonalise clusters of (near-)degenerate eigenvalues
+// exactly with a small Jacobi, verify the off-diagonal coupling between
+// clusters, write D (ascending) and the eigenvalues.  One CTA.
+__global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const double* __restrict__ X,
+                                      const double* __restrict__ rscal, double* __restrict__ D,
+                                      double* __restrict__ evals, int* __restrict__ perm_ws, int* rflag) {
+  __shared__ int cl_start[513];
+  __shared__ int ncl;
+  __shared__ int fail;
+  __shared__ double red[256];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int* perm = perm_ws;        // sorted position -> original column
+  int* cid = perm_ws + n;     // original column -> cluster id
+  if (tid == 0) fail = 0;
+  for (int i = tid; i < n; i += nt) {
+    const double v = S[i + size_t(i) * n];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const double u = S[j + size_t(j) * n];
+      rank += (u < v || (u == v && j < i)) ? 1 : 0;
+    }
+    perm[rank] = i;
+  }
+  __syncthreads();
+  const double nA = rscal[1];
+  const double tau = fmax(rscal[0], 1.0e-13 * nA);
+  if (tid == 0) {
+    int c = 0;
+    cl_start[0] = 0;
+    for (int k = 0; k < n; ++k) {
+      if (k > 0) {
+        const double gap = S[perm[k] + size_t(perm[k]) * n] - S[perm[k - 1] + size_t(perm[k - 1]) * n];
+        if (gap > tau) cl_start[++c] = k;
+      }
+      cid[perm[k]] = c;
+    }
+    ncl = c + 1;
+    cl_start[ncl] = n;
+  }
+  __syncthreads();
+  // coupling between different clusters must be negligible
+  double mx = 0.0;
+  for (size_t e = tid; e < size_t(n) * n; e += nt) {
+    const int i = int(e % n), j = int(e / n);
+    if (cid[i] != cid[j]) mx = fmax(mx, fabs(S[e]));
+  }
+  red[tid] = mx;
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s) red[tid] = fmax(red[tid], red[tid + s]);
+    __syncthreads();
+  }
+  // X orthonormal and X^T A X block diagonal over clusters <=> invariant subspaces
+  if (tid == 0 && (red[0] > 1.0e-12 * fmax(nA, 1e-300) || rscal[3] > 1.0e-12 * sqrt(double(n)))) fail = 1;
+  __syncthreads();
+  // per cluster: Jacobi on the cluster block, rotate the columns
+  constexpr int CM = 8;
+  for (int c = tid; c < ncl; c += nt) {
+    const int k0 = cl_start[c], m = cl_start[c + 1] - k0;
+    if (m > CM) {
+      atomicOr(&fail, 1);
+      continue;
+    }
+    double a[CM][CM], q[CM][CM];
+    for (int r = 0; r < m; ++r)
+      for (int t = 0; t < m; ++t) {
+        a[r][t] = S[perm[k0 + r] + size_t(perm[k0 + t]) * n];
+        q[r][t] = (r == t) ? 1.0 : 0.0;
+      }
+    for (int sweep = 0; sweep < 30 && m > 1; ++sweep) {
+      double off = 0.0;
+      for (int r = 0; r < m; ++r)
+        for (int t = r + 1; t < m; ++t) off += a[r][t] * a[r][t];
+      if (off == 0.0) break;
+      for (int pp = 0; pp < m; ++pp)
+        for (int qq = pp + 1; qq < m; ++qq) {
+          if (a[pp][qq] == 0.0) continue;
+          const double theta = (a[qq][qq] - a[pp][pp]) / (2.0 * a[pp][qq]);
+          const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+          const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+          for (int r = 0; r < m; ++r) {
+            const double ap = a[r][pp], aq = a[r][qq];
+            a[r][pp] = cs * ap - sn * aq;
+            a[r][qq] = sn * ap + cs * aq;
+          }
+          for (int r = 0; r < m; ++r) {
+            const double ap = a[pp][r], aq = a[qq][r];
+            a[pp][r] = cs * ap - sn * aq;
+            a[qq][r] = sn * ap + cs * aq;
+          }
+          for (int r = 0; r < m; ++r) {
+            const double qp = q[r][pp], qv = q[r][qq];
+            q[r][pp] = cs * qp - sn * qv;
+            q[r][qq] = sn * qp + cs * qv;
+          }
+        }
+    }
+    // order inside the cluster by the diagonalised values
+    int ord[CM];
+    for (int r = 0; r < m; ++r) ord[r] = r;
+    for (int r = 1; r < m; ++r)
+      for (int t = r; t > 0 && a[ord[t]][ord[t]] < a[ord[t - 1]][ord[t - 1]]; --t) {
+        const int x = ord[t];
+        ord[t] = ord[t - 1];
+        ord[t - 1] = x;
+      }
+    for (int r = 0; r < m; ++r) {
+      const int src = ord[r];
+      evals[k0 + r] = a[src][src];
+      for (int row = 0; row < n; ++row) {
+        double v = 0.0;
+        for (int t = 0; t < m; ++t) v = fma(X[row + size_t(perm[k0 + t]) * n], q[t][src], v);
+        D[row + size_t(k0 + r) * n] = v;
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) rflag[0] = fail;
+}
+
+__global__ void copy_kernel(size_t m, const double* __restrict__ a, double* __restrict__ b) {
+  const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < m) b[i] = a[i];
+}
+
 inline unsigned nblk(size_t total, int tb) { return unsigned((total + tb - 1) / tb); }
 
 // host-side angle table (assign_angles, module_projection.f90:112-185)
@@ -669,6 +857,51 @@ int real_gemm(int M, int N, int K, View A, View B, double* C, int ldc, double al
 
 }  // namespace
 
+// Eigenvectors of rho (w->rho) into w->D (ascending), warm-started from the
+// previous basis of this context when there is one, exact Jacobi otherwise.
+int eigen_canonical(tvap_ctx* c) {
+  Workspace* w = c->ws;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  int rc;
+  if (w->have_basis) {
+    double* X = w->Xr;
+    double* Xn = w->Xn;
+    copy_kernel<<<nblk(nn, 256), 256, 0, s>>>(nn, w->D, X);
+    const View Rho = view_cm(w->rho, n, 0);
+    for (int step = 0; step < 3; ++step) {
+      const View Xv = view_cm(X, n, 0);
+      if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
+      if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
+      if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+      refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+      refine_update_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
+      if ((rc = real_gemm(n, n, n, Xv, view_cm(w->Mr, n, 0), Xn, n, 1.0, 0.0, s))) return rc;
+      std::swap(X, Xn);
+    }
+    const View Xv = view_cm(X, n, 0);
+    if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
+    if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
+    if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+    refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+    cluster_finish_kernel<<<1, 256, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals,
+                                            reinterpret_cast<int*>(w->jwork), w->rflag);
+    TVAP_CUDA(cudaGetLastError());
+    c->kernel_launches += 3 * 6 + 5;
+    int fail = 1;
+    TVAP_CUDA(cudaMemcpyAsync(&fail, w->rflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TVAP_CUDA(cudaStreamSynchronize(s));
+    if (!fail) return TVAP_OK;
+  }
+  // exact cyclic Jacobi (cold start or refinement rejected)
+  TVAP_CUDA(cudaMemcpyAsync(w->jac, w->rho, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+  if ((rc = jacobi_eigen(n, w->jac, w->D, w->evals, w->jwork, c->d_flags, s))) return rc;
+  c->kernel_launches += 1;
+  w->have_basis = true;
+  return TVAP_OK;
+}
+
 // Canonical basis + angle-independent blocks for state (w->U, w->V).
 int prepare_state(tvap_ctx* c, double occeps, double allemp_d, int* host_canon /*[3] or null*/) {
   Workspace* w = c->ws;
@@ -681,8 +914,7 @@ int prepare_state(tvap_ctx* c, double occeps, double allemp_d, int* host_canon /
   // rho = V V^T, kappa = V U^T (construct_canonical_basis :826, :862)
   if ((rc = real_gemm(n, n, n, Vn, view_t(Vn), w->rho, n, 1.0, 0.0, s))) return rc;
   if ((rc = real_gemm(n, n, n, Vn, view_t(Un), w->kap, n, 1.0, 0.0, s))) return rc;
-  TVAP_CUDA(cudaMemcpyAsync(w->jac, w->rho, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
-  if ((rc = jacobi_eigen(n, w->jac, w->D, w->evals, w->jwork, c->d_flags, s))) return rc;
+  if ((rc = eigen_canonical(c))) return rc;
   const View Dn = view_cm(w->D, n, 0);
   // rhoc = D^T rho D, kappac = D^T kappa D
   if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->rho, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;

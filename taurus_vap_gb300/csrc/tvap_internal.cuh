@@ -177,6 +177,8 @@ int fields_batched(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
 int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s);
 // symmetric eigen-decomposition by cyclic Jacobi (one matrix), ascending order
 int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s);
+// same in FP32 (cold start of the refinement); tolerance ~1e-6.5 ||A||
+int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s);
 // Cholesky L L^T = A (lower), then L^{-1} in place
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
 

@@ -179,3 +179,23 @@ def test_energy_adjoint(sd):
     om = O.OracleModel(mdl)
     ref = om.project(U, V, 5, 5, 2 * np.pi, 4, 4, nthreads=1)
     assert relerr(G0.reshape(-1, order="F"), ref["H20v"]) < 1e-9
+
+
+def test_warm_started_canonical_basis(emax4):
+    # successive projections in one context refine the previous canonical
+    # basis instead of re-diagonalising; results must still match the oracle
+    mdl, U, V = emax4
+    n = mdl.n
+    ctx = Context(mdl.basis, mdl.ham)
+    om = O.OracleModel(mdl)
+    rng = np.random.default_rng(9)
+    for step in range(3):
+        pnp, H20v = ctx.project(U, V, 3, 3, 2 * np.pi, 8, 8)
+        ref = om.project(U, V, 3, 3, 2 * np.pi, 8, 8)
+        e_got = (pnp.c("ener") / pnp.c("over")).real
+        e_ref = (ref["pnp"].c("ener") / ref["pnp"].c("over")).real
+        assert abs(e_got - e_ref) < 1e-9, step
+        assert relerr(H20v, ref["H20v"]) < 1e-9, step
+        Z = 1e-3 * rng.normal(size=(n, n))
+        Z = Z - Z.T
+        U, V = ctx.evolve(U, V, Z)
