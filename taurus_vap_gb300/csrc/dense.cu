@@ -495,6 +495,140 @@ int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int
   return TVAP_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// FP32 parallel cyclic Jacobi with the matrix and the rotations resident in
+// shared memory (n <= 160): the cheap first stage of the canonical-basis
+// eigensolver; the FP64 refinement that follows restores full accuracy.
+// Writes the (unsorted) eigenvectors as FP64 columns of W.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double* __restrict__ A64,
+                                                              double* __restrict__ W64, int* flags) {
+  extern __shared__ float js[];
+  const int m = (n + 1) & ~1;
+  float* A = js;                         // n*n
+  float* W = A + size_t(n) * n;          // n*n
+  float* cs = W + size_t(n) * n;         // m/2
+  float* sn = cs + m / 2;                // m/2
+  int* pairs = reinterpret_cast<int*>(sn + m / 2);  // m
+  int* pp = pairs + m;                   // m/2
+  int* qq = pp + m / 2;                  // m/2
+  __shared__ float red[1024];
+  __shared__ int done;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  float fro = 0.f;
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) {
+    const float a = float(A64[idx]);
+    A[idx] = a;
+    W[idx] = ((idx % n) == (idx / n)) ? 1.f : 0.f;
+    fro += a * a;
+  }
+  for (int i = tid; i < m; i += nt) pairs[i] = i;
+  red[tid] = fro;
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s) red[tid] += red[tid + s];
+    __syncthreads();
+  }
+  const float tol2 = red[0] * 1.0e-12f;  // off-diagonal <= 1e-6 ||A||: enough for the FP64 refinement
+  __syncthreads();
+  int sweep;
+  for (sweep = 0; sweep < 40; ++sweep) {
+    float off = 0.f;
+    for (size_t idx = tid; idx < size_t(n) * n; idx += nt)
+      if ((idx % n) != (idx / n)) off += A[idx] * A[idx];
+    red[tid] = off;
+    __syncthreads();
+    for (int s = nt / 2; s > 0; s >>= 1) {
+      if (tid < s) red[tid] += red[tid + s];
+      __syncthreads();
+    }
+    if (tid == 0) done = (red[0] <= tol2) ? 1 : 0;
+    __syncthreads();
+    if (done) break;
+    for (int round = 0; round < m - 1; ++round) {
+      for (int k = tid; k < m / 2; k += nt) {
+        int p = pairs[k], q = pairs[m - 1 - k];
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        float c = 1.f, s = 0.f;
+        if (q < n) {
+          const float apq = A[p + size_t(q) * n];
+          if (apq != 0.f) {
+            const float theta = (A[q + size_t(q) * n] - A[p + size_t(p) * n]) / (2.f * apq);
+            const float t = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+            c = rsqrtf(t * t + 1.f);
+            s = t * c;
+          }
+        }
+        pp[k] = p;
+        qq[k] = q;
+        cs[k] = c;
+        sn[k] = s;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < n * (m / 2); idx += nt) {
+        const int r = idx % n, k = idx / n;
+        const int p = pp[k], q = qq[k];
+        const float s = sn[k];
+        if (q >= n || s == 0.f) continue;
+        const float c = cs[k];
+        const float ap = A[r + p * n], aq = A[r + q * n];
+        A[r + p * n] = c * ap - s * aq;
+        A[r + q * n] = s * ap + c * aq;
+        const float wp = W[r + p * n], wq = W[r + q * n];
+        W[r + p * n] = c * wp - s * wq;
+        W[r + q * n] = s * wp + c * wq;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < n * (m / 2); idx += nt) {
+        const int col = idx % n, k = idx / n;
+        const int p = pp[k], q = qq[k];
+        const float s = sn[k];
+        if (q >= n || s == 0.f) continue;
+        const float c = cs[k];
+        const float ap = A[p + col * n], aq = A[q + col * n];
+        A[p + col * n] = c * ap - s * aq;
+        A[q + col * n] = s * ap + c * aq;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const int last = pairs[m - 1];
+        for (int i = m - 1; i > 1; --i) pairs[i] = pairs[i - 1];
+        pairs[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  // no error flag here: the FP64 refinement's final check decides
+  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) W64[idx] = double(W[idx]);
+}
+
+}  // namespace
+
+size_t jacobi32_smem_bytes(int n) {
+  const int m = (n + 1) & ~1;
+  return sizeof(float) * (2 * size_t(n) * n + m) + sizeof(int) * 2 * m + 64;
+}
+
+int jacobi32_smem(int n, const double* A, double* W, int* flags, cudaStream_t s) {
+  const size_t shm = jacobi32_smem_bytes(n);
+  static bool attr_set = false;
+  if (!attr_set) {
+    TVAP_CUDA(cudaFuncSetAttribute(jacobi32_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr_set = true;
+  }
+  if (shm > 227 * 1024) return TVAP_ERR_ARG;
+  jacobi32_smem_kernel<<<1, 1024, shm, s>>>(n, A, W, flags);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Cholesky L L^T = A (lower, right-looking) followed by L^{-1} in place
 // (DPBTRF + DTRTRI of cholesky_factorization / evolve_wavefunction,

@@ -670,7 +670,12 @@ __global__ void refine_update_kernel(int n, const double* __restrict__ XtX, cons
   const int i = int(e % n), j = int(e / n);
   const double r = ((i == j) ? 1.0 : 0.0) - XtX[e];
   const double dl = lam[j] - lam[i];
-  const double E = (fabs(dl) > rscal[0]) ? (S[e] + lam[j] * r) / dl : 0.5 * r;
+  // Newton correction where the gap dominates the coupling; pairs that are
+  // (nearly) degenerate relative to their coupling are only re-orthonormalised
+  // and diagonalised exactly at the end
+  const double sij = fmax(fabs(S[e]), fabs(S[j + size_t(i) * n]));
+  const bool newton = (i != j) && fabs(dl) > 4.0 * sij + 1.0e-13 * rscal[1];
+  const double E = newton ? (S[e] + lam[j] * r) / dl : 0.5 * r;
   M[e] = ((i == j) ? 1.0 : 0.0) + E;
 }
 
@@ -857,18 +862,21 @@ int real_gemm(int M, int N, int K, View A, View B, double* C, int ldc, double al
 
 }  // namespace
 
-// Eigenvectors of rho (w->rho) into w->D (ascending), warm-started from the
-// previous basis of this context when there is one, exact Jacobi otherwise.
+// Eigenvectors of rho (w->rho) into w->D (ascending): FP32 Jacobi in shared
+// memory, three FP64 refinement steps on all SMs, exact diagonalisation of
+// degenerate clusters; the exact FP64 Jacobi runs only if the final check
+// (orthonormality, decoupled clusters) fails or n is too large for the
+// shared-memory stage.
 int eigen_canonical(tvap_ctx* c) {
   Workspace* w = c->ws;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;
   int rc;
-  if (w->have_basis) {
+  if (jacobi32_smem_bytes(n) <= 227 * 1024) {
     double* X = w->Xr;
     double* Xn = w->Xn;
-    copy_kernel<<<nblk(nn, 256), 256, 0, s>>>(nn, w->D, X);
+    if ((rc = jacobi32_smem(n, w->rho, X, c->d_flags, s))) return rc;
     const View Rho = view_cm(w->rho, n, 0);
     for (int step = 0; step < 3; ++step) {
       const View Xv = view_cm(X, n, 0);
@@ -888,17 +896,16 @@ int eigen_canonical(tvap_ctx* c) {
     cluster_finish_kernel<<<1, 256, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals,
                                             reinterpret_cast<int*>(w->jwork), w->rflag);
     TVAP_CUDA(cudaGetLastError());
-    c->kernel_launches += 3 * 6 + 5;
+    c->kernel_launches += 1 + 3 * 6 + 5;
     int fail = 1;
     TVAP_CUDA(cudaMemcpyAsync(&fail, w->rflag, sizeof(int), cudaMemcpyDeviceToHost, s));
     TVAP_CUDA(cudaStreamSynchronize(s));
     if (!fail) return TVAP_OK;
   }
-  // exact cyclic Jacobi (cold start or refinement rejected)
+  // exact cyclic Jacobi in FP64
   TVAP_CUDA(cudaMemcpyAsync(w->jac, w->rho, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   if ((rc = jacobi_eigen(n, w->jac, w->D, w->evals, w->jwork, c->d_flags, s))) return rc;
   c->kernel_launches += 1;
-  w->have_basis = true;
   return TVAP_OK;
 }
 

@@ -179,6 +179,10 @@ int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cuda
 int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s);
 // same in FP32 (cold start of the refinement); tolerance ~1e-6.5 ||A||
 int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s);
+// FP32 Jacobi with A and W in shared memory (n <= 160); W64 gets the unsorted
+// eigenvectors of A64 as FP64 columns.
+size_t jacobi32_smem_bytes(int n);
+int jacobi32_smem(int n, const double* A64, double* W64, int* flags, cudaStream_t s);
 // Cholesky L L^T = A (lower), then L^{-1} in place
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
 
