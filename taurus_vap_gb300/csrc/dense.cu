@@ -616,14 +616,29 @@ size_t jacobi32_smem_bytes(int n) {
   return sizeof(float) * (2 * size_t(n) * n + m) + sizeof(int) * 2 * m + 64;
 }
 
+// largest dynamic shared memory the FP32 Jacobi kernel may request on this device
+size_t jacobi32_smem_limit() {
+  static size_t limit = 0;
+  if (limit == 0) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, jacobi32_smem_kernel);
+    const size_t lim = (size_t(optin) > fa.sharedSizeBytes) ? size_t(optin) - fa.sharedSizeBytes : 0;
+    if (cudaFuncSetAttribute(jacobi32_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lim)) ==
+        cudaSuccess)
+      limit = lim;
+    else
+      limit = 1;  // unusable: callers fall back to the FP64 solver
+    cudaGetLastError();
+  }
+  return limit;
+}
+
 int jacobi32_smem(int n, const double* A, double* W, int* flags, cudaStream_t s) {
   const size_t shm = jacobi32_smem_bytes(n);
-  static bool attr_set = false;
-  if (!attr_set) {
-    TVAP_CUDA(cudaFuncSetAttribute(jacobi32_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr_set = true;
-  }
-  if (shm > 227 * 1024) return TVAP_ERR_ARG;
+  if (shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
   jacobi32_smem_kernel<<<1, 1024, shm, s>>>(n, A, W, flags);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;

@@ -873,7 +873,7 @@ int eigen_canonical(tvap_ctx* c) {
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;
   int rc;
-  if (jacobi32_smem_bytes(n) <= 227 * 1024) {
+  if (jacobi32_smem_bytes(n) <= jacobi32_smem_limit()) {
     double* X = w->Xr;
     double* Xn = w->Xn;
     if ((rc = jacobi32_smem(n, w->rho, X, c->d_flags, s))) return rc;

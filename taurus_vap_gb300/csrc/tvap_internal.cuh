@@ -182,6 +182,7 @@ int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int
 // FP32 Jacobi with A and W in shared memory (n <= 160); W64 gets the unsorted
 // eigenvectors of A64 as FP64 columns.
 size_t jacobi32_smem_bytes(int n);
+size_t jacobi32_smem_limit();
 int jacobi32_smem(int n, const double* A64, double* W64, int* flags, cudaStream_t s);
 // Cholesky L L^T = A (lower), then L^{-1} in place
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
