@@ -148,6 +148,70 @@ __global__ void __launch_bounds__((TM / 2) * (TN / 2)) gemm_kernel(GemmArgs g) {
     }
 }
 
+// Complex x complex with three real products per multiply-add (the 3M form):
+//   t1 = sum Ar Br,  t2 = sum Ai Bi,  t3 = sum (Ar + Ai)(Br + Bi),
+//   Re C = t1 - t2,  Im C = t3 - t1 - t2,
+// the sums Ar + Ai, Br + Bi being formed once per element when the tile is
+// staged.  3 DFMA instead of 4 per complex multiply-add.
+template <int TM, int TN>
+__global__ void __launch_bounds__((TM / 2) * (TN / 2)) gemm3m_kernel(GemmArgs g) {
+  constexpr int BK = 16;
+  constexpr int HM = TM / 2, HN = TN / 2;
+  constexpr int NT = HM * HN;
+  __shared__ double3 As[BK][TM + 1];
+  __shared__ double3 Bs[BK][TN + 1];
+  const long long b = blockIdx.z;
+  const int i0 = blockIdx.y * TM, j0 = blockIdx.x * TN;
+  const int tid = threadIdx.x;
+  const int ty = tid / HN, tx = tid % HN;
+  double t1[2][2], t2[2][2], t3[2][2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) t1[r][c] = t2[r][c] = t3[r][c] = 0.0;
+  const bool live = (i0 + ty < g.M) && (j0 + tx < g.N);
+  for (int k0 = 0; k0 < g.K; k0 += BK) {
+    const int kt = min(BK, g.K - k0);
+    for (int idx = tid; idx < TM * BK; idx += NT) {
+      const int ii = idx % TM, kk = idx / TM;
+      double2 v = make_double2(0.0, 0.0);
+      if (i0 + ii < g.M && kk < kt) v = load_el<double2>(g.A, i0 + ii, k0 + kk, b, g.conj_a);
+      As[kk][ii] = make_double3(v.x, v.y, v.x + v.y);
+    }
+    for (int idx = tid; idx < TN * BK; idx += NT) {
+      const int jj = idx % TN, kk = idx / TN;
+      double2 v = make_double2(0.0, 0.0);
+      if (j0 + jj < g.N && kk < kt) v = load_el<double2>(g.B, k0 + kk, j0 + jj, b, g.conj_b);
+      Bs[kk][jj] = make_double3(v.x, v.y, v.x + v.y);
+    }
+    __syncthreads();
+    if (live) {
+      for (int kk = 0; kk < kt; ++kk) {
+        const double3 a0 = As[kk][ty], a1 = As[kk][ty + HM];
+        const double3 b0 = Bs[kk][tx], b1 = Bs[kk][tx + HN];
+        t1[0][0] = fma(a0.x, b0.x, t1[0][0]); t2[0][0] = fma(a0.y, b0.y, t2[0][0]); t3[0][0] = fma(a0.z, b0.z, t3[0][0]);
+        t1[0][1] = fma(a0.x, b1.x, t1[0][1]); t2[0][1] = fma(a0.y, b1.y, t2[0][1]); t3[0][1] = fma(a0.z, b1.z, t3[0][1]);
+        t1[1][0] = fma(a1.x, b0.x, t1[1][0]); t2[1][0] = fma(a1.y, b0.y, t2[1][0]); t3[1][0] = fma(a1.z, b0.z, t3[1][0]);
+        t1[1][1] = fma(a1.x, b1.x, t1[1][1]); t2[1][1] = fma(a1.y, b1.y, t2[1][1]); t3[1][1] = fma(a1.z, b1.z, t3[1][1]);
+      }
+    }
+    __syncthreads();
+  }
+  double2 alpha = g.alpha;
+  if (g.alpha_vec) alpha = cmul(alpha, g.alpha_vec[b]);
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int i = i0 + ty + r * HM, j = j0 + tx + c * HN;
+      if (i < g.M && j < g.N) {
+        const long long idx = i * g.crs + j * g.ccs + b * g.cbs;
+        const double2 acc = make_double2(t1[r][c] - t2[r][c], t3[r][c] - t1[r][c] - t2[r][c]);
+        store_out(g, idx, acc, alpha);
+      }
+    }
+}
+
 template <int T, typename TA, typename TB>
 void launch_gemm_t(const GemmArgs& g, cudaStream_t s) {
   dim3 grid((g.N + T - 1) / T, (g.M + T - 1) / T, g.batch);
@@ -162,7 +226,10 @@ void launch_gemm_tile(const GemmArgs& g, cudaStream_t s) {
     launch_gemm_t<T, double, double2>(g, s);
   else if (g.b_real)
     launch_gemm_t<T, double2, double>(g, s);
-  else
+  else if (g.three_m) {
+    dim3 grid((g.N + T - 1) / T, (g.M + T - 1) / T, g.batch);
+    gemm3m_kernel<T, T><<<grid, (T / 2) * (T / 2), 0, s>>>(g);
+  } else
     launch_gemm_t<T, double2, double2>(g, s);
 }
 
@@ -505,12 +572,14 @@ int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int
 namespace {
 
 __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double* __restrict__ A64,
+                                                              const double* __restrict__ W0,
                                                               double* __restrict__ W64, int* flags) {
   extern __shared__ float js[];
   const int m = (n + 1) & ~1;
-  float* A = js;                         // n*n
-  float* W = A + size_t(n) * n;          // n*n
-  float* cs = W + size_t(n) * n;         // m/2
+  const int ld = n | 1;                  // odd leading dimension: conflict-free row access
+  float* A = js;                         // n x ld
+  float* W = A + size_t(n) * ld;         // n x ld
+  float* cs = W + size_t(n) * ld;        // m/2
   float* sn = cs + m / 2;                // m/2
   int* pairs = reinterpret_cast<int*>(sn + m / 2);  // m
   int* pp = pairs + m;                   // m/2
@@ -519,10 +588,11 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
   __shared__ int done;
   const int tid = threadIdx.x, nt = blockDim.x;
   float fro = 0.f;
-  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) {
+  for (int idx = tid; idx < n * n; idx += nt) {
+    const int i = idx % n, j = idx / n;
     const float a = float(A64[idx]);
-    A[idx] = a;
-    W[idx] = ((idx % n) == (idx / n)) ? 1.f : 0.f;
+    A[i + j * ld] = a;
+    W[i + j * ld] = W0 ? float(W0[idx]) : ((i == j) ? 1.f : 0.f);
     fro += a * a;
   }
   for (int i = tid; i < m; i += nt) pairs[i] = i;
@@ -534,11 +604,12 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
   }
   const float tol2 = red[0] * 1.0e-12f;  // off-diagonal <= 1e-6 ||A||: enough for the FP64 refinement
   __syncthreads();
-  int sweep;
-  for (sweep = 0; sweep < 40; ++sweep) {
+  for (int sweep = 0; sweep < 40; ++sweep) {
     float off = 0.f;
-    for (size_t idx = tid; idx < size_t(n) * n; idx += nt)
-      if ((idx % n) != (idx / n)) off += A[idx] * A[idx];
+    for (int idx = tid; idx < n * n; idx += nt) {
+      const int i = idx % n, j = idx / n;
+      if (i != j) off += A[i + j * ld] * A[i + j * ld];
+    }
     red[tid] = off;
     __syncthreads();
     for (int s = nt / 2; s > 0; s >>= 1) {
@@ -558,9 +629,9 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
         }
         float c = 1.f, s = 0.f;
         if (q < n) {
-          const float apq = A[p + size_t(q) * n];
+          const float apq = A[p + q * ld];
           if (apq != 0.f) {
-            const float theta = (A[q + size_t(q) * n] - A[p + size_t(p) * n]) / (2.f * apq);
+            const float theta = (A[q + q * ld] - A[p + p * ld]) / (2.f * apq);
             const float t = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
             c = rsqrtf(t * t + 1.f);
             s = t * c;
@@ -578,12 +649,12 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
         const float s = sn[k];
         if (q >= n || s == 0.f) continue;
         const float c = cs[k];
-        const float ap = A[r + p * n], aq = A[r + q * n];
-        A[r + p * n] = c * ap - s * aq;
-        A[r + q * n] = s * ap + c * aq;
-        const float wp = W[r + p * n], wq = W[r + q * n];
-        W[r + p * n] = c * wp - s * wq;
-        W[r + q * n] = s * wp + c * wq;
+        const float ap = A[r + p * ld], aq = A[r + q * ld];
+        A[r + p * ld] = c * ap - s * aq;
+        A[r + q * ld] = s * ap + c * aq;
+        const float wp = W[r + p * ld], wq = W[r + q * ld];
+        W[r + p * ld] = c * wp - s * wq;
+        W[r + q * ld] = s * wp + c * wq;
       }
       __syncthreads();
       for (int idx = tid; idx < n * (m / 2); idx += nt) {
@@ -592,9 +663,9 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
         const float s = sn[k];
         if (q >= n || s == 0.f) continue;
         const float c = cs[k];
-        const float ap = A[p + col * n], aq = A[q + col * n];
-        A[p + col * n] = c * ap - s * aq;
-        A[q + col * n] = s * ap + c * aq;
+        const float ap = A[p + col * ld], aq = A[q + col * ld];
+        A[p + col * ld] = c * ap - s * aq;
+        A[q + col * ld] = s * ap + c * aq;
       }
       __syncthreads();
       if (tid == 0) {
@@ -606,14 +677,14 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
     }
   }
   // no error flag here: the FP64 refinement's final check decides
-  for (size_t idx = tid; idx < size_t(n) * n; idx += nt) W64[idx] = double(W[idx]);
+  for (int idx = tid; idx < n * n; idx += nt) W64[idx] = double(W[(idx % n) + (idx / n) * ld]);
 }
 
 }  // namespace
 
 size_t jacobi32_smem_bytes(int n) {
   const int m = (n + 1) & ~1;
-  return sizeof(float) * (2 * size_t(n) * n + m) + sizeof(int) * 2 * m + 64;
+  return sizeof(float) * (2 * size_t(n) * (n | 1) + m) + sizeof(int) * 2 * m + 64;
 }
 
 // largest dynamic shared memory the FP32 Jacobi kernel may request on this device
@@ -636,10 +707,10 @@ size_t jacobi32_smem_limit() {
   return limit;
 }
 
-int jacobi32_smem(int n, const double* A, double* W, int* flags, cudaStream_t s) {
+int jacobi32_smem(int n, const double* A, const double* W0, double* W, int* flags, cudaStream_t s) {
   const size_t shm = jacobi32_smem_bytes(n);
   if (shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
-  jacobi32_smem_kernel<<<1, 1024, shm, s>>>(n, A, W, flags);
+  jacobi32_smem_kernel<<<1, 1024, shm, s>>>(n, A, W0, W, flags);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }

@@ -71,6 +71,8 @@ struct Workspace {
   // eigenvector refinement (warm start from the previous canonical basis)
   double *Xr = nullptr, *Xn = nullptr, *Rr = nullptr, *Br = nullptr, *Sr = nullptr, *Mr = nullptr,
          *lam = nullptr, *rscal = nullptr;
+  // overlap chain scratch (runs on the second stream)
+  double2 *OW = nullptr, *OX = nullptr, *OY = nullptr;
   int* rflag = nullptr;
   bool have_basis = false;
   size_t bytes = 0;
@@ -93,7 +95,7 @@ void ws_free(Workspace* w) {
                   w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
                   w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
                   w->H20v,  w->Xr,    w->Xn,     w->Rr,    w->Br,     w->Sr,    w->Mr,     w->lam,   w->rscal,
-                  w->rflag};
+                  w->rflag, w->OW,    w->OX,     w->OY};
   for (void* p : ptrs) cudaFree(p);
   *w = Workspace();
 }
@@ -122,6 +124,7 @@ int ws_ensure(tvap_ctx* c, int G) {
   A_(dRL, nG) A_(ephase, 2 * G) A_(weight, G) A_(mult, G) A_(obs, 8 * G) A_(pf, 2 * G) A_(detR22, 2 * G)
   A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
   A_(Xr, nn) A_(Xn, nn) A_(Rr, nn) A_(Br, nn) A_(Sr, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
+  A_(OW, nG) A_(OX, nG) A_(OY, nG)
 #undef A_
   return TVAP_OK;
 }
@@ -876,8 +879,16 @@ int eigen_canonical(tvap_ctx* c) {
   if (jacobi32_smem_bytes(n) <= jacobi32_smem_limit()) {
     double* X = w->Xr;
     double* Xn = w->Xn;
-    if ((rc = jacobi32_smem(n, w->rho, X, c->d_flags, s))) return rc;
     const View Rho = view_cm(w->rho, n, 0);
+    if (w->have_basis) {
+      // warm start: rotate rho into the previous canonical basis (FP64 GEMMs)
+      const View Dp = view_cm(w->D, n, 0);
+      if ((rc = real_gemm(n, n, n, Rho, Dp, w->Br, n, 1.0, 0.0, s))) return rc;
+      if ((rc = real_gemm(n, n, n, view_t(Dp), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+      if ((rc = jacobi32_smem(n, w->Sr, w->D, X, c->d_flags, s))) return rc;
+    } else {
+      if ((rc = jacobi32_smem(n, w->rho, nullptr, X, c->d_flags, s))) return rc;
+    }
     for (int step = 0; step < 3; ++step) {
       const View Xv = view_cm(X, n, 0);
       if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
@@ -900,12 +911,16 @@ int eigen_canonical(tvap_ctx* c) {
     int fail = 1;
     TVAP_CUDA(cudaMemcpyAsync(&fail, w->rflag, sizeof(int), cudaMemcpyDeviceToHost, s));
     TVAP_CUDA(cudaStreamSynchronize(s));
-    if (!fail) return TVAP_OK;
+    if (!fail) {
+      w->have_basis = true;
+      return TVAP_OK;
+    }
   }
   // exact cyclic Jacobi in FP64
   TVAP_CUDA(cudaMemcpyAsync(w->jac, w->rho, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   if ((rc = jacobi_eigen(n, w->jac, w->D, w->evals, w->jwork, c->d_flags, s))) return rc;
   c->kernel_launches += 1;
+  w->have_basis = true;
   return TVAP_OK;
 }
 
@@ -973,6 +988,60 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
   build_angle_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(n, G, w->blocks, d_ephase, w->canon_i, w->Uphi, w->Vphi,
                                                      w->Rn);
   TVAP_CUDA(cudaGetLastError());
+  // overlap chain on the second stream (depends only on R_n and the
+  // canonical basis): runs concurrently with the Thouless chain below
+  const int n2 = n - nemp, nb = n2 - nocc;
+  if (have_overlap) {
+    cudaStream_t s2 = c->stream2;
+    TVAP_CUDA(cudaEventRecord(c->ev_fork, s));
+    TVAP_CUDA(cudaStreamWaitEvent(s2, c->ev_fork, 0));
+    sec_begin_on(c, SEC_OVERLAP, s2);
+    const double2* S = w->Rn;
+    int ldS = n2;
+    long long bsS = (long long)n2 * n2;
+    if (nocc > 0) {
+      // Z = R22^{-1} R21 (nocc x nb), det(R22); S = R11 - R12 Z
+      left_solve_kernel<<<G, kLsThreads, 0, s2>>>(
+          nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
+          View{w->Rn + nb, 1, n2, (long long)n2 * n2}, w->OW, w->OX, 1, nocc, (long long)nocc * nb, 0, w->detR22,
+          G, c->d_flags, DEV_SINGULAR_RN);
+      schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n2, nb, G, w->Rn, w->OX, w->SZ);
+      TVAP_CUDA(cudaGetLastError());
+      S = w->SZ;
+      ldS = nb;
+      bsS = (long long)nb * nb;
+    } else {
+      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->detR22);
+    }
+    if (nb > 0) {
+      overlap_prep_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n, G, w->canon_i, w->canon_d, S, ldS, bsS,
+                                                                        w->K, w->OY);
+      TVAP_CUDA(cudaGetLastError());
+      // K += S^T Y
+      GemmArgs g{};
+      g.M = g.N = g.K = nb;
+      g.batch = G;
+      g.A = View{S, (long long)ldS, 1, bsS};
+      g.B = view_cm(w->OY, nb, (long long)nb * nb);
+      g.C = w->K;
+      g.crs = 1;
+      g.ccs = nb;
+      g.cbs = (long long)nb * nb;
+      g.alpha = make_double2(1.0, 0.0);
+      g.beta = make_double2(1.0, 0.0);
+      g.three_m = true;
+      if ((rc = gemm(g, s2))) return rc;
+      sec_end_on(c, SEC_OVERLAP, s2);
+      sec_begin_on(c, SEC_PFAFFIAN, s2);
+      if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s2))) return rc;
+      sec_end_on(c, SEC_PFAFFIAN, s2);
+    } else {
+      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->pf);
+      sec_end_on(c, SEC_OVERLAP, s2);
+    }
+    TVAP_CUDA(cudaEventRecord(c->ev_join, s2));
+  }
+
   // A_phi = conj(V_phi U_phi^{-1}): solve U_phi^T Y = V_phi^T, A = conj(Y^T)
   left_solve_kernel<<<G, kLsThreads, 0, s>>>(n, n, View{w->Uphi, (long long)n, 1, (long long)nn},
                                              View{w->Vphi, (long long)n, 1, (long long)nn}, w->W, w->A, n, 1,
@@ -1049,6 +1118,7 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
     g.crs = 1;
     g.ccs = n;
     g.cbs = (long long)nn;
+    g.three_m = true;
     g.A = hv;
     g.B = view_cm(w->Vt, n, (long long)nn);
     g.C = w->X;
@@ -1077,54 +1147,7 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
     if ((rc = gemm(g, s))) return rc;
   }
   sec_end(c, SEC_H20);
-  sec_begin(c, SEC_OVERLAP);
-  // overlap
-  const int n2 = n - nemp, nb = n2 - nocc;
-  if (have_overlap) {
-    const double2* S = w->Rn;
-    int ldS = n2;
-    long long bsS = (long long)n2 * n2;
-    if (nocc > 0) {
-      // Z = R22^{-1} R21 (nocc x nb), det(R22); S = R11 - R12 Z
-      left_solve_kernel<<<G, kLsThreads, 0, s>>>(
-          nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
-          View{w->Rn + nb, 1, n2, (long long)n2 * n2}, w->W, w->X, 1, nocc, (long long)nocc * nb, 0, w->detR22, G,
-          c->d_flags, DEV_SINGULAR_RN);
-      schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s>>>(n2, nb, G, w->Rn, w->X, w->SZ);
-      TVAP_CUDA(cudaGetLastError());
-      S = w->SZ;
-      ldS = nb;
-      bsS = (long long)nb * nb;
-    } else {
-      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s>>>(G, w->detR22);
-    }
-    if (nb > 0) {
-      overlap_prep_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s>>>(n, G, w->canon_i, w->canon_d, S, ldS, bsS,
-                                                                       w->K, w->Y);
-      TVAP_CUDA(cudaGetLastError());
-      // K += S^T Y
-      GemmArgs g{};
-      g.M = g.N = g.K = nb;
-      g.batch = G;
-      g.A = View{S, (long long)ldS, 1, bsS};
-      g.B = view_cm(w->Y, nb, (long long)nb * nb);
-      g.C = w->K;
-      g.crs = 1;
-      g.ccs = nb;
-      g.cbs = (long long)nb * nb;
-      g.alpha = make_double2(1.0, 0.0);
-      g.beta = make_double2(1.0, 0.0);
-      if ((rc = gemm(g, s))) return rc;
-      sec_end(c, SEC_OVERLAP);
-      sec_begin(c, SEC_PFAFFIAN);
-      if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s))) return rc;
-      sec_end(c, SEC_PFAFFIAN);
-      sec_begin(c, SEC_OVERLAP);
-    } else {
-      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s>>>(G, w->pf);
-    }
-  }
-  sec_end(c, SEC_OVERLAP);
+  if (have_overlap) TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
   sec_begin(c, SEC_SUMS);
   overlap_finish_kernel<<<nblk(G, tb), tb, 0, s>>>(n, G, have_overlap ? 1 : 0, w->canon_i, w->canon_d, w->pf,
                                                     w->detR22, d_weight, d_mult, w->obs, w->coefA, w->coefAE);

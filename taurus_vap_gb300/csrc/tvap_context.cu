@@ -38,22 +38,25 @@ static cudaEvent_t take_event(tvap_ctx* c) {
   return e;
 }
 
-void sec_begin(tvap_ctx* c, int sec) {
+void sec_begin_on(tvap_ctx* c, int sec, cudaStream_t s) {
   if (!c->timing) return;
   cudaEvent_t a = take_event(c), b = take_event(c);
-  cudaEventRecord(a, c->stream);
+  cudaEventRecord(a, s);
   c->ev_open.push_back({sec, {a, b}});
 }
 
-void sec_end(tvap_ctx* c, int sec) {
+void sec_end_on(tvap_ctx* c, int sec, cudaStream_t s) {
   if (!c->timing) return;
   for (auto it = c->ev_open.rbegin(); it != c->ev_open.rend(); ++it)
     if (it->first == sec && it->second.second) {
-      cudaEventRecord(it->second.second, c->stream);
+      cudaEventRecord(it->second.second, s);
       it->first = sec + 1000;  // closed
       return;
     }
 }
+
+void sec_begin(tvap_ctx* c, int sec) { sec_begin_on(c, sec, c->stream); }
+void sec_end(tvap_ctx* c, int sec) { sec_end_on(c, sec, c->stream); }
 
 static void collect_sections(tvap_ctx* c) {
   if (c->ev_open.empty()) return;
@@ -156,6 +159,9 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
   c->own_stream = true;
+  if ((e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_2mj, sizeof(int) * n)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_tr, sizeof(int) * n)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_l, sizeof(int) * n)) != cudaSuccess) return fail(e);
@@ -172,6 +178,7 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
 void tvap_destroy(tvap_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->stream2) cudaStreamSynchronize(c->stream2);
   destroy_workspace(c);
   free_field_csr(c->csr);
   cudaFree(c->d_sp_2mj);
@@ -188,6 +195,9 @@ void tvap_destroy(tvap_ctx* c) {
   }
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   delete c;
 }
 

@@ -92,6 +92,7 @@ struct GemmArgs {
   const double2* alpha_vec;
   bool a_real, b_real, c_real;
   bool conj_a, conj_b;
+  bool three_m;  // complex x complex with three real products (3M)
 };
 int gemm(const GemmArgs& g, cudaStream_t s);
 
@@ -138,6 +139,8 @@ struct tvap_ctx {
   double2 H0 = {0.0, 0.0};
   bool have_ham = false;
   tvap::FieldCSR csr;
+  cudaStream_t stream2 = nullptr;  // overlap chain, concurrent with the Thouless chain
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
   int kernel_launches = 0;  // launches issued by the last top-level call
@@ -157,6 +160,8 @@ enum Section : int {
 // brackets a section with events when timing is on (no-ops otherwise)
 void sec_begin(tvap_ctx* c, int sec);
 void sec_end(tvap_ctx* c, int sec);
+void sec_begin_on(tvap_ctx* c, int sec, cudaStream_t s);
+void sec_end_on(tvap_ctx* c, int sec, cudaStream_t s);
 }  // namespace tvap
 
 namespace tvap {
@@ -180,10 +185,11 @@ int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* 
 // same in FP32 (cold start of the refinement); tolerance ~1e-6.5 ||A||
 int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s);
 // FP32 Jacobi with A and W in shared memory (n <= 160); W64 gets the unsorted
-// eigenvectors of A64 as FP64 columns.
+// eigenvectors of A64 as FP64 columns.  With W0 != null the rotations start
+// from W0 and A64 must be W0^T A W0 (warm start); W64 = W0 J.
 size_t jacobi32_smem_bytes(int n);
 size_t jacobi32_smem_limit();
-int jacobi32_smem(int n, const double* A64, double* W64, int* flags, cudaStream_t s);
+int jacobi32_smem(int n, const double* A64, const double* W0, double* W64, int* flags, cudaStream_t s);
 // Cholesky L L^T = A (lower), then L^{-1} in place
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
 
