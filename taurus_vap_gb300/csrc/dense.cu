@@ -161,6 +161,7 @@ __global__ void __launch_bounds__((TM / 2) * (TN / 2)) gemm3m_kernel(GemmArgs g)
   __shared__ double3 As[BK][TM + 1];
   __shared__ double3 Bs[BK][TN + 1];
   const long long b = blockIdx.z;
+  if (g.upper_only && blockIdx.y > blockIdx.x) return;
   const int i0 = blockIdx.y * TM, j0 = blockIdx.x * TN;
   const int tid = threadIdx.x;
   const int ty = tid / HN, tx = tid % HN;
@@ -372,17 +373,22 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_kernel(int N, double2* Aa
       }
       __syncthreads();
       // A(I,J) += X(I) * (alpha Y(J)) - Y(I) * (alpha X(J)),  I < J <= nn
-      // (ZSKR2 skips a column J whose X(J) and Y(J) are both zero)
-      for (long long idx = tid; idx < (long long)nn * nn; idx += nt) {
-        const int I = 1 + int(idx % nn), J = 1 + int(idx / nn);
-        if (I >= J) continue;
-        const double2 xj = xcol[J], yj = ycol[J];
-        if (xj.x == 0.0 && xj.y == 0.0 && yj.x == 0.0 && yj.y == 0.0) continue;
-        const double2 t1 = cmul(alpha, yj), t2 = cmul(alpha, xj);
-        double2 v = a(I, J);
-        cfma(v, xcol[I], t1);
-        cfma(v, cneg(ycol[I]), t2);
-        a(I, J) = v;
+      // (ZSKR2 skips a column J whose X(J) and Y(J) are both zero);
+      // one warp per column J, lanes over I (coalesced, no index division)
+      {
+        const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+        for (int J = 2 + warp; J <= nn; J += nw) {
+          const double2 xj = xcol[J], yj = ycol[J];
+          if (xj.x == 0.0 && xj.y == 0.0 && yj.x == 0.0 && yj.y == 0.0) continue;
+          const double2 t1 = cmul(alpha, yj), t2 = cmul(alpha, xj);
+          double2* colJ = A + size_t(J - 1) * N;
+          for (int I = 1 + lane; I <= J - 1; I += 32) {
+            double2 v = colJ[I - 1];
+            cfma(v, xcol[I], t1);
+            cfma(v, cneg(ycol[I]), t2);
+            colJ[I - 1] = v;
+          }
+        }
       }
       __syncthreads();
       for (int i = 1 + tid; i <= nn; i += nt) a(i, K) = cmul(alpha, a(i, K));
@@ -442,6 +448,9 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
   const double fro2 = red[0];
   __syncthreads();
   const double tol2 = fro2 * tolfac;  // converged when off-diagonal^2 <= tolfac ||A||_F^2
+  const int kstep = nt / n;
+  const int r0 = (tid < kstep * n) ? tid % n : n;
+  const int k0 = (tid < kstep * n) ? tid / n : 0;
   int sweep = 0;
   for (sweep = 0; sweep < 60; ++sweep) {
     // off-diagonal norm
@@ -486,10 +495,10 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
       }
       __syncthreads();
       // columns: A <- A J, W <- W J
-      for (long long idx = tid; idx < (long long)n * (m / 2); idx += nt) {
-        const int r = int(idx % n), k = int(idx / n);
+      for (int k = k0; k < m / 2; k += kstep) {
+        const int r = r0;
         const int p = pp[k], q = qq[k];
-        if (q >= n || sn[k] == 0.0) continue;
+        if (r >= n || q >= n || sn[k] == 0.0) continue;
         const T c = T(cs[k]), s = T(sn[k]);
         const T ap = Ael(r, p), aq = Ael(r, q);
         Ael(r, p) = c * ap - s * aq;
@@ -500,10 +509,10 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
       }
       __syncthreads();
       // rows: A <- J^T A
-      for (long long idx = tid; idx < (long long)n * (m / 2); idx += nt) {
-        const int col = int(idx % n), k = int(idx / n);
+      for (int k = k0; k < m / 2; k += kstep) {
+        const int col = r0;
         const int p = pp[k], q = qq[k];
-        if (q >= n || sn[k] == 0.0) continue;
+        if (col >= n || q >= n || sn[k] == 0.0) continue;
         const T c = T(cs[k]), s = T(sn[k]);
         const T ap = Ael(p, col), aq = Ael(q, col);
         Ael(p, col) = c * ap - s * aq;
@@ -603,13 +612,16 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
     __syncthreads();
   }
   const float tol2 = red[0] * 1.0e-12f;  // off-diagonal <= 1e-6 ||A||: enough for the FP64 refinement
+  // fixed thread -> (row, first pair) assignment: no index division in the sweeps
+  const int kstep = nt / n;           // threads per row group (>= 1 for n <= 1024)
+  const int r0 = (tid < kstep * n) ? tid % n : n;
+  const int k0 = (tid < kstep * n) ? tid / n : 0;
   __syncthreads();
   for (int sweep = 0; sweep < 40; ++sweep) {
     float off = 0.f;
-    for (int idx = tid; idx < n * n; idx += nt) {
-      const int i = idx % n, j = idx / n;
-      if (i != j) off += A[i + j * ld] * A[i + j * ld];
-    }
+    if (r0 < n)
+      for (int j = k0; j < n; j += kstep)
+        if (j != r0) off += A[r0 + j * ld] * A[r0 + j * ld];
     red[tid] = off;
     __syncthreads();
     for (int s = nt / 2; s > 0; s >>= 1) {
@@ -643,11 +655,11 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
         sn[k] = s;
       }
       __syncthreads();
-      for (int idx = tid; idx < n * (m / 2); idx += nt) {
-        const int r = idx % n, k = idx / n;
+      for (int k = k0; k < m / 2; k += kstep) {
         const int p = pp[k], q = qq[k];
         const float s = sn[k];
-        if (q >= n || s == 0.f) continue;
+        if (r0 >= n || q >= n || s == 0.f) continue;
+        const int r = r0;
         const float c = cs[k];
         const float ap = A[r + p * ld], aq = A[r + q * ld];
         A[r + p * ld] = c * ap - s * aq;
@@ -657,11 +669,11 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
         W[r + q * ld] = s * wp + c * wq;
       }
       __syncthreads();
-      for (int idx = tid; idx < n * (m / 2); idx += nt) {
-        const int col = idx % n, k = idx / n;
+      for (int k = k0; k < m / 2; k += kstep) {
         const int p = pp[k], q = qq[k];
         const float s = sn[k];
-        if (q >= n || s == 0.f) continue;
+        if (r0 >= n || q >= n || s == 0.f) continue;
+        const int col = r0;
         const float c = cs[k];
         const float ap = A[p + col * ld], aq = A[q + col * ld];
         A[p + col * ld] = c * ap - s * aq;
@@ -740,10 +752,12 @@ __global__ void __launch_bounds__(1024) cholesky_inverse_kernel(int n, double* A
     if (bad) break;
     for (int i = k + 1 + tid; i < n; i += nt) a(i, k) = a(i, k) / dkk;
     __syncthreads();
-    const int rows = n - k - 1;
-    for (long long idx = tid; idx < (long long)rows * rows; idx += nt) {
-      const int i = k + 1 + int(idx % rows), j = k + 1 + int(idx / rows);
-      if (j <= i) a(i, j) = fma(-a(i, k), a(j, k), a(i, j));
+    {
+      const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+      for (int j = k + 1 + warp; j < n; j += nw) {
+        const double ljk = a(j, k);
+        for (int i = j + lane; i < n; i += 32) a(i, j) = fma(-a(i, k), ljk, a(i, j));
+      }
     }
     __syncthreads();
   }
@@ -752,10 +766,8 @@ __global__ void __launch_bounds__(1024) cholesky_inverse_kernel(int n, double* A
     return;
   }
   // zero the strict upper triangle
-  for (long long idx = tid; idx < (long long)n * n; idx += nt) {
-    const int i = int(idx % n), j = int(idx / n);
-    if (i < j) a(i, j) = 0.0;
-  }
+  for (int j = tid >> 5; j < n; j += nt >> 5)
+    for (int i = tid & 31; i < j; i += 32) a(i, j) = 0.0;
   __syncthreads();
   // inverse of lower-triangular L, column by column from the right:
   // for j = n-1..0: L^{-1}(j,j) = 1/L(j,j); L^{-1}(i,j) = -(sum_{k=j+1..i} L^{-1}(i,k) L(k,j)) / L(j,j)

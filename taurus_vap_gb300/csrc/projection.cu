@@ -313,8 +313,8 @@ __global__ void traces_kernel(int n, int G, const double2* __restrict__ rho, con
   double2 a[9];
   for (int q = 0; q < 9; ++q) a[q] = make_double2(0.0, 0.0);
   auto at = [G, n, b](const double2* X, int i, int j) { return X[(size_t(i) + size_t(j) * n) * G + b]; };
-  for (size_t e = tid; e < size_t(n) * n; e += nt) {
-    const int i = int(e % n), j = int(e / n);
+  for (int e = tid; e < n * n; e += nt) {
+    const int j = e / n, i = e - j * n;
     const double2 rij = at(rho, i, j), rji = at(rho, j, i);
     if (i == j) {
       if (i < h)
@@ -484,10 +484,10 @@ __global__ void __launch_bounds__(kLsThreads)
   const int tid = threadIdx.x, nt = blockDim.x;
   const double2* Ap = static_cast<const double2*>(Av.p);
   const double2* Bp = static_cast<const double2*>(Bv.p);
-  for (size_t idx = tid; idx < size_t(m) * w; idx += nt) {
-    const int r = int(idx % m), c = int(idx / m);
-    W[idx] = (c < m) ? Ap[r * Av.rs + c * Av.cs + b * Av.bs] : Bp[r * Bv.rs + (c - m) * Bv.cs + b * Bv.bs];
-  }
+  for (int c = tid >> 5; c < w; c += nt >> 5)
+    for (int r = tid & 31; r < m; r += 32)
+      W[r + size_t(c) * m] =
+          (c < m) ? Ap[r * Av.rs + c * Av.cs + b * Av.bs] : Bp[r * Bv.rs + (c - m) * Bv.cs + b * Bv.bs];
   __syncthreads();
   bool singular = false;
   double logdet = 0.0;
@@ -543,16 +543,23 @@ __global__ void __launch_bounds__(kLsThreads)
     const double2 rp = (pv == 0.0) ? make_double2(0.0, 0.0) : crcp(piv);
     for (int i = kk + 1 + tid; i < m; i += nt) mult[i] = cmul(W[i + size_t(kk) * m], rp);
     __syncthreads();
-    const int rows = m - kk - 1, cols = w - kk - 1;
-    for (long long idx = tid; idx < (long long)rows * cols; idx += nt) {
-      const int i = kk + 1 + int(idx % rows), c = kk + 1 + int(idx / rows);
-      double2 v = W[i + size_t(c) * m];
-      const double2 mu = mult[i], r = prow[c];
-      v.x = fma(-mu.x, r.x, v.x);
-      v.x = fma(mu.y, r.y, v.x);
-      v.y = fma(-mu.x, r.y, v.y);
-      v.y = fma(-mu.y, r.x, v.y);
-      W[i + size_t(c) * m] = v;
+    // rank-1 update of rows kk+1.. over columns kk+1..w-1: one warp per column,
+    // lanes over rows (column-major: coalesced), no index division
+    {
+      const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+      for (int c = kk + 1 + warp; c < w; c += nw) {
+        const double2 r = prow[c];
+        double2* col = W + size_t(c) * m;
+        for (int i = kk + 1 + lane; i < m; i += 32) {
+          double2 v = col[i];
+          const double2 mu = mult[i];
+          v.x = fma(-mu.x, r.x, v.x);
+          v.x = fma(mu.y, r.y, v.x);
+          v.y = fma(-mu.x, r.y, v.y);
+          v.y = fma(-mu.y, r.x, v.y);
+          col[i] = v;
+        }
+      }
     }
     __syncthreads();
   }
@@ -564,25 +571,31 @@ __global__ void __launch_bounds__(kLsThreads)
       prow[c] = y;
     }
     __syncthreads();
-    for (long long idx = tid; idx < (long long)kk * k; idx += nt) {
-      const int i = int(idx % kk), c = int(idx / kk);
-      double2 v = W[i + size_t(m + c) * m];
-      const double2 mu = W[i + size_t(kk) * m], r = prow[c];
-      v.x = fma(-mu.x, r.x, v.x);
-      v.x = fma(mu.y, r.y, v.x);
-      v.y = fma(-mu.x, r.y, v.y);
-      v.y = fma(-mu.y, r.x, v.y);
-      W[i + size_t(m + c) * m] = v;
+    {
+      const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+      for (int c = warp; c < k; c += nw) {
+        const double2 r = prow[c];
+        double2* col = W + size_t(m + c) * m;
+        for (int i = lane; i < kk; i += 32) {
+          double2 v = col[i];
+          const double2 mu = W[i + size_t(kk) * m];
+          v.x = fma(-mu.x, r.x, v.x);
+          v.x = fma(mu.y, r.y, v.x);
+          v.y = fma(-mu.x, r.y, v.y);
+          v.y = fma(-mu.y, r.x, v.y);
+          col[i] = v;
+        }
+      }
     }
     __syncthreads();
   }
   if (X) {
-    for (size_t idx = tid; idx < size_t(m) * k; idx += nt) {
-      const int r = int(idx % m), c = int(idx / m);
-      double2 v = W[r + size_t(m + c) * m];
-      if (conj_out) v.y = -v.y;
-      X[r * xrs + c * xcs + b * xbs] = v;
-    }
+    for (int c = tid >> 5; c < k; c += nt >> 5)
+      for (int r = tid & 31; r < m; r += 32) {
+        double2 v = W[r + size_t(m + c) * m];
+        if (conj_out) v.y = -v.y;
+        X[r * xrs + c * xcs + b * xbs] = v;
+      }
   }
   if (tid == 0) {
     if (det) {
@@ -1030,6 +1043,7 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
       g.alpha = make_double2(1.0, 0.0);
       g.beta = make_double2(1.0, 0.0);
       g.three_m = true;
+      g.upper_only = true;  // the Pfaffian reads the upper triangle only
       if ((rc = gemm(g, s2))) return rc;
       sec_end_on(c, SEC_OVERLAP, s2);
       sec_begin_on(c, SEC_PFAFFIAN, s2);

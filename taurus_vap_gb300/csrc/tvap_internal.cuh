@@ -92,7 +92,8 @@ struct GemmArgs {
   const double2* alpha_vec;
   bool a_real, b_real, c_real;
   bool conj_a, conj_b;
-  bool three_m;  // complex x complex with three real products (3M)
+  bool three_m;     // complex x complex with three real products (3M)
+  bool upper_only;  // square tiles strictly below the diagonal are skipped
 };
 int gemm(const GemmArgs& g, cudaStream_t s);
 

@@ -199,3 +199,27 @@ def test_warm_started_canonical_basis(emax4):
         Z = 1e-3 * rng.normal(size=(n, n))
         Z = Z - Z.T
         U, V = ctx.evolve(U, V, Z)
+
+
+def test_autograd_function_matches_finite_differences(sd):
+    torch = pytest.importorskip("torch")
+    from taurus_vap_gb300.autograd import projected_energy
+
+    mdl, U, V = sd
+    n = mdl.n
+    ctx = Context(mdl.basis, mdl.ham)
+    rng = np.random.default_rng(12)
+    Z0 = 0.05 * rng.normal(size=(n, n))
+    Z0 = Z0 - Z0.T
+    # the Thouless matrix enters in Fortran order: pass Z as the (n, n) array
+    # whose [i, j] is Z(i, j)
+    Z = torch.tensor(Z0, dtype=torch.float64, requires_grad=True)
+    E = projected_energy(Z, ctx, U, V, 5, 5, 4, 4)
+    E.backward()
+    D = rng.normal(size=(n, n))
+    D = D - D.T
+    h = 1e-5
+    Ep = projected_energy(torch.tensor(Z0 + h * D), ctx, U, V, 5, 5, 4, 4).item()
+    Em = projected_energy(torch.tensor(Z0 - h * D), ctx, U, V, 5, 5, 4, 4).item()
+    fd = (Ep - Em) / (2 * h)
+    assert abs(fd - float((Z.grad.numpy() * D).sum())) < 1e-6 * max(1.0, abs(fd))
