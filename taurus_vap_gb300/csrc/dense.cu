@@ -471,7 +471,14 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
     for (int round = 0; round < m - 1; ++round) {
       // pairs (pairs[k], pairs[m-1-k]) for k < m/2
       for (int k = tid; k < m / 2; k += nt) {
-        int p = pairs[k], q = pairs[m - 1 - k];
+        int p, q;
+        if (k == 0) {
+          p = round;
+          q = m - 1;
+        } else {
+          p = (round + k) % (m - 1);
+          q = (round - k + (m - 1)) % (m - 1);
+        }
         if (p > q) {
           const int t = p;
           p = q;
@@ -517,13 +524,6 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
         const T ap = Ael(p, col), aq = Ael(q, col);
         Ael(p, col) = c * ap - s * aq;
         Ael(q, col) = s * ap + c * aq;
-      }
-      __syncthreads();
-      // rotate the round-robin schedule (slot 0 fixed)
-      if (tid == 0) {
-        const int last = pairs[m - 1];
-        for (int i = m - 1; i > 1; --i) pairs[i] = pairs[i - 1];
-        pairs[1] = last;
       }
       __syncthreads();
     }
@@ -633,7 +633,15 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
     if (done) break;
     for (int round = 0; round < m - 1; ++round) {
       for (int k = tid; k < m / 2; k += nt) {
-        int p = pairs[k], q = pairs[m - 1 - k];
+        // circle method: player m-1 fixed, the others rotate with the round
+        int p, q;
+        if (k == 0) {
+          p = round;
+          q = m - 1;
+        } else {
+          p = (round + k) % (m - 1);
+          q = (round - k + (m - 1)) % (m - 1);
+        }
         if (p > q) {
           const int t = p;
           p = q;
@@ -678,12 +686,6 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
         const float ap = A[p + col * ld], aq = A[q + col * ld];
         A[p + col * ld] = c * ap - s * aq;
         A[q + col * ld] = s * ap + c * aq;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        const int last = pairs[m - 1];
-        for (int i = m - 1; i > 1; --i) pairs[i] = pairs[i - 1];
-        pairs[1] = last;
       }
       __syncthreads();
     }

@@ -139,28 +139,44 @@ int ws_ensure(tvap_ctx* c, int G) {
 __global__ void canon_kernel(int n, const double* __restrict__ rhoc, const double* __restrict__ kapc, double eps,
                              int allemp, int* canon_i, double* canon_d) {
   __shared__ int submax[1024];
-  __shared__ int s_nocc, s_nemp;
+  __shared__ double rd[256];
+  __shared__ int ri[3][256];
+  __shared__ int s_nocc, s_nemp, s_nlow, s_bad;
   const int tid = threadIdx.x, nt = blockDim.x;
-  if (tid == 0) {
-    int nocc = 0, nemp = 0;
-    double ovac = 0.0;
-    for (int i = 0; i < n; ++i) {
-      const double v2 = fabs(rhoc[i + size_t(i) * n]);
-      const double u = sqrt(fabs(1.0 - v2));
-      if (v2 >= 1.0 - eps)
-        ++nocc;
-      else if (v2 <= eps && allemp == 0)
-        ++nemp;
-      else
-        ovac += log(u);
+  // occupation counts and ovac = sum log u over paired states (parallel)
+  double ov = 0.0;
+  int cocc = 0, cemp = 0, clow = 0;
+  for (int i = tid; i < n; i += nt) {
+    const double v2 = fabs(rhoc[i + size_t(i) * n]);
+    if (v2 >= 1.0 - eps)
+      ++cocc;
+    else if (v2 <= eps && allemp == 0)
+      ++cemp;
+    else
+      ov += log(sqrt(fabs(1.0 - v2)));
+    if (v2 <= eps) ++clow;
+  }
+  rd[tid] = ov;
+  ri[0][tid] = cocc;
+  ri[1][tid] = cemp;
+  ri[2][tid] = clow;
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s) {
+      rd[tid] += rd[tid + s];
+      for (int q = 0; q < 3; ++q) ri[q][tid] += ri[q][tid + s];
     }
-    if (n - nocc - nemp == 0) ovac = 0.0;
-    s_nocc = nocc;
-    s_nemp = nemp;
-    canon_d[0] = ovac;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    s_nocc = ri[0][0];
+    s_nemp = ri[1][0];
+    s_nlow = ri[2][0];
+    s_bad = 0;
+    canon_d[0] = (n - s_nocc - s_nemp == 0) ? 0.0 : rd[0];
   }
   __syncthreads();
-  const int nocc = s_nocc, nemp = s_nemp;
+  const int nocc = s_nocc, nemp = s_nemp, nlow = s_nlow;
   // submax (1-based indices as in the reference)
   for (int i = 1 + nemp + tid; i <= n - nocc; i += nt) {
     int sm = i;
@@ -170,7 +186,6 @@ __global__ void canon_kernel(int n, const double* __restrict__ rhoc, const doubl
   }
   __syncthreads();
   if (tid == 0) {
-    int bad = 0;
     // subspace dimensions (the reference merges overlapping ranges)
     int k = 1 + nemp;
     while (k < n - nocc) {
@@ -184,46 +199,64 @@ __global__ void canon_kernel(int n, const double* __restrict__ rhoc, const doubl
     while (k < n - nocc) {
       int d = submax[k] - k + 1;
       if (d > 2 && (d % 2) != 0) d = 2;
-      if (d > 2) bad = 1;  // the reference would Schur-reduce this block (DGEES)
+      if (d > 2) s_bad = 1;  // the reference would Schur-reduce this block (DGEES)
       k += d;
     }
-    // v/u with the sign of kappa in the canonical basis
-    double* vu = canon_d + 8;
-    for (int i = 0; i < n; ++i) vu[i] = 0.0;
-    int kk = 0, j = 1;
-    for (int i = 1; i <= n; ++i) {
-      const double v2 = fabs(rhoc[(i - 1) + size_t(i - 1) * n]);
-      const double v = sqrt(v2), u = sqrt(fabs(1.0 - v2));
-      double vc = 0.0;  // zVc(i, i+1) or zVc(i, i-1)
-      const bool paired = !(v2 > 1.0 - eps) && !(v2 <= eps);
-      if (paired) {
-        if (kk % 2 == 0)
-          vc = (i < n) ? copysign(v, kapc[(i - 1) + size_t(i) * n]) : 0.0;
-        else
-          vc = copysign(v, kapc[(i - 1) + size_t(i - 2) * n]);
-        ++kk;
-      }
-      if (i >= 1 + nemp && i <= n - nocc) {
-        // the reference reads zVc(i,i+1) for odd j and zVc(i,i-1) for even j
-        vu[i - 1] = paired ? vc / u : 0.0;
-        ++j;
-      }
+    if ((n - nocc - nemp) % 2 != 0) s_bad = 1;
+  }
+  __syncthreads();
+  // v/u with the sign of kappa in the canonical basis; the paired states are
+  // contiguous after the nlow states with v^2 <= eps, so the reference's
+  // running counter k of paired states is i - 1 - nlow
+  double* vu = canon_d + 8;
+  for (int i = 1 + tid; i <= n; i += nt) {
+    const double v2 = fabs(rhoc[(i - 1) + size_t(i - 1) * n]);
+    const double v = sqrt(v2), u = sqrt(fabs(1.0 - v2));
+    const bool paired = !(v2 > 1.0 - eps) && !(v2 <= eps);
+    double val = 0.0;
+    if (i >= 1 + nemp && i <= n - nocc) {
+      // zVc(i, i+1) / zVc(i, i-1) as construct_canonical_basis places them
+      // (running count kk of paired states), read back with the parity of
+      // j = i - nemp as project_wavefunction does
+      const int kk = i - 1 - nlow;
+      const double vplus = (paired && kk % 2 == 0 && i < n) ? copysign(v, kapc[(i - 1) + size_t(i) * n]) : 0.0;
+      const double vminus = (paired && kk % 2 == 1) ? copysign(v, kapc[(i - 1) + size_t(i - 2) * n]) : 0.0;
+      const int j = i - nemp;
+      val = ((j % 2) == 1 ? vplus : vminus) / u;
     }
-    const int nbloc = n - nocc - nemp;
-    if (nbloc % 2 != 0) bad = 1;
-    // Pf(A1) = prod over odd i of vu(i + nemp), as (log|.|, sign)
-    double lp = 0.0, sg = 1.0;
-    for (int i = 1; i <= nbloc - 1; i += 2) {
-      const double a = vu[i + nemp - 1];
-      if (a == 0.0) bad = 1;
+    vu[i - 1] = val;
+  }
+  __syncthreads();
+  // Pf(A1) = prod over odd i of vu(i + nemp), as (log|.|, sign)
+  const int nbloc = n - nocc - nemp;
+  double lp = 0.0;
+  int neg = 0, zero = 0;
+  for (int i = 1 + 2 * tid; i <= nbloc - 1; i += 2 * nt) {
+    const double a = vu[i + nemp - 1];
+    if (a == 0.0)
+      zero = 1;
+    else
       lp += log(fabs(a));
-      if (a < 0.0) sg = -sg;
+    if (a < 0.0) neg ^= 1;
+  }
+  rd[tid] = lp;
+  ri[0][tid] = neg;
+  ri[1][tid] = zero;
+  __syncthreads();
+  for (int s = nt / 2; s > 0; s >>= 1) {
+    if (tid < s) {
+      rd[tid] += rd[tid + s];
+      ri[0][tid] ^= ri[0][tid + s];
+      ri[1][tid] |= ri[1][tid + s];
     }
-    canon_d[1] = lp;
-    canon_d[2] = sg;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    canon_d[1] = rd[0];
+    canon_d[2] = ri[0][0] ? -1.0 : 1.0;
     canon_i[0] = nocc;
     canon_i[1] = nemp;
-    canon_i[2] = bad;
+    canon_i[2] = s_bad | ri[1][0];
   }
 }
 
@@ -750,66 +783,86 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
   // X orthonormal and X^T A X block diagonal over clusters <=> invariant subspaces
   if (tid == 0 && (red[0] > 1.0e-12 * fmax(nA, 1e-300) || rscal[3] > 1.0e-12 * sqrt(double(n)))) fail = 1;
   __syncthreads();
-  // per cluster: Jacobi on the cluster block, rotate the columns
+  // per cluster: Jacobi on the cluster block (lane 0), then the warp rotates
+  // the cluster's columns of X into D
   constexpr int CM = 8;
-  for (int c = tid; c < ncl; c += nt) {
-    const int k0 = cl_start[c], m = cl_start[c + 1] - k0;
-    if (m > CM) {
-      atomicOr(&fail, 1);
-      continue;
+  __shared__ double qsh[8][CM * CM];
+  __shared__ double lsh[8][CM];
+  __shared__ int osh[8][CM];
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  for (int cbase = 0; cbase < ncl; cbase += nwarp) {
+    const int c = cbase + warp;
+    int k0 = 0, m = 0;
+    if (c < ncl) {
+      k0 = cl_start[c];
+      m = cl_start[c + 1] - k0;
     }
-    double a[CM][CM], q[CM][CM];
-    for (int r = 0; r < m; ++r)
-      for (int t = 0; t < m; ++t) {
-        a[r][t] = S[perm[k0 + r] + size_t(perm[k0 + t]) * n];
-        q[r][t] = (r == t) ? 1.0 : 0.0;
-      }
-    for (int sweep = 0; sweep < 30 && m > 1; ++sweep) {
-      double off = 0.0;
-      for (int r = 0; r < m; ++r)
-        for (int t = r + 1; t < m; ++t) off += a[r][t] * a[r][t];
-      if (off == 0.0) break;
-      for (int pp = 0; pp < m; ++pp)
-        for (int qq = pp + 1; qq < m; ++qq) {
-          if (a[pp][qq] == 0.0) continue;
-          const double theta = (a[qq][qq] - a[pp][pp]) / (2.0 * a[pp][qq]);
-          const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-          const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
-          for (int r = 0; r < m; ++r) {
-            const double ap = a[r][pp], aq = a[r][qq];
-            a[r][pp] = cs * ap - sn * aq;
-            a[r][qq] = sn * ap + cs * aq;
+    if (c < ncl && lane == 0) {
+      if (m > CM) {
+        atomicOr(&fail, 1);
+      } else {
+        double a[CM][CM], q[CM][CM];
+        for (int r = 0; r < m; ++r)
+          for (int t = 0; t < m; ++t) {
+            a[r][t] = S[perm[k0 + r] + size_t(perm[k0 + t]) * n];
+            q[r][t] = (r == t) ? 1.0 : 0.0;
           }
-          for (int r = 0; r < m; ++r) {
-            const double ap = a[pp][r], aq = a[qq][r];
-            a[pp][r] = cs * ap - sn * aq;
-            a[qq][r] = sn * ap + cs * aq;
-          }
-          for (int r = 0; r < m; ++r) {
-            const double qp = q[r][pp], qv = q[r][qq];
-            q[r][pp] = cs * qp - sn * qv;
-            q[r][qq] = sn * qp + cs * qv;
-          }
+        for (int sweep = 0; sweep < 30 && m > 1; ++sweep) {
+          double off = 0.0;
+          for (int r = 0; r < m; ++r)
+            for (int t = r + 1; t < m; ++t) off += a[r][t] * a[r][t];
+          if (off == 0.0) break;
+          for (int pp = 0; pp < m; ++pp)
+            for (int qq = pp + 1; qq < m; ++qq) {
+              if (a[pp][qq] == 0.0) continue;
+              const double theta = (a[qq][qq] - a[pp][pp]) / (2.0 * a[pp][qq]);
+              const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+              const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+              for (int r = 0; r < m; ++r) {
+                const double ap = a[r][pp], aq = a[r][qq];
+                a[r][pp] = cs * ap - sn * aq;
+                a[r][qq] = sn * ap + cs * aq;
+              }
+              for (int r = 0; r < m; ++r) {
+                const double ap = a[pp][r], aq = a[qq][r];
+                a[pp][r] = cs * ap - sn * aq;
+                a[qq][r] = sn * ap + cs * aq;
+              }
+              for (int r = 0; r < m; ++r) {
+                const double qp = q[r][pp], qv = q[r][qq];
+                q[r][pp] = cs * qp - sn * qv;
+                q[r][qq] = sn * qp + cs * qv;
+              }
+            }
         }
-    }
-    // order inside the cluster by the diagonalised values
-    int ord[CM];
-    for (int r = 0; r < m; ++r) ord[r] = r;
-    for (int r = 1; r < m; ++r)
-      for (int t = r; t > 0 && a[ord[t]][ord[t]] < a[ord[t - 1]][ord[t - 1]]; --t) {
-        const int x = ord[t];
-        ord[t] = ord[t - 1];
-        ord[t - 1] = x;
-      }
-    for (int r = 0; r < m; ++r) {
-      const int src = ord[r];
-      evals[k0 + r] = a[src][src];
-      for (int row = 0; row < n; ++row) {
-        double v = 0.0;
-        for (int t = 0; t < m; ++t) v = fma(X[row + size_t(perm[k0 + t]) * n], q[t][src], v);
-        D[row + size_t(k0 + r) * n] = v;
+        int ord[CM];
+        for (int r = 0; r < m; ++r) ord[r] = r;
+        for (int r = 1; r < m; ++r)
+          for (int t = r; t > 0 && a[ord[t]][ord[t]] < a[ord[t - 1]][ord[t - 1]]; --t) {
+            const int x = ord[t];
+            ord[t] = ord[t - 1];
+            ord[t - 1] = x;
+          }
+        for (int r = 0; r < m; ++r) {
+          osh[warp][r] = ord[r];
+          lsh[warp][r] = a[ord[r]][ord[r]];
+          for (int t = 0; t < m; ++t) qsh[warp][t * CM + r] = q[t][r];
+        }
       }
     }
+    __syncwarp();
+    if (c < ncl && m <= CM) {
+      for (int r = 0; r < m; ++r) {
+        const int src = osh[warp][r];
+        if (lane == 0) evals[k0 + r] = lsh[warp][r];
+        for (int row = lane; row < n; row += 32) {
+          double v = 0.0;
+          for (int t = 0; t < m; ++t) v = fma(X[row + size_t(perm[k0 + t]) * n], qsh[warp][t * CM + src], v);
+          D[row + size_t(k0 + r) * n] = v;
+        }
+      }
+    }
+    __syncwarp();
   }
   __syncthreads();
   if (tid == 0) rflag[0] = fail;
