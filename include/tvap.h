@@ -93,6 +93,12 @@ int tvap_kernel_launches(const tvap_ctx* ctx);
  * Pfaffian, sums, gradient, evolve).  tvap_set_timing resets the totals;
  * tvap_get_timing returns milliseconds and call counts per section. */
 int tvap_set_timing(tvap_ctx* ctx, int on);
+/* Arithmetic of the dense products: 0 = the FP64 pipe (DFMA);
+ * 1 (default) = FP64 emulated on the bf16 tensor cores by exact integer
+ * splitting (8 balanced 7-bit digits per FP64 value, exact FP32 partial sums,
+ * FP64 recombination).  The sparse field contraction, the factorisations and
+ * all reductions run on the FP64 pipe in both modes. */
+int tvap_set_gemm_mode(tvap_ctx* ctx, int mode);
 int tvap_get_timing(tvap_ctx* ctx, double* ms, long long* calls, int nsec);
 
 /* One upload of the reduced two-body list and the one-body part:

@@ -29,6 +29,7 @@ GPU_SOURCES = [
     "dense.cu",
     "projection.cu",
     "gradient.cu",
+    "ozaki.cu",
 ]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -155,6 +155,7 @@ int tvap_calculate_gradient(tvap_ctx* c, const double* H20v, int cdim, const dou
 int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z, double* U1, double* V1) {
   if (!c || !U0 || !V0 || !Z || !U1 || !V1) return TVAP_ERR_ARG;
   c->kernel_launches = 0;
+  g_gemm_mode = c->gemm_mode;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;
@@ -190,6 +191,7 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
   int rc;
   if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
   c->kernel_launches = 0;
+  g_gemm_mode = c->gemm_mode;
   double* buf = nullptr;
   TVAP_CUDA(cudaMalloc(&buf, sizeof(double) * (7 * nn + n)));
   EvolveBuf b;

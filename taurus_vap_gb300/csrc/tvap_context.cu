@@ -115,6 +115,12 @@ int tvap_set_timing(tvap_ctx* c, int on) {
   return TVAP_OK;
 }
 
+int tvap_set_gemm_mode(tvap_ctx* c, int mode) {
+  if (!c || (mode != 0 && mode != 1)) return TVAP_ERR_ARG;
+  c->gemm_mode = mode;
+  return TVAP_OK;
+}
+
 int tvap_get_timing(tvap_ctx* c, double* ms, long long* calls, int nsec) {
   if (!c || !ms) return TVAP_ERR_ARG;
   collect_sections(c);
@@ -293,6 +299,7 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   if (!c || !U0 || !V0 || !opts || opts->Mphip < 1 || opts->Mphin < 1) return TVAP_ERR_ARG;
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   c->kernel_launches = 0;
+  g_gemm_mode = c->gemm_mode;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   int rc;

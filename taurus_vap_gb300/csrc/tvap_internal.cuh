@@ -96,6 +96,11 @@ struct GemmArgs {
   bool upper_only;  // square tiles strictly below the diagonal are skipped
 };
 int gemm(const GemmArgs& g, cudaStream_t s);
+// the same product with the FP64 arithmetic emulated on the bf16 tensor cores
+int gemm_ozaki(const GemmArgs& g, cudaStream_t s);
+// GEMM arithmetic of the calls in flight: 0 FP64 pipe, 1 emulated (set by
+// every C-ABI entry point from its context)
+extern int g_gemm_mode;
 
 // ---------------------------------------------------------------------------
 // Hamiltonian in gather form (built once from the reference's element list)
@@ -145,6 +150,7 @@ struct tvap_ctx {
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
   int kernel_launches = 0;  // launches issued by the last top-level call
+  int gemm_mode = 1;        // 0: FP64 pipe, 1: FP64 emulated on the bf16 tensor cores
   // optional section timing with CUDA events on the context's stream
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;

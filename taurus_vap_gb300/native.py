@@ -76,6 +76,8 @@ def lib():
         L.tvap_set_timing.restype = ci
         L.tvap_get_timing.argtypes = [vp, vp, vp, ci]
         L.tvap_get_timing.restype = ci
+        L.tvap_set_gemm_mode.argtypes = [vp, ci]
+        L.tvap_set_gemm_mode.restype = ci
         L.tvap_set_hamiltonian.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp, vp]
         L.tvap_set_hamiltonian.restype = ci
         L.tvap_calculate_fields.argtypes = [vp] * 8
@@ -149,6 +151,13 @@ class Context:
         calls = np.zeros(16, dtype=np.int64)
         _check(lib().tvap_get_timing(self.h, _p(ms), _p(calls), 16), "tvap_get_timing")
         return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(self.SECTIONS)}
+
+    GEMM_FP64, GEMM_EMULATED = 0, 1
+
+    def set_gemm_mode(self, mode: int):
+        """0: dense products on the FP64 pipe; 1 (default): FP64 emulated on
+        the bf16 tensor cores."""
+        _check(lib().tvap_set_gemm_mode(self.h, int(mode)), "tvap_set_gemm_mode")
 
     def set_stream(self, stream_handle: int):
         lib().tvap_set_stream(self.h, ctypes.c_void_p(stream_handle))

@@ -87,11 +87,12 @@ def test_calculate_fields_batched(emax2):
             assert relerr(got[q][c], ref[q]) < FIELD_TOL
 
 
-def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0):
+def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0, gemm_mode=1):
     om = O.OracleModel(mdl)
     ref = om.project(U, V, Mp, Mn, 2 * np.pi, Z, N, nthreads=nthreads)
     assert ref["status"] == 0
     ctx = Context(mdl.basis, mdl.ham)
+    ctx.set_gemm_mode(gemm_mode)
     pnp, H20v = ctx.project(U, V, Mp, Mn, 2 * np.pi, Z, N, mode=mode)
     rp = ref["pnp"]
     e_ref = (rp.c("ener") / rp.c("over")).real
@@ -104,14 +105,16 @@ def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0):
     return pnp, H20v
 
 
+@pytest.mark.parametrize("gemm_mode", [0, 1])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_project_sd(sd, mode):
+def test_project_sd(sd, mode, gemm_mode):
     mdl, U, V = sd
-    check_projection(mdl, U, V, 9, 9, 4, 4, mode)
+    check_projection(mdl, U, V, 9, 9, 4, 4, mode, gemm_mode=gemm_mode)
 
 
-def test_project_mg24_usdb(usdb_model, mg24_seed):
-    check_projection(usdb_model, *mg24_seed, 5, 5, 4, 4, 0)
+@pytest.mark.parametrize("gemm_mode", [0, 1])
+def test_project_mg24_usdb(usdb_model, mg24_seed, gemm_mode):
+    check_projection(usdb_model, *mg24_seed, 5, 5, 4, 4, 0, gemm_mode=gemm_mode)
 
 
 def test_project_even_angles(sd):
@@ -124,9 +127,25 @@ def test_project_emax2(emax2):
     check_projection(mdl, U, V, 5, 5, 4, 4, 0)
 
 
-def test_project_emax4_small_grid(emax4):
+@pytest.mark.parametrize("gemm_mode", [0, 1])
+def test_project_emax4_small_grid(emax4, gemm_mode):
     mdl, U, V = emax4
-    check_projection(mdl, U, V, 3, 3, 8, 8, 0)
+    check_projection(mdl, U, V, 3, 3, 8, 8, 0, gemm_mode=gemm_mode)
+
+
+def test_emulated_gemm_matches_fp64_pipe(emax4):
+    # the two arithmetic modes of the dense products agree to FP64 rounding
+    mdl, U, V = emax4
+    ctx = Context(mdl.basis, mdl.ham)
+    res = []
+    for gm in (0, 1):
+        ctx.set_gemm_mode(gm)
+        res.append(ctx.project(U, V, 5, 5, 2 * np.pi, 8, 8))
+    (p0, h0), (p1, h1) = res
+    e0 = (p0.c("ener") / p0.c("over")).real
+    e1 = (p1.c("ener") / p1.c("over")).real
+    assert abs(e0 - e1) < 1e-10 * max(1.0, abs(e0))
+    assert relerr(h1, h0) < 1e-11
 
 
 def test_plain_equals_batched(emax2):
