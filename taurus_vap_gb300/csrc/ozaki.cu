@@ -306,6 +306,19 @@ int oz_reserve(cudaStream_t s, size_t bytes, size_t ex_count, OzScratch** out) {
 
 }  // namespace
 
+// Frees the slice scratch of a stream (called when a context destroys or
+// replaces the stream).
+void oz_release(cudaStream_t s) {
+  std::lock_guard<std::mutex> lock(g_oz_mutex);
+  for (auto& e : g_oz)
+    if (e.buf && e.stream == s) {
+      cudaStreamSynchronize(s);
+      cudaFree(e.buf);
+      cudaFree(e.ex);
+      e = OzScratch();
+    }
+}
+
 // Returns TVAP_OK after launching, or TVAP_ERR_ARG when the shape is not
 // supported (the caller then uses the FP64 pipe).
 int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {

@@ -200,6 +200,8 @@ void tvap_destroy(tvap_ctx* c) {
     cudaEventDestroy(e.second.second);
   }
   for (auto e : c->ev_pool) cudaEventDestroy(e);
+  if (c->stream) oz_release(c->stream);
+  if (c->stream2) oz_release(c->stream2);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -209,6 +211,7 @@ void tvap_destroy(tvap_ctx* c) {
 
 int tvap_set_stream(tvap_ctx* c, void* stream) {
   if (!c) return TVAP_ERR_ARG;
+  if (c->stream) oz_release(c->stream);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   c->stream = static_cast<cudaStream_t>(stream);
   c->own_stream = false;

@@ -98,6 +98,7 @@ struct GemmArgs {
 int gemm(const GemmArgs& g, cudaStream_t s);
 // the same product with the FP64 arithmetic emulated on the bf16 tensor cores
 int gemm_ozaki(const GemmArgs& g, cudaStream_t s);
+void oz_release(cudaStream_t s);
 // GEMM arithmetic of the calls in flight: 0 FP64 pipe, 1 emulated (set by
 // every C-ABI entry point from its context)
 extern int g_gemm_mode;
