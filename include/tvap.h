@@ -140,6 +140,24 @@ int tvap_calculate_gradient(tvap_ctx* ctx, const double* H20v, int cdim, const d
  * V1 = (V0 + U0 Z) L^-T with L L^T = 1 + Z^T Z. */
 int tvap_evolve(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z, double* U1, double* V1);
 
+/* tvap_evolve for callers that cannot allocate device memory: the same
+ * Thouless evolution, with every matrix (U0, V0, Z in; U1, V1 out) in device
+ * memory and the work buffers taken from a fixed array inside the library
+ * instead of cudaMalloc.  tvap_evolve allocates and frees its buffers on every
+ * call, and cudaFree waits for the whole device; a caller that keeps other
+ * work running on the GPU, or whose device memory is owned by its own pool
+ * allocator, cannot accept that.  No counterpart in the reference.
+ *   - limit: n <= 336 (the array holds 3 n^2 + n doubles for n = 336, about
+ *     2.6 MB, kept on every GPU that loads the library until the process ends);
+ *     larger n is rejected with TVAP_ERR_ARG;
+ *   - the first call on a device looks up the array's device address; make
+ *     that first call before any stream capture;
+ *   - all calls share the array: calls that overlap on the GPU (from several
+ *     contexts or streams at once) race on it;
+ *   - the dense products run on the FP64 pipe in this variant;
+ *   - the context's device must be the current device. */
+int tvap_evolve_noalloc(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z, double* U1, double* V1);
+
 /* Adjoint of the projected energy E(Z) = <Phi(Z)|H P|Phi(Z)>/<Phi(Z)|P|Phi(Z)>
  * of the state Phi(Z) = evolve(U0, V0, Z) with respect to the real Thouless
  * matrix Z: writes E and dE/dZ (n*n reals).  The per-angle densities are

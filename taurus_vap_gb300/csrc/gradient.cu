@@ -109,6 +109,52 @@ double* ws_U(tvap_ctx* c);
 double* ws_V(tvap_ctx* c);
 double* ws_H20v(tvap_ctx* c);
 
+// ---------------------------------------------------------------------------
+// Scratch of tvap_evolve_noalloc: a file-scope device array, so that the
+// entry point never allocates.  Layout for a basis of n states:
+// L (n*n + n: the Cholesky factor and its scratch row), A1 (n*n), A2 (n*n).
+// Every GPU that loads this library holds the array until the process exits.
+// ---------------------------------------------------------------------------
+constexpr int kNoallocMaxN = 336;
+constexpr size_t kNoallocScratchDoubles = 3 * size_t(kNoallocMaxN) * kNoallocMaxN + kNoallocMaxN;
+static __device__ __align__(256) double g_noalloc_scratch[kNoallocScratchDoubles];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device, looked up once
+// per device with that device current (the host-side symbol is only a
+// stand-in, not a device address).
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  TVAP_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_last_error("tvap_evolve_noalloc: device ordinal out of range", __FILE__, __LINE__);
+    return TVAP_ERR_ARG;
+  }
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    TVAP_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return TVAP_OK;
+}
+
+bool is_device_pointer(const void* p) {
+  cudaPointerAttributes at{};
+  const cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
 }  // namespace tvap
 
 using namespace tvap;
@@ -179,6 +225,61 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   if (!rc) rc = check_flags(c);
   cudaFree(buf);
   return rc;
+}
+
+int tvap_evolve_noalloc(tvap_ctx* c, const double* U0, const double* V0, const double* Z, double* U1, double* V1) {
+  if (!c || !U0 || !V0 || !Z || !U1 || !V1) return TVAP_ERR_ARG;
+  const int n = c->n;
+  if (n > kNoallocMaxN) {
+    set_last_error("tvap_evolve_noalloc: basis larger than the static scratch (n > 336)", __FILE__, __LINE__);
+    return TVAP_ERR_ARG;
+  }
+  if (!is_device_pointer(U0) || !is_device_pointer(V0) || !is_device_pointer(Z) || !is_device_pointer(U1) ||
+      !is_device_pointer(V1)) {
+    set_last_error("tvap_evolve_noalloc: all matrices must be device memory", __FILE__, __LINE__);
+    return TVAP_ERR_ARG;
+  }
+  int dev = 0;
+  TVAP_CUDA(cudaGetDevice(&dev));
+  if (dev != c->device) {
+    set_last_error("tvap_evolve_noalloc: the context's device must be current", __FILE__, __LINE__);
+    return TVAP_ERR_ARG;
+  }
+  double* scratch = nullptr;
+  int rc;
+  if ((rc = noalloc_scratch(&scratch))) return rc;
+  c->kernel_launches = 0;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  double* L = scratch;               // n*n + n
+  double* A1 = scratch + nn + n;     // n*n
+  double* A2 = A1 + nn;              // n*n
+  // dense products on the FP64 pipe: the emulated GEMM would need slice buffers
+  const int saved_mode = g_gemm_mode;
+  g_gemm_mode = 0;
+  const View Zv = view_cm(Z, n, 0);
+  rc = rgemm(n, n, n, view_t(Zv), Zv, L, n, 1.0, 0.0, s);  // Z^T Z (every entry written)
+  if (!rc) {
+    add_identity_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, L);
+    rc = cholesky_inverse(n, L, c->d_flags, s);
+  }
+  if (!rc) {
+    const cudaError_t e1 = cudaMemcpyAsync(A1, U0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s);
+    const cudaError_t e2 = cudaMemcpyAsync(A2, V0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      set_last_error(cudaGetErrorString(e1 != cudaSuccess ? e1 : e2), __FILE__, __LINE__);
+      rc = TVAP_ERR_CUDA;
+    }
+  }
+  if (!rc) rc = rgemm(n, n, n, view_cm(V0, n, 0), Zv, A1, n, 1.0, 1.0, s);
+  if (!rc) rc = rgemm(n, n, n, view_cm(U0, n, 0), Zv, A2, n, 1.0, 1.0, s);
+  const View LinvT = view_t(view_cm(L, n, 0));
+  if (!rc) rc = rgemm(n, n, n, view_cm(A1, n, 0), LinvT, U1, n, 1.0, 0.0, s);
+  if (!rc) rc = rgemm(n, n, n, view_cm(A2, n, 0), LinvT, V1, n, 1.0, 0.0, s);
+  g_gemm_mode = saved_mode;
+  if (rc) return rc;
+  c->kernel_launches += 8;
+  return check_flags(c);
 }
 
 int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const double* Z,

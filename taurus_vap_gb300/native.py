@@ -90,6 +90,8 @@ def lib():
         L.tvap_calculate_gradient.restype = ci
         L.tvap_evolve.argtypes = [vp] * 6
         L.tvap_evolve.restype = ci
+        L.tvap_evolve_noalloc.argtypes = [vp] * 6
+        L.tvap_evolve_noalloc.restype = ci
         L.tvap_energy_adjoint.argtypes = [vp, vp, vp, vp, ctypes.POINTER(TvapProjOpts), vp, vp]
         L.tvap_energy_adjoint.restype = ci
         _lib = L
