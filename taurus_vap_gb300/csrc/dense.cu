@@ -257,7 +257,10 @@ int g_gemm_mode = 1;
 
 int gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return TVAP_OK;
-  if (g_gemm_mode == 1 && g.K >= 16) return gemm_ozaki(g, s);
+  // the emulated product pays off for batched work; small single products
+  // (canonical-basis refinement, per-iteration blocks, evolution) stay on the
+  // FP64 pipe
+  if (g_gemm_mode == 1 && g.K >= 16 && double(g.M) * g.N * g.K * g.batch >= 2.0e7) return gemm_ozaki(g, s);
   switch (pick_tile(g.M, g.N)) {
     case 16: launch_gemm_tile<16>(g, s); break;
     case 24: launch_gemm_tile<24>(g, s); break;

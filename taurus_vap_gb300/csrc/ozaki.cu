@@ -12,17 +12,21 @@
 //     (d_0 most significant), using integer operations only;
 //   * every digit is exactly representable in bf16, every digit product
 //     (|d d'| <= 2^12) exactly in FP32, and the tensor core sums them in FP32;
-//     with K split in chunks of 128 a group of digit pairs of equal weight
-//     (s + t = g, at most 8 pairs) stays below 2^22, and the complex
-//     combination rr - ii below 2^23, so every FP32 group sum is exact;
+//     with K split in chunks of 64 a group of digit pairs of equal weight
+//     (s + t = g, at most 8 pairs) stays below 2^21, and the complex
+//     combination rr - ii below 2^22, so every FP32 group sum is exact;
 //   * pairs with s + t <= 7 are kept (the dropped ones weigh < 2^-56 of the
-//     leading term); each group sum is folded into an FP64 accumulator with its
-//     weight 2^(7 (14 - g)), and the result is scaled by 2^(e_i + f_j - 106).
+//     leading term); the group sums of each chunk are converted to integers
+//     and folded, with their weights 2^(7 (14 - g)), into two 64-bit integer
+//     accumulators per output, which are converted to FP64 once at the end and
+//     scaled by 2^(e_i + f_j - 106).
 //
-// The FP64 pipe then does ~4 operations per output and group and K-chunk
-// instead of 3-4 per multiply-add.  Complex operands carry real and imaginary
-// digit planes with a shared exponent per row/column; conjugation flips the
-// imaginary plane.
+// The FP64 pipe then does a few operations per output instead of 3-4 per
+// multiply-add.  Complex operands carry real and imaginary digit planes with a
+// shared exponent per row/column; conjugation flips the imaginary plane; a
+// complex x complex product takes three real products per digit pair
+// (rr, ii and (r + i)(r + i); digit sums |d_r + d_i| <= 128 stay exact in
+// bf16 and their products, summed over a chunk and a group, below 2^23).
 
 #include <cuda_bf16.h>
 
@@ -36,7 +40,6 @@ namespace {
 
 constexpr int kDigits = 8;
 constexpr int kKeep = 7;     // keep digit pairs with s + t <= kKeep
-constexpr int kChunk = 128;  // K chunk: FP32 group sums stay exact
 
 __device__ __forceinline__ int dexp(double x) {
   // unbiased exponent of a finite non-zero double (subnormals treated as 0)
@@ -126,6 +129,13 @@ __global__ void slice_kernel(int rows, int K, int rows_pad, int kpad, const void
   }
 }
 
+// element-wise sum of two bf16 pairs (exact for the small integers used here)
+__device__ __forceinline__ uint32_t bsum(uint32_t a, uint32_t b) {
+  __nv_bfloat162 x = *reinterpret_cast<__nv_bfloat162*>(&a), y = *reinterpret_cast<__nv_bfloat162*>(&b);
+  __nv_bfloat162 r = __hadd2(x, y);
+  return *reinterpret_cast<uint32_t*>(&r);
+}
+
 __device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -134,127 +144,207 @@ __device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// one warp computes a 16 x 16 output tile (two m16n8 sub-tiles); a CTA holds
-// 4 warps (32 x 32).  PA / PB: 1 real, 2 complex planes.
+// A CTA computes a 32 x 32 output tile with 8 warps, each warp one m16n8
+// sub-tile.  K is walked in chunks of 64: the chunk's 8 digit planes of A
+// (32 rows) and B (32 columns) are staged in shared memory once, and every
+// digit pair of the chunk goes to the tensor cores with the FP32 sums of all
+// 8 weight groups held in registers; at the end of each chunk the group sums
+// (exact integers) are folded into FP64.  PA / PB: 1 real, 2 complex planes.
+constexpr int kKc = 64;        // K chunk staged in shared memory
+constexpr int kRowPad = 8;     // bf16 padding per staged row (conflict-free fragment loads)
+constexpr int kLd = kKc + kRowPad;
+
 template <int PA, int PB>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256, 1)
     ozaki_mma_kernel(int M, int N, int K, int mpad, int npad, int kpad, const __nv_bfloat16* __restrict__ As,
                      const int* __restrict__ ea, const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb,
                      GemmArgs g) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  extern __shared__ __align__(16) __nv_bfloat16 sm[];
+  __nv_bfloat16* sA = sm;                                // [kDigits][PA][32][kLd]
+  __nv_bfloat16* sB = sm + size_t(kDigits) * PA * 32 * kLd;  // [kDigits][PB][32][kLd]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int gq = lane >> 2, tq = lane & 3;
   const int b = blockIdx.z;
-  const int m0 = blockIdx.y * 32 + (warp >> 1) * 16;
-  const int n0 = blockIdx.x * 32 + (warp & 1) * 16;
-  if (m0 >= mpad || n0 >= npad) return;
-  constexpr int CRE = (PA == 2 && PB == 2) ? 2 : 1;  // accumulators per output component
+  const int mt0 = blockIdx.y * 32, nt0 = blockIdx.x * 32;
+  const int wm = (warp >> 2) * 16, wn = (warp & 3) * 8;  // warp sub-tile inside the CTA tile
+  // products per digit pair: 3 (3M) for complex x complex, 2 mixed, 1 real
+  constexpr int NC = (PA == 2 && PB == 2) ? 3 : ((PA == 2 || PB == 2) ? 2 : 1);
+  constexpr int PAX = (PA == 2 && PB == 2) ? 3 : PA;  // fragment planes incl. the r + i sum
+  constexpr int PBX = (PA == 2 && PB == 2) ? 3 : PB;
   const size_t aplane = size_t(mpad) * kpad, bplane = size_t(npad) * kpad;
-  // FP64 accumulators: [sub-tile][element 0..3] for re and im
-  double cre[2][4], cim[2][4];
+  long long hre[4], lre[4], him[4], lim[4];
 #pragma unroll
-  for (int u = 0; u < 2; ++u)
+  for (int q = 0; q < 4; ++q) hre[q] = lre[q] = him[q] = lim[q] = 0;
+  for (int kc = 0; kc < kpad; kc += kKc) {
+    // ---- stage the chunk: 16-byte vectors, zero beyond kpad
+    {
+      const int vecs_per_row = kKc / 8;
+      const int totA = kDigits * PA * 32 * vecs_per_row;
+      for (int v = tid; v < totA; v += blockDim.x) {
+        const int kv = v % vecs_per_row, r = (v / vecs_per_row) % 32, dp = v / (vecs_per_row * 32);
+        const int k = kc + kv * 8;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (k < kpad) {
+          const int dgt = dp / PA, part = dp % PA;
+          val = *reinterpret_cast<const uint4*>(As + ((size_t(b) * kDigits + dgt) * PA + part) * aplane +
+                                                size_t(mt0 + r) * kpad + k);
+        }
+        *reinterpret_cast<uint4*>(sA + (size_t(dp) * 32 + r) * kLd + kv * 8) = val;
+      }
+      const int totB = kDigits * PB * 32 * vecs_per_row;
+      for (int v = tid; v < totB; v += blockDim.x) {
+        const int kv = v % vecs_per_row, r = (v / vecs_per_row) % 32, dp = v / (vecs_per_row * 32);
+        const int k = kc + kv * 8;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (k < kpad) {
+          const int dgt = dp / PB, part = dp % PB;
+          val = *reinterpret_cast<const uint4*>(Bs + ((size_t(b) * kDigits + dgt) * PB + part) * bplane +
+                                                size_t(nt0 + r) * kpad + k);
+        }
+        *reinterpret_cast<uint4*>(sB + (size_t(dp) * 32 + r) * kLd + kv * 8) = val;
+      }
+    }
+    __syncthreads();
+    float acc[kKeep + 1][NC][4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) cre[u][q] = cim[u][q] = 0.0;
-  for (int kc = 0; kc < kpad; kc += kChunk) {
-    const int kend = min(kpad, kc + kChunk);
-    for (int grp = 0; grp <= kKeep; ++grp) {
-      // FP32 group sums: [combo][sub-tile][4]
-      float acc[2 * CRE][2][4];
+    for (int gg = 0; gg <= kKeep; ++gg)
 #pragma unroll
-      for (int c = 0; c < 2 * CRE; ++c)
+      for (int c = 0; c < NC; ++c)
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int q = 0; q < 4; ++q) acc[gg][c][q] = 0.f;
+    const int kvalid = min(kKc, kpad - kc);
+    for (int ks = 0; ks < kvalid; ks += 16) {
+      // B fragments of all digits (and, for complex x complex, the digit sums
+      // r + i, exact in bf16: |d_r + d_i| <= 128)
+      uint32_t bf[kDigits][PBX][2];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) acc[c][u][q] = 0.f;
-      for (int s = max(0, grp - (kDigits - 1)); s <= min(grp, kDigits - 1); ++s) {
-        const int t = grp - s;
-        const __nv_bfloat16* Ab = As + (size_t(b) * kDigits + s) * PA * aplane;
-        const __nv_bfloat16* Bb = Bs + (size_t(b) * kDigits + t) * PB * bplane;
-        for (int ks = kc; ks < kend; ks += 16) {
-          uint32_t af[PA][4], bf[PB][2][2];
+      for (int t = 0; t < kDigits; ++t) {
 #pragma unroll
-          for (int pa = 0; pa < PA; ++pa) {
-            const __nv_bfloat16* A0 = Ab + pa * aplane + size_t(m0 + gq) * kpad + ks + 2 * tq;
-            const __nv_bfloat16* A8 = A0 + size_t(8) * kpad;
-            af[pa][0] = *reinterpret_cast<const uint32_t*>(A0);
-            af[pa][1] = *reinterpret_cast<const uint32_t*>(A8);
-            af[pa][2] = *reinterpret_cast<const uint32_t*>(A0 + 8);
-            af[pa][3] = *reinterpret_cast<const uint32_t*>(A8 + 8);
-          }
+        for (int pb = 0; pb < PB; ++pb) {
+          const __nv_bfloat16* B0 = sB + (size_t(t * PB + pb) * 32 + wn + gq) * kLd + ks + 2 * tq;
+          bf[t][pb][0] = *reinterpret_cast<const uint32_t*>(B0);
+          bf[t][pb][1] = *reinterpret_cast<const uint32_t*>(B0 + 8);
+        }
+        if (PBX == 3) {
+          bf[t][PBX - 1][0] = bsum(bf[t][0][0], bf[t][PB - 1][0]);
+          bf[t][PBX - 1][1] = bsum(bf[t][0][1], bf[t][PB - 1][1]);
+        }
+      }
 #pragma unroll
-          for (int pb = 0; pb < PB; ++pb)
+      for (int s = 0; s < kDigits; ++s) {
+        uint32_t af[PAX][4];
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-              const __nv_bfloat16* B0 = Bb + pb * bplane + size_t(n0 + u * 8 + gq) * kpad + ks + 2 * tq;
-              bf[pb][u][0] = *reinterpret_cast<const uint32_t*>(B0);
-              bf[pb][u][1] = *reinterpret_cast<const uint32_t*>(B0 + 8);
-            }
+        for (int pa = 0; pa < PA; ++pa) {
+          const __nv_bfloat16* A0 = sA + (size_t(s * PA + pa) * 32 + wm + gq) * kLd + ks + 2 * tq;
+          const __nv_bfloat16* A8 = A0 + 8 * kLd;
+          af[pa][0] = *reinterpret_cast<const uint32_t*>(A0);
+          af[pa][1] = *reinterpret_cast<const uint32_t*>(A8);
+          af[pa][2] = *reinterpret_cast<const uint32_t*>(A0 + 8);
+          af[pa][3] = *reinterpret_cast<const uint32_t*>(A8 + 8);
+        }
+        if (PAX == 3) {
 #pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            if (PA == 2 && PB == 2) {
-              mma16816(acc[0][u], af[0], bf[0][u]);  // rr
-              mma16816(acc[1][u], af[1], bf[1][u]);  // ii
-              mma16816(acc[2][u], af[0], bf[1][u]);  // ri
-              mma16816(acc[3][u], af[1], bf[0][u]);  // ir
-            } else if (PA == 2) {
-              mma16816(acc[0][u], af[0], bf[0][u]);  // re
-              mma16816(acc[1][u], af[1], bf[0][u]);  // im
-            } else if (PB == 2) {
-              mma16816(acc[0][u], af[0], bf[0][u]);
-              mma16816(acc[1][u], af[0], bf[1][u]);
-            } else {
-              mma16816(acc[0][u], af[0], bf[0][u]);
-            }
+          for (int v = 0; v < 4; ++v) af[PAX - 1][v] = bsum(af[0][v], af[PA - 1][v]);
+        }
+#pragma unroll
+        for (int t = 0; t <= kKeep - s; ++t) {
+          const int gg = s + t;
+          if (PA == 2 && PB == 2) {
+            // 3M: rr, ii and (r + i)(r + i)
+            mma16816(acc[gg][0], af[0], bf[t][0]);
+            mma16816(acc[gg][1], af[1], bf[t][1]);
+            mma16816(acc[gg][2], af[PAX - 1], bf[t][PBX - 1]);
+          } else if (PA == 2) {
+            mma16816(acc[gg][0], af[0], bf[t][0]);
+            mma16816(acc[gg][1], af[1], bf[t][0]);
+          } else if (PB == 2) {
+            mma16816(acc[gg][0], af[0], bf[t][0]);
+            mma16816(acc[gg][1], af[0], bf[t][1]);
+          } else {
+            mma16816(acc[gg][0], af[0], bf[t][0]);
           }
         }
       }
-      const double w = ldexp(1.0, 7 * (2 * (kDigits - 1) - grp));
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          if (PA == 2 && PB == 2) {
-            cre[u][q] = fma(double(acc[0][u][q] - acc[1][u][q]), w, cre[u][q]);
-            cim[u][q] = fma(double(acc[2][u][q] + acc[3][u][q]), w, cim[u][q]);
-          } else if (PA == 2 || PB == 2) {
-            cre[u][q] = fma(double(acc[0][u][q]), w, cre[u][q]);
-            cim[u][q] = fma(double(acc[1][u][q]), w, cim[u][q]);
-          } else {
-            cre[u][q] = fma(double(acc[0][u][q]), w, cre[u][q]);
-          }
-        }
     }
+    // ---- fold the exact group sums of this chunk into the integer
+    // accumulators: the real and imaginary group sums are exact FP32
+    // integers below 2^22 (rr - ii and ss - rr - ii included), so they
+    // convert exactly; groups 0-3 go to hi, 4-7 to lo (weights 2^(7 (3 - g))
+    // and 2^(7 (7 - g))).
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int pr[kKeep + 1], pi[kKeep + 1];
+#pragma unroll
+      for (int gg = 0; gg <= kKeep; ++gg) {
+        float re, im = 0.f;
+        if (PA == 2 && PB == 2) {
+          re = acc[gg][0][q] - acc[gg][1][q];
+          im = acc[gg][2][q] - (acc[gg][0][q] + acc[gg][1][q]);
+        } else if (PA == 2 || PB == 2) {
+          re = acc[gg][0][q];
+          im = acc[gg][1][q];
+        } else {
+          re = acc[gg][0][q];
+        }
+        pr[gg] = __float2int_rn(re);
+        pi[gg] = __float2int_rn(im);
+      }
+      hre[q] += ((long long)(pr[0] * 128 + pr[1]) << 14) + (pr[2] * 128 + pr[3]);
+      lre[q] += ((long long)(pr[4] * 128 + pr[5]) << 14) + (pr[6] * 128 + pr[7]);
+      if (NC > 1) {
+        him[q] += ((long long)(pi[0] * 128 + pi[1]) << 14) + (pi[2] * 128 + pi[3]);
+        lim[q] += ((long long)(pi[4] * 128 + pi[5]) << 14) + (pi[6] * 128 + pi[7]);
+      }
+    }
+    __syncthreads();
+  }
+  double cre[4], cim[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    cre[q] = fma(double(hre[q]), 0x1p28, double(lre[q]));
+    cim[q] = fma(double(him[q]), 0x1p28, double(lim[q]));
   }
   // epilogue: scale by 2^(ea + eb - 106), alpha/beta, store
   double2 alpha = g.alpha;
   if (g.alpha_vec) alpha = cmul(alpha, g.alpha_vec[b]);
   const bool cplx_out = !g.c_real;
 #pragma unroll
-  for (int u = 0; u < 2; ++u)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = m0 + gq + ((q & 2) ? 8 : 0);
-      const int j = n0 + u * 8 + 2 * tq + (q & 1);
-      if (i >= M || j >= N) continue;
-      const int sc = ea[size_t(b) * mpad + i] + eb[size_t(b) * npad + j] - 106;
-      const double vr = ldexp(cre[u][q], sc), vi = ldexp(cim[u][q], sc);
-      const long long idx = i * g.crs + j * g.ccs + b * g.cbs;
-      if (cplx_out) {
-        double2* C = static_cast<double2*>(g.C);
-        double2 v = cmul(alpha, make_double2(vr, vi));
-        if (g.beta.x != 0.0 || g.beta.y != 0.0) v = cadd(v, cmul(g.beta, C[idx]));
-        C[idx] = v;
-      } else {
-        double* C = static_cast<double*>(g.C);
-        double v = (cmul(alpha, make_double2(vr, vi))).x;
-        if (g.beta.x != 0.0) v = fma(g.beta.x, C[idx], v);
-        C[idx] = v;
-      }
+  for (int q = 0; q < 4; ++q) {
+    const int i = mt0 + wm + gq + ((q & 2) ? 8 : 0);
+    const int j = nt0 + wn + 2 * tq + (q & 1);
+    if (i >= M || j >= N) continue;
+    const int sc = ea[size_t(b) * mpad + i] + eb[size_t(b) * npad + j] - 106 + 49;
+    const double vr = ldexp(cre[q], sc), vi = ldexp(cim[q], sc);
+    const long long idx = i * g.crs + j * g.ccs + b * g.cbs;
+    if (cplx_out) {
+      double2* C = static_cast<double2*>(g.C);
+      double2 v = cmul(alpha, make_double2(vr, vi));
+      if (g.beta.x != 0.0 || g.beta.y != 0.0) v = cadd(v, cmul(g.beta, C[idx]));
+      C[idx] = v;
+    } else {
+      double* C = static_cast<double*>(g.C);
+      double v = (cmul(alpha, make_double2(vr, vi))).x;
+      if (g.beta.x != 0.0) v = fma(g.beta.x, C[idx], v);
+      C[idx] = v;
     }
+  }
 }
 
-// Slice scratch, one per stream (GEMMs on different streams run concurrently);
-// grown on demand and kept for the life of the process.
+template <int PA, int PB>
+int launch_ozaki_mma(int M, int N, int K, int mpad, int npad, int kpad, const __nv_bfloat16* As, const int* ea,
+                     const __nv_bfloat16* Bs, const int* eb, const GemmArgs& g, cudaStream_t s) {
+  const size_t shm = sizeof(__nv_bfloat16) * size_t(kDigits) * (PA + PB) * 32 * kLd;
+  static bool attr = false;
+  if (!attr) {
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_mma_kernel<PA, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    attr = true;
+  }
+  dim3 grid(npad / 32, mpad / 32, g.batch);
+  ozaki_mma_kernel<PA, PB><<<grid, 256, shm, s>>>(M, N, K, mpad, npad, kpad, As, ea, Bs, eb, g);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
 struct OzScratch {
   cudaStream_t stream = nullptr;
   __nv_bfloat16* buf = nullptr;
@@ -349,17 +439,10 @@ int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
     else
       slice_kernel<false><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, false, Bs, eb);
   }
-  dim3 grid(npad / 32, mpad / 32, g.batch);
-  if (PA == 2 && PB == 2)
-    ozaki_mma_kernel<2, 2><<<grid, 128, 0, s>>>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g);
-  else if (PA == 2)
-    ozaki_mma_kernel<2, 1><<<grid, 128, 0, s>>>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g);
-  else if (PB == 2)
-    ozaki_mma_kernel<1, 2><<<grid, 128, 0, s>>>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g);
-  else
-    ozaki_mma_kernel<1, 1><<<grid, 128, 0, s>>>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g);
-  TVAP_CUDA(cudaGetLastError());
-  return TVAP_OK;
+  if (PA == 2 && PB == 2) return launch_ozaki_mma<2, 2>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g, s);
+  if (PA == 2) return launch_ozaki_mma<2, 1>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g, s);
+  if (PB == 2) return launch_ozaki_mma<1, 2>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g, s);
+  return launch_ozaki_mma<1, 1>(g.M, g.N, g.K, mpad, npad, kpad, As, ea, Bs, eb, g, s);
 }
 
 }  // namespace tvap
