@@ -30,6 +30,7 @@ GPU_SOURCES = [
     "projection.cu",
     "gradient.cu",
     "ozaki.cu",
+    "field_blocks.cu",
 ]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -66,7 +67,9 @@ def build_setup(force: bool = False) -> str:
 
 def build_gpu(force: bool = False, verbose_ptxas: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in GPU_SOURCES]
-    deps = srcs + [os.path.join(CSRC, "tvap_internal.cuh"), os.path.join(INCLUDE, "tvap.h")]
+    deps = srcs + [os.path.join(CSRC, h) for h in ("tvap_internal.cuh", "ozaki_core.cuh")] + [
+        os.path.join(INCLUDE, "tvap.h")
+    ]
     if not (force or _stale(GPU_LIB, deps)):
         return GPU_LIB
     nvcc = _nvcc()

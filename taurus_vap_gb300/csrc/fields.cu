@@ -240,6 +240,8 @@ int build_field_csr(tvap_ctx* c) {
 }
 
 void free_field_csr(FieldCSR& f) {
+  free_field_dense(f.dense_g);
+  free_field_dense(f.dense_d);
   cudaFree(f.g_rowptr);
   cudaFree(f.g_src);
   cudaFree(f.g_coef);
@@ -396,9 +398,16 @@ void launch_fields(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
 
 }  // namespace
 
+// below this many columns the 32-wide tiles of the dense path are mostly
+// padding and the gather kernels are faster
+constexpr int kDenseMinCols = 16;
+
 int fields_batched(tvap_ctx* c, int ncol, int ldc, const double2* rho, const double2* kLR, const double2* kRL,
                    double2* gamma, double2* hsp, double2* dLR, double2* dRL, cudaStream_t s) {
   if (ncol <= 0) return TVAP_OK;
+  // many gauge angles at once: dense symmetry blocks on the tensor cores
+  if (c->gemm_mode == 1 && c->csr.dense_ok && ncol >= kDenseMinCols)
+    return fields_dense(c, ncol, ldc, rho, kLR, kRL, gamma, hsp, dLR, dRL, s);
   if (ncol <= 32)
     launch_fields<1>(c, ncol, ldc, rho, kLR, kRL, gamma, hsp, dLR, dRL, s);
   else if (ncol <= 64)

@@ -248,6 +248,7 @@ int tvap_set_hamiltonian(tvap_ctx* c, int64_t S, const int16_t* abcd, const floa
   c->H0 = make_double2(H0[0], H0[1]);
   TVAP_CUDA(cudaStreamSynchronize(c->stream));
   if ((rc = build_field_csr(c))) return rc;
+  if ((rc = build_field_dense(c))) return rc;
   c->have_ham = true;
   return TVAP_OK;
 }

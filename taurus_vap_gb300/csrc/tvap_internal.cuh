@@ -1,6 +1,7 @@
 // Internal declarations of the sm_103a device path (not part of the C ABI).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -99,6 +100,8 @@ int gemm(const GemmArgs& g, cudaStream_t s);
 // the same product with the FP64 arithmetic emulated on the bf16 tensor cores
 int gemm_ozaki(const GemmArgs& g, cudaStream_t s);
 void oz_release(cudaStream_t s);
+// per-stream scratch of the emulated products (grown on demand, stream-ordered)
+int oz_scratch(cudaStream_t s, size_t bytes, size_t ex_count, __nv_bfloat16** buf, int** ex);
 // GEMM arithmetic of the calls in flight: 0 FP64 pipe, 1 emulated (set by
 // every C-ABI entry point from its context)
 extern int g_gemm_mode;
@@ -106,6 +109,21 @@ extern int g_gemm_mode;
 // ---------------------------------------------------------------------------
 // Hamiltonian in gather form (built once from the reference's element list)
 // ---------------------------------------------------------------------------
+// One field operator as dense symmetry blocks (field_blocks.cu)
+struct FieldBlockDesc {
+  long long aoff;  // first digit-plane element of the block
+  int r_pad, kb_pad, kbeg, row_base;
+};
+struct FieldDense {
+  int nblk = 0, ntiles = 0, nrows = 0, ktot = 0;
+  void* wd = nullptr;       // bf16 digit planes of W, block by block
+  int* ea = nullptr;        // exponent per permuted output row
+  int* rowperm = nullptr;   // permuted row -> output entry (-1: padding)
+  int* colperm = nullptr;   // permuted input index -> input entry (-1: padding)
+  int2* tiles = nullptr;    // (block, first row) of every 32-row tile
+  FieldBlockDesc* blocks = nullptr;
+};
+
 struct FieldCSR {
   // Gamma: one row per output entry (x + y n), entries: src index (z + w n), coef
   int* g_rowptr = nullptr;
@@ -119,6 +137,9 @@ struct FieldCSR {
   double* d_coef = nullptr;
   int d_nrows = 0;
   long long d_nnz = 0;
+  // the same operators as dense symmetry blocks (when block-dense)
+  FieldDense dense_g, dense_d;
+  bool dense_ok = false;
 };
 
 struct Workspace;
@@ -176,6 +197,11 @@ namespace tvap {
 
 int build_field_csr(tvap_ctx* c);
 void free_field_csr(FieldCSR& f);
+int build_field_dense(tvap_ctx* c);
+void free_field_dense(FieldDense& f);
+// fields of ncol gauge-angle columns through the dense blocks (emulated FP64)
+int fields_dense(tvap_ctx* c, int ncol, int ldc, const double2* rho, const double2* kLR, const double2* kRL,
+                 double2* gamma, double2* hsp, double2* dLR, double2* dRL, cudaStream_t s);
 
 // Fields for `ncol` columns (angles) in angle-innermost layout:
 // X[(i + j n) * ldc + col].  hsp/dLR/dRL outputs in the same layout.

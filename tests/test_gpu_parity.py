@@ -87,6 +87,29 @@ def test_calculate_fields_batched(emax2):
             assert relerr(got[q][c], ref[q]) < FIELD_TOL
 
 
+@pytest.mark.parametrize("case,ncol", [("emax2", 20), ("emax4", 37)])
+def test_calculate_fields_dense_blocks(case, ncol, request):
+    # many angle columns take the dense symmetry-block path (FP64 emulated on
+    # the tensor cores): against the oracle, and against the gather kernels
+    # (FP64 pipe) on every column
+    mdl, U, V = request.getfixturevalue(case)
+    om = O.OracleModel(mdl)
+    angles = [(0.13 * k, 0.29 * k + 0.05) for k in range(ncol)]
+    sets = [om.angle_densities(U, V, a, b)[1][:3] for a, b in angles]
+    rho, kLR, kRL = (np.stack([s[q] for s in sets]) for q in range(3))
+    ctx = Context(mdl.basis, mdl.ham)
+    got = ctx.calculate_fields_batched(rho, kLR, kRL)
+    ctx.set_gemm_mode(0)
+    gathered = ctx.calculate_fields_batched(rho, kLR, kRL)
+    for c in range(0, ncol, 6):
+        ref = om.calculate_fields(rho[c], kLR[c], kRL[c], nthreads=0)
+        for q, name in enumerate(("gamma", "h", "deltaLR", "deltaRL")):
+            assert relerr(got[q][c], ref[q]) < FIELD_TOL, (c, name)
+    for c in range(ncol):
+        for q in range(4):
+            assert relerr(got[q][c], gathered[q][c]) < FIELD_TOL, (c, q)
+
+
 def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0, gemm_mode=1):
     om = O.OracleModel(mdl)
     ref = om.project(U, V, Mp, Mn, 2 * np.pi, Z, N, nthreads=nthreads)
@@ -122,9 +145,11 @@ def test_project_even_angles(sd):
     check_projection(mdl, U, V, 4, 6, 4, 4, 0)
 
 
-def test_project_emax2(emax2):
+@pytest.mark.parametrize("grid", [5, 7])
+def test_project_emax2(emax2, grid):
+    # 7 x 7 angles (25 folded columns) runs the fields on the dense blocks
     mdl, U, V = emax2
-    check_projection(mdl, U, V, 5, 5, 4, 4, 0)
+    check_projection(mdl, U, V, grid, grid, 4, 4, 0)
 
 
 @pytest.mark.parametrize("gemm_mode", [0, 1])
