@@ -74,6 +74,7 @@ struct Workspace {
   // overlap chain scratch (runs on the second stream)
   double2 *OW = nullptr, *OX = nullptr, *OY = nullptr;
   int* rflag = nullptr;
+  int* piv = nullptr;  // [G][n] row interchanges of the Thouless LU
   bool have_basis = false;
   size_t bytes = 0;
 };
@@ -95,7 +96,7 @@ void ws_free(Workspace* w) {
                   w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
                   w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
                   w->H20v,  w->Xr,    w->Xn,     w->Rr,    w->Br,     w->Sr,    w->Mr,     w->lam,   w->rscal,
-                  w->rflag, w->OW,    w->OX,     w->OY};
+                  w->rflag, w->OW,    w->OX,     w->OY,     w->piv};
   for (void* p : ptrs) cudaFree(p);
   *w = Workspace();
 }
@@ -124,7 +125,7 @@ int ws_ensure(tvap_ctx* c, int G) {
   A_(dRL, nG) A_(ephase, 2 * G) A_(weight, G) A_(mult, G) A_(obs, 8 * G) A_(pf, 2 * G) A_(detR22, 2 * G)
   A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
   A_(Xr, nn) A_(Xn, nn) A_(Rr, nn) A_(Br, nn) A_(Sr, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
-  A_(OW, nG) A_(OX, nG) A_(OY, nG)
+  A_(OW, nG) A_(OX, nG) A_(OY, nG) A_(piv, size_t(n) * G)
 #undef A_
   return TVAP_OK;
 }
@@ -1031,6 +1032,168 @@ __global__ void __launch_bounds__(kPanelThreads)
   }
 }
 
+// Panel of at most kPanelMax columns factored in shared memory (one CTA per
+// angle): partial pivoting by max |re| + |im| (first row on ties, as izamax),
+// multipliers and the updated panel written back, pivots (absolute rows) to
+// piv[b * n + j].  The interchanges of the other columns and the block row
+// U12 are left to panel_apply_kernel.
+constexpr int kPanelMax = 32;
+constexpr int kFactorThreads = 256;
+constexpr int kApplyThreads = 32;  // one warp: L11 + the column buffers stay under 48 KB
+
+__global__ void __launch_bounds__(kFactorThreads)
+    panel_factor_kernel(int n, int j0, int nbp, double2* __restrict__ Wall, int* __restrict__ piv, int* flags) {
+  extern __shared__ double2 P[];  // rows j0..n-1 of the panel, column-major, ld m
+  __shared__ int s_piv;
+  __shared__ double s_pv;
+  const int b = blockIdx.x;
+  double2* W = Wall + size_t(b) * 2 * n * n;
+  const int m = n - j0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int idx = tid; idx < m * nbp; idx += blockDim.x) {
+    const int r = idx % m, c = idx / m;
+    P[c * m + r] = W[(j0 + r) + size_t(j0 + c) * n];
+  }
+  __syncthreads();
+  bool singular = false;
+  for (int jj = 0; jj < nbp; ++jj) {
+    if (warp == 0) {
+      double best = -1.0;
+      int bi = m;
+      for (int r = jj + lane; r < m; r += 32) {
+        const double v = cabs1(P[jj * m + r]);
+        if (v > best) {
+          best = v;
+          bi = r;
+        }
+      }
+      warp_argmax(best, bi);
+      if (lane == 0) {
+        s_piv = bi;
+        s_pv = best;
+      }
+    }
+    __syncthreads();
+    int p = s_piv;
+    const double pv = s_pv;
+    if (pv == 0.0) {
+      singular = true;
+      p = jj;
+    }
+    if (tid == 0) piv[size_t(b) * n + j0 + jj] = j0 + p;
+    if (p != jj)
+      for (int c = tid; c < nbp; c += blockDim.x) {
+        const double2 t = P[c * m + jj];
+        P[c * m + jj] = P[c * m + p];
+        P[c * m + p] = t;
+      }
+    __syncthreads();
+    const double2 rp = (pv == 0.0) ? make_double2(0.0, 0.0) : crcp(P[jj * m + jj]);
+    for (int r = jj + 1 + tid; r < m; r += blockDim.x) {
+      const double2 mu = cmul(P[jj * m + r], rp);
+      P[jj * m + r] = mu;
+      for (int c = jj + 1; c < nbp; ++c) {
+        const double2 top = P[c * m + jj];
+        double2 v = P[c * m + r];
+        v.x = fma(-mu.x, top.x, v.x);
+        v.x = fma(mu.y, top.y, v.x);
+        v.y = fma(-mu.x, top.y, v.y);
+        v.y = fma(-mu.y, top.x, v.y);
+        P[c * m + r] = v;
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < m * nbp; idx += blockDim.x) {
+    const int r = idx % m, c = idx / m;
+    W[(j0 + r) + size_t(j0 + c) * n] = P[c * m + r];
+  }
+  if (singular && tid == 0) atomicOr(flags, DEV_SINGULAR_UPHI);
+}
+
+// Columns j1 .. 2n-1 (one thread each): the panel's row interchanges, then
+// U12 = L11^{-1} A12 on the block row j0 .. j1-1.
+__global__ void __launch_bounds__(kApplyThreads)
+    panel_apply_kernel(int n, int j0, int nbp, double2* __restrict__ Wall, const int* __restrict__ piv) {
+  __shared__ double2 L[kPanelMax][kPanelMax + 1];
+  __shared__ double2 xb[kPanelMax][kApplyThreads];
+  __shared__ int sp[kPanelMax];
+  const int b = blockIdx.y;
+  double2* W = Wall + size_t(b) * 2 * n * n;
+  const int j1 = j0 + nbp;
+  for (int idx = threadIdx.x; idx < nbp * nbp; idx += blockDim.x) {
+    const int i = idx % nbp, k = idx / nbp;
+    L[i][k] = W[(j0 + i) + size_t(j0 + k) * n];
+  }
+  for (int i = threadIdx.x; i < nbp; i += blockDim.x) sp[i] = piv[size_t(b) * n + j0 + i] - j0;
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int c = j1 + blockIdx.x * kApplyThreads + t;
+  if (c >= 2 * n) return;
+  double2* col = W + size_t(c) * n;
+  for (int i = 0; i < nbp; ++i) xb[i][t] = col[j0 + i];
+  for (int jj = 0; jj < nbp; ++jj) {
+    const int p = sp[jj];
+    if (p == jj) continue;
+    if (p < nbp) {
+      const double2 tmp = xb[jj][t];
+      xb[jj][t] = xb[p][t];
+      xb[p][t] = tmp;
+    } else {
+      const double2 tmp = col[j0 + p];
+      col[j0 + p] = xb[jj][t];
+      xb[jj][t] = tmp;
+    }
+  }
+  for (int i = 1; i < nbp; ++i) {
+    double2 v = xb[i][t];
+    for (int k = 0; k < i; ++k) {
+      const double2 mu = L[i][k], x = xb[k][t];
+      v.x = fma(-mu.x, x.x, v.x);
+      v.x = fma(mu.y, x.y, v.x);
+      v.y = fma(-mu.x, x.y, v.y);
+      v.y = fma(-mu.y, x.x, v.y);
+    }
+    xb[i][t] = v;
+  }
+  for (int i = 0; i < nbp; ++i) col[j0 + i] = xb[i][t];
+}
+
+// X_i = U_ii^{-1} Y_i on block row i0 .. i0+nbp-1, right-hand sides the
+// columns n .. 2n-1 (one thread each)
+__global__ void __launch_bounds__(kApplyThreads)
+    backsolve_apply_kernel(int n, int i0, int nbp, double2* __restrict__ Wall) {
+  __shared__ double2 Us[kPanelMax][kPanelMax + 1];
+  __shared__ double2 rd[kPanelMax];
+  __shared__ double2 xb[kPanelMax][kApplyThreads];
+  const int b = blockIdx.y;
+  double2* W = Wall + size_t(b) * 2 * n * n;
+  for (int idx = threadIdx.x; idx < nbp * nbp; idx += blockDim.x) {
+    const int i = idx % nbp, k = idx / nbp;
+    if (k >= i) Us[i][k] = W[(i0 + i) + size_t(i0 + k) * n];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbp; i += blockDim.x) rd[i] = crcp(Us[i][i]);
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int c = n + blockIdx.x * kApplyThreads + t;
+  if (c >= 2 * n) return;
+  double2* col = W + size_t(c) * n;
+  for (int i = 0; i < nbp; ++i) xb[i][t] = col[i0 + i];
+  for (int i = nbp - 1; i >= 0; --i) {
+    double2 v = xb[i][t];
+    for (int k = i + 1; k < nbp; ++k) {
+      const double2 u = Us[i][k], x = xb[k][t];
+      v.x = fma(-u.x, x.x, v.x);
+      v.x = fma(u.y, x.y, v.x);
+      v.y = fma(-u.x, x.y, v.y);
+      v.y = fma(-u.y, x.x, v.y);
+    }
+    xb[i][t] = cmul(v, rd[i]);
+  }
+  for (int i = 0; i < nbp; ++i) col[i0 + i] = xb[i][t];
+}
+
 // A_phi(i, j) = conj(X(i, j)) = conj(Y(j, i)), Y = W(:, n:2n)
 __global__ void thouless_out_kernel(int n, int G, const double2* __restrict__ Wall, double2* __restrict__ A) {
   const size_t nn = size_t(n) * n;
@@ -1106,8 +1269,22 @@ int blocked_thouless_solve(tvap_ctx* c, int G) {
   const int n = c->n;
   cudaStream_t s = c->stream;
   const long long bsW = 2LL * n * n;
-  const int nb = (n <= 64) ? n : 28;
+  // panels of at most kPanelMax columns, equal widths; the shared-memory panel
+  // (n x nb complex) must fit, else the former wider kernels run from global
+  const int npanels = (n + kPanelMax - 1) / kPanelMax;
+  const int nb_smem = (n + npanels - 1) / npanels;
+  const size_t panel_bytes = sizeof(double2) * size_t(n) * nb_smem;
+  const bool smem_path = panel_bytes <= size_t(jacobi32_smem_limit());
+  const int nb = smem_path ? nb_smem : ((n <= 64) ? n : 28);
   int rc;
+  if (smem_path && panel_bytes > 48 * 1024) {
+    static bool attr = false;
+    if (!attr) {
+      TVAP_CUDA(cudaFuncSetAttribute(panel_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(jacobi32_smem_limit())));
+      attr = true;
+    }
+  }
   {
     dim3 grid(std::max(1, (2 * n + 15) / 16), G);
     build_augmented_kernel<<<grid, kPanelThreads, 0, s>>>(n, w->Uphi, w->Vphi, w->W);
@@ -1116,8 +1293,16 @@ int blocked_thouless_solve(tvap_ctx* c, int G) {
   for (int j0 = 0; j0 < n; j0 += nb) {
     const int nbp = std::min(nb, n - j0);
     const int j1 = j0 + nbp;
-    panel_kernel<<<G, kPanelThreads, 0, s>>>(n, j0, nbp, w->W, c->d_flags);
-    ++launches;
+    if (smem_path) {
+      panel_factor_kernel<<<G, kFactorThreads, sizeof(double2) * size_t(n - j0) * nbp, s>>>(n, j0, nbp, w->W, w->piv,
+                                                                                             c->d_flags);
+      dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, G);
+      panel_apply_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
+      launches += 2;
+    } else {
+      panel_kernel<<<G, kPanelThreads, 0, s>>>(n, j0, nbp, w->W, c->d_flags);
+      ++launches;
+    }
     if (j1 < n) {
       // A22 -= L21 U12 over columns j1 .. 2n-1
       GemmArgs g{};
@@ -1161,7 +1346,12 @@ int blocked_thouless_solve(tvap_ctx* c, int G) {
       if ((rc = gemm(g, s))) return rc;
       ++launches;
     }
-    block_backsolve_kernel<<<G, kPanelThreads, 0, s>>>(n, i0, nbp, w->W);
+    if (smem_path) {
+      dim3 gb((n + kApplyThreads - 1) / kApplyThreads, G);
+      backsolve_apply_kernel<<<gb, kApplyThreads, 0, s>>>(n, i0, nbp, w->W);
+    } else {
+      block_backsolve_kernel<<<G, kPanelThreads, 0, s>>>(n, i0, nbp, w->W);
+    }
     ++launches;
   }
   const size_t tot = size_t(n) * n * G;
