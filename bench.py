@@ -193,7 +193,7 @@ def run_ours(args):
         it.step()
     torch.cuda.synchronize()
     barrier()
-    ctx.set_timing(True)
+    ctx.set_timing(False)
     it.launches = 0
     clocks = ClockSampler(local)
     clocks.start()
@@ -208,7 +208,15 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     ms = t0.elapsed_time(t1)
+    launches = it.launches
+    # per-section times from separate instrumented steps (events on the streams)
+    ctx.set_timing(True)
+    sec_steps = max(1, min(args.steps, 5))
+    for _ in range(sec_steps):
+        it.step()
+    torch.cuda.synchronize()
     sections = ctx.get_timing()
+    canon_paths = ctx.canonical_paths()
     ctx.set_timing(False)
     if world > 1:
         import torch.distributed as dist
@@ -218,7 +226,6 @@ def run_ours(args):
         ms = float(tt.item())
     ms_per_step = ms / args.steps
     value = world * args.steps / (ms / 1000.0)
-    launches = it.launches
 
     # ---- same iteration with every dense product on the FP64 pipe (DFMA)
     ctx.set_gemm_mode(0)
@@ -285,7 +292,7 @@ def run_ours(args):
     except OSError:
         pass
     steps = args.steps
-    fld_ms = (sections["fields_gamma"][0] + sections["fields_delta"][0]) / steps
+    fld_ms = (sections["fields_gamma"][0] + sections["fields_delta"][0]) / sec_steps
     fld_bytes = 13 * S + 16 * n * n * 7 * G
     dom = max(sections.items(), key=lambda kv: kv[1][0])
     roofline = {
@@ -300,7 +307,7 @@ def run_ours(args):
         "ms_per_launch": fld_ms,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
     }
-    sec_ms = {k: v[0] / steps for k, v in sections.items()}
+    sec_ms = {k: v[0] / sec_steps for k, v in sections.items()}
     total_sec = sum(sec_ms.values())
     fp64 = fp64_flops_per_iteration(n, G) + 4 * 8 * (S * 1.65) * G  # dense + fields (48 flops x passes)
     roofline_fp64 = {
@@ -329,7 +336,7 @@ def run_ours(args):
                    "eta": ETA, "mu": MU},
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "roofline_fp64": roofline_fp64,
         "sections_ms_per_step": {k: round(v, 4) for k, v in sec_ms.items()},
-        "dominant_section": dom[0], "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
+        "dominant_section": dom[0], "canonical_paths": canon_paths, "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
         "final_energy": it.energy,
     }
     if rank == 0:

@@ -96,10 +96,17 @@ int tvap_set_timing(tvap_ctx* ctx, int on);
 /* Arithmetic of the dense products: 0 = the FP64 pipe (DFMA);
  * 1 (default) = FP64 emulated on the bf16 tensor cores by exact integer
  * splitting (8 balanced 7-bit digits per FP64 value, exact FP32 partial sums,
- * FP64 recombination).  The sparse field contraction, the factorisations and
- * all reductions run on the FP64 pipe in both modes. */
+ * integer recombination).  In mode 1 the field contraction over 16 or more
+ * gauge angles also runs on the tensor cores (dense symmetry blocks of the
+ * interaction); the factorisations and all reductions run on the FP64 pipe
+ * in both modes. */
 int tvap_set_gemm_mode(tvap_ctx* ctx, int mode);
 int tvap_get_timing(tvap_ctx* ctx, double* ms, long long* calls, int nsec);
+/* Diagnostic counters since the last tvap_set_timing, for the canonical
+ * basis: [0] FP32 Jacobi + FP64 refinement attempts, [1] of them accepted by
+ * the final check, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in
+ * total.  No reference counterpart. */
+int tvap_get_counters(tvap_ctx* ctx, long long* out, int nout);
 
 /* One upload of the reduced two-body list and the one-body part:
  * hamil_H2dim, hamil_abcd (i16, 1-based, 4 per element), hamil_H2 (f32),

@@ -588,7 +588,7 @@ namespace {
 
 __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double* __restrict__ A64,
                                                               const double* __restrict__ W0,
-                                                              double* __restrict__ W64, int* flags) {
+                                                              double* __restrict__ W64, int* sweeps_out) {
   extern __shared__ float js[];
   const int m = (n + 1) & ~1;
   const int ld = n | 1;                  // odd leading dimension: conflict-free row access
@@ -618,12 +618,16 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
     __syncthreads();
   }
   const float tol2 = red[0] * 1.0e-12f;  // off-diagonal <= 1e-6 ||A||: enough for the FP64 refinement
+  const int h = m / 2;
+  // fixed thread -> first 2 x 2 block (k1, k2) and its stride over the h x h blocks
+  const int b1 = tid / h, b2 = tid % h, d1 = nt / h, d2 = nt % h;
   // fixed thread -> (row, first pair) assignment: no index division in the sweeps
   const int kstep = nt / n;           // threads per row group (>= 1 for n <= 1024)
   const int r0 = (tid < kstep * n) ? tid % n : n;
   const int k0 = (tid < kstep * n) ? tid / n : 0;
   __syncthreads();
-  for (int sweep = 0; sweep < 40; ++sweep) {
+  int sweep = 0;
+  for (; sweep < 40; ++sweep) {
     float off = 0.f;
     if (r0 < n)
       for (int j = k0; j < n; j += kstep)
@@ -638,7 +642,7 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
     __syncthreads();
     if (done) break;
     for (int round = 0; round < m - 1; ++round) {
-      for (int k = tid; k < m / 2; k += nt) {
+      for (int k = tid; k < h; k += nt) {
         // circle method: player m-1 fixed, the others rotate with the round
         int p, q;
         if (k == 0) {
@@ -669,35 +673,49 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
         sn[k] = s;
       }
       __syncthreads();
-      for (int k = k0; k < m / 2; k += kstep) {
-        const int p = pp[k], q = qq[k];
-        const float s = sn[k];
-        if (r0 >= n || q >= n || s == 0.f) continue;
-        const int r = r0;
-        const float c = cs[k];
-        const float ap = A[r + p * ld], aq = A[r + q * ld];
-        A[r + p * ld] = c * ap - s * aq;
-        A[r + q * ld] = s * ap + c * aq;
-        const float wp = W[r + p * ld], wq = W[r + q * ld];
-        W[r + p * ld] = c * wp - s * wq;
-        W[r + q * ld] = s * wp + c * wq;
+      // A <- J^T A J one 2 x 2 block (row pair k1, column pair k2) per item;
+      // W <- W J one (row, pair) per item.  Blocks are disjoint: no hazards.
+      {
+        int k1 = b1, k2 = b2;
+        while (k1 < h) {
+          const float s1 = sn[k1], s2 = sn[k2];
+          if (s1 != 0.f || s2 != 0.f) {
+            const int p1 = pp[k1], q1 = qq[k1], p2 = pp[k2], q2 = qq[k2];
+            if (q1 < n && q2 < n) {
+              const float c1 = cs[k1], c2 = cs[k2];
+              const float a = A[p1 + p2 * ld], b = A[p1 + q2 * ld], cc = A[q1 + p2 * ld], d = A[q1 + q2 * ld];
+              const float xa = c2 * a - s2 * b, xb = s2 * a + c2 * b;    // row p1 after the column rotation
+              const float xc = c2 * cc - s2 * d, xd = s2 * cc + c2 * d;  // row q1
+              A[p1 + p2 * ld] = c1 * xa - s1 * xc;
+              A[p1 + q2 * ld] = c1 * xb - s1 * xd;
+              A[q1 + p2 * ld] = s1 * xa + c1 * xc;
+              A[q1 + q2 * ld] = s1 * xb + c1 * xd;
+            }
+          }
+          k2 += d2;
+          k1 += d1;
+          if (k2 >= h) {
+            k2 -= h;
+            ++k1;
+          }
+        }
       }
-      __syncthreads();
-      for (int k = k0; k < m / 2; k += kstep) {
-        const int p = pp[k], q = qq[k];
+      for (int k = k0; k < h; k += kstep) {
         const float s = sn[k];
+        const int q = qq[k];
         if (r0 >= n || q >= n || s == 0.f) continue;
-        const int col = r0;
+        const int p = pp[k];
         const float c = cs[k];
-        const float ap = A[p + col * ld], aq = A[q + col * ld];
-        A[p + col * ld] = c * ap - s * aq;
-        A[q + col * ld] = s * ap + c * aq;
+        const float wp = W[r0 + p * ld], wq = W[r0 + q * ld];
+        W[r0 + p * ld] = c * wp - s * wq;
+        W[r0 + q * ld] = s * wp + c * wq;
       }
       __syncthreads();
     }
   }
   // no error flag here: the FP64 refinement's final check decides
   for (int idx = tid; idx < n * n; idx += nt) W64[idx] = double(W[(idx % n) + (idx / n) * ld]);
+  if (tid == 0 && sweeps_out) *sweeps_out = sweep;
 }
 
 }  // namespace
@@ -727,10 +745,10 @@ size_t jacobi32_smem_limit() {
   return limit;
 }
 
-int jacobi32_smem(int n, const double* A, const double* W0, double* W, int* flags, cudaStream_t s) {
+int jacobi32_smem(int n, const double* A, const double* W0, double* W, int* sweeps_out, cudaStream_t s) {
   const size_t shm = jacobi32_smem_bytes(n);
   if (shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
-  jacobi32_smem_kernel<<<1, 1024, shm, s>>>(n, A, W0, W, flags);
+  jacobi32_smem_kernel<<<1, 1024, shm, s>>>(n, A, W0, W, sweeps_out);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }

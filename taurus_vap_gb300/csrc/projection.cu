@@ -261,10 +261,9 @@ __global__ void canon_kernel(int n, const double* __restrict__ rhoc, const doubl
   }
 }
 
-// per angle: U_phi, V_phi and the trailing n2 block of R_n
-__global__ void build_angle_kernel(int n, int G, const double* __restrict__ blk, const double2* __restrict__ eph,
-                                   const int* __restrict__ canon_i, double2* __restrict__ Uphi,
-                                   double2* __restrict__ Vphi, double2* __restrict__ Rn) {
+// per angle: U_phi, V_phi from the angle-independent blocks of U and V
+__global__ void build_uv_kernel(int n, int G, const double* __restrict__ blk, const double2* __restrict__ eph,
+                                double2* __restrict__ Uphi, double2* __restrict__ Vphi) {
   const size_t nn = size_t(n) * n;
   const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (idx >= nn * G) return;
@@ -282,14 +281,22 @@ __global__ void build_angle_kernel(int n, int G, const double* __restrict__ blk,
   vp.y = (vup - uvp) * pp.y + (vun - uvn) * pn.y;
   Uphi[idx] = up;
   Vphi[idx] = vp;
-  const int nemp = canon_i[1];
-  const int n2 = n - nemp;
-  const int i = int(e % n), j = int(e / n);
-  if (i >= nemp && j >= nemp) {
-    const double dp = blk[8 * nn + e], dn = blk[9 * nn + e];
-    Rn[size_t(b) * n2 * n2 + (i - nemp) + size_t(j - nemp) * n2] =
-        make_double2(dp * pp.x + dn * pn.x, dp * pp.y + dn * pn.y);
-  }
+}
+
+// per angle: the trailing n2 x n2 block (n2 = n - nemp) of R_n = D^T R D
+__global__ void build_rn_kernel(int n, int n2, int G, const double* __restrict__ blk,
+                                const double2* __restrict__ eph, double2* __restrict__ Rn) {
+  const size_t nn = size_t(n) * n, m2 = size_t(n2) * n2;
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= m2 * G) return;
+  const int b = int(idx / m2);
+  const size_t e2 = idx % m2;
+  const int i2 = int(e2 % n2), j2 = int(e2 / n2);
+  const int nemp = n - n2;
+  const size_t e = size_t(i2 + nemp) + size_t(j2 + nemp) * n;
+  const double2 pp = eph[2 * b], pn = eph[2 * b + 1];
+  const double dp = blk[8 * nn + e], dn = blk[9 * nn + e];
+  Rn[idx] = make_double2(dp * pp.x + dn * pn.x, dp * pp.y + dn * pn.y);
 }
 
 // broadcast a real n x n matrix into a complex batch
@@ -782,7 +789,10 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
     __syncthreads();
   }
   // X orthonormal and X^T A X block diagonal over clusters <=> invariant subspaces
-  if (tid == 0 && (red[0] > 1.0e-12 * fmax(nA, 1e-300) || rscal[3] > 1.0e-12 * sqrt(double(n)))) fail = 1;
+  if (tid == 0) {
+    if (red[0] > 1.0e-12 * fmax(nA, 1e-300)) fail |= 1;  // clusters still coupled
+    if (rscal[3] > 1.0e-12 * sqrt(double(n))) fail |= 2;  // not orthonormal
+  }
   __syncthreads();
   // per cluster: Jacobi on the cluster block (lane 0), then the warp rotates
   // the cluster's columns of X into D
@@ -800,7 +810,7 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
     }
     if (c < ncl && lane == 0) {
       if (m > CM) {
-        atomicOr(&fail, 1);
+        atomicOr(&fail, 4);  // cluster too large
       } else {
         double a[CM][CM], q[CM][CM];
         for (int r = 0; r < m; ++r)
@@ -1264,10 +1274,9 @@ int real_gemm(int M, int N, int K, View A, View B, double* C, int ldc, double al
 }  // namespace
 
 
-int blocked_thouless_solve(tvap_ctx* c, int G) {
+int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
   Workspace* w = c->ws;
   const int n = c->n;
-  cudaStream_t s = c->stream;
   const long long bsW = 2LL * n * n;
   // panels of at most kPanelMax columns, equal widths; the shared-memory panel
   // (n x nb complex) must fit, else the former wider kernels run from global
@@ -1366,12 +1375,59 @@ int blocked_thouless_solve(tvap_ctx* c, int G) {
 // degenerate clusters; the exact FP64 Jacobi runs only if the final check
 // (orthonormality, decoupled clusters) fails or n is too large for the
 // shared-memory stage.
-int eigen_canonical(tvap_ctx* c) {
+namespace {
+
+// Refinement steps from the approximate eigenvectors in *X (Xn scratch), the
+// exact treatment of near-degenerate clusters and the final check; *fail is
+// the check's verdict (read back on the host).
+int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, cudaStream_t s) {
   Workspace* w = c->ws;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
-  cudaStream_t s = c->stream;
+  const View Rho = view_cm(w->rho, n, 0);
   int rc;
+  for (int step = 0; step < steps; ++step) {
+    const View Xv = view_cm(X, n, 0);
+    if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
+    if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
+    if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+    refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+    refine_update_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
+    if ((rc = real_gemm(n, n, n, Xv, view_cm(w->Mr, n, 0), Xn, n, 1.0, 0.0, s))) return rc;
+    std::swap(X, Xn);
+  }
+  const View Xv = view_cm(X, n, 0);
+  if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+  refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+  cluster_finish_kernel<<<1, 256, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals,
+                                          reinterpret_cast<int*>(w->jwork), w->rflag);
+  TVAP_CUDA(cudaGetLastError());
+  c->kernel_launches += steps * 6 + 5;
+  int hr[2] = {1, 0};
+  TVAP_CUDA(cudaMemcpyAsync(hr, w->rflag, sizeof(hr), cudaMemcpyDeviceToHost, s));
+  TVAP_CUDA(cudaStreamSynchronize(s));
+  *fail = hr[0];
+  c->canon_attempts[3] += hr[1];
+  return TVAP_OK;
+}
+
+}  // namespace
+
+// Eigenvectors of rho (w->rho) into w->D (ascending): FP32 Jacobi in shared
+// memory (on rho rotated into the previous canonical basis when there is
+// one), three FP64 refinement steps on all SMs, exact diagonalisation of
+// degenerate clusters; the exact FP64 Jacobi runs only if the final check
+// (orthonormality, decoupled clusters) fails or n is too large for the
+// shared-memory stage.  (Refining the previous basis directly, without the
+// Jacobi stage, does not converge when the state moves by a full gradient
+// step: couplings exceed the gaps between canonical pairs.)
+int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
+  Workspace* w = c->ws;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  int rc, fail = 1;
   if (jacobi32_smem_bytes(n) <= jacobi32_smem_limit()) {
     double* X = w->Xr;
     double* Xn = w->Xn;
@@ -1381,38 +1437,21 @@ int eigen_canonical(tvap_ctx* c) {
       const View Dp = view_cm(w->D, n, 0);
       if ((rc = real_gemm(n, n, n, Rho, Dp, w->Br, n, 1.0, 0.0, s))) return rc;
       if ((rc = real_gemm(n, n, n, view_t(Dp), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
-      if ((rc = jacobi32_smem(n, w->Sr, w->D, X, c->d_flags, s))) return rc;
+      if ((rc = jacobi32_smem(n, w->Sr, w->D, X, w->rflag + 1, s))) return rc;
     } else {
-      if ((rc = jacobi32_smem(n, w->rho, nullptr, X, c->d_flags, s))) return rc;
+      if ((rc = jacobi32_smem(n, w->rho, nullptr, X, w->rflag + 1, s))) return rc;
     }
-    for (int step = 0; step < 3; ++step) {
-      const View Xv = view_cm(X, n, 0);
-      if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
-      if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
-      if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
-      refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
-      refine_update_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
-      if ((rc = real_gemm(n, n, n, Xv, view_cm(w->Mr, n, 0), Xn, n, 1.0, 0.0, s))) return rc;
-      std::swap(X, Xn);
-    }
-    const View Xv = view_cm(X, n, 0);
-    if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
-    if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
-    if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
-    refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
-    cluster_finish_kernel<<<1, 256, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals,
-                                            reinterpret_cast<int*>(w->jwork), w->rflag);
-    TVAP_CUDA(cudaGetLastError());
-    c->kernel_launches += 1 + 3 * 6 + 5;
-    int fail = 1;
-    TVAP_CUDA(cudaMemcpyAsync(&fail, w->rflag, sizeof(int), cudaMemcpyDeviceToHost, s));
-    TVAP_CUDA(cudaStreamSynchronize(s));
+    c->kernel_launches += 1;
+    ++c->canon_attempts[0];
+    if ((rc = refine_canonical(c, X, Xn, 3, &fail, s))) return rc;
     if (!fail) {
+      ++c->canon_attempts[1];
       w->have_basis = true;
       return TVAP_OK;
     }
   }
   // exact cyclic Jacobi in FP64
+  ++c->canon_attempts[2];
   TVAP_CUDA(cudaMemcpyAsync(w->jac, w->rho, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   if ((rc = jacobi_eigen(n, w->jac, w->D, w->evals, w->jwork, c->d_flags, s))) return rc;
   c->kernel_launches += 1;
@@ -1421,30 +1460,14 @@ int eigen_canonical(tvap_ctx* c) {
 }
 
 // Canonical basis + angle-independent blocks for state (w->U, w->V).
-int prepare_state(tvap_ctx* c, double occeps, double allemp_d, int* host_canon /*[3] or null*/) {
+// Angle-independent real blocks of U and V (0..7) on stream s.
+int prepare_uv_blocks(tvap_ctx* c, cudaStream_t s) {
   Workspace* w = c->ws;
   const int n = c->n, h = n / 2;
   const size_t nn = size_t(n) * n;
-  cudaStream_t s = c->stream;
   int rc;
-  const View Vn = view_cm(w->V, n, 0), Un = view_cm(w->U, n, 0);
-  sec_begin(c, SEC_CANONICAL);
-  // rho = V V^T, kappa = V U^T (construct_canonical_basis :826, :862)
-  if ((rc = real_gemm(n, n, n, Vn, view_t(Vn), w->rho, n, 1.0, 0.0, s))) return rc;
-  if ((rc = real_gemm(n, n, n, Vn, view_t(Un), w->kap, n, 1.0, 0.0, s))) return rc;
-  if ((rc = eigen_canonical(c))) return rc;
-  const View Dn = view_cm(w->D, n, 0);
-  // rhoc = D^T rho D, kappac = D^T kappa D
-  if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->rho, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
-  if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->rhoc, n, 1.0, 0.0, s))) return rc;
-  if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->kap, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
-  if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->kapc, n, 1.0, 0.0, s))) return rc;
-  const double eps = (occeps < 2.2250738585072014e-308) ? 1.0e-8 : occeps;
-  canon_kernel<<<1, 256, 0, s>>>(n, w->rhoc, w->kapc, eps, int(allemp_d), w->canon_i, w->canon_d);
-  TVAP_CUDA(cudaGetLastError());
-  sec_end(c, SEC_CANONICAL);
-  sec_begin(c, SEC_BLOCKS);
-  // angle-independent blocks (row halves p = 0..h-1, n = h..n-1)
+  sec_begin_on(c, SEC_BLOCKS, s);
+  // row halves p = 0..h-1, n = h..n-1
   const double* Xs[4][2] = {{w->V, w->V}, {w->U, w->U}, {w->V, w->U}, {w->U, w->V}};
   for (int q = 0; q < 4; ++q)
     for (int t = 0; t < 2; ++t) {
@@ -1455,94 +1478,121 @@ int prepare_state(tvap_ctx* c, double occeps, double allemp_d, int* host_canon /
                           s)))
         return rc;
     }
+  sec_end_on(c, SEC_BLOCKS, s);
+  c->kernel_launches += 8;
+  return TVAP_OK;
+}
+
+// Canonical basis (construct_canonical_basis) and its blocks (8, 9) on stream
+// s; host_canon receives nocc, nemp and the bad-block flag (s is
+// synchronised).
+int prepare_canonical(tvap_ctx* c, double occeps, double allemp_d, int* host_canon, cudaStream_t s) {
+  Workspace* w = c->ws;
+  const int n = c->n, h = n / 2;
+  const size_t nn = size_t(n) * n;
+  int rc;
+  const View Vn = view_cm(w->V, n, 0), Un = view_cm(w->U, n, 0);
+  sec_begin_on(c, SEC_CANONICAL, s);
+  // rho = V V^T, kappa = V U^T (construct_canonical_basis :826, :862)
+  if ((rc = real_gemm(n, n, n, Vn, view_t(Vn), w->rho, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, Vn, view_t(Un), w->kap, n, 1.0, 0.0, s))) return rc;
+  if ((rc = eigen_canonical(c, s))) return rc;
+  const View Dn = view_cm(w->D, n, 0);
+  // rhoc = D^T rho D, kappac = D^T kappa D
+  if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->rho, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->rhoc, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->kap, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
+  if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->kapc, n, 1.0, 0.0, s))) return rc;
+  const double eps = (occeps < 2.2250738585072014e-308) ? 1.0e-8 : occeps;
+  canon_kernel<<<1, 256, 0, s>>>(n, w->rhoc, w->kapc, eps, int(allemp_d), w->canon_i, w->canon_d);
+  TVAP_CUDA(cudaGetLastError());
   for (int t = 0; t < 2; ++t) {
     const double* L = w->D + t * h;
     if ((rc = real_gemm(n, n, h, View{L, n, 1, 0}, View{L, 1, n, 0}, w->blocks + (8 + t) * nn, n, 1.0, 0.0, s)))
       return rc;
   }
-  sec_end(c, SEC_BLOCKS);
-  c->kernel_launches += 13 + 1 + 2;
-  if (host_canon) {
-    TVAP_CUDA(cudaMemcpyAsync(host_canon, w->canon_i, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
-    TVAP_CUDA(cudaStreamSynchronize(s));
-  }
+  sec_end_on(c, SEC_CANONICAL, s);
+  c->kernel_launches += 2 + 4 + 1 + 2;
+  TVAP_CUDA(cudaMemcpyAsync(host_canon, w->canon_i, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+  TVAP_CUDA(cudaStreamSynchronize(s));
   return TVAP_OK;
 }
 
-// Angles [0, G) of the table: rotated quantities and their contribution to
-// the sums (accumulate = 0 starts new sums).  nocc/nemp are the host copies
-// of the canonical counts.
-int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d_weight, const double* d_mult,
-                   bool have_overlap, int nocc, int nemp, double factor_delta, int accumulate) {
+// Overlap chain of angles [0, G) on stream s2 (needs the canonical basis):
+// R_n, Z = R22^{-1} R21 and det R22, the Schur complement S, K = A1^{-1} +
+// S^T C0 S and its Pfaffian.
+int angles_overlap(tvap_ctx* c, int G, const double2* d_ephase, int nocc, int nemp, cudaStream_t s2) {
+  Workspace* w = c->ws;
+  const int n = c->n;
+  const int tb = 256;
+  int rc;
+  const int n2 = n - nemp, nb = n2 - nocc;
+  sec_begin_on(c, SEC_OVERLAP, s2);
+  build_rn_kernel<<<nblk(size_t(n2) * n2 * G, tb), tb, 0, s2>>>(n, n2, G, w->blocks, d_ephase, w->Rn);
+  const double2* S = w->Rn;
+  int ldS = n2;
+  long long bsS = (long long)n2 * n2;
+  if (nocc > 0) {
+    // Z = R22^{-1} R21 (nocc x nb), det(R22); S = R11 - R12 Z
+    left_solve_kernel<<<G, kLsThreads, 0, s2>>>(nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
+                                                View{w->Rn + nb, 1, n2, (long long)n2 * n2}, w->OW, w->OX, 1, nocc,
+                                                (long long)nocc * nb, 0, w->detR22, G, c->d_flags, DEV_SINGULAR_RN);
+    schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n2, nb, G, w->Rn, w->OX, w->SZ);
+    TVAP_CUDA(cudaGetLastError());
+    S = w->SZ;
+    ldS = nb;
+    bsS = (long long)nb * nb;
+  } else {
+    fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->detR22);
+  }
+  if (nb > 0) {
+    overlap_prep_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n, G, w->canon_i, w->canon_d, S, ldS, bsS,
+                                                                      w->K, w->OY);
+    TVAP_CUDA(cudaGetLastError());
+    // K += S^T Y
+    GemmArgs g{};
+    g.M = g.N = g.K = nb;
+    g.batch = G;
+    g.A = View{S, (long long)ldS, 1, bsS};
+    g.B = view_cm(w->OY, nb, (long long)nb * nb);
+    g.C = w->K;
+    g.crs = 1;
+    g.ccs = nb;
+    g.cbs = (long long)nb * nb;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(1.0, 0.0);
+    g.three_m = true;
+    g.upper_only = true;  // the Pfaffian reads the upper triangle only
+    if ((rc = gemm(g, s2))) return rc;
+    sec_end_on(c, SEC_OVERLAP, s2);
+    sec_begin_on(c, SEC_PFAFFIAN, s2);
+    if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s2))) return rc;
+    sec_end_on(c, SEC_PFAFFIAN, s2);
+  } else {
+    fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->pf);
+    sec_end_on(c, SEC_OVERLAP, s2);
+  }
+  TVAP_CUDA(cudaGetLastError());
+  c->kernel_launches += 1 + (nocc > 0 ? 2 : 1) + (nb > 0 ? 3 : 1);
+  return TVAP_OK;
+}
+
+// Thouless chain of angles [0, G) on stream s (needs only U, V and their
+// blocks): U_phi, V_phi, A_phi, U~, V~, the transition densities, the fields,
+// the traces and H20.
+int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_delta, cudaStream_t s) {
   Workspace* w = c->ws;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
-  cudaStream_t s = c->stream;
   const int tb = 256;
   int rc;
-  sec_begin(c, SEC_SOLVE);
-  build_angle_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(n, G, w->blocks, d_ephase, w->canon_i, w->Uphi, w->Vphi,
-                                                     w->Rn);
+  sec_begin_on(c, SEC_SOLVE, s);
+  build_uv_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(n, G, w->blocks, d_ephase, w->Uphi, w->Vphi);
   TVAP_CUDA(cudaGetLastError());
-  // overlap chain on the second stream (depends only on R_n and the
-  // canonical basis): runs concurrently with the Thouless chain below
-  const int n2 = n - nemp, nb = n2 - nocc;
-  if (have_overlap) {
-    cudaStream_t s2 = c->stream2;
-    TVAP_CUDA(cudaEventRecord(c->ev_fork, s));
-    TVAP_CUDA(cudaStreamWaitEvent(s2, c->ev_fork, 0));
-    sec_begin_on(c, SEC_OVERLAP, s2);
-    const double2* S = w->Rn;
-    int ldS = n2;
-    long long bsS = (long long)n2 * n2;
-    if (nocc > 0) {
-      // Z = R22^{-1} R21 (nocc x nb), det(R22); S = R11 - R12 Z
-      left_solve_kernel<<<G, kLsThreads, 0, s2>>>(
-          nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
-          View{w->Rn + nb, 1, n2, (long long)n2 * n2}, w->OW, w->OX, 1, nocc, (long long)nocc * nb, 0, w->detR22,
-          G, c->d_flags, DEV_SINGULAR_RN);
-      schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n2, nb, G, w->Rn, w->OX, w->SZ);
-      TVAP_CUDA(cudaGetLastError());
-      S = w->SZ;
-      ldS = nb;
-      bsS = (long long)nb * nb;
-    } else {
-      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->detR22);
-    }
-    if (nb > 0) {
-      overlap_prep_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n, G, w->canon_i, w->canon_d, S, ldS, bsS,
-                                                                        w->K, w->OY);
-      TVAP_CUDA(cudaGetLastError());
-      // K += S^T Y
-      GemmArgs g{};
-      g.M = g.N = g.K = nb;
-      g.batch = G;
-      g.A = View{S, (long long)ldS, 1, bsS};
-      g.B = view_cm(w->OY, nb, (long long)nb * nb);
-      g.C = w->K;
-      g.crs = 1;
-      g.ccs = nb;
-      g.cbs = (long long)nb * nb;
-      g.alpha = make_double2(1.0, 0.0);
-      g.beta = make_double2(1.0, 0.0);
-      g.three_m = true;
-      g.upper_only = true;  // the Pfaffian reads the upper triangle only
-      if ((rc = gemm(g, s2))) return rc;
-      sec_end_on(c, SEC_OVERLAP, s2);
-      sec_begin_on(c, SEC_PFAFFIAN, s2);
-      if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s2))) return rc;
-      sec_end_on(c, SEC_PFAFFIAN, s2);
-    } else {
-      fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->pf);
-      sec_end_on(c, SEC_OVERLAP, s2);
-    }
-    TVAP_CUDA(cudaEventRecord(c->ev_join, s2));
-  }
-
   // A_phi = conj(V_phi U_phi^{-1}): solve U_phi^T Y = V_phi^T, A = conj(Y^T)
-  if ((rc = blocked_thouless_solve(c, G))) return rc;
-  sec_end(c, SEC_SOLVE);
-  sec_begin(c, SEC_UV);
+  if ((rc = blocked_thouless_solve(c, G, s))) return rc;
+  sec_end_on(c, SEC_SOLVE, s);
+  sec_begin_on(c, SEC_UV, s);
   // U~ = U + V A, V~ = V + U A
   broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(nn, G, w->U, w->Ut);
   broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(nn, G, w->V, w->Vt);
@@ -1564,8 +1614,8 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
     g.C = w->Vt;
     if ((rc = gemm(g, s))) return rc;
   }
-  sec_end(c, SEC_UV);
-  sec_begin(c, SEC_DENSITIES);
+  sec_end_on(c, SEC_UV, s);
+  sec_begin_on(c, SEC_DENSITIES, s);
   // densities in angle-innermost layout: X[(i + j n) G + b]
   {
     GemmArgs g{};
@@ -1594,13 +1644,13 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
     g.C = w->kRL;
     if ((rc = gemm(g, s))) return rc;
   }
-  sec_end(c, SEC_DENSITIES);
+  sec_end_on(c, SEC_DENSITIES, s);
   if ((rc = fields_batched(c, G, G, w->rhoL, w->kLR, w->kRL, w->gam, w->hsp, w->dLR, w->dRL, s))) return rc;
-  sec_begin(c, SEC_TRACES);
+  sec_begin_on(c, SEC_TRACES, s);
   traces_kernel<<<G, 256, 0, s>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR, c->d_H1, c->H0, w->obs);
   TVAP_CUDA(cudaGetLastError());
-  sec_end(c, SEC_TRACES);
-  sec_begin(c, SEC_H20);
+  sec_end_on(c, SEC_TRACES, s);
+  sec_begin_on(c, SEC_H20, s);
   // H20: T = U~^T (h V~ + fd/2 DeltaLR U~) - fd/2 V~^T DeltaRL V~, H20 = T - T^T
   {
     const View hv{w->hsp, (long long)G, (long long)n * G, 1};
@@ -1640,18 +1690,47 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
     g.beta = make_double2(1.0, 0.0);
     if ((rc = gemm(g, s))) return rc;
   }
-  sec_end(c, SEC_H20);
-  if (have_overlap) TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
-  sec_begin(c, SEC_SUMS);
+  sec_end_on(c, SEC_H20, s);
+  c->kernel_launches += 1 + 2 + 2 + 3 + 1 + 5;
+  return TVAP_OK;
+}
+
+// Contribution of angles [0, G) to the gauge sums (accumulate = 0 starts new
+// sums), after both chains.
+int angles_sums(tvap_ctx* c, int G, const double2* d_weight, const double* d_mult, bool have_overlap,
+                int accumulate, cudaStream_t s) {
+  Workspace* w = c->ws;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  const int tb = 256;
+  sec_begin_on(c, SEC_SUMS, s);
   overlap_finish_kernel<<<nblk(G, tb), tb, 0, s>>>(n, G, have_overlap ? 1 : 0, w->canon_i, w->canon_d, w->pf,
                                                     w->detR22, d_weight, d_mult, w->obs, w->coefA, w->coefAE);
   sum_scalars_kernel<<<1, 32, 0, s>>>(G, w->obs, d_mult, d_weight, w->pscal, accumulate);
   sum_matrices_kernel<<<nblk(nn, tb), tb, 0, s>>>(n, G, w->A, w->T, w->coefA, w->coefAE, d_mult, w->pA, w->pH,
                                                   w->pAH, accumulate);
   TVAP_CUDA(cudaGetLastError());
-  sec_end(c, SEC_SUMS);
-  c->kernel_launches += 1 + 1 + 2 + 2 + 3 + 1 + 5 + (have_overlap ? (nocc > 0 ? 2 : 1) + (nb > 0 ? 3 : 1) : 0) + 3;
+  sec_end_on(c, SEC_SUMS, s);
+  c->kernel_launches += 3;
   return TVAP_OK;
+}
+
+// Angles [0, G) with the canonical basis already known (nocc/nemp its host
+// counts): overlap chain on the second stream, concurrent with the Thouless
+// chain, then the sums.
+int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d_weight, const double* d_mult,
+                   bool have_overlap, int nocc, int nemp, double factor_delta, int accumulate) {
+  cudaStream_t s = c->stream, s2 = c->stream2;
+  int rc;
+  if (have_overlap) {
+    TVAP_CUDA(cudaEventRecord(c->ev_fork, s));
+    TVAP_CUDA(cudaStreamWaitEvent(s2, c->ev_fork, 0));
+    if ((rc = angles_overlap(c, G, d_ephase, nocc, nemp, s2))) return rc;
+    TVAP_CUDA(cudaEventRecord(c->ev_join, s2));
+  }
+  if ((rc = angles_thouless(c, G, d_ephase, factor_delta, s))) return rc;
+  if (have_overlap) TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+  return angles_sums(c, G, d_weight, d_mult, have_overlap, accumulate, s);
 }
 
 int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s) {
@@ -1691,16 +1770,10 @@ int check_flags(tvap_ctx* c) {
 int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
   const int n = c->n;
   const size_t nn = size_t(n) * n;
-  cudaStream_t s = c->stream;
+  cudaStream_t s = c->stream, s2 = c->stream2;
   int canon[3] = {0, 0, 0};
   int rc;
-  if ((rc = prepare_state(c, o.seed_occeps, o.seed_allemp, canon))) return rc;
   const bool have_overlap = std::max(o.Mphip, o.Mphin) > 1;
-  if (canon[2] && have_overlap) {
-    set_last_error("canonical basis has a degenerate block larger than 2 or an odd paired block", __FILE__,
-                   __LINE__);
-    return TVAP_ERR_CANONICAL;
-  }
   const bool fold = (o.mode == 0) && std::fabs(o.facpi - 2.0 * M_PI) < 1e-12 && is_integer(o.valence_Z) &&
                     is_integer(o.valence_N);
   AngleTable t = make_angles(o, fold);
@@ -1717,12 +1790,30 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
   TVAP_CUDA(cudaMemcpyAsync(w->ephase, eph.data(), sizeof(double2) * 2 * G, cudaMemcpyHostToDevice, s));
   TVAP_CUDA(cudaMemcpyAsync(w->weight, wt.data(), sizeof(double2) * G, cudaMemcpyHostToDevice, s));
   TVAP_CUDA(cudaMemcpyAsync(w->mult, t.mult.data(), sizeof(double) * G, cudaMemcpyHostToDevice, s));
+  auto canon_error = [&]() {
+    set_last_error("canonical basis has a degenerate block larger than 2 or an odd paired block", __FILE__,
+                   __LINE__);
+    return TVAP_ERR_CANONICAL;
+  };
   if (o.mode == 0) {
-    if ((rc = project_angles(c, G, w->ephase, w->weight, w->mult, have_overlap, canon[0], canon[1], o.factor_delta,
-                             0)))
-      return rc;
+    // The Thouless chain needs only U and V: it is queued first on the main
+    // stream; the canonical basis (with its host-side checks) and the
+    // overlap chain follow on the second stream and run concurrently.
+    TVAP_CUDA(cudaEventRecord(c->ev_fork, s));
+    TVAP_CUDA(cudaStreamWaitEvent(s2, c->ev_fork, 0));
+    if ((rc = prepare_uv_blocks(c, s))) return rc;
+    if ((rc = angles_thouless(c, G, w->ephase, o.factor_delta, s))) return rc;
+    if ((rc = prepare_canonical(c, o.seed_occeps, o.seed_allemp, canon, s2))) return rc;
+    if (canon[2] && have_overlap) return canon_error();
+    if (have_overlap && (rc = angles_overlap(c, G, w->ephase, canon[0], canon[1], s2))) return rc;
+    TVAP_CUDA(cudaEventRecord(c->ev_join, s2));
+    TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+    if ((rc = angles_sums(c, G, w->weight, w->mult, have_overlap, 0, s))) return rc;
   } else {
     // plain form: one angle per launch sequence
+    if ((rc = prepare_uv_blocks(c, s))) return rc;
+    if ((rc = prepare_canonical(c, o.seed_occeps, o.seed_allemp, canon, s))) return rc;
+    if (canon[2] && have_overlap) return canon_error();
     for (int b = 0; b < G; ++b)
       if ((rc = project_angles(c, 1, w->ephase + 2 * b, w->weight + b, w->mult + b, have_overlap, canon[0],
                                canon[1], o.factor_delta, b > 0 ? 1 : 0)))

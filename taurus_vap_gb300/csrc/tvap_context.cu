@@ -112,6 +112,7 @@ int tvap_set_timing(tvap_ctx* c, int on) {
     c->section_ms[i] = 0.0;
     c->section_calls[i] = 0;
   }
+  for (long long& v : c->canon_attempts) v = 0;
   return TVAP_OK;
 }
 
@@ -128,6 +129,12 @@ int tvap_get_timing(tvap_ctx* c, double* ms, long long* calls, int nsec) {
     ms[i] = c->section_ms[i];
     if (calls) calls[i] = c->section_calls[i];
   }
+  return TVAP_OK;
+}
+
+int tvap_get_counters(tvap_ctx* c, long long* out, int nout) {
+  if (!c || !out) return TVAP_ERR_ARG;
+  for (int i = 0; i < nout && i < 4; ++i) out[i] = c->canon_attempts[i];
   return TVAP_OK;
 }
 

@@ -179,6 +179,9 @@ struct tvap_ctx {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_open;
   double section_ms[16] = {0};
   long long section_calls[16] = {0};
+  // canonical bases: [0] FP32 Jacobi + refinement attempts, [1] of them
+  // accepted, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in total
+  long long canon_attempts[4] = {0, 0, 0, 0};
 };
 
 namespace tvap {
@@ -223,7 +226,8 @@ int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int
 // from W0 and A64 must be W0^T A W0 (warm start); W64 = W0 J.
 size_t jacobi32_smem_bytes(int n);
 size_t jacobi32_smem_limit();
-int jacobi32_smem(int n, const double* A64, const double* W0, double* W64, int* flags, cudaStream_t s);
+// FP32 Jacobi in shared memory (one CTA); the number of sweeps goes to *sweeps_out (may be null)
+int jacobi32_smem(int n, const double* A64, const double* W0, double* W64, int* sweeps_out, cudaStream_t s);
 // Cholesky L L^T = A (lower), then L^{-1} in place
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
 

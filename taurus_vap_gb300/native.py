@@ -76,6 +76,8 @@ def lib():
         L.tvap_set_timing.restype = ci
         L.tvap_get_timing.argtypes = [vp, vp, vp, ci]
         L.tvap_get_timing.restype = ci
+        L.tvap_get_counters.argtypes = [vp, vp, ci]
+        L.tvap_get_counters.restype = ci
         L.tvap_set_gemm_mode.argtypes = [vp, ci]
         L.tvap_set_gemm_mode.restype = ci
         L.tvap_set_hamiltonian.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp, vp]
@@ -153,6 +155,13 @@ class Context:
         calls = np.zeros(16, dtype=np.int64)
         _check(lib().tvap_get_timing(self.h, _p(ms), _p(calls), 16), "tvap_get_timing")
         return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(self.SECTIONS)}
+
+    def canonical_paths(self):
+        """Canonical-basis counters since the last set_timing: (FP32 Jacobi +
+        refinement attempts, accepted, exact FP64 Jacobi runs, FP32 sweeps)."""
+        out = np.zeros(4, dtype=np.int64)
+        _check(lib().tvap_get_counters(self.h, _p(out), 4), "tvap_get_counters")
+        return tuple(int(v) for v in out)
 
     GEMM_FP64, GEMM_EMULATED = 0, 1
 
