@@ -261,7 +261,11 @@ int gemm(const GemmArgs& g, cudaStream_t s) {
   // (canonical-basis refinement, per-iteration blocks, evolution) stay on the
   // FP64 pipe
   if (g_gemm_mode == 1 && g.K >= 16 && double(g.M) * g.N * g.K * g.batch >= 2.0e7) return gemm_ozaki(g, s);
-  switch (pick_tile(g.M, g.N)) {
+  // few tiles in all (single small products): the smallest tile, to spread
+  // the latency-bound work over more SMs
+  const long long t28 = (long long)((g.M + 27) / 28) * ((g.N + 27) / 28) * g.batch;
+  const int tile = (t28 < 76) ? 16 : pick_tile(g.M, g.N);
+  switch (tile) {
     case 16: launch_gemm_tile<16>(g, s); break;
     case 24: launch_gemm_tile<24>(g, s); break;
     case 28: launch_gemm_tile<28>(g, s); break;
@@ -829,8 +833,80 @@ __global__ void __launch_bounds__(1024) cholesky_inverse_kernel(int n, double* A
 }  // namespace
 
 // A must have room for n*n + n doubles (scratch row).
+// The same factorisation with the matrix in shared memory (n^2 doubles): the
+// right-looking Cholesky with two barriers per column, then L^{-1} one
+// column per thread (forward substitution L x = e_j, no barriers), x kept in
+// the free upper triangle.
+constexpr int kCholThreads = 512;
+__global__ void __launch_bounds__(kCholThreads) cholesky_inverse_smem_kernel(int n, double* A, int* flags) {
+  extern __shared__ double chol_smem[];  // n x n column-major, then dinv[n]
+  double* Ls = chol_smem;
+  double* dinv = Ls + size_t(n) * n;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  auto L = [Ls, n](int i, int j) -> double& { return Ls[i + size_t(j) * n]; };
+  for (int idx = tid; idx < n * n; idx += nt) Ls[idx] = A[idx];
+  __syncthreads();
+  bool bad = false;
+  for (int k = 0; k < n; ++k) {
+    const double d = L(k, k);
+    if (!(d > 0.0)) {
+      bad = true;  // uniform: every thread read the same value
+      break;
+    }
+    const double dk = sqrt(d);
+    for (int i = k + 1 + tid; i < n; i += nt) L(i, k) = L(i, k) / dk;
+    __syncthreads();
+    if (tid == 0) L(k, k) = dk;
+    for (int j = k + 1 + warp; j < n; j += nw) {
+      const double ljk = L(j, k);
+      for (int i = j + lane; i < n; i += 32) L(i, j) = fma(-L(i, k), ljk, L(i, j));
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (tid == 0) atomicOr(flags, DEV_CHOLESKY);
+    return;
+  }
+  for (int i = tid; i < n; i += nt) {
+    if (L(i, i) == 0.0) atomicOr(flags, DEV_TRTRI);
+    dinv[i] = 1.0 / L(i, i);
+  }
+  __syncthreads();
+  // column j of L^{-1}: x_j = 1/L_jj, x_i = -(sum_{k=j..i-1} L_ik x_k) / L_ii,
+  // x_i (i > j) stored at the upper-triangle position (j, i)
+  for (int j = tid; j < n; j += nt) {
+    const double xj = dinv[j];
+    for (int i = j + 1; i < n; ++i) {
+      double s0 = L(i, j) * xj, s1 = 0.0;
+      int k = j + 1;
+      for (; k + 1 < i; k += 2) {
+        s0 = fma(L(i, k), L(j, k), s0);
+        s1 = fma(L(i, k + 1), L(j, k + 1), s1);
+      }
+      if (k < i) s0 = fma(L(i, k), L(j, k), s0);
+      L(j, i) = -(s0 + s1) * dinv[i];
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < n * n; idx += nt) {
+    const int i = idx % n, j = idx / n;
+    A[idx] = (i == j) ? dinv[j] : (i > j ? L(j, i) : 0.0);
+  }
+}
+
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s) {
-  cholesky_inverse_kernel<<<1, 1024, 0, s>>>(n, A, flags);
+  const size_t shm = sizeof(double) * (size_t(n) * n + n);
+  if (shm <= jacobi32_smem_limit()) {
+    static bool attr = false;
+    if (!attr) {
+      TVAP_CUDA(cudaFuncSetAttribute(cholesky_inverse_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(jacobi32_smem_limit())));
+      attr = true;
+    }
+    cholesky_inverse_smem_kernel<<<1, kCholThreads, shm, s>>>(n, A, flags);
+  } else {
+    cholesky_inverse_kernel<<<1, 1024, 0, s>>>(n, A, flags);
+  }
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }

@@ -172,7 +172,12 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
   c->own_stream = true;
-  if ((e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  // the second stream carries the latency-bound chain (canonical basis,
+  // Pfaffians): it gets the highest priority so that its few CTAs are
+  // scheduled ahead of the wide kernels of the main stream
+  int prio_lo = 0, prio_hi = 0;
+  if ((e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithPriority(&c->stream2, cudaStreamNonBlocking, prio_hi)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_2mj, sizeof(int) * n)) != cudaSuccess) return fail(e);
