@@ -590,22 +590,24 @@ int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int
 // ---------------------------------------------------------------------------
 namespace {
 
+struct __align__(16) JRot {
+  float c, s;
+  int p, q;
+};
+
 __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double* __restrict__ A64,
                                                               const double* __restrict__ W0,
                                                               double* __restrict__ W64, int* sweeps_out) {
   extern __shared__ float js[];
   const int m = (n + 1) & ~1;
+  const int h = m / 2;
   const int ld = n | 1;                  // odd leading dimension: conflict-free row access
   float* A = js;                         // n x ld
   float* W = A + size_t(n) * ld;         // n x ld
-  float* cs = W + size_t(n) * ld;        // m/2
-  float* sn = cs + m / 2;                // m/2
-  int* pairs = reinterpret_cast<int*>(sn + m / 2);  // m
-  int* pp = pairs + m;                   // m/2
-  int* qq = pp + m / 2;                  // m/2
+  JRot* rot = reinterpret_cast<JRot*>(W + size_t(n) * ld);  // 16-byte aligned: n is even
   __shared__ float red[1024];
   __shared__ int done;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   float fro = 0.f;
   for (int idx = tid; idx < n * n; idx += nt) {
     const int i = idx % n, j = idx / n;
@@ -614,7 +616,6 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
     W[i + j * ld] = W0 ? float(W0[idx]) : ((i == j) ? 1.f : 0.f);
     fro += a * a;
   }
-  for (int i = tid; i < m; i += nt) pairs[i] = i;
   red[tid] = fro;
   __syncthreads();
   for (int s = nt / 2; s > 0; s >>= 1) {
@@ -622,11 +623,8 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
     __syncthreads();
   }
   const float tol2 = red[0] * 1.0e-12f;  // off-diagonal <= 1e-6 ||A||: enough for the FP64 refinement
-  const int h = m / 2;
-  // fixed thread -> first 2 x 2 block (k1, k2) and its stride over the h x h blocks
-  const int b1 = tid / h, b2 = tid % h, d1 = nt / h, d2 = nt % h;
-  // fixed thread -> (row, first pair) assignment: no index division in the sweeps
-  const int kstep = nt / n;           // threads per row group (>= 1 for n <= 1024)
+  // off-norm: thread -> (row, first column) with a fixed stride
+  const int kstep = nt / n;
   const int r0 = (tid < kstep * n) ? tid % n : n;
   const int k0 = (tid < kstep * n) ? tid / n : 0;
   __syncthreads();
@@ -670,49 +668,54 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
             c = rsqrtf(t * t + 1.f);
             s = t * c;
           }
+        } else {
+          q = p;  // padding player: no rotation, keep the indices in range
         }
-        pp[k] = p;
-        qq[k] = q;
-        cs[k] = c;
-        sn[k] = s;
+        rot[k] = JRot{c, s, p, q};
       }
       __syncthreads();
-      // A <- J^T A J one 2 x 2 block (row pair k1, column pair k2) per item;
-      // W <- W J one (row, pair) per item.  Blocks are disjoint: no hazards.
+      // A <- J^T A J: warp w takes the row pairs w, w + nw, ..., its lanes the
+      // column pairs lane, lane + 32, lane + 64; every 2 x 2 block is read and
+      // written once.  W <- W J: warp per pair, lanes over rows.
       {
-        int k1 = b1, k2 = b2;
-        while (k1 < h) {
-          const float s1 = sn[k1], s2 = sn[k2];
-          if (s1 != 0.f || s2 != 0.f) {
-            const int p1 = pp[k1], q1 = qq[k1], p2 = pp[k2], q2 = qq[k2];
-            if (q1 < n && q2 < n) {
-              const float c1 = cs[k1], c2 = cs[k2];
-              const float a = A[p1 + p2 * ld], b = A[p1 + q2 * ld], cc = A[q1 + p2 * ld], d = A[q1 + q2 * ld];
-              const float xa = c2 * a - s2 * b, xb = s2 * a + c2 * b;    // row p1 after the column rotation
-              const float xc = c2 * cc - s2 * d, xd = s2 * cc + c2 * d;  // row q1
-              A[p1 + p2 * ld] = c1 * xa - s1 * xc;
-              A[p1 + q2 * ld] = c1 * xb - s1 * xd;
-              A[q1 + p2 * ld] = s1 * xa + c1 * xc;
-              A[q1 + q2 * ld] = s1 * xb + c1 * xd;
-            }
-          }
-          k2 += d2;
-          k1 += d1;
-          if (k2 >= h) {
-            k2 -= h;
-            ++k1;
+        JRot r2[3];
+        int o2p[3], o2q[3];
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          const int k2 = lane + 32 * jj;
+          r2[jj] = (k2 < h) ? rot[k2] : JRot{1.f, 0.f, 0, 0};
+          o2p[jj] = r2[jj].p * ld;
+          o2q[jj] = r2[jj].q * ld;
+        }
+        for (int k1 = warp; k1 < h; k1 += nw) {
+          const JRot r1 = rot[k1];
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            const int k2 = lane + 32 * jj;
+            if (k2 >= h || (r1.s == 0.f && r2[jj].s == 0.f) || r1.p == r1.q || r2[jj].p == r2[jj].q) continue;
+            const float c1 = r1.c, s1 = r1.s, c2 = r2[jj].c, s2 = r2[jj].s;
+            float* a0 = A + r1.p;
+            float* a1 = A + r1.q;
+            const float a = a0[o2p[jj]], b = a0[o2q[jj]], cc = a1[o2p[jj]], d = a1[o2q[jj]];
+            const float xa = c2 * a - s2 * b, xb = s2 * a + c2 * b;    // row p1 after the column rotation
+            const float xc = c2 * cc - s2 * d, xd = s2 * cc + c2 * d;  // row q1
+            a0[o2p[jj]] = c1 * xa - s1 * xc;
+            a0[o2q[jj]] = c1 * xb - s1 * xd;
+            a1[o2p[jj]] = s1 * xa + c1 * xc;
+            a1[o2q[jj]] = s1 * xb + c1 * xd;
           }
         }
-      }
-      for (int k = k0; k < h; k += kstep) {
-        const float s = sn[k];
-        const int q = qq[k];
-        if (r0 >= n || q >= n || s == 0.f) continue;
-        const int p = pp[k];
-        const float c = cs[k];
-        const float wp = W[r0 + p * ld], wq = W[r0 + q * ld];
-        W[r0 + p * ld] = c * wp - s * wq;
-        W[r0 + q * ld] = s * wp + c * wq;
+        for (int k = warp; k < h; k += nw) {
+          const JRot r = rot[k];
+          if (r.s == 0.f || r.p == r.q) continue;
+          float* wp = W + r.p * ld;
+          float* wq = W + r.q * ld;
+          for (int row = lane; row < n; row += 32) {
+            const float x = wp[row], y = wq[row];
+            wp[row] = r.c * x - r.s * y;
+            wq[row] = r.s * x + r.c * y;
+          }
+        }
       }
       __syncthreads();
     }
@@ -726,7 +729,7 @@ __global__ void __launch_bounds__(1024) jacobi32_smem_kernel(int n, const double
 
 size_t jacobi32_smem_bytes(int n) {
   const int m = (n + 1) & ~1;
-  return sizeof(float) * (2 * size_t(n) * (n | 1) + m) + sizeof(int) * 2 * m + 64;
+  return sizeof(float) * (2 * size_t(n) * (n | 1) + 4) + 16 * size_t(m / 2) + 64;
 }
 
 // largest dynamic shared memory the FP32 Jacobi kernel may request on this device
