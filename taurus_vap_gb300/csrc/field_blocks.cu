@@ -135,9 +135,9 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
     const int j = nt0 + wn + 2 * (lane & 3) + (q & 1);
     const int p = rowperm[rr];
     if (p < 0 || j >= ncols_tot) continue;
-    const int sc = ea[rr] + col_exp(eb_enc, j) - 57;
+    const double p2 = oz::pow2(ea[rr] + col_exp(eb_enc, j) - 57);
     const double2 v0 = oz::acc_value(o, q);
-    const double2 v = make_double2(ldexp(v0.x, sc), ldexp(v0.y, sc));
+    const double2 v = make_double2(v0.x * p2, v0.y * p2);
     if (!DELTA) {
       out0[(long long)p * ldc + j] = v;
       out1[(long long)p * ldc + j] = cadd(v, H1[p]);

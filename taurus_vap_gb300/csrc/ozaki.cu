@@ -95,25 +95,40 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
   double2 alpha = g.alpha;
   if (g.alpha_vec) alpha = cmul(alpha, g.alpha_vec[b]);
   const bool cplx_out = !g.c_real;
+  const bool alpha_real = alpha.y == 0.0;
+  const bool beta_zero = g.beta.x == 0.0 && g.beta.y == 0.0;
+  const bool beta_one = g.beta.x == 1.0 && g.beta.y == 0.0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int i = mt0 + wm + (lane >> 2) + ((q & 2) ? 8 : 0);
     const int j = nt0 + wn + 2 * (lane & 3) + (q & 1);
     if (i >= M || j >= N) continue;
-    const int sc = ea[size_t(b) * mpad + i] + eb[size_t(b) * npad + j] - 57;
+    // the power-of-two scale is exact: folding it into alpha rounds as
+    // scaling first would
+    const double p2 = oz::pow2(ea[size_t(b) * mpad + i] + eb[size_t(b) * npad + j] - 57);
     const double2 v0 = oz::acc_value(o, q);
-    const double vr = ldexp(v0.x, sc), vi = ldexp(v0.y, sc);
     const long long idx = i * g.crs + j * g.ccs + b * g.cbs;
+    double2 v;
+    if (alpha_real) {
+      const double f = alpha.x * p2;
+      v = make_double2(v0.x * f, v0.y * f);
+    } else {
+      v = cmul(alpha, make_double2(v0.x * p2, v0.y * p2));
+    }
     if (cplx_out) {
       double2* C = static_cast<double2*>(g.C);
-      double2 v = cmul(alpha, make_double2(vr, vi));
-      if (g.beta.x != 0.0 || g.beta.y != 0.0) v = cadd(v, cmul(g.beta, C[idx]));
+      if (beta_one) {
+        const double2 c0 = C[idx];
+        v = make_double2(v.x + c0.x, v.y + c0.y);
+      } else if (!beta_zero) {
+        v = cadd(v, cmul(g.beta, C[idx]));
+      }
       C[idx] = v;
     } else {
       double* C = static_cast<double*>(g.C);
-      double v = (cmul(alpha, make_double2(vr, vi))).x;
-      if (g.beta.x != 0.0) v = fma(g.beta.x, C[idx], v);
-      C[idx] = v;
+      double r = v.x;
+      if (!beta_zero) r = fma(g.beta.x, C[idx], r);
+      C[idx] = r;
     }
   }
 }

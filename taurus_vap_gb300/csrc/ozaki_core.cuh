@@ -286,6 +286,11 @@ __device__ __forceinline__ void mainloop(const __nv_bfloat16* A, size_t a_plane,
   }
 }
 
+// 2^e as a double: built from its bits in the normal range, ldexp outside
+__device__ __forceinline__ double pow2(int e) {
+  return (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : ldexp(1.0, e);
+}
+
 // value of output q, before the exponent scale 2^(ea + eb - 57)
 __device__ __forceinline__ double2 acc_value(const Acc& o, int q) {
   return make_double2(fma(double(o.hr[q]), 0x1p28, double(o.lr[q])), fma(double(o.hi[q]), 0x1p28, double(o.li[q])));
