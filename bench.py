@@ -156,6 +156,11 @@ def host_iteration(ctx, state, mode):
     return (U1, V1, Zi), (pnp.c("ener") / pnp.c("over")).real
 
 
+# DRAM bytes (read + write) of one H20-shaped ozaki_mma_kernel<2,2> launch at
+# n = 140, G = 113, from `ncu --set full` (profiles/ozaki_mma_h20_emax4.md)
+H20_TRAFFIC_PER_LAUNCH = 191.9e6
+
+
 def fp64_flops_per_iteration(n, G):
     """Algorithmic FP64 flops of the reduced per-angle formulation."""
     return G * (10.7 + 8 + 12 + 40 + 4 + 1.4) * n ** 3
@@ -193,7 +198,10 @@ def run_ours(args):
         it.step()
     torch.cuda.synchronize()
     barrier()
-    ctx.set_timing(False)
+    # section events on the launching streams stay on in the timed region:
+    # they give the per-launch times of the roofline (a few event records per
+    # step, no synchronisation)
+    ctx.set_timing(True)
     it.launches = 0
     clocks = ClockSampler(local)
     clocks.start()
@@ -209,14 +217,9 @@ def run_ours(args):
     clk = clocks.stop()
     ms = t0.elapsed_time(t1)
     launches = it.launches
-    # per-section times from separate instrumented steps (events on the streams)
-    ctx.set_timing(True)
-    sec_steps = max(1, min(args.steps, 5))
-    for _ in range(sec_steps):
-        it.step()
-    torch.cuda.synchronize()
     sections = ctx.get_timing()
     canon_paths = ctx.canonical_paths()
+    sec_steps = args.steps
     ctx.set_timing(False)
     if world > 1:
         import torch.distributed as dist
@@ -228,20 +231,22 @@ def run_ours(args):
     value = world * args.steps / (ms / 1000.0)
 
     # ---- same iteration with every dense product on the FP64 pipe (DFMA)
-    ctx.set_gemm_mode(0)
-    itf = DeviceIteration(ctx, U, V, 0, torch)
-    itf.step()
-    torch.cuda.synchronize()
-    fa = torch.cuda.Event(enable_timing=True)
-    fb = torch.cuda.Event(enable_timing=True)
-    fa.record(stream)
-    for _ in range(args.steps):
+    fp64_pipe = None
+    if not args.no_fp64_leg:
+        ctx.set_gemm_mode(0)
+        itf = DeviceIteration(ctx, U, V, 0, torch)
         itf.step()
-    fb.record(stream)
-    torch.cuda.synchronize()
-    fp64_pipe = {"value": world * args.steps / (fa.elapsed_time(fb) / 1000.0), "unit": "iters/s",
-                 "ms_per_step": fa.elapsed_time(fb) / args.steps}
-    ctx.set_gemm_mode(1)
+        torch.cuda.synchronize()
+        fa = torch.cuda.Event(enable_timing=True)
+        fb = torch.cuda.Event(enable_timing=True)
+        fa.record(stream)
+        for _ in range(args.steps):
+            itf.step()
+        fb.record(stream)
+        torch.cuda.synchronize()
+        fp64_pipe = {"value": world * args.steps / (fa.elapsed_time(fb) / 1000.0), "unit": "iters/s",
+                     "ms_per_step": fa.elapsed_time(fb) / args.steps}
+        ctx.set_gemm_mode(1)
 
     # ---- plain form (one angle per launch sequence), same state
     plain = None
@@ -274,7 +279,12 @@ def run_ours(args):
     d2h = 8 * n * n * (1 + 1 + 2)
     e2e = {"value": world * 1000.0 / e_ms, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
-    # ---- roofline of the dominant kernel, from the live section timings
+    # ---- roofline of the dominant kernel, from the live section timings.
+    # The dominant kernel (launch list in profiles/) is the emulated complex
+    # GEMM ozaki_mma_kernel<2,2>; its largest use is H20: 5 products of
+    # n x n x n complex per angle (3M: 3 real products per digit pair, 36 digit
+    # pairs, bf16 m16n8k16 on the tensor cores).  The H20 section also holds
+    # the 10 operand-splitting launches (about 15 % of it in the launch list).
     G_total = MPHI * MPHI
     G = (G_total + 1) // 2  # folded angle pairs computed
     S = mdl.ham.S
@@ -284,31 +294,45 @@ def run_ours(args):
     except (OSError, ValueError):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    fp64_peak = 1.25  # TFLOP/s nominal; see profiles/fp64_peak.md for the measured figure
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    peak_src = "MEASURED_PEAKS.json" if "bf16_tflops" in peaks else "fallback"
+    fp64_peak = 1.25  # TFLOP/s nominal; profiles/fp64_peak.md holds the measured figure
     try:
         for line in open(os.path.join(ROOT, "profiles", "fp64_peak.md")):
             if line.startswith("measured_fp64_tflops:"):
                 fp64_peak = float(line.split(":")[1])
     except OSError:
         pass
-    steps = args.steps
+    h20_launch_ms = sections["h20"][0] / sec_steps / 5.0
+    h20_flops = 2.0 * n ** 3 * 36 * 3 * G  # bf16 tensor flops per launch (unpadded)
+    h20_tflops = h20_flops / (h20_launch_ms / 1000.0) / 1e12
+    roofline = {
+        "kernel": "ozaki_mma_kernel<2,2>: H20 complex GEMM n x n x n x G, FP64 emulated on bf16 mma (per launch, "
+                  "incl. operand splitting)",
+        "bound": "tensor",
+        "achieved": h20_tflops,
+        "peak": bf16_peak,
+        "unit": "TFLOP/s",
+        "frac": h20_tflops / bf16_peak,
+        "traffic": H20_TRAFFIC_PER_LAUNCH,
+        "algorithmic_flops_per_launch": h20_flops,
+        "ms_per_launch": h20_launch_ms,
+        "peak_source": f"{peak_src} bf16_tflops (burst, of measured)",
+        "fp64_equivalent_tflops": 2.0 * 3 * n ** 3 * G / (h20_launch_ms / 1000.0) / 1e12,
+    }
     fld_ms = (sections["fields_gamma"][0] + sections["fields_delta"][0]) / sec_steps
     fld_bytes = 13 * S + 16 * n * n * 7 * G
-    dom = max(sections.items(), key=lambda kv: kv[1][0])
-    roofline = {
-        "kernel": "fields (calculate_fields gather, Gamma + Delta, all angles)",
-        "bound": "hbm",
-        "achieved": fld_bytes / (fld_ms / 1000.0) / 1e9,
-        "peak": hbm_peak,
-        "unit": "GB/s",
-        "frac": (fld_bytes / (fld_ms / 1000.0) / 1e9) / hbm_peak,
-        "traffic": None,
-        "algorithmic_bytes_per_launch": fld_bytes,
-        "ms_per_launch": fld_ms,
-        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+    roofline_fields = {
+        "kernel": "calculate_fields (Gamma + Delta, all angles): dense symmetry blocks, FP64 emulated on bf16 mma",
+        "bound": "tensor",
+        "algorithmic_bytes": fld_bytes,
+        "achieved_gbs": fld_bytes / (fld_ms / 1000.0) / 1e9,
+        "hbm_frac": (fld_bytes / (fld_ms / 1000.0) / 1e9) / hbm_peak,
+        "fp64_equivalent_tflops": 4 * 8 * (S * 1.65) * G * 1.0 / (fld_ms / 1000.0) / 1e12,
+        "ms_per_step": fld_ms,
     }
+    dom = max(sections.items(), key=lambda kv: kv[1][0])
     sec_ms = {k: v[0] / sec_steps for k, v in sections.items()}
-    total_sec = sum(sec_ms.values())
     fp64 = fp64_flops_per_iteration(n, G) + 4 * 8 * (S * 1.65) * G  # dense + fields (48 flops x passes)
     roofline_fp64 = {
         "scope": "whole iteration",
@@ -335,6 +359,7 @@ def run_ours(args):
                    "dense_products": "FP64 emulated on the bf16 tensor cores (exact integer splitting)",
                    "eta": ETA, "mu": MU},
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "roofline_fp64": roofline_fp64,
+        "roofline_fields": roofline_fields,
         "sections_ms_per_step": {k: round(v, 4) for k, v in sec_ms.items()},
         "dominant_section": dom[0], "canonical_paths": canon_paths, "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
         "final_energy": it.energy,
@@ -350,61 +375,68 @@ def run_ours(args):
 # --------------------------------------------------------------------------
 # CPU legs (oracle)
 # --------------------------------------------------------------------------
-def _oracle_iteration_time(mdl, U, V, Mp, Mn, nthreads, reps=1):
+def _oracle_vap(mdl, U, V, nthreads):
+    """The oracle's gradient loop on the full workload (15 x 15 angles)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
 
     import oracle as O
 
     om = O.OracleModel(mdl)
-    vap = O.OracleVAP(om, U, V, Mp, Mn, 2 * math.pi, ZV, NV, ETA, MU, 0.0, np.zeros((0, mdl.n * mdl.n)),
-                      np.zeros(0), nthreads=nthreads)
-    best = None
-    for _ in range(reps):
+    return O.OracleVAP(om, U, V, MPHI, MPHI, 2 * math.pi, ZV, NV, ETA, MU, 0.0, np.zeros((0, mdl.n * mdl.n)),
+                       np.zeros(0), nthreads=nthreads)
+
+
+def _timed_iterations(vap, count, budget_s):
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < count and (not times or time.perf_counter() - t_start < budget_s):
         t = time.perf_counter()
         vap.iterate()
-        dt = time.perf_counter() - t
-        best = dt if best is None else min(best, dt)
-    return best
+        times.append(time.perf_counter() - t)
+    return times
 
 
 def cpu_baseline(mdl, U, V, args):
+    """Oracle (CPU restatement of the reference path) on all host cores: one
+    warm-up iteration, then up to 3 timed iterations of the full workload
+    (stopping once 20 s have passed); the median is reported."""
     cores = os.cpu_count() or 1
-    t2 = _oracle_iteration_time(mdl, U, V, 1, 2, cores)
-    t9 = _oracle_iteration_time(mdl, U, V, 3, 3, cores)
-    per_angle = max((t9 - t2) / 7.0, 1e-9)
-    t225 = t2 + (MPHI * MPHI - 2) * per_angle
-    return {"value": 1.0 / t225, "unit": "iters/s", "cores": cores, "kind": "port",
-            "sample": f"oracle iterations with 1x2 and 3x3 angle grids ({t2:.2f} s, {t9:.2f} s), "
-                      f"extrapolated linearly in the angle count to 15x15 ({t225:.1f} s/iteration)"}
+    vap = _oracle_vap(mdl, U, V, cores)
+    vap.iterate()
+    times = sorted(_timed_iterations(vap, 3, 20.0))
+    med = times[len(times) // 2]
+    return {"value": 1.0 / med, "unit": "iters/s", "cores": cores, "kind": "port",
+            "sample": f"{len(times)} oracle iterations of the full workload (15x15 angles, n = 140) after one "
+                      f"warm-up, {cores} threads; median {med:.2f} s/iteration"}
 
 
 def run_reference(args):
+    """--impl reference: the oracle's gradient loop on the host cores, W
+    warm-up and K timed iterations of the full workload (rank 0 only)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     mdl, U, V = build_workload()
     cores = os.cpu_count() or 1
+    vap = _oracle_vap(mdl, U, V, cores)
     for _ in range(args.warmup):
-        pass
-    samples = []
+        vap.iterate()
     t_start = time.perf_counter()
-    base = cpu_baseline(mdl, U, V, args)
-    for _ in range(max(1, args.steps)):
-        t9 = _oracle_iteration_time(mdl, U, V, 3, 3, cores)
-        samples.append(t9)
+    times = _timed_iterations(vap, max(1, args.steps), 1e30)
     elapsed = time.perf_counter() - t_start
-    value = base["value"]
-    ms = 1000.0 / value
+    value = len(times) / elapsed
+    ms = 1000.0 * elapsed / len(times)
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": WORKLOAD, "form": "CPU restatement of the reference path (oracle/), OpenMP fields + "
                                                  "threaded BLAS/LAPACK"},
-        "cpu_baseline": {"value": value, "unit": "iters/s", "cores": cores, "kind": "port", "sample": base["sample"]},
+        "cpu_baseline": {"value": value, "unit": "iters/s", "cores": cores, "kind": "port",
+                         "sample": f"{len(times)} oracle iterations of the full workload after {args.warmup} "
+                                   f"warm-up, {cores} threads"},
         "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "wall_s": elapsed,
     }
     print(json.dumps(out))
 
@@ -417,6 +449,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64-pipe comparison run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
