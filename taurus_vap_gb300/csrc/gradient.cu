@@ -93,11 +93,47 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1) {
   if ((rc = cholesky_inverse(n, b.L, c->d_flags, s))) return rc;
   TVAP_CUDA(cudaMemcpyAsync(b.A1, b.U0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   TVAP_CUDA(cudaMemcpyAsync(b.A2, b.V0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
-  if ((rc = rgemm(n, n, n, view_cm(b.V0, n, 0), Zv, b.A1, n, 1.0, 1.0, s))) return rc;
-  if ((rc = rgemm(n, n, n, view_cm(b.U0, n, 0), Zv, b.A2, n, 1.0, 1.0, s))) return rc;
   const View LinvT = view_t(view_cm(b.L, n, 0));
-  if ((rc = rgemm(n, n, n, view_cm(b.A1, n, 0), LinvT, U1, n, 1.0, 0.0, s))) return rc;
-  if ((rc = rgemm(n, n, n, view_cm(b.A2, n, 0), LinvT, V1, n, 1.0, 0.0, s))) return rc;
+  // A1 = U0 + V0 Z, A2 = V0 + U0 Z as one batch of two when A2 follows A1
+  // (then U1 = A1 L^-T, V1 = A2 L^-T likewise when V1 follows U1)
+  const bool pair_a = (b.A2 == b.A1 + nn);
+  const bool pair_u = pair_a && (V1 == U1 + nn);
+  if (pair_a) {
+    GemmArgs g{};
+    g.M = g.N = g.K = n;
+    g.batch = 2;
+    g.A = View{b.V0, 1, n, (long long)(b.U0 - b.V0)};
+    g.B = View{b.Z, 1, n, 0};
+    g.C = b.A1;
+    g.crs = 1;
+    g.ccs = n;
+    g.cbs = (long long)nn;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(1.0, 0.0);
+    g.a_real = g.b_real = g.c_real = true;
+    if ((rc = gemm(g, s))) return rc;
+  } else {
+    if ((rc = rgemm(n, n, n, view_cm(b.V0, n, 0), Zv, b.A1, n, 1.0, 1.0, s))) return rc;
+    if ((rc = rgemm(n, n, n, view_cm(b.U0, n, 0), Zv, b.A2, n, 1.0, 1.0, s))) return rc;
+  }
+  if (pair_u) {
+    GemmArgs g{};
+    g.M = g.N = g.K = n;
+    g.batch = 2;
+    g.A = View{b.A1, 1, n, (long long)nn};
+    g.B = View{LinvT.p, LinvT.rs, LinvT.cs, 0};
+    g.C = U1;
+    g.crs = 1;
+    g.ccs = n;
+    g.cbs = (long long)nn;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    g.a_real = g.b_real = g.c_real = true;
+    if ((rc = gemm(g, s))) return rc;
+  } else {
+    if ((rc = rgemm(n, n, n, view_cm(b.A1, n, 0), LinvT, U1, n, 1.0, 0.0, s))) return rc;
+    if ((rc = rgemm(n, n, n, view_cm(b.A2, n, 0), LinvT, V1, n, 1.0, 0.0, s))) return rc;
+  }
   sec_end(c, SEC_EVOLVE);
   c->kernel_launches += 8;
   return TVAP_OK;

@@ -44,8 +44,8 @@ namespace tvap {
 // ---------------------------------------------------------------------------
 struct Workspace {
   int n = 0, G = 0;
-  // real n x n
-  double *U = nullptr, *V = nullptr, *rho = nullptr, *kap = nullptr, *jac = nullptr, *D = nullptr,
+  // real n x n (V and U adjacent: VU = [V | U], n x 2n)
+  double *VU = nullptr, *U = nullptr, *V = nullptr, *rho = nullptr, *kap = nullptr, *jac = nullptr, *D = nullptr,
          *evals = nullptr, *jwork = nullptr, *rhoc = nullptr, *kapc = nullptr, *tmp = nullptr, *blocks = nullptr;
   // canonical summary (device): ints [nocc, nemp, bad], doubles [ovac, logPfA1, signPfA1], voveru[n]
   int* canon_i = nullptr;
@@ -68,9 +68,10 @@ struct Workspace {
   // sums
   double2 *pA = nullptr, *pH = nullptr, *pAH = nullptr, *pscal = nullptr;
   double* H20v = nullptr;
-  // eigenvector refinement (warm start from the previous canonical basis)
-  double *Xr = nullptr, *Xn = nullptr, *Rr = nullptr, *Br = nullptr, *Sr = nullptr, *Mr = nullptr,
-         *lam = nullptr, *rscal = nullptr;
+  // eigenvector refinement (warm start from the previous canonical basis):
+  // XB = [X0 | rho X0 | X1 | rho X1], RS = [X^T X | X^T rho X]
+  double *XB = nullptr, *Xr = nullptr, *Xn = nullptr, *RS = nullptr, *Rr = nullptr, *Br = nullptr, *Sr = nullptr,
+         *Mr = nullptr, *lam = nullptr, *rscal = nullptr;
   // overlap chain scratch (runs on the second stream)
   double2 *OW = nullptr, *OX = nullptr, *OY = nullptr;
   int* rflag = nullptr;
@@ -90,12 +91,12 @@ int dalloc(T** p, size_t count, size_t& total) {
 }
 
 void ws_free(Workspace* w) {
-  void* ptrs[] = {w->U,   w->V,     w->rho,    w->kap,   w->jac,    w->D,     w->evals,  w->jwork, w->rhoc,
+  void* ptrs[] = {w->VU,  w->rho,    w->kap,   w->jac,    w->D,     w->evals,  w->jwork, w->rhoc,
                   w->kapc, w->tmp,  w->blocks, w->canon_i, w->canon_d, w->Uphi, w->Vphi,   w->W,     w->A,
                   w->Ut,  w->Vt,    w->X,      w->Y,     w->T,      w->Rn,    w->K,      w->SZ,    w->rhoL,
                   w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
                   w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
-                  w->H20v,  w->Xr,    w->Xn,     w->Rr,    w->Br,     w->Sr,    w->Mr,     w->lam,   w->rscal,
+                  w->H20v,  w->XB,    w->RS,     w->Br,    w->Mr,     w->lam,   w->rscal,
                   w->rflag, w->OW,    w->OX,     w->OY,     w->piv};
   for (void* p : ptrs) cudaFree(p);
   *w = Workspace();
@@ -118,15 +119,21 @@ int ws_ensure(tvap_ctx* c, int G) {
   int rc = TVAP_OK;
 #define A_(p, cnt) \
   if ((rc = dalloc(&w->p, (cnt), t)) != TVAP_OK) return rc;
-  A_(U, nn) A_(V, nn) A_(rho, nn) A_(kap, nn) A_(jac, nn) A_(D, nn) A_(evals, n) A_(jwork, 2 * n + 2)
+  A_(VU, 2 * nn) A_(rho, nn) A_(kap, nn) A_(jac, nn) A_(D, nn) A_(evals, n) A_(jwork, 2 * n + 2)
   A_(rhoc, nn) A_(kapc, nn) A_(tmp, nn + n) A_(blocks, 10 * nn) A_(canon_i, 8) A_(canon_d, 8 + n)
   A_(Uphi, nG) A_(Vphi, nG) A_(W, 2 * nG) A_(A, nG) A_(Ut, nG) A_(Vt, nG) A_(X, nG) A_(Y, nG) A_(T, nG)
   A_(Rn, nG) A_(K, nG) A_(SZ, nG) A_(rhoL, nG) A_(kLR, nG) A_(kRL, nG) A_(gam, nG) A_(hsp, nG) A_(dLR, nG)
   A_(dRL, nG) A_(ephase, 2 * G) A_(weight, G) A_(mult, G) A_(obs, 8 * G) A_(pf, 2 * G) A_(detR22, 2 * G)
   A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
-  A_(Xr, nn) A_(Xn, nn) A_(Rr, nn) A_(Br, nn) A_(Sr, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
+  A_(XB, 4 * nn) A_(RS, 2 * nn) A_(Br, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
   A_(OW, nG) A_(OX, nG) A_(OY, nG) A_(piv, size_t(n) * G)
 #undef A_
+  w->V = w->VU;
+  w->U = w->VU + nn;
+  w->Xr = w->XB;
+  w->Xn = w->XB + 2 * nn;
+  w->Rr = w->RS;
+  w->Sr = w->RS + nn;
   return TVAP_OK;
 }
 
@@ -270,9 +277,15 @@ __global__ void build_uv_kernel(int n, int G, const double* __restrict__ blk, co
   const int b = int(idx / nn);
   const size_t e = idx % nn;
   const double2 pp = eph[2 * b], pn = eph[2 * b + 1];  // e^{i phi_p}, e^{i phi_n}
-  // blocks: 0 VpVp 1 VnVn 2 UpUp 3 UnUn 4 VpUp 5 VnUn 6 UpVp 7 UnVn 8 DpDp 9 DnDn
-  const double vvp = blk[0 * nn + e], vvn = blk[1 * nn + e], uup = blk[2 * nn + e], uun = blk[3 * nn + e];
-  const double vup = blk[4 * nn + e], vun = blk[5 * nn + e], uvp = blk[6 * nn + e], uvn = blk[7 * nn + e];
+  // blocks: the Gram matrices C_t = W_t^T W_t of W_t = [V_t | U_t] (rows of
+  // isospin t; 2n x 2n at blk + 4 n^2 t), then D_p^T D_p, D_n^T D_n
+  const int i = int(e % n), j = int(e / n);
+  const size_t n2 = 2 * size_t(n);
+  const double* Cp = blk;
+  const double* Cn = blk + 4 * nn;
+  const size_t vv = i + j * n2, vu = i + (n + j) * n2, uv = (n + i) + j * n2, uu = (n + i) + (n + j) * n2;
+  const double vvp = Cp[vv], vvn = Cn[vv], uup = Cp[uu], uun = Cn[uu];
+  const double vup = Cp[vu], vun = Cn[vu], uvp = Cp[uv], uvn = Cn[uv];
   double2 up;
   up.x = (vvp + uup) * pp.x + (vvn + uun) * pn.x;
   up.y = (uup - vvp) * pp.y + (uun - vvn) * pn.y;
@@ -819,10 +832,13 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
             q[r][t] = (r == t) ? 1.0 : 0.0;
           }
         for (int sweep = 0; sweep < 30 && m > 1; ++sweep) {
-          double off = 0.0;
-          for (int r = 0; r < m; ++r)
+          double off = 0.0, dia = 0.0;
+          for (int r = 0; r < m; ++r) {
+            dia += a[r][r] * a[r][r];
             for (int t = r + 1; t < m; ++t) off += a[r][t] * a[r][t];
-          if (off == 0.0) break;
+          }
+          // converged to rounding: further rotations only move noise
+          if (off <= 1.0e-32 * dia) break;
           for (int pp = 0; pp < m; ++pp)
             for (int qq = pp + 1; qq < m; ++qq) {
               if (a[pp][qq] == 0.0) continue;
@@ -1386,25 +1402,27 @@ int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, c
   const size_t nn = size_t(n) * n;
   const View Rho = view_cm(w->rho, n, 0);
   int rc;
+  // R = X^T X and S = X^T rho X in one product X^T [X | rho X] (rho X is kept
+  // right after X in its buffer, R and S are adjacent)
+  auto gram = [&](double* Xc) -> int {
+    int r;
+    if ((r = real_gemm(n, n, n, Rho, view_cm(Xc, n, 0), Xc + nn, n, 1.0, 0.0, s))) return r;
+    return real_gemm(n, 2 * n, n, view_t(view_cm(Xc, n, 0)), view_cm(Xc, n, 0), w->RS, n, 1.0, 0.0, s);
+  };
   for (int step = 0; step < steps; ++step) {
     const View Xv = view_cm(X, n, 0);
-    if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
-    if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
-    if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+    if ((rc = gram(X))) return rc;
     refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
     refine_update_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
     if ((rc = real_gemm(n, n, n, Xv, view_cm(w->Mr, n, 0), Xn, n, 1.0, 0.0, s))) return rc;
     std::swap(X, Xn);
   }
-  const View Xv = view_cm(X, n, 0);
-  if ((rc = real_gemm(n, n, n, view_t(Xv), Xv, w->Rr, n, 1.0, 0.0, s))) return rc;
-  if ((rc = real_gemm(n, n, n, Rho, Xv, w->Br, n, 1.0, 0.0, s))) return rc;
-  if ((rc = real_gemm(n, n, n, view_t(Xv), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+  if ((rc = gram(X))) return rc;
   refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
   cluster_finish_kernel<<<1, 256, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals,
                                           reinterpret_cast<int*>(w->jwork), w->rflag);
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += steps * 6 + 5;
+  c->kernel_launches += steps * 5 + 4;
   int hr[2] = {1, 0};
   TVAP_CUDA(cudaMemcpyAsync(hr, w->rflag, sizeof(hr), cudaMemcpyDeviceToHost, s));
   TVAP_CUDA(cudaStreamSynchronize(s));
@@ -1467,19 +1485,25 @@ int prepare_uv_blocks(tvap_ctx* c, cudaStream_t s) {
   const size_t nn = size_t(n) * n;
   int rc;
   sec_begin_on(c, SEC_BLOCKS, s);
-  // row halves p = 0..h-1, n = h..n-1
-  const double* Xs[4][2] = {{w->V, w->V}, {w->U, w->U}, {w->V, w->U}, {w->U, w->V}};
-  for (int q = 0; q < 4; ++q)
-    for (int t = 0; t < 2; ++t) {
-      const double* L = Xs[q][0] + t * h;
-      const double* R = Xs[q][1] + t * h;
-      // (L_t)^T R_t: A(i,k) = L(k,i) -> rs = n, cs = 1; B(k,j) = R(k,j)
-      if ((rc = real_gemm(n, n, h, View{L, n, 1, 0}, View{R, 1, n, 0}, w->blocks + (2 * q + t) * nn, n, 1.0, 0.0,
-                          s)))
-        return rc;
-    }
+  // C_t = W_t^T W_t, W_t = rows t h .. t h + h - 1 of W = [V | U] (n x 2n), batch t = p, n
+  {
+    GemmArgs g{};
+    g.M = g.N = 2 * n;
+    g.K = h;
+    g.batch = 2;
+    g.A = View{w->VU, n, 1, h};  // (i, k) = W(t h + k, i)
+    g.B = View{w->VU, 1, n, h};  // (k, j) = W(t h + k, j)
+    g.C = w->blocks;
+    g.crs = 1;
+    g.ccs = 2 * n;
+    g.cbs = 4 * (long long)nn;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    g.a_real = g.b_real = g.c_real = true;
+    if ((rc = gemm(g, s))) return rc;
+  }
   sec_end_on(c, SEC_BLOCKS, s);
-  c->kernel_launches += 8;
+  c->kernel_launches += 1;
   return TVAP_OK;
 }
 
@@ -1506,13 +1530,25 @@ int prepare_canonical(tvap_ctx* c, double occeps, double allemp_d, int* host_can
   const double eps = (occeps < 2.2250738585072014e-308) ? 1.0e-8 : occeps;
   canon_kernel<<<1, 256, 0, s>>>(n, w->rhoc, w->kapc, eps, int(allemp_d), w->canon_i, w->canon_d);
   TVAP_CUDA(cudaGetLastError());
-  for (int t = 0; t < 2; ++t) {
-    const double* L = w->D + t * h;
-    if ((rc = real_gemm(n, n, h, View{L, n, 1, 0}, View{L, 1, n, 0}, w->blocks + (8 + t) * nn, n, 1.0, 0.0, s)))
-      return rc;
+  {
+    // D_t^T D_t over the rows of isospin t, batch t = p, n
+    GemmArgs g{};
+    g.M = g.N = n;
+    g.K = h;
+    g.batch = 2;
+    g.A = View{w->D, n, 1, h};
+    g.B = View{w->D, 1, n, h};
+    g.C = w->blocks + 8 * nn;
+    g.crs = 1;
+    g.ccs = n;
+    g.cbs = (long long)nn;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    g.a_real = g.b_real = g.c_real = true;
+    if ((rc = gemm(g, s))) return rc;
   }
   sec_end_on(c, SEC_CANONICAL, s);
-  c->kernel_launches += 2 + 4 + 1 + 2;
+  c->kernel_launches += 2 + 4 + 1 + 1;
   TVAP_CUDA(cudaMemcpyAsync(host_canon, w->canon_i, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
   TVAP_CUDA(cudaStreamSynchronize(s));
   return TVAP_OK;
