@@ -412,11 +412,150 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_kernel(int N, double2* Aa
   }
 }
 
+// The same elimination with the packed upper triangle in shared memory
+// (N (N + 1) / 2 entries, column-major): every access stays on the SM, the
+// pivot search is a warp reduction plus one block step, and the already
+// eliminated columns (which no longer enter the Pfaffian) are neither
+// exchanged nor scaled.
+__global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const double2* __restrict__ Aall,
+                                                                   double2* pf, int batch, int* flags) {
+  extern __shared__ double2 pf_smem[];
+  double2* pk = pf_smem;
+  double2* xcol = pk + size_t(N) * (N + 1) / 2;  // 1-based, N + 1 entries
+  double2* ycol = xcol + N + 1;
+  __shared__ double wv[kPfThreads / 32];
+  __shared__ int wi[kPfThreads / 32];
+  __shared__ int s_kp;
+  __shared__ double s_pv;
+  const int b = blockIdx.x;
+  const double2* A = Aall + size_t(b) * N * N;
+  auto a = [pk](int i, int j) -> double2& { return pk[(i - 1) + (size_t(j) * (j - 1)) / 2]; };  // 1 <= i <= j
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int j = 1 + warp; j <= N; j += nw)
+    for (int i = 1 + lane; i <= j; i += 32) a(i, j) = A[(i - 1) + size_t(j - 1) * N];
+  __syncthreads();
+  double logmag = 0.0;
+  double2 phase = make_double2(1.0, 0.0);
+  bool zero = false;
+  for (int K = N; K >= 2; K -= 2) {
+    double best = -1.0;
+    int bi = N + 1;
+    for (int i = 1 + tid; i <= K - 1; i += nt) {
+      const double v = cabs1(a(i, K));
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const double v2 = __shfl_down_sync(0xffffffffu, best, off);
+      const int i2 = __shfl_down_sync(0xffffffffu, bi, off);
+      if (v2 > best || (v2 == best && i2 < bi)) {
+        best = v2;
+        bi = i2;
+      }
+    }
+    if (lane == 0) {
+      wv[warp] = best;
+      wi[warp] = bi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double v = (lane < nw) ? wv[lane] : -1.0;
+      int i = (lane < nw) ? wi[lane] : N + 1;
+      for (int off = 16; off > 0; off >>= 1) {
+        const double v2 = __shfl_down_sync(0xffffffffu, v, off);
+        const int i2 = __shfl_down_sync(0xffffffffu, i, off);
+        if (v2 > v || (v2 == v && i2 < i)) {
+          v = v2;
+          i = i2;
+        }
+      }
+      if (lane == 0) {
+        s_kp = i;
+        s_pv = v;
+      }
+    }
+    __syncthreads();
+    int KP = s_kp;
+    const double pv = s_pv;
+    const int KK = K - 1;
+    if (pv == 0.0) {
+      zero = true;
+      KP = KK;
+    }
+    if (KP != KK) {
+      for (int i = 1 + tid; i <= KP - 1; i += nt) {
+        const double2 t = a(i, KK);
+        a(i, KK) = a(i, KP);
+        a(i, KP) = t;
+      }
+      for (int t = tid; t < KK - KP - 1; t += nt) {
+        const double2 u = a(KP + 1 + t, KK);
+        a(KP + 1 + t, KK) = a(KP, KP + 1 + t);
+        a(KP, KP + 1 + t) = u;
+      }
+      if (tid == 0) {
+        const double2 u = a(KK, K);
+        a(KK, K) = a(KP, K);
+        a(KP, K) = u;
+      }
+      __syncthreads();
+      for (int i = KP + tid; i <= KK - 1; i += nt) a(i, KK) = cneg(a(i, KK));
+      for (int j = KP + 1 + tid; j <= KK - 1; j += nt) a(KP, j) = cneg(a(KP, j));
+      __syncthreads();
+    }
+    if (zero) break;
+    const double2 piv = a(K - 1, K);
+    const double m = hypot(piv.x, piv.y);
+    logmag += log(m);
+    phase = cmul(phase, make_double2(piv.x / m, piv.y / m));
+    if (KP != KK) phase = cneg(phase);
+    const double2 alpha = crcp(piv);
+    const int nn = K - 2;
+    for (int i = 1 + tid; i <= nn; i += nt) {
+      xcol[i] = a(i, K);
+      ycol[i] = a(i, K - 1);
+    }
+    __syncthreads();
+    // A(I,J) += X(I) (alpha Y(J)) - Y(I) (alpha X(J)), I < J <= nn
+    for (int J = 2 + warp; J <= nn; J += nw) {
+      const double2 xj = xcol[J], yj = ycol[J];
+      if (xj.x == 0.0 && xj.y == 0.0 && yj.x == 0.0 && yj.y == 0.0) continue;
+      const double2 t1 = cmul(alpha, yj), t2 = cmul(alpha, xj);
+      double2* colJ = &a(1, J);
+      for (int I = 1 + lane; I <= J - 1; I += 32) {
+        double2 v = colJ[I - 1];
+        cfma(v, xcol[I], t1);
+        cfma(v, cneg(ycol[I]), t2);
+        colJ[I - 1] = v;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    pf[b] = make_double2(zero ? -INFINITY : logmag, 0.0);
+    pf[batch + b] = zero ? make_double2(0.0, 0.0) : phase;
+    if (zero) atomicOr(flags, DEV_PFAFF_ZERO);
+  }
+}
+
 }  // namespace
 
 int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s) {
   if (n > 512 || (n & 1)) return TVAP_ERR_ARG;
-  pfaffian_kernel<<<batch, kPfThreads, 0, s>>>(n, A, pf, batch, flags);
+  const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 2 * size_t(n + 1));
+  if (shm <= jacobi32_smem_limit()) {
+    static bool attr = false;
+    if (!attr) {
+      TVAP_CUDA(cudaFuncSetAttribute(pfaffian_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(jacobi32_smem_limit())));
+      attr = true;
+    }
+    pfaffian_smem_kernel<<<batch, kPfThreads, shm, s>>>(n, A, pf, batch, flags);
+  } else {
+    pfaffian_kernel<<<batch, kPfThreads, 0, s>>>(n, A, pf, batch, flags);
+  }
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }
