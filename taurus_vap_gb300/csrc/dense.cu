@@ -996,7 +996,8 @@ __global__ void __launch_bounds__(kCholThreads) cholesky_inverse_smem_kernel(int
       break;
     }
     const double dk = sqrt(d);
-    for (int i = k + 1 + tid; i < n; i += nt) L(i, k) = L(i, k) / dk;
+    const double rdk = 1.0 / dk;  // the column is scaled by the reciprocal, as DPBTF2 does
+    for (int i = k + 1 + tid; i < n; i += nt) L(i, k) = L(i, k) * rdk;
     __syncthreads();
     if (tid == 0) L(k, k) = dk;
     for (int j = k + 1 + warp; j < n; j += nw) {

@@ -209,7 +209,7 @@ int tvap_calculate_gradient(tvap_ctx* c, const double* H20v, int cdim, const dou
   const int nblocks = int((nn + tb - 1) / tb);
   double* buf = nullptr;
   const size_t tot = nn * (3 + size_t(cdim)) + cdim + nblocks + 1;
-  TVAP_CUDA(cudaMalloc(&buf, sizeof(double) * tot));
+  if (int r0 = ctx_scratch(c, tot, &buf)) return r0;
   double *dH = buf, *dZm = buf + nn, *dZ = buf + 2 * nn, *dC = buf + 3 * nn, *dl = dC + nn * cdim,
          *part = dl + cdim, *sum = part + nblocks;
   int rc = upload_matrix(H20v, dH, sizeof(double) * nn, s);
@@ -230,7 +230,6 @@ int tvap_calculate_gradient(tvap_ctx* c, const double* H20v, int cdim, const dou
       *gradient_norm = std::sqrt(h) / eta;
     }
   }
-  cudaFree(buf);
   return rc;
 }
 
@@ -242,7 +241,7 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;
   double* buf = nullptr;
-  TVAP_CUDA(cudaMalloc(&buf, sizeof(double) * (8 * nn + n)));
+  if (int r0 = ctx_scratch(c, 8 * nn + n, &buf)) return r0;
   EvolveBuf b;
   b.Z = buf;
   b.U0 = buf + nn;
@@ -259,7 +258,6 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   if (!rc) rc = download_matrix(dU1, U1, sizeof(double) * nn, s);
   if (!rc) rc = download_matrix(dV1, V1, sizeof(double) * nn, s);
   if (!rc) rc = check_flags(c);
-  cudaFree(buf);
   return rc;
 }
 
@@ -330,7 +328,7 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
   c->kernel_launches = 0;
   g_gemm_mode = c->gemm_mode;
   double* buf = nullptr;
-  TVAP_CUDA(cudaMalloc(&buf, sizeof(double) * (7 * nn + n)));
+  if ((rc = ctx_scratch(c, 7 * nn + n, &buf))) return rc;
   EvolveBuf b;
   b.Z = buf;
   b.U0 = buf + nn;
@@ -359,7 +357,6 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
       *energy = (ere * ore + eim * oim) / d;
     }
   }
-  cudaFree(buf);
   return rc;
 }
 

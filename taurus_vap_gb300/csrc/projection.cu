@@ -448,27 +448,33 @@ __global__ void overlap_finish_kernel(int n, int G, int have_overlap, const int*
 }
 
 // sum_gauge of the scalars (module_projection.f90:425-458), folded pairs as 2 Re
+// one warp: lanes over the angles, then a shuffle reduction (order differs
+// from the serial sum only by rounding)
 __global__ void sum_scalars_kernel(int G, const double2* __restrict__ obs, const double* __restrict__ mult,
                                    const double2* __restrict__ weight, double2* __restrict__ pscal, int accumulate) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
   double2 s[6];
-  for (int q = 0; q < 6; ++q) s[q] = accumulate ? pscal[q] : make_double2(0.0, 0.0);
-  for (int b = 0; b < G; ++b) {
+  for (int q = 0; q < 6; ++q) s[q] = make_double2(0.0, 0.0);
+  for (int b = lane; b < G; b += 32) {
     const double2 f1 = cmul(weight[b], obs[8 * b]);
     const double2 terms[6] = {f1, cmul(obs[8 * b + 1], f1), cmul(obs[8 * b + 2], f1), cmul(obs[8 * b + 3], f1),
                               cmul(obs[8 * b + 4], f1), cmul(obs[8 * b + 5], f1)};
+    const bool folded = mult[b] == 2.0;
     for (int q = 0; q < 6; ++q) {
-      if (mult[b] == 2.0)
+      if (folded)
         s[q].x += 2.0 * terms[q].x;
       else
         s[q] = cadd(s[q], terms[q]);
     }
   }
-  for (int q = 0; q < 6; ++q) pscal[q] = s[q];
+  for (int q = 0; q < 6; ++q)
+    for (int off = 16; off > 0; off >>= 1) {
+      s[q].x += __shfl_down_sync(0xffffffffu, s[q].x, off);
+      s[q].y += __shfl_down_sync(0xffffffffu, s[q].y, off);
+    }
+  if (lane == 0)
+    for (int q = 0; q < 6; ++q) pscal[q] = accumulate ? cadd(pscal[q], s[q]) : s[q];
 }
-
-// pnp_A, pnp_H20, pnp_AH20: sums over angles of c_b A_b, c_b H20_b,
-// c_b E_b A_b with H20_b = T_b - T_b^T (skew).
 __global__ void sum_matrices_kernel(int n, int G, const double2* __restrict__ A, const double2* __restrict__ T,
                                     const double2* __restrict__ coefA, const double2* __restrict__ coefAE,
                                     const double* __restrict__ mult, double2* __restrict__ pA, double2* __restrict__ pH,
@@ -476,14 +482,15 @@ __global__ void sum_matrices_kernel(int n, int G, const double2* __restrict__ A,
   const size_t nn = size_t(n) * n;
   const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (e >= nn) return;
-  const int i = int(e % n), j = int(e / n);
-  const size_t et = j + size_t(i) * n;
   double2 sa = accumulate ? pA[e] : make_double2(0.0, 0.0);
   double2 sh = accumulate ? pH[e] : make_double2(0.0, 0.0);
   double2 sah = accumulate ? pAH[e] : make_double2(0.0, 0.0);
+  // H20_b = T_b - T_b^T enters as 2 T_b: the sum is antisymmetrised once, in
+  // projected_h20_kernel (1/2 (X - X^T)), which gives sum c_b (T_b - T_b^T)
+#pragma unroll 4
   for (int b = 0; b < G; ++b) {
     const double2 a = A[size_t(b) * nn + e];
-    const double2 h = csub(T[size_t(b) * nn + e], T[size_t(b) * nn + et]);
+    const double2 h = cscale(T[size_t(b) * nn + e], 2.0);
     const double2 t1 = cmul(a, coefA[b]), t2 = cmul(h, coefA[b]), t3 = cmul(a, coefAE[b]);
     if (mult[b] == 2.0) {
       sa.x += 2.0 * t1.x;
@@ -516,7 +523,8 @@ __global__ void projected_h20_kernel(int n, const double2* __restrict__ pA, cons
   const double2 H = cmul(cscale(csub(pH[e], pH[et]), 0.5), rov);
   const double2 AH = cmul(cscale(csub(pAH[e], pAH[et]), 0.5), rov);
   H20v[e] = (cadd(csub(AH, cmul(ener, A)), H)).x;
-  const double ig = cmul(cadd(csub(pAH[e], cmul(ener, pA[e])), pH[e]), rov).y;
+  const double2 Hraw = cscale(csub(pH[e], pH[et]), 0.5);  // the antisymmetric sum of the H20_b
+  const double ig = cmul(cadd(csub(pAH[e], cmul(ener, pA[e])), Hraw), rov).y;
   if (ig > 1.0e-8) atomicOr(flags, DEV_IMAG_GRAD);
 }
 

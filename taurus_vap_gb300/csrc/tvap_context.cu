@@ -98,6 +98,25 @@ __global__ void from_inner_kernel(size_t nn, int ncol, const double2* __restrict
 
 using namespace tvap;
 
+namespace tvap {
+
+int ctx_scratch(tvap_ctx* c, size_t count, double** out) {
+  if (count > c->scratch_count) {
+    if (c->scratch) {
+      TVAP_CUDA(cudaStreamSynchronize(c->stream));
+      cudaFree(c->scratch);
+    }
+    c->scratch = nullptr;
+    c->scratch_count = 0;
+    TVAP_CUDA(cudaMalloc(&c->scratch, sizeof(double) * count));
+    c->scratch_count = count;
+  }
+  *out = c->scratch;
+  return TVAP_OK;
+}
+
+}  // namespace tvap
+
 extern "C" {
 
 const char* tvap_last_error(void) { return g_last_error.c_str(); }
@@ -197,6 +216,7 @@ void tvap_destroy(tvap_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->stream2) cudaStreamSynchronize(c->stream2);
+  cudaFree(c->scratch);
   destroy_workspace(c);
   free_field_csr(c->csr);
   cudaFree(c->d_sp_2mj);

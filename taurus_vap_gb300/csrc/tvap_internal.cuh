@@ -179,6 +179,10 @@ struct tvap_ctx {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_open;
   double section_ms[16] = {0};
   long long section_calls[16] = {0};
+  // work buffer of the per-call entry points (gradient, evolution), grown on
+  // demand and reused: no allocation (and no device-wide cudaFree) per call
+  double* scratch = nullptr;
+  size_t scratch_count = 0;
   // canonical bases: [0] FP32 Jacobi + refinement attempts, [1] of them
   // accepted, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in total
   long long canon_attempts[4] = {0, 0, 0, 0};
@@ -200,6 +204,8 @@ namespace tvap {
 
 int build_field_csr(tvap_ctx* c);
 void free_field_csr(FieldCSR& f);
+// the context's work buffer with at least count doubles (stream-ordered reuse)
+int ctx_scratch(tvap_ctx* c, size_t count, double** out);
 int build_field_dense(tvap_ctx* c);
 void free_field_dense(FieldDense& f);
 // fields of ncol gauge-angle columns through the dense blocks (emulated FP64)
