@@ -1849,8 +1849,12 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
     if ((rc = angles_thouless(c, G, w->ephase, o.factor_delta, s))) return rc;
     if ((rc = prepare_canonical(c, o.seed_occeps, o.seed_allemp, canon, s2))) return rc;
     if (canon[2] && have_overlap) return canon_error();
-    if (have_overlap && (rc = angles_overlap(c, G, w->ephase, canon[0], canon[1], s2))) return rc;
-    TVAP_CUDA(cudaEventRecord(c->ev_join, s2));
+    // the overlap chain (wide kernels) runs at the main stream's priority
+    cudaStream_t s3 = c->stream3;
+    TVAP_CUDA(cudaEventRecord(c->ev_canon, s2));
+    TVAP_CUDA(cudaStreamWaitEvent(s3, c->ev_canon, 0));
+    if (have_overlap && (rc = angles_overlap(c, G, w->ephase, canon[0], canon[1], s3))) return rc;
+    TVAP_CUDA(cudaEventRecord(c->ev_join, s3));
     TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
     if ((rc = angles_sums(c, G, w->weight, w->mult, have_overlap, 0, s))) return rc;
   } else {

@@ -197,6 +197,8 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
   int prio_lo = 0, prio_hi = 0;
   if ((e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithPriority(&c->stream2, cudaStreamNonBlocking, prio_hi)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithPriority(&c->stream3, cudaStreamNonBlocking, prio_lo)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_canon, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_2mj, sizeof(int) * n)) != cudaSuccess) return fail(e);
@@ -216,6 +218,7 @@ void tvap_destroy(tvap_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->stream2) cudaStreamSynchronize(c->stream2);
+  if (c->stream3) cudaStreamSynchronize(c->stream3);
   cudaFree(c->scratch);
   destroy_workspace(c);
   free_field_csr(c->csr);
@@ -234,10 +237,13 @@ void tvap_destroy(tvap_ctx* c) {
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   if (c->stream) oz_release(c->stream);
   if (c->stream2) oz_release(c->stream2);
+  if (c->stream3) oz_release(c->stream3);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
+  if (c->stream3) cudaStreamDestroy(c->stream3);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_canon) cudaEventDestroy(c->ev_canon);
   delete c;
 }
 

@@ -167,8 +167,9 @@ struct tvap_ctx {
   double2 H0 = {0.0, 0.0};
   bool have_ham = false;
   tvap::FieldCSR csr;
-  cudaStream_t stream2 = nullptr;  // overlap chain, concurrent with the Thouless chain
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t stream2 = nullptr;  // canonical basis (high priority), concurrent with the Thouless chain
+  cudaStream_t stream3 = nullptr;  // overlap chain and Pfaffians (normal priority)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_canon = nullptr;
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
   int kernel_launches = 0;  // launches issued by the last top-level call
