@@ -81,14 +81,16 @@ template <int PA, int PB>
 __global__ void __launch_bounds__(oz::kThreads, 1)
     ozaki_mma_kernel(int M, int N, int mpad, int npad, int kpad, const __nv_bfloat16* __restrict__ As,
                      const int* __restrict__ ea, const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb,
-                     GemmArgs g) {
+                     GemmArgs g, int a_shared, int b_shared) {
   extern __shared__ __align__(16) __nv_bfloat16 sm[];
   const int b = blockIdx.z;
   const int mt0 = blockIdx.y * oz::kTile, nt0 = blockIdx.x * oz::kTile;
   const size_t aplane = size_t(mpad) * kpad, bplane = size_t(npad) * kpad;
   oz::Acc o;
-  oz::mainloop<PA, PB>(As + size_t(b) * kDigits * PA * aplane + size_t(mt0) * kpad, aplane, kpad,
-                       Bs + size_t(b) * kDigits * PB * bplane + size_t(nt0) * kpad, bplane, kpad, kpad, sm, o);
+  // an operand shared by all batch entries (batch stride 0) is split once
+  const int ba = a_shared ? 0 : b, bb = b_shared ? 0 : b;
+  oz::mainloop<PA, PB>(As + size_t(ba) * kDigits * PA * aplane + size_t(mt0) * kpad, aplane, kpad,
+                       Bs + size_t(bb) * kDigits * PB * bplane + size_t(nt0) * kpad, bplane, kpad, kpad, sm, o);
   // epilogue: scale by 2^(ea + eb - 57), alpha/beta, store
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wm = (warp >> 2) * 16, wn = (warp & 3) * 8;
@@ -105,7 +107,7 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
     if (i >= M || j >= N) continue;
     // the power-of-two scale is exact: folding it into alpha rounds as
     // scaling first would
-    const double p2 = oz::pow2(ea[size_t(b) * mpad + i] + eb[size_t(b) * npad + j] - 57);
+    const double p2 = oz::pow2(ea[size_t(ba) * mpad + i] + eb[size_t(bb) * npad + j] - 57);
     const double2 v0 = oz::acc_value(o, q);
     const long long idx = i * g.crs + j * g.ccs + b * g.cbs;
     double2 v;
@@ -136,6 +138,7 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
 template <int PA, int PB>
 int launch_ozaki_mma(int M, int N, int mpad, int npad, int kpad, const __nv_bfloat16* As, const int* ea,
                      const __nv_bfloat16* Bs, const int* eb, const GemmArgs& g, cudaStream_t s) {
+  const int a_shared = g.A.bs == 0 ? 1 : 0, b_shared = g.B.bs == 0 ? 1 : 0;
   const size_t shm = oz::Shape<PA, PB>::kSmemBytes;
   static bool attr = false;
   if (!attr) {
@@ -143,7 +146,8 @@ int launch_ozaki_mma(int M, int N, int mpad, int npad, int kpad, const __nv_bflo
     attr = true;
   }
   dim3 grid(npad / oz::kTile, mpad / oz::kTile, g.batch);
-  ozaki_mma_kernel<PA, PB><<<grid, oz::kThreads, shm, s>>>(M, N, mpad, npad, kpad, As, ea, Bs, eb, g);
+  ozaki_mma_kernel<PA, PB><<<grid, oz::kThreads, shm, s>>>(M, N, mpad, npad, kpad, As, ea, Bs, eb, g, a_shared,
+                                                            b_shared);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }
@@ -227,25 +231,28 @@ int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.batch <= 0) return TVAP_OK;
   const int PA = g.a_real ? 1 : 2, PB = g.b_real ? 1 : 2;
   const int mpad = (g.M + 31) / 32 * 32, npad = (g.N + 31) / 32 * 32, kpad = (g.K + 15) / 16 * 16;
-  const size_t asz = size_t(g.batch) * kDigits * PA * mpad * kpad;
-  const size_t bsz = size_t(g.batch) * kDigits * PB * npad * kpad;
+  // operands with batch stride 0 are split once for the whole batch
+  const int abatch = g.A.bs == 0 ? 1 : g.batch, bbatch = g.B.bs == 0 ? 1 : g.batch;
+  const size_t asz = size_t(abatch) * kDigits * PA * mpad * kpad;
+  const size_t bsz = size_t(bbatch) * kDigits * PB * npad * kpad;
   int rc;
   OzScratch* sc = nullptr;
-  if ((rc = oz_reserve(s, sizeof(__nv_bfloat16) * (asz + bsz), size_t(g.batch) * (mpad + npad), &sc))) return rc;
+  if ((rc = oz_reserve(s, sizeof(__nv_bfloat16) * (asz + bsz), size_t(abatch) * mpad + size_t(bbatch) * npad, &sc)))
+    return rc;
   __nv_bfloat16* As = sc->buf;
   __nv_bfloat16* Bs = sc->buf + asz;
   int* ea = sc->ex;
-  int* eb = sc->ex + size_t(g.batch) * mpad;
+  int* eb = sc->ex + size_t(abatch) * mpad;
   // A rows: element (i, k) at A.p[i rs + k cs]; B columns: element (j, k) = B(k, j) at B.p[k rs + j cs]
   {
-    dim3 grid((mpad + 7) / 8, g.batch);
+    dim3 grid((mpad + 7) / 8, abatch);
     if (PA == 2)
       slice_kernel<true><<<grid, 256, 0, s>>>(g.M, g.K, mpad, kpad, g.A.p, g.A.rs, g.A.cs, g.A.bs, g.conj_a, As, ea);
     else
       slice_kernel<false><<<grid, 256, 0, s>>>(g.M, g.K, mpad, kpad, g.A.p, g.A.rs, g.A.cs, g.A.bs, false, As, ea);
   }
   {
-    dim3 grid((npad + 7) / 8, g.batch);
+    dim3 grid((npad + 7) / 8, bbatch);
     if (PB == 2)
       slice_kernel<true><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, g.conj_b, Bs, eb);
     else
