@@ -183,6 +183,7 @@ def run_ours(args):
     mdl, U, V = build_workload()
     n = mdl.n
     ctx = N.Context(mdl.basis, mdl.ham, device=local)
+    ctx.set_gemm_mode(args.gemm_mode)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
 
@@ -246,7 +247,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         fp64_pipe = {"value": world * args.steps / (fa.elapsed_time(fb) / 1000.0), "unit": "iters/s",
                      "ms_per_step": fa.elapsed_time(fb) / args.steps}
-        ctx.set_gemm_mode(1)
+        ctx.set_gemm_mode(args.gemm_mode)
 
     # ---- plain form (one angle per launch sequence), same state
     plain = None
@@ -450,6 +451,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64-pipe comparison run")
+    ap.add_argument("--gemm-mode", type=int, default=1,
+                    help="dense products: 1 emulated with mma.sync (default), 2 emulated with tcgen05, 0 FP64 pipe")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

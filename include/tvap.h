@@ -54,8 +54,10 @@ enum {
   TVAP_ERR_TRTRI = 15,        /* dtrtri failed (module_constraints.f90:568-571) */
   TVAP_ERR_CANONICAL = 16,    /* canonical basis: eigen solver did not converge or a
                                  degenerate block larger than 2 (DGEES case) */
-  TVAP_ERR_NUMBER_DRIFT = 18  /* particle numbers wrong 3 times in 5 iterations
+  TVAP_ERR_NUMBER_DRIFT = 18, /* particle numbers wrong 3 times in 5 iterations
                                  (module_gradient.f90:528-545) */
+  TVAP_ERR_DEVICE_TIMEOUT = 19 /* a bounded wait inside a tensor-core kernel ran out
+                                  (the kernel stopped and freed its tensor memory) */
 };
 
 /* Projected sums of one call of the gauge-angle loop: pnp_over, pnp_ener,
@@ -96,7 +98,8 @@ int tvap_set_timing(tvap_ctx* ctx, int on);
 /* Arithmetic of the dense products: 0 = the FP64 pipe (DFMA);
  * 1 (default) = FP64 emulated on the bf16 tensor cores by exact integer
  * splitting (8 balanced 7-bit digits per FP64 value, exact FP32 partial sums,
- * integer recombination).  In mode 1 the field contraction over 16 or more
+ * integer recombination) with warp-level mma.sync; 2 = the same splitting
+ * with tcgen05 MMAs and tensor-memory accumulators.  In mode 1 the field contraction over 16 or more
  * gauge angles also runs on the tensor cores (dense symmetry blocks of the
  * interaction); the factorisations and all reductions run on the FP64 pipe
  * in both modes. */

@@ -406,7 +406,7 @@ int fields_batched(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
                    double2* gamma, double2* hsp, double2* dLR, double2* dRL, cudaStream_t s) {
   if (ncol <= 0) return TVAP_OK;
   // many gauge angles at once: dense symmetry blocks on the tensor cores
-  if (c->gemm_mode == 1 && c->csr.dense_ok && ncol >= kDenseMinCols)
+  if (c->gemm_mode >= 1 && c->csr.dense_ok && ncol >= kDenseMinCols)
     return fields_dense(c, ncol, ldc, rho, kLR, kRL, gamma, hsp, dLR, dRL, s);
   if (ncol <= 32)
     launch_fields<1>(c, ncol, ldc, rho, kLR, kRL, gamma, hsp, dLR, dRL, s);

@@ -237,6 +237,7 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   if (!c || !U0 || !V0 || !Z || !U1 || !V1) return TVAP_ERR_ARG;
   c->kernel_launches = 0;
   g_gemm_mode = c->gemm_mode;
+  g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;
@@ -327,6 +328,7 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
   if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
   c->kernel_launches = 0;
   g_gemm_mode = c->gemm_mode;
+  g_dev_flags = c->d_flags;
   double* buf = nullptr;
   if ((rc = ctx_scratch(c, 7 * nn + n, &buf))) return rc;
   EvolveBuf b;

@@ -14,6 +14,7 @@
 #include <mutex>
 
 #include "ozaki_core.cuh"
+#include "ozaki_tc.cuh"
 #include "tvap_internal.cuh"
 
 namespace tvap {
@@ -152,6 +153,69 @@ int launch_ozaki_mma(int M, int N, int mpad, int npad, int kpad, const __nv_bflo
   return TVAP_OK;
 }
 
+// One CTA per (128 x 64 output tile, component) of one batch entry, tcgen05
+// MMAs with tensor-memory accumulators (ozaki_tc.cuh).  alpha and beta are
+// real here (the components are then independent).
+template <int PA, int PB>
+__global__ void __launch_bounds__(oztc::kThreads, 1)
+    ozaki_tc_kernel(int M, int N, int mpad, int npad, int kpad, const __nv_bfloat16* __restrict__ As,
+                    const int* __restrict__ ea, const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb,
+                    GemmArgs g, int ncomp, int a_shared, int b_shared, int* flags) {
+  extern __shared__ __align__(1024) __nv_bfloat16 tsm[];
+  __shared__ oztc::Ctl ctl;
+  const int b = blockIdx.z / ncomp, comp = blockIdx.z - b * ncomp;
+  const int ba = a_shared ? 0 : b, bb = b_shared ? 0 : b;
+  const int mt0 = blockIdx.y * oztc::kM, nt0 = blockIdx.x * oztc::kN;
+  const size_t aplane = size_t(mpad) * kpad, bplane = size_t(npad) * kpad;
+  const __nv_bfloat16* A = As + size_t(ba) * kDigits * PA * aplane + size_t(mt0) * kpad;
+  const __nv_bfloat16* B = Bs + size_t(bb) * kDigits * PB * bplane + size_t(nt0) * kpad;
+  oztc::setup(ctl);
+  oztc::Acc o;
+  bool ok;
+  if (comp == 0)
+    ok = oztc::mainloop<PA, PB, 0>(A, aplane, kpad, mpad - mt0, B, bplane, kpad, npad - nt0, kpad, tsm, ctl, o);
+  else
+    ok = oztc::mainloop<PA, PB, 1>(A, aplane, kpad, mpad - mt0, B, bplane, kpad, npad - nt0, kpad, tsm, ctl, o);
+  oztc::teardown(ctl);
+  if (!ok) {
+    if (threadIdx.x == 0 && flags) atomicOr(flags, DEV_TC_TIMEOUT);
+    return;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = mt0 + 32 * (warp & 3) + lane;
+  if (i >= M) return;
+  const double alpha = g.alpha.x, beta = g.beta.x;
+  const int eai = ea[size_t(ba) * mpad + i] - 57;
+  double* C = static_cast<double*>(g.C);
+  const int cw = g.c_real ? 1 : 2;  // doubles per element
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const int j = nt0 + 16 * (warp >> 2) + c;
+    if (j >= N) continue;
+    const double v = oztc::value(o, c) * (alpha * oz::pow2(eai + eb[size_t(bb) * npad + j]));
+    const long long idx = (i * g.crs + j * g.ccs + b * g.cbs) * cw + comp;
+    C[idx] = (beta == 0.0) ? v : fma(beta, C[idx], v);
+  }
+}
+
+template <int PA, int PB>
+int launch_ozaki_tc(int M, int N, int mpad, int npad, int kpad, const __nv_bfloat16* As, const int* ea,
+                    const __nv_bfloat16* Bs, const int* eb, const GemmArgs& g, cudaStream_t s) {
+  const size_t shm = oztc::kSmemBytes;
+  static bool attr = false;
+  if (!attr) {
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<PA, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    attr = true;
+  }
+  const int ncomp = (g.c_real || (PA == 1 && PB == 1)) ? 1 : 2;
+  const int a_shared = g.A.bs == 0 ? 1 : 0, b_shared = g.B.bs == 0 ? 1 : 0;
+  dim3 grid((npad + oztc::kN - 1) / oztc::kN, (mpad + oztc::kM - 1) / oztc::kM, g.batch * ncomp);
+  ozaki_tc_kernel<PA, PB><<<grid, oztc::kThreads, shm, s>>>(M, N, mpad, npad, kpad, As, ea, Bs, eb, g, ncomp,
+                                                             a_shared, b_shared, g_dev_flags);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
 struct OzScratch {
   cudaStream_t stream = nullptr;
   __nv_bfloat16* buf = nullptr;
@@ -257,6 +321,14 @@ int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
       slice_kernel<true><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, g.conj_b, Bs, eb);
     else
       slice_kernel<false><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, false, Bs, eb);
+  }
+  // tensor-memory path: real alpha / beta (the components are then independent)
+  const bool real_scalars = g.alpha.y == 0.0 && g.beta.y == 0.0 && !g.alpha_vec;
+  if (g_gemm_mode == 2 && real_scalars && g.batch * 2 <= 65535) {
+    if (PA == 2 && PB == 2) return launch_ozaki_tc<2, 2>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
+    if (PA == 2) return launch_ozaki_tc<2, 1>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
+    if (PB == 2) return launch_ozaki_tc<1, 2>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
+    return launch_ozaki_tc<1, 1>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
   }
   if (PA == 2 && PB == 2) return launch_ozaki_mma<2, 2>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
   if (PA == 2) return launch_ozaki_mma<2, 1>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);

@@ -1806,6 +1806,10 @@ int check_flags(tvap_ctx* c) {
   if (f & DEV_CHOLESKY) return TVAP_ERR_CHOLESKY;
   if (f & DEV_TRTRI) return TVAP_ERR_TRTRI;
   if (f & DEV_IMAG_GRAD) return TVAP_ERR_IMAG_GRADIENT;
+  if (f & DEV_TC_TIMEOUT) {
+    set_last_error("a tensor-core kernel ran out of its bounded wait", __FILE__, __LINE__);
+    return TVAP_ERR_DEVICE_TIMEOUT;
+  }
   return TVAP_OK;
 }
 

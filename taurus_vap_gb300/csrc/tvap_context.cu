@@ -136,7 +136,7 @@ int tvap_set_timing(tvap_ctx* c, int on) {
 }
 
 int tvap_set_gemm_mode(tvap_ctx* c, int mode) {
-  if (!c || (mode != 0 && mode != 1)) return TVAP_ERR_ARG;
+  if (!c || mode < 0 || mode > 2) return TVAP_ERR_ARG;
   c->gemm_mode = mode;
   return TVAP_OK;
 }
@@ -342,6 +342,7 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   c->kernel_launches = 0;
   g_gemm_mode = c->gemm_mode;
+  g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   int rc;

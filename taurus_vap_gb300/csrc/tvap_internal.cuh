@@ -68,6 +68,7 @@ enum DevFlag : int {
   DEV_CHOLESKY = 32,
   DEV_TRTRI = 64,
   DEV_IMAG_GRAD = 128,
+  DEV_TC_TIMEOUT = 256,
 };
 
 // ---------------------------------------------------------------------------
@@ -102,9 +103,11 @@ int gemm_ozaki(const GemmArgs& g, cudaStream_t s);
 void oz_release(cudaStream_t s);
 // per-stream scratch of the emulated products (grown on demand, stream-ordered)
 int oz_scratch(cudaStream_t s, size_t bytes, size_t ex_count, __nv_bfloat16** buf, int** ex);
-// GEMM arithmetic of the calls in flight: 0 FP64 pipe, 1 emulated (set by
-// every C-ABI entry point from its context)
+// GEMM arithmetic of the calls in flight: 0 FP64 pipe, 1 emulated with
+// mma.sync, 2 emulated with tcgen05 (set by every C-ABI entry point from its
+// context), and the status word of that context
 extern int g_gemm_mode;
+extern int* g_dev_flags;
 
 // ---------------------------------------------------------------------------
 // Hamiltonian in gather form (built once from the reference's element list)

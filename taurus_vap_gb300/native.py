@@ -167,7 +167,8 @@ class Context:
 
     def set_gemm_mode(self, mode: int):
         """0: dense products on the FP64 pipe; 1 (default): FP64 emulated on
-        the bf16 tensor cores."""
+        the bf16 tensor cores with mma.sync; 2: the same with tcgen05 MMAs and
+        tensor-memory accumulators."""
         _check(lib().tvap_set_gemm_mode(self.h, int(mode)), "tvap_set_gemm_mode")
 
     def set_stream(self, stream_handle: int):
