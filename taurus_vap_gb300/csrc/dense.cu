@@ -261,7 +261,7 @@ int gemm(const GemmArgs& g, cudaStream_t s) {
   // the emulated product pays off for batched work; small single products
   // (canonical-basis refinement, per-iteration blocks, evolution) stay on the
   // FP64 pipe
-  if (g_gemm_mode >= 1 && g.K >= 16 && double(g.M) * g.N * g.K * g.batch >= 2.0e7) return gemm_ozaki(g, s);
+  if (g_gemm_mode >= 1 && g.K >= 16 && double(g.M) * g.N * g.K * g.batch >= 1.0e6) return gemm_ozaki(g, s);
   // few tiles in all (single small products): the smallest tile, to spread
   // the latency-bound work over more SMs
   const long long t28 = (long long)((g.M + 27) / 28) * ((g.N + 27) / 28) * g.batch;
