@@ -451,8 +451,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64-pipe comparison run")
-    ap.add_argument("--gemm-mode", type=int, default=1,
-                    help="dense products: 1 emulated with mma.sync (default), 2 emulated with tcgen05, 0 FP64 pipe")
+    ap.add_argument("--gemm-mode", type=int, default=2,
+                    help="dense products: 2 emulated with tcgen05 (default), 1 emulated with mma.sync, 0 FP64 pipe")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

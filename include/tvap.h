@@ -96,13 +96,14 @@ int tvap_kernel_launches(const tvap_ctx* ctx);
  * tvap_get_timing returns milliseconds and call counts per section. */
 int tvap_set_timing(tvap_ctx* ctx, int on);
 /* Arithmetic of the dense products: 0 = the FP64 pipe (DFMA);
- * 1 (default) = FP64 emulated on the bf16 tensor cores by exact integer
- * splitting (8 balanced 7-bit digits per FP64 value, exact FP32 partial sums,
- * integer recombination) with warp-level mma.sync; 2 = the same splitting
- * with tcgen05 MMAs and tensor-memory accumulators.  In mode 1 the field contraction over 16 or more
- * gauge angles also runs on the tensor cores (dense symmetry blocks of the
- * interaction); the factorisations and all reductions run on the FP64 pipe
- * in both modes. */
+ * 1 = FP64 emulated on the bf16 tensor cores by exact integer splitting (8
+ * balanced 7-bit digits per FP64 value, exact FP32 partial sums, integer
+ * recombination) with warp-level mma.sync; 2 (default) = the same splitting
+ * with tcgen05 MMAs and tensor-memory accumulators for the batched products
+ * (small single products keep the mma.sync kernel).  In modes 1 and 2 the
+ * field contraction over 16 or more gauge angles also runs on the tensor
+ * cores (dense symmetry blocks of the interaction); the factorisations and
+ * all reductions run on the FP64 pipe in every mode. */
 int tvap_set_gemm_mode(tvap_ctx* ctx, int mode);
 int tvap_get_timing(tvap_ctx* ctx, double* ms, long long* calls, int nsec);
 /* Diagnostic counters since the last tvap_set_timing, for the canonical

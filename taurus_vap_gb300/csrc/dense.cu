@@ -253,14 +253,13 @@ int pick_tile(int M, int N) {
 
 }  // namespace
 
-int g_gemm_mode = 1;
+int g_gemm_mode = 2;
 int* g_dev_flags = nullptr;
 
 int gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return TVAP_OK;
-  // the emulated product pays off for batched work; small single products
-  // (canonical-basis refinement, per-iteration blocks, evolution) stay on the
-  // FP64 pipe
+  // every product of at least 10^6 multiply-adds runs emulated on the tensor
+  // cores; the smaller ones (few-column blocks, short K) stay on the FP64 pipe
   if (g_gemm_mode >= 1 && g.K >= 16 && double(g.M) * g.N * g.K * g.batch >= 1.0e6) return gemm_ozaki(g, s);
   // few tiles in all (single small products): the smallest tile, to spread
   // the latency-bound work over more SMs

@@ -11,7 +11,10 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <climits>
 #include <mutex>
+#include <utility>
 
 #include "ozaki_core.cuh"
 #include "ozaki_tc.cuh"
@@ -153,67 +156,222 @@ int launch_ozaki_mma(int M, int N, int mpad, int npad, int kpad, const __nv_bflo
   return TVAP_OK;
 }
 
-// One CTA per (128 x 64 output tile, component) of one batch entry, tcgen05
-// MMAs with tensor-memory accumulators (ozaki_tc.cuh).  alpha and beta are
-// real here (the components are then independent).
-template <int PA, int PB>
-__global__ void __launch_bounds__(oztc::kThreads, 1)
-    ozaki_tc_kernel(int M, int N, int mpad, int npad, int kpad, const __nv_bfloat16* __restrict__ As,
-                    const int* __restrict__ ea, const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb,
-                    GemmArgs g, int ncomp, int a_shared, int b_shared, int* flags) {
-  extern __shared__ __align__(1024) __nv_bfloat16 tsm[];
-  __shared__ oztc::Ctl ctl;
-  const int b = blockIdx.z / ncomp, comp = blockIdx.z - b * ncomp;
-  const int ba = a_shared ? 0 : b, bb = b_shared ? 0 : b;
-  const int mt0 = blockIdx.y * oztc::kM, nt0 = blockIdx.x * oztc::kN;
-  const size_t aplane = size_t(mpad) * kpad, bplane = size_t(npad) * kpad;
-  const __nv_bfloat16* A = As + size_t(ba) * kDigits * PA * aplane + size_t(mt0) * kpad;
-  const __nv_bfloat16* B = Bs + size_t(bb) * kDigits * PB * bplane + size_t(nt0) * kpad;
-  oztc::setup(ctl);
-  oztc::Acc o;
-  bool ok;
-  if (comp == 0)
-    ok = oztc::mainloop<PA, PB, 0>(A, aplane, kpad, mpad - mt0, B, bplane, kpad, npad - nt0, kpad, tsm, ctl, o);
-  else
-    ok = oztc::mainloop<PA, PB, 1>(A, aplane, kpad, mpad - mt0, B, bplane, kpad, npad - nt0, kpad, tsm, ctl, o);
-  oztc::teardown(ctl);
-  if (!ok) {
-    if (threadIdx.x == 0 && flags) atomicOr(flags, DEV_TC_TIMEOUT);
-    return;
+// ---------------------------------------------------------------------------
+// tensor-memory path (ozaki_tc.cuh): real products of tiled digit planes
+// ---------------------------------------------------------------------------
+
+// Real operand X' of a product, built from a strided batched source operand X
+// (element (r, k) of batch b at p[r sr + k sk + b bs]; r a row of op(A) or a
+// column of op(B), k the contraction index).  Forms:
+//   0  real:                        X'(r, k) = X(r, k)                      (rows x K)
+//   1  complex, planes stacked:     X' = [Re X; Im X]                       (2 rows x K)
+//   2  complex, real representation X' = [[Re X, -Im X], [Im X, Re X]]      (2 rows x 2 kp)
+//   3  complex, planes side by side X' = [Re X, Im X]                       (rows x 2 kp)
+// so that A' B'^T of (2, 3) holds [Re C; Im C] of a complex x complex
+// product, of (1, 0) [Re C; Im C] and of (0, 1) [Re C, Im C].  In forms 2 and
+// 3 each column block is padded with zeros from K to kp (a multiple of 16).
+// nstack > 1 stacks the rows of nstack batch entries (X' row b xrows + r).
+struct TcSrc {
+  const void* p;
+  long long sr, sk, bs;
+  int rows, K, form;
+  bool conj;
+  int xrows, xk, nstack, kp;
+};
+
+// Digit planes of X' in the tiled layout of ozaki_tc.cuh.  One CTA per 8
+// source rows of one slot: the rows are gathered into shared memory
+// (independent loads, consecutive threads on the source's contiguous index),
+// one warp per row takes the exponents, then every thread converts 8
+// consecutive k of one part (real or imaginary) of one row to 8 digits and
+// stores one 16-byte core-matrix row per digit at each place of X' that
+// holds them (twice in form 2: the imaginary block negated by its sign bits).
+constexpr int kSliceThreads = 256;
+__global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int tile_rows, int rows_pad, int nks,
+                                                                  __nv_bfloat16* __restrict__ out,
+                                                                  int* __restrict__ ex) {
+  extern __shared__ double2 xs[];  // 8 rows x K (real sources use .x)
+  __shared__ int e_s[8][2];        // exponent of the real / imaginary part
+  const int t = threadIdx.x;
+  const int K = x.K, form = x.form;
+  const bool cplx = form != 0;
+  const int sq0 = blockIdx.x * 8;
+  const int slot = blockIdx.y;
+  const int nsrc = x.nstack * x.rows;
+  auto src_row = [&](int row, int& b, int& i) {
+    const int sq = sq0 + row;
+    b = x.nstack > 1 ? sq / x.rows : slot;
+    i = x.nstack > 1 ? sq - b * x.rows : sq;
+  };
+  const bool k_fast = (x.sk == 1);
+#pragma unroll 4
+  for (int idx = t; idx < 8 * K; idx += kSliceThreads) {
+    int row, k;
+    if (k_fast) {
+      row = idx / K;
+      k = idx - row * K;
+    } else {
+      row = idx & 7;
+      k = idx >> 3;
+    }
+    double2 v = make_double2(0.0, 0.0);
+    if (sq0 + row < nsrc) {
+      int b, i;
+      src_row(row, b, i);
+      const long long off = b * x.bs + i * x.sr + k * x.sk;
+      if (cplx) {
+        v = static_cast<const double2*>(x.p)[off];
+        if (x.conj) v.y = -v.y;
+      } else {
+        v.x = static_cast<const double*>(x.p)[off];
+      }
+    }
+    xs[row * K + k] = v;
   }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = mt0 + 32 * (warp & 3) + lane;
-  if (i >= M) return;
-  const double alpha = g.alpha.x, beta = g.beta.x;
-  const int eai = ea[size_t(ba) * mpad + i] - 57;
-  double* C = static_cast<double*>(g.C);
-  const int cw = g.c_real ? 1 : 2;  // doubles per element
+  __syncthreads();
+  {
+    const int w = t >> 5, lane = t & 31;
+    int er = oz::kExpZero, ei = oz::kExpZero;
+    for (int k = lane; k < K; k += 32) {
+      const double2 v = xs[w * K + k];
+      if (v.x != 0.0) er = max(er, oz::dexp(v.x));
+      if (v.y != 0.0) ei = max(ei, oz::dexp(v.y));
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      er = max(er, __shfl_xor_sync(0xffffffffu, er, off));
+      ei = max(ei, __shfl_xor_sync(0xffffffffu, ei, off));
+    }
+    if (form >= 2) er = ei = max(er, ei);  // one exponent for the whole X' row
+    if (er == oz::kExpZero) er = 0;
+    if (ei == oz::kExpZero) ei = 0;
+    if (lane == 0) {
+      e_s[w][0] = er;
+      e_s[w][1] = ei;
+      if (sq0 + w < nsrc) {
+        int b, i;
+        src_row(w, b, i);
+        const size_t qtop = size_t(x.nstack > 1 ? b * x.xrows : 0) + i;
+        ex[size_t(slot) * rows_pad + qtop] = er;
+        if (form == 1 || form == 2) ex[size_t(slot) * rows_pad + qtop + x.rows] = ei;
+      }
+    }
+  }
+  __syncthreads();
+  // work items: (row, chunk of 8 k, part), rows fastest so that a half-warp
+  // writes whole 256-byte core-matrix row groups
+  const int nchunk = form >= 2 ? x.kp / 8 : nks * 2;
+  const int nparts = cplx ? 2 : 1;
+  const int tiles = rows_pad / tile_rows;
+  const size_t tile_elems = size_t(tile_rows) * 16;
+  for (int item = t; item < 8 * nchunk * nparts; item += kSliceThreads) {
+    const int row = item & 7;
+    const int c = (item >> 3) % nchunk, part = (item >> 3) / nchunk;
+    if (sq0 + row >= nsrc) continue;
+    int b, i;
+    src_row(row, b, i);
+    const int qtop = (x.nstack > 1 ? b * x.xrows : 0) + i;
+    const int emax = e_s[row][part];
+    const int k0 = 8 * c;
+    uint32_t w[kDigits][4];
 #pragma unroll
-  for (int c = 0; c < 16; ++c) {
-    const int j = nt0 + 16 * (warp >> 2) + c;
-    if (j >= N) continue;
-    const double v = oztc::value(o, c) * (alpha * oz::pow2(eai + eb[size_t(bb) * npad + j]));
-    const long long idx = (i * g.crs + j * g.ccs + b * g.cbs) * cw + comp;
-    C[idx] = (beta == 0.0) ? v : fma(beta, C[idx], v);
+    for (int j = 0; j < 8; j += 2) {
+      int d0[kDigits], d1[kDigits];
+      const double2 v0 = (k0 + j < K) ? xs[row * K + k0 + j] : make_double2(0.0, 0.0);
+      const double2 v1 = (k0 + j + 1 < K) ? xs[row * K + k0 + j + 1] : make_double2(0.0, 0.0);
+      oz::to_digits(oz::to_fixed(part ? v0.y : v0.x, emax), d0);
+      oz::to_digits(oz::to_fixed(part ? v1.y : v1.x, emax), d1);
+#pragma unroll
+      for (int s = 0; s < kDigits; ++s) w[s][j >> 1] = oz::bf16x2_of_ints(d0[s], d1[s]);
+    }
+    auto put = [&](int q, int kq, uint32_t flip) {
+      const size_t tb = (size_t(slot) * tiles + q / tile_rows) * nks + (kq >> 4);
+      const int toff = oztc::tile_offset(q % tile_rows, kq);
+#pragma unroll
+      for (int s = 0; s < kDigits; ++s) {
+        __nv_bfloat16* dst = out + (tb * kDigits + s) * tile_elems + toff;
+        *reinterpret_cast<uint4*>(dst) = make_uint4(w[s][0] ^ flip, w[s][1] ^ flip, w[s][2] ^ flip, w[s][3] ^ flip);
+      }
+    };
+    switch (form) {
+      case 0: put(qtop, k0, 0u); break;
+      case 1: put(part ? qtop + x.rows : qtop, k0, 0u); break;
+      case 2:
+        if (part == 0) {
+          put(qtop, k0, 0u);
+          put(qtop + x.rows, x.kp + k0, 0u);
+        } else {
+          put(qtop + x.rows, k0, 0u);
+          put(qtop, x.kp + k0, 0x80008000u);
+        }
+        break;
+      default: put(qtop, part ? x.kp + k0 : k0, 0u); break;
+    }
   }
 }
 
-template <int PA, int PB>
-int launch_ozaki_tc(int M, int N, int mpad, int npad, int kpad, const __nv_bfloat16* As, const int* ea,
-                    const __nv_bfloat16* Bs, const int* eb, const GemmArgs& g, cudaStream_t s) {
-  const size_t shm = oztc::kSmemBytes;
-  static bool attr = false;
-  if (!attr) {
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<PA, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
-    attr = true;
-  }
-  const int ncomp = (g.c_real || (PA == 1 && PB == 1)) ? 1 : 2;
-  const int a_shared = g.A.bs == 0 ? 1 : 0, b_shared = g.B.bs == 0 ? 1 : 0;
-  dim3 grid((npad + oztc::kN - 1) / oztc::kN, (mpad + oztc::kM - 1) / oztc::kM, g.batch * ncomp);
-  ozaki_tc_kernel<PA, PB><<<grid, oztc::kThreads, shm, s>>>(M, N, mpad, npad, kpad, As, ea, Bs, eb, g, ncomp,
-                                                             a_shared, b_shared, g_dev_flags);
-  TVAP_CUDA(cudaGetLastError());
-  return TVAP_OK;
+// Output mapping of the tensor-memory product: row q of A' (slot z) and row
+// col of B' hold component comp = (r >= a_split) + (col >= b_split) of
+// C(i, j) of batch entry b; alpha and beta are real.
+struct TcOut {
+  void* C;
+  long long crs, ccs, cbs;
+  bool c_real;
+  double alpha, beta;
+  int a_rows, a_split, b_rows, b_split, nstack;
+};
+
+// Persistent CTAs over the (128 x 64 tile of A' B'^T, slot) tiles; tile
+// numbers run over the N tiles fastest, then the M tiles, then the slots, so
+// that the CTAs working at one time share their A and B tiles through L2.
+__global__ void __launch_bounds__(oztc::kThreads, 1)
+    ozaki_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ ea, int a_rows_pad,
+                    const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb, int b_rows_pad, int b_shared,
+                    int nslots, int nks, TcOut o, int* flags) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ oztc::Ctl ctl;
+  const int a_tiles = a_rows_pad / oztc::kM, b_tiles = b_rows_pad / oztc::kN;
+  const int ntiles = a_tiles * b_tiles * nslots;
+  auto tile_ptrs = [&](int tile, const unsigned char*& A, const unsigned char*& B) {
+    const int nt = tile % b_tiles, rest = tile / b_tiles;
+    const int mt = rest % a_tiles, z = rest / a_tiles;
+    const int bz = b_shared ? 0 : z;
+    A = reinterpret_cast<const unsigned char*>(As) + (size_t(z) * a_tiles + mt) * nks * size_t(oztc::kABytes);
+    B = reinterpret_cast<const unsigned char*>(Bs) + (size_t(bz) * b_tiles + nt) * nks * size_t(oztc::kBBytes);
+  };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto store = [&](int tile, const oztc::Acc& acc) {
+    const int nt = tile % b_tiles, rest = tile / b_tiles;
+    const int mt = rest % a_tiles, z = rest / a_tiles;
+    const int bz = b_shared ? 0 : z;
+    const int q = mt * oztc::kM + 32 * (warp & 3) + lane;
+    if (q >= o.nstack * o.a_rows) return;
+    const int b = o.nstack > 1 ? q / o.a_rows : z;
+    int i = o.nstack > 1 ? q - b * o.a_rows : q;
+    int comp_a = 0;
+    if (i >= o.a_split) {
+      i -= o.a_split;
+      comp_a = 1;
+    }
+    const int eai = ea[size_t(z) * a_rows_pad + q] - 57;
+    double* C = static_cast<double*>(o.C);
+    const int cw = o.c_real ? 1 : 2;  // doubles per element
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int col = nt * oztc::kN + 16 * (warp >> 2) + c;
+      if (col >= o.b_rows) continue;
+      int j = col, comp = comp_a;
+      if (j >= o.b_split) {
+        j -= o.b_split;
+        comp += 1;
+      }
+      if (comp > 0 && o.c_real) continue;
+      const double v = oztc::value(acc, c) * (o.alpha * oz::pow2(eai + eb[size_t(bz) * b_rows_pad + col]));
+      const long long idx = (i * o.crs + j * o.ccs + b * o.cbs) * cw + comp;
+      C[idx] = (o.beta == 0.0) ? v : fma(o.beta, C[idx], v);
+    }
+  };
+  if (!oztc::run_tiles(blockIdx.x, gridDim.x, ntiles, nks, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
+    atomicOr(flags, DEV_TC_TIMEOUT);
 }
 
 struct OzScratch {
@@ -289,10 +447,124 @@ void oz_release(cudaStream_t s) {
     }
 }
 
+namespace {
+
+constexpr int kTcMinTiles = 152;
+
+// The tensor-memory path for one product (mode 2).  Returns TVAP_ERR_ARG
+// without launching anything when the product is not of a supported kind.
+int gemm_tc(const GemmArgs& g, cudaStream_t s) {
+  const bool real_scalars = g.alpha.y == 0.0 && g.beta.y == 0.0 && !g.alpha_vec;
+  if (!real_scalars || g.upper_only || (g.a_real && g.b_real && !g.c_real)) return TVAP_ERR_ARG;
+  const bool a_sh = g.A.bs == 0 && g.batch > 1, b_sh = g.B.bs == 0 && g.batch > 1;
+  if (a_sh && b_sh) return TVAP_ERR_ARG;
+  // rows of op(A): element (i, k) at A.p[i rs + k cs]; rows of op(B)^T:
+  // element (j, k) at B.p[k rs + j cs].  With a shared A the transposed
+  // product C^T = op(B)^T op(A)^T is formed, so that the per-batch operand is
+  // always the left one and can be stacked along the rows.
+  struct Side {
+    const void* p;
+    long long sr, sk, bs;
+    int rows;
+    bool real, conj;
+  };
+  Side L{g.A.p, g.A.rs, g.A.cs, g.A.bs, g.M, g.a_real, g.conj_a};
+  Side R{g.B.p, g.B.cs, g.B.rs, g.B.bs, g.N, g.b_real, g.conj_b};
+  long long crs = g.crs, ccs = g.ccs;
+  if (a_sh) {
+    std::swap(L, R);
+    std::swap(crs, ccs);
+  }
+  const int K = g.K, kp = (K + 15) / 16 * 16;
+  TcSrc xa{L.p, L.sr, L.sk, L.bs, L.rows, K, 0, L.conj, L.rows, K, 1, K};
+  TcSrc xb{R.p, R.sr, R.sk, R.bs, R.rows, K, 0, R.conj, R.rows, K, 1, K};
+  TcOut o{};
+  o.a_split = o.b_split = INT_MAX;
+  if (!L.real && !R.real) {
+    xa.form = 2;
+    xa.xrows = 2 * L.rows;
+    xa.xk = 2 * kp;
+    xa.kp = kp;
+    xb.form = 3;
+    xb.xk = 2 * kp;
+    xb.kp = kp;
+    o.a_split = L.rows;
+  } else if (!L.real) {
+    xa.form = 1;
+    xa.xrows = 2 * L.rows;
+    o.a_split = L.rows;
+  } else if (!R.real) {
+    xb.form = 1;
+    xb.xrows = 2 * R.rows;
+    o.b_split = R.rows;
+  }
+  const bool stack = g.batch > 1 && (a_sh || b_sh);
+  xa.nstack = stack ? g.batch : 1;
+  const int a_slots = stack ? 1 : g.batch, b_slots = stack ? 1 : g.batch;
+  const int a_rows_pad = (xa.nstack * xa.xrows + oztc::kM - 1) / oztc::kM * oztc::kM;
+  const int b_rows_pad = (xb.xrows + oztc::kN - 1) / oztc::kN * oztc::kN;
+  const int nks = (xa.xk + 15) / 16;
+  const size_t asz = size_t(a_slots) * (a_rows_pad / oztc::kM) * nks * (oztc::kABytes / 2);
+  const size_t bsz = size_t(b_slots) * (b_rows_pad / oztc::kN) * nks * (oztc::kBBytes / 2);
+  // products of few tiles (the single small products of the canonical basis
+  // and the evolution) are latency-bound: the 32 x 32 mma.sync tiles spread
+  // them over more SMs
+  if (size_t(a_rows_pad / oztc::kM) * (b_rows_pad / oztc::kN) * a_slots < size_t(kTcMinTiles)) return TVAP_ERR_ARG;
+  int rc;
+  OzScratch* sc = nullptr;
+  if ((rc = oz_reserve(s, sizeof(__nv_bfloat16) * (asz + bsz), size_t(a_slots) * a_rows_pad +
+                                                                   size_t(b_slots) * b_rows_pad, &sc)))
+    return rc;
+  __nv_bfloat16* As = sc->buf;
+  __nv_bfloat16* Bs = sc->buf + asz;
+  int* ea = sc->ex;
+  int* eb = sc->ex + size_t(a_slots) * a_rows_pad;
+  const size_t slice_shm = sizeof(double2) * 8 * size_t(K);
+  if (slice_shm > 48 * 1024) {
+    static size_t granted = 48 * 1024;
+    if (slice_shm > size_t(227) * 1024) return TVAP_ERR_ARG;
+    if (slice_shm > granted) {
+      TVAP_CUDA(cudaFuncSetAttribute(slice_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(slice_shm)));
+      granted = slice_shm;
+    }
+  }
+  slice_tc_kernel<<<dim3((xa.nstack * xa.rows + 7) / 8, a_slots), kSliceThreads, slice_shm, s>>>(
+      xa, oztc::kM, a_rows_pad, nks, As, ea);
+  slice_tc_kernel<<<dim3((xb.rows + 7) / 8, b_slots), kSliceThreads, slice_shm, s>>>(xb, oztc::kN, b_rows_pad, nks,
+                                                                                     Bs, eb);
+  o.C = g.C;
+  o.crs = crs;
+  o.ccs = ccs;
+  o.cbs = g.cbs;
+  o.c_real = g.c_real;
+  o.alpha = g.alpha.x;
+  o.beta = g.beta.x;
+  o.a_rows = xa.xrows;
+  o.b_rows = xb.xrows;
+  o.nstack = xa.nstack;
+  static bool attr = false;
+  if (!attr) {
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(oztc::kSmemBytes)));
+    attr = true;
+  }
+  static int sms = 0;
+  if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+  const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / oztc::kN) * a_slots;
+  const int grid = int(std::min<long long>(ntiles, sms));
+  ozaki_tc_kernel<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
+                                                                  b_slots == 1 ? 1 : 0, a_slots, nks, o, g_dev_flags);
+  TVAP_CUDA(cudaGetLastError());
+  return TVAP_OK;
+}
+
+}  // namespace
+
 // Returns TVAP_OK after launching, or TVAP_ERR_ARG when the shape is not
 // supported (the caller then uses the FP64 pipe).
 int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.batch <= 0) return TVAP_OK;
+  if (g_gemm_mode == 2 && gemm_tc(g, s) == TVAP_OK) return TVAP_OK;
   const int PA = g.a_real ? 1 : 2, PB = g.b_real ? 1 : 2;
   const int mpad = (g.M + 31) / 32 * 32, npad = (g.N + 31) / 32 * 32, kpad = (g.K + 15) / 16 * 16;
   // operands with batch stride 0 are split once for the whole batch
@@ -321,14 +593,6 @@ int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
       slice_kernel<true><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, g.conj_b, Bs, eb);
     else
       slice_kernel<false><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, false, Bs, eb);
-  }
-  // tensor-memory path: real alpha / beta (the components are then independent)
-  const bool real_scalars = g.alpha.y == 0.0 && g.beta.y == 0.0 && !g.alpha_vec;
-  if (g_gemm_mode == 2 && real_scalars && g.batch * 2 <= 65535) {
-    if (PA == 2 && PB == 2) return launch_ozaki_tc<2, 2>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
-    if (PA == 2) return launch_ozaki_tc<2, 1>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
-    if (PB == 2) return launch_ozaki_tc<1, 2>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
-    return launch_ozaki_tc<1, 1>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
   }
   if (PA == 2 && PB == 2) return launch_ozaki_mma<2, 2>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
   if (PA == 2) return launch_ozaki_mma<2, 1>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);

@@ -70,15 +70,38 @@ __host__ __device__ __forceinline__ long long to_fixed(double x, int emax) {
   return (b < 0) ? -m : m;
 }
 
-// balanced base-128 digits, d[0] most significant
+// balanced base-128 digits, d[0] most significant.  X = hi 2^28 + lo with
+// 0 <= lo < 2^28: the low four digits come from lo (leaving a carry of 0 or
+// 1), the high four from hi + carry, all in 32-bit arithmetic.
 __host__ __device__ __forceinline__ void to_digits(long long X, int* d) {
+  int lo = int(X & 0x0FFFFFFFLL);
+  int hi = int(X >> 28);
 #pragma unroll
-  for (int s = kDigits - 1; s >= 0; --s) {
-    const int r = int(((X + 64) & 127)) - 64;
+  for (int s = kDigits - 1; s >= 4; --s) {
+    const int r = ((lo + 64) & 127) - 64;
     d[s] = r;
-    X = (X - r) >> 7;
+    lo = (lo - r) >> 7;
+  }
+  hi += lo;
+#pragma unroll
+  for (int s = 3; s >= 0; --s) {
+    const int r = ((hi + 64) & 127) - 64;
+    d[s] = r;
+    hi = (hi - r) >> 7;
   }
 }
+
+#ifdef __CUDACC__
+// bf16 bit patterns of two small integers (|v| < 2^22) packed into one word
+// (a in the low half): 1.5 * 2^23 + v is exact in FP32, subtracting
+// 1.5 * 2^23 leaves v as an FP32 value whose upper 16 bits are its bf16
+// pattern (v has at most 8 significant bits)
+__device__ __forceinline__ uint32_t bf16x2_of_ints(int a, int b) {
+  const float fa = __int_as_float(0x4B400000 + a) - 12582912.0f;
+  const float fb = __int_as_float(0x4B400000 + b) - 12582912.0f;
+  return __byte_perm(__float_as_uint(fa), __float_as_uint(fb), 0x7632);
+}
+#endif
 
 // bf16 bit pattern of a small integer (|v| <= 256: exact)
 __host__ __device__ __forceinline__ uint16_t bf16_bits_of_int(int v) {

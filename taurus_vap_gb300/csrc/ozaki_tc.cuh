@@ -1,33 +1,37 @@
 // The integer-splitting products of ozaki_core.cuh on the 5th-generation
-// tensor cores (tcgen05): accumulators in tensor memory, one thread issuing
-// the MMAs, operands in shared memory.
+// tensor cores (tcgen05): a warp-specialised pipeline fed by bulk asynchronous
+// copies, accumulators in tensor memory, one thread issuing the MMAs.
 //
-// A CTA computes one real component (the real or the imaginary part) of a
-// 128 x 64 output tile (MMA shape M128 N64 K16, bf16 x bf16 -> f32; on this
-// part an M128 x N x K16 MMA costs the same for every N <= 64, so the widest
-// N that tensor memory allows is used).  The component is a sum of one or two
-// "segments" of real digit-plane products: real part of complex x complex =
-// A_r B_r^T + (-A_i) B_i^T (the minus sign is the MMA's negate-A bit),
-// imaginary part = A_r B_i^T + A_i B_r^T; with one real operand one segment.
-// For every digit pair (s, t) with s + t <= 7 one MMA accumulates into the
-// TMEM accumulator of weight group g = s + t: 8 groups x 64 columns = all 512
-// TMEM columns.  Over a fold interval of 384 k (both segments counted) a
-// group sum stays below 2^24 and is an exact FP32 integer; at the end of an
-// interval the epilogue warps read the accumulators (tcgen05.ld), convert
-// them to integers and fold them into 64-bit integer accumulators in
-// registers.
+// Every product reaching this path is a REAL product C' = A' B'^T of digit
+// planes (complex operands are turned into real ones by the slicing pass:
+// the real representation [[Ar, -Ai], [Ai, Ar]] for complex x complex, stacked
+// real/imaginary rows otherwise).  The slicing pass writes each digit plane
+// already tiled in the tensor cores' canonical no-swizzle K-major layout, so
+// that the operands of one k-step (16 k, all 8 digits) of a 128-row A tile and
+// of a 64-row B tile are two contiguous blocks of 32 KB and 16 KB, fetched by
+// two cp.async.bulk copies that complete on the stage's mbarrier.
 //
-// Pipeline: two shared-memory stages of two k-steps (32) each; all threads
-// fill a stage with cp.async (zero-fill beyond the valid rows / K), a proxy
-// fence and a barrier hand it to the MMA thread, whose tcgen05.commit on the
-// stage's mbarrier releases it again.  Every wait is bounded: on a timeout
-// the CTA stops issuing, waits (bounded) for its MMAs, reports through the
-// status word and frees its tensor memory.
+// Tile layout (bf16 elements) of R rows x 16 k of one digit plane: R/8 row
+// groups x 2 k-blocks of 8 x 8 "core matrices" (8 rows x 16 bytes, 128 bytes
+// contiguous): element (r, k) at (r / 8) * 128 + (k / 8) * 64 + (r % 8) * 8 +
+// k % 8.  Descriptor LBO = 128 B (next k-block), SBO = 256 B (next row group).
+// The tiles of one operand are ordered [slot][row tile][k-step][digit].
 //
-// Shared-memory operand layout (no swizzle, K-major): a tile of R rows x 16 k
-// of one digit plane is R/8 row groups x 2 k-blocks of 8 x 8 "core matrices"
-// (8 rows x 16 bytes each, 128 bytes contiguous); descriptor LBO = 128 B
-// (next k-block), SBO = 256 B (next row group).
+// Persistent CTAs (one per SM) loop over output tiles.  Roles (576 threads):
+// warps 0-15 read the accumulators (warp w: TMEM lanes
+// 32 (w % 4) .. + 32 = tile rows, columns 16 (w / 4) .. + 16), warp 16 issues
+// the copies, warp 17 allocates tensor memory and one of its threads issues
+// the MMAs.  The product of every digit pair (s, t) with s + t <= 7 (M128
+// N64 K16) accumulates into the TMEM accumulator of weight group g = s + t
+// (8 groups x 64 columns = all 512 columns); pairs with the same s and
+// adjacent t run as one wider MMA (issue_kstep).  Over a fold interval of 384 k a group sum
+// (<= 8 pairs x 2^12 per k) stays below 2^24 and is an exact FP32 integer; at
+// the end of an interval the epilogue warps read the accumulators (tcgen05.ld)
+// and fold them into 64-bit integer accumulators in registers.
+//
+// Every wait is bounded: on a timeout the CTA raises its abort flag, stops
+// issuing, waits (bounded) for the copies and MMAs it has issued and frees its
+// tensor memory; the kernel then reports through the status word.
 #pragma once
 
 #include "ozaki_core.cuh"
@@ -38,36 +42,32 @@ namespace oztc {
 using oz::kDigits;
 using oz::kKeep;
 
-constexpr int kM = 128;          // rows of op(A) per CTA
-constexpr int kN = 64;           // columns of op(B) per CTA
-constexpr int kThreads = 512;    // 16 warps: loaders, MMA issuer (thread 0), epilogue
-constexpr int kTmemCols = 512;   // 8 groups x 64 columns
-constexpr int kStages = 2;
-constexpr int kKs = 2;           // k-steps (of 16) per stage
-constexpr int kFoldSteps = 12;   // stages per fold interval: 8 x 384 x 2^12 < 2^24
-constexpr long long kSpin = 1LL << 22;  // bounded waits
+constexpr int kM = 128;                 // rows of A' per CTA (TMEM lanes)
+constexpr int kN = 64;                  // rows of B' (output columns) per CTA
+constexpr int kEpiWarps = 16;           // accumulator readers
+constexpr int kProducerWarp = 16;       // bulk copies
+constexpr int kMmaWarp = 17;            // TMEM allocation + MMA issue
+constexpr int kThreads = 32 * (kEpiWarps + 2);
+constexpr int kTmemCols = 512;          // 8 groups x 64 columns
+constexpr int kStages = 4;
+constexpr int kFoldKs = 24;             // k-steps per fold interval: 8 x 2^12 x 384 < 2^24
+constexpr long long kSpin = 1LL << 21;  // bounded waits (polls)
 
-constexpr int kATile = kM * 16;  // bf16 per digit tile of a stage
-constexpr int kBTile = kN * 16;
-constexpr int kKsElems = kDigits * (kATile + kBTile);  // bf16 per k-step of a stage
-constexpr int kStage = kKs * kKsElems;                 // bf16 per stage
-constexpr size_t kSmemBytes = kStages * sizeof(__nv_bfloat16) * size_t(kStage);
+constexpr int kATileElems = kM * 16;                // one digit plane of a k-step
+constexpr int kBTileElems = kN * 16;
+constexpr int kABytes = kDigits * kATileElems * 2;  // 32 KB per k-step
+constexpr int kBBytes = kDigits * kBTileElems * 2;  // 16 KB per k-step
+constexpr int kStageBytes = kABytes + kBBytes;
+constexpr size_t kSmemBytes = size_t(kStages) * kStageBytes;
+// one CTA per SM: two CTAs could never hold 512 TMEM columns each
+static_assert(2 * kSmemBytes > 228 * 1024, "the tcgen05 kernel must not share an SM with itself");
 
-// segments of a component: (A plane, B plane, negate A)
-struct Seg {
-  int pa, pb;
-  bool neg;
-};
-template <int PA, int PB, int COMP>
-struct Segs {
-  static constexpr int n = (PA == 2 && PB == 2) ? 2 : 1;
-  __host__ __device__ static constexpr Seg get(int i) {
-    return (PA == 2 && PB == 2)
-               ? (COMP == 0 ? (i == 0 ? Seg{0, 0, false} : Seg{1, 1, true})
-                            : (i == 0 ? Seg{0, 1, false} : Seg{1, 0, false}))
-               : (PA == 2 ? Seg{COMP, 0, false} : (PB == 2 ? Seg{0, COMP, false} : Seg{0, 0, false}));
-  }
-};
+// element offset of (row r, k) inside the k-step tile of one digit plane
+__host__ __device__ __forceinline__ int tile_offset(int r, int k) {
+  return (r >> 3) * 128 + ((k >> 3) & 1) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+#ifdef __CUDACC__
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -79,10 +79,9 @@ __device__ __forceinline__ uint64_t desc(uint32_t addr) {
          (uint64_t(1) << 46);
 }
 
-// kind::f16, bf16 x bf16 -> f32, both K-major, M = 128, N = 64
-__device__ __forceinline__ uint32_t idesc(bool negate_a) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(negate_a) << 13) | (uint32_t(kN >> 3) << 17) |
-         (uint32_t(kM >> 4) << 24);
+// kind::f16, bf16 x bf16 -> f32, both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(kM >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t id, uint32_t accumulate) {
@@ -97,17 +96,53 @@ __device__ __forceinline__ void commit(uint64_t* mbar) {
                : "memory");
 }
 
-// bounded wait for the completion of phase `parity` of an mbarrier
-__device__ __forceinline__ bool wait_parity(uint64_t* mbar, uint32_t parity) {
-  uint32_t done = 0;
-  for (long long it = 0; it < kSpin && !done; ++it) {
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(smem_u32(mbar)), "r"(parity)
-        : "memory");
-  }
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(mbar))
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(
+                   smem_u32(mbar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// bulk global -> shared copy completing `bytes` on an mbarrier (addresses
+// 16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool try_parity(uint64_t* mbar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(mbar)), "r"(parity)
+      : "memory");
   return done != 0;
+}
+
+// bounded wait for the completion of phase `parity`; gives up early when the
+// CTA's abort flag (if given) is raised.  `sleep` backs off between polls
+// (for the many epilogue threads, so that they do not take issue slots from
+// the producer and the MMA thread).
+__device__ __forceinline__ bool wait_parity(uint64_t* mbar, uint32_t parity, volatile int* abort, bool sleep) {
+  for (long long it = 0; it < kSpin; ++it) {
+    if (try_parity(mbar, parity)) return true;
+    if (abort && *abort) return false;
+    if (sleep) __nanosleep(128);
+  }
+  return false;
 }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
@@ -123,60 +158,42 @@ __device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* r) {
 }
 __device__ __forceinline__ void ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 
-// integer accumulators of one epilogue thread: row (warp % 4) * 32 + lane,
-// columns (warp / 4) * 16 .. + 16; groups 0-3 (h) and 4-7 (l)
+// integer accumulators of one epilogue thread (16 columns): groups 0-3 (h)
+// and 4-7 (l)
 struct Acc {
   long long h[16], l[16];
 };
 
 // shared control block
 struct Ctl {
-  uint64_t mbar[kStages];
+  uint64_t full[kStages], empty[kStages];
+  uint64_t acc_full, acc_empty, mma_done;
   uint32_t tmem;
+  int abort;
 };
 
-// kKs k-steps of one digit plane of A (128 rows) and of B (64 rows) into a
-// stage; digit s at X + s * dstride; a_rows / b_rows valid rows, k >= klen zero
-__device__ __forceinline__ void stage_load(const __nv_bfloat16* A, size_t a_dstride, int a_ld, int a_rows,
-                                           const __nv_bfloat16* B, size_t b_dstride, int b_ld, int b_rows, int k0,
-                                           int klen, __nv_bfloat16* st) {
-#pragma unroll
-  for (int q = 0; q < kKs; ++q) {
-    __nv_bfloat16* sA = st + q * kKsElems;
-    __nv_bfloat16* sB = sA + kDigits * kATile;
-    const int kq = k0 + 16 * q;
-    for (int v = threadIdx.x; v < kDigits * kM * 2; v += kThreads) {
-      const int kb = v & 1, r = (v >> 1) & (kM - 1), dg = v >> 8;
-      const int k = kq + kb * 8;
-      const bool ok = r < a_rows && k < klen;
-      __nv_bfloat16* dst = sA + dg * kATile + (((r >> 3) * 2 + kb) * 8 + (r & 7)) * 8;
-      oz::cp_async16(dst, ok ? A + dg * a_dstride + size_t(r) * a_ld + k : A, ok);
-    }
-    for (int v = threadIdx.x; v < kDigits * kN * 2; v += kThreads) {
-      const int kb = v & 1, r = (v >> 1) & (kN - 1), dg = v >> 7;
-      const int k = kq + kb * 8;
-      const bool ok = r < b_rows && k < klen;
-      __nv_bfloat16* dst = sB + dg * kBTile + (((r >> 3) * 2 + kb) * 8 + (r & 7)) * 8;
-      oz::cp_async16(dst, ok ? B + dg * b_dstride + size_t(r) * b_ld + k : B, ok);
-    }
-  }
-}
-
-// MMAs of one k-step for all digit pairs; FIRST = the k-step opens a fold
-// interval (the first product into each group, at s = 0, overwrites it).
-// Fully unrolled: every descriptor is the stage's base descriptor plus a
-// constant (the start-address field is the low 14 bits and shared addresses
-// stay below 2^18, so the addition never carries into the other fields).
+// MMAs of one k-step for all digit pairs (s, t), s + t <= 7.  The B digit
+// tiles of a stage lie back to back (digit t at + t * 2 KB, row groups 256 B
+// apart), so digits t0 .. t0 + c - 1 form ONE K-major operand of 64 c rows,
+// and the accumulators of groups s + t0 .. s + t0 + c - 1 are adjacent TMEM
+// column ranges: one MMA of N = 64 c covers c digit pairs.  Per digit s of A
+// that is one MMA of N <= 256 (c <= 4) for t = 0..3 and one for t = 4..7-s:
+// 12 MMAs per k-step, each A tile read from shared memory once or twice
+// instead of 8 - s times.  FIRST = the k-step opens a fold interval (the
+// products of s = 0, which reach every group, overwrite the accumulators).
+// Every descriptor is the stage's base descriptor plus a constant (the
+// start-address field is the low 14 bits and shared addresses stay below
+// 2^18, so the addition never carries into the other fields).
 template <bool FIRST>
-__device__ __forceinline__ void issue_kstep(uint32_t tmem, const __nv_bfloat16* st, uint32_t id) {
-  const uint64_t da = desc(smem_u32(st)), db = desc(smem_u32(st + kDigits * kATile));
-  constexpr uint32_t kAT = uint32_t(kATile * 2) >> 4, kBT = uint32_t(kBTile * 2) >> 4;
+__device__ __forceinline__ void issue_kstep(uint32_t tmem, const unsigned char* st) {
+  const uint64_t da = desc(smem_u32(st)), db = desc(smem_u32(st + kABytes));
+  constexpr uint32_t kAT = uint32_t(kATileElems * 2) >> 4, kBT = uint32_t(kBTileElems * 2) >> 4;
 #pragma unroll
   for (int s = 0; s < kDigits; ++s) {
 #pragma unroll
-    for (int t = 0; t < kDigits; ++t) {
-      if (s + t > kKeep) continue;
-      mma(tmem + uint32_t((s + t) * kN), da + uint64_t(s * kAT), db + uint64_t(t * kBT), id,
+    for (int t0 = 0; t0 <= kKeep - s; t0 += 4) {
+      const int c = (kKeep - s - t0 + 1) < 4 ? (kKeep - s - t0 + 1) : 4;
+      mma(tmem + uint32_t((s + t0) * kN), da + uint64_t(s * kAT), db + uint64_t(t0 * kBT), idesc(c * kN),
           (FIRST && s == 0) ? 0u : 1u);
     }
   }
@@ -204,109 +221,31 @@ __device__ __forceinline__ void fold(uint32_t tmem, Acc& o) {
   }
 }
 
-// The K loop of one component of a 128 x 64 tile.  A/B point at digit 0,
-// plane 0 of the tile's first row; digit s, plane p at + (s * P + p) * plane;
-// row r at + r * ld; rows >= a_rows / b_rows and k >= klen read as zero.
-// Returns false on a timeout (the accumulators are then incomplete).
-template <int PA, int PB, int COMP>
-__device__ bool mainloop(const __nv_bfloat16* A, size_t a_plane, int a_ld, int a_rows, const __nv_bfloat16* B,
-                         size_t b_plane, int b_ld, int b_rows, int klen, __nv_bfloat16* smem, Ctl& ctl, Acc& o) {
-  using SG = Segs<PA, PB, COMP>;
-  const int tid = threadIdx.x;
-#pragma unroll
-  for (int c = 0; c < 16; ++c) o.h[c] = o.l[c] = 0;
-  const int nks = (klen + 16 * kKs - 1) / (16 * kKs);  // stages per segment
-  const int ksteps = (klen + 15) / 16;                  // k-steps of 16 with data
-  const int nsteps = SG::n * nks;
-  bool ok = true;
-  // commits issued on / completions consumed from each stage's mbarrier
-  // (identical in every thread: the control flow is uniform)
-  uint32_t committed[kStages] = {}, waited[kStages] = {};
-  auto wait_stage = [&](int st) -> bool {
-#pragma unroll
-    for (int q = 0; q < kStages; ++q)
-      if (q == st)
-        while (waited[q] < committed[q]) {
-          if (!wait_parity(&ctl.mbar[q], waited[q] & 1u)) return false;
-          ++waited[q];
-        }
-    return true;
-  };
-  auto load = [&](int step) {
-    const int seg = step / nks, ks = step - seg * nks;
-    const Seg sg = SG::get(seg);
-    stage_load(A + sg.pa * a_plane, a_plane * PA, a_ld, a_rows, B + sg.pb * b_plane, b_plane * PB, b_ld, b_rows,
-               ks * 16 * kKs, klen, smem + (step % kStages) * kStage);
-  };
-  for (int j = 0; j < kStages - 1; ++j) {
-    if (j < nsteps) load(j);
-    oz::cp_async_commit();
-  }
-  for (int i = 0; i < nsteps; ++i) {
-    const int st = i % kStages;
-    const int j = i + kStages - 1;  // step to prefetch, into the stage step i - 1 used
-    if (j < nsteps) {
-      if (__syncthreads_or(!wait_stage(j % kStages))) {
-        ok = false;
-        break;
-      }
-      load(j);
-    }
-    oz::cp_async_commit();
-    oz::cp_async_wait<kStages - 1>();
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    fence_before();
-    __syncthreads();
-    fence_after();
-    const bool opens = (i % kFoldSteps) == 0;
-    if (tid == 0) {
-      const uint32_t id = idesc(SG::get(i / nks).neg);
-      const int kchunk = i - (i / nks) * nks;
-#pragma unroll
-      for (int q = 0; q < kKs; ++q) {
-        if (kchunk * kKs + q >= ksteps) break;  // k-steps beyond K hold only zeros
-        if (opens && q == 0)
-          issue_kstep<true>(ctl.tmem, smem + st * kStage + q * kKsElems, id);
-        else
-          issue_kstep<false>(ctl.tmem, smem + st * kStage + q * kKsElems, id);
-      }
-      commit(&ctl.mbar[st]);
-    }
-#pragma unroll
-    for (int q = 0; q < kStages; ++q)
-      if (q == st) ++committed[q];
-    const bool closes = ((i + 1) % kFoldSteps) == 0 || i + 1 == nsteps;
-    if (closes) {
-      // every MMA issued so far completes with this step's commit
-      if (__syncthreads_or(!wait_stage(st))) {
-        ok = false;
-        break;
-      }
-      fence_after();
-      fold(ctl.tmem, o);
-      fence_before();
-      __syncthreads();
-      fence_after();
-    }
-  }
-  if (!ok) {
-    // let the MMAs in flight finish (bounded) before the tensor memory is freed
-    oz::cp_async_wait<0>();
-#pragma unroll
-    for (int q = 0; q < kStages; ++q) wait_stage(q);
-  }
-  return ok;
-}
-
-// tensor memory and barriers of a CTA (warp 0 allocates)
-__device__ __forceinline__ void setup(Ctl& ctl) {
-  const int warp = threadIdx.x >> 5;
+// Persistent driver, called by every thread of the CTA: the CTA runs the
+// tiles first, first + step, ... below ntiles.  tile_ptrs(tile, A, B) gives
+// the tile's first k-step blocks (digit 0; nks k-steps of kABytes / kBBytes
+// each follow contiguously); store(tile, acc) is called by the epilogue
+// threads with the tile's integer accumulators, after the tensor memory has
+// been handed back to the MMA thread, so that the stores of one tile overlap
+// the MMAs of the next.  The producer runs ahead across tile boundaries.
+// Returns false on a timeout (the CTA's remaining outputs are then missing).
+template <class TilePtrs, class Store>
+__device__ bool run_tiles(int first, int step, int ntiles, int nks, unsigned char* smem, Ctl& ctl,
+                          TilePtrs tile_ptrs, Store store) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  volatile int* abort = &ctl.abort;
   if (threadIdx.x == 0) {
-    for (int q = 0; q < kStages; ++q)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&ctl.mbar[q])));
+    for (int q = 0; q < kStages; ++q) {
+      mbar_init(&ctl.full[q], 1);
+      mbar_init(&ctl.empty[q], 1);
+    }
+    mbar_init(&ctl.acc_full, 1);
+    mbar_init(&ctl.acc_empty, 32 * kEpiWarps);
+    mbar_init(&ctl.mma_done, 1);
+    ctl.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&ctl.tmem)),
                  "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
@@ -314,17 +253,104 @@ __device__ __forceinline__ void setup(Ctl& ctl) {
   fence_before();
   __syncthreads();
   fence_after();
-}
-
-__device__ __forceinline__ void teardown(Ctl& ctl) {
+  const uint32_t tmem = ctl.tmem;
+  const int nfold = (nks + kFoldKs - 1) / kFoldKs;  // fold intervals per tile
+  bool ok = true;
+  long long issued = 0;  // copies issued (producer thread)
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      long long it = 0;  // k-steps over all tiles of the CTA
+      for (int tile = first; tile < ntiles && ok; tile += step) {
+        const unsigned char *A, *B;
+        tile_ptrs(tile, A, B);
+        for (int ks = 0; ks < nks; ++ks, ++it) {
+          const int st = int(it % kStages);
+          if (it >= kStages && !wait_parity(&ctl.empty[st], uint32_t((it / kStages - 1) & 1), abort, false)) {
+            ok = false;
+            break;
+          }
+          unsigned char* dst = smem + size_t(st) * kStageBytes;
+          mbar_expect_tx(&ctl.full[st], uint32_t(kStageBytes));
+          bulk_load(dst, A + size_t(ks) * kABytes, uint32_t(kABytes), &ctl.full[st]);
+          bulk_load(dst + kABytes, B + size_t(ks) * kBBytes, uint32_t(kBBytes), &ctl.full[st]);
+          issued = it + 1;
+        }
+      }
+    }
+  } else if (warp == kMmaWarp) {
+    if (lane == 0) {
+      long long it = 0, fc = 0;  // k-steps and fold intervals over all tiles
+      for (int tile = first; tile < ntiles && ok; tile += step) {
+        for (int ks = 0; ks < nks; ++ks, ++it) {
+          const int st = int(it % kStages);
+          if (!wait_parity(&ctl.full[st], uint32_t((it / kStages) & 1), abort, false)) {
+            ok = false;
+            break;
+          }
+          const bool opens = (ks % kFoldKs) == 0;
+          // a new interval overwrites the accumulators: the epilogue must have
+          // read the previous one
+          if (opens && fc > 0 && !wait_parity(&ctl.acc_empty, uint32_t((fc - 1) & 1), abort, false)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const unsigned char* sb = smem + size_t(st) * kStageBytes;
+          if (opens)
+            issue_kstep<true>(tmem, sb);
+          else
+            issue_kstep<false>(tmem, sb);
+          commit(&ctl.empty[st]);
+          if ((ks + 1) % kFoldKs == 0 || ks + 1 == nks) {
+            commit(&ctl.acc_full);
+            ++fc;
+          }
+        }
+      }
+      // every MMA issued by this thread has completed once mma_done flips
+      commit(&ctl.mma_done);
+      wait_parity(&ctl.mma_done, 0u, nullptr, false);
+    }
+  } else {
+    long long fc = 0;
+    for (int tile = first; tile < ntiles && ok; tile += step) {
+      Acc o;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) o.h[c] = o.l[c] = 0;
+      for (int f = 0; f < nfold; ++f, ++fc) {
+        if (!wait_parity(&ctl.acc_full, uint32_t(fc & 1), abort, true)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        fold(tmem, o);
+        fence_before();
+        mbar_arrive(&ctl.acc_empty);
+      }
+      if (ok) store(tile, o);
+    }
+  }
+  if (!ok) ctl.abort = 1;
   fence_before();
   __syncthreads();
-  if ((threadIdx.x >> 5) == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(ctl.tmem), "r"(kTmemCols));
+  const bool all_ok = ctl.abort == 0;
+  if (!all_ok && warp == kProducerWarp && lane == 0) {
+    // the copies in flight land before the shared memory is released: the
+    // last phase of each stage's barrier is that of its last copy
+    for (long long it = (issued > kStages ? issued - kStages : 0); it < issued; ++it)
+      wait_parity(&ctl.full[it % kStages], uint32_t((it / kStages) & 1), nullptr, false);
+  }
+  if (warp == kMmaWarp) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
+  }
+  return all_ok;
 }
 
 // value of column c (0..15 of the thread's quarter) before the exponent scale
 __device__ __forceinline__ double value(const Acc& o, int c) { return fma(double(o.h[c]), 0x1p28, double(o.l[c])); }
+
+#endif  // __CUDACC__
 
 }  // namespace oztc
 }  // namespace tvap

@@ -176,7 +176,7 @@ struct tvap_ctx {
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
   int kernel_launches = 0;  // launches issued by the last top-level call
-  int gemm_mode = 1;        // 0: FP64 pipe, 1: FP64 emulated on the bf16 tensor cores
+  int gemm_mode = 2;        // 0: FP64 pipe, 1/2: FP64 emulated on the bf16 tensor cores (mma.sync / tcgen05)
   // optional section timing with CUDA events on the context's stream
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;

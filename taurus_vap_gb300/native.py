@@ -163,12 +163,13 @@ class Context:
         _check(lib().tvap_get_counters(self.h, _p(out), 4), "tvap_get_counters")
         return tuple(int(v) for v in out)
 
-    GEMM_FP64, GEMM_EMULATED = 0, 1
+    GEMM_FP64, GEMM_MMA_SYNC, GEMM_TCGEN05 = 0, 1, 2
+    GEMM_EMULATED = GEMM_TCGEN05
 
     def set_gemm_mode(self, mode: int):
-        """0: dense products on the FP64 pipe; 1 (default): FP64 emulated on
-        the bf16 tensor cores with mma.sync; 2: the same with tcgen05 MMAs and
-        tensor-memory accumulators."""
+        """0: dense products on the FP64 pipe; 1: FP64 emulated on the bf16
+        tensor cores with mma.sync; 2 (default): the same with tcgen05 MMAs and
+        tensor-memory accumulators for the batched products."""
         _check(lib().tvap_set_gemm_mode(self.h, int(mode)), "tvap_set_gemm_mode")
 
     def set_stream(self, stream_handle: int):

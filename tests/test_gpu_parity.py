@@ -110,7 +110,7 @@ def test_calculate_fields_dense_blocks(case, ncol, request):
             assert relerr(got[q][c], gathered[q][c]) < FIELD_TOL, (c, q)
 
 
-def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0, gemm_mode=1):
+def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0, gemm_mode=2):
     om = O.OracleModel(mdl)
     ref = om.project(U, V, Mp, Mn, 2 * np.pi, Z, N, nthreads=nthreads)
     assert ref["status"] == 0
