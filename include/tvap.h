@@ -109,7 +109,9 @@ int tvap_get_timing(tvap_ctx* ctx, double* ms, long long* calls, int nsec);
 /* Diagnostic counters since the last tvap_set_timing, for the canonical
  * basis: [0] FP32 Jacobi + FP64 refinement attempts, [1] of them accepted by
  * the final check, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in
- * total.  No reference counterpart. */
+ * total, [4..6] attempts rejected because clusters stayed coupled / the
+ * basis was not orthonormal / a cluster of near-degenerate levels was too
+ * large.  No reference counterpart. */
 int tvap_get_counters(tvap_ctx* ctx, long long* out, int nout);
 
 /* One upload of the reduced two-body list and the one-body part:

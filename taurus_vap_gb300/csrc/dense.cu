@@ -1054,4 +1054,281 @@ int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s) {
   return TVAP_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Cholesky factorisation of S (lower, L L^T = S; S has n x n + n doubles, the
+// last n receive 1 / L_jj) and the evolution solves
+// X L^T = A for two n x n matrices A (U1 = A1 L^{-T}, V1 = A2 L^{-T}) in one
+// cooperative launch.  GB300's FP64 pipe gives one SM about 2 FMAs per clock,
+// so the factorisation is spread over the grid: panels of kCoopNb columns; CTA
+// 0 factors each diagonal block, all CTAs solve the panel rows below it and
+// apply the trailing update (CTA 0 updating and factoring the next diagonal
+// block meanwhile); then one warp per row of A1 / A2 runs the forward
+// substitution L x = a with L in shared memory.  Grid-wide barriers between
+// the phases are bounded spins (all CTAs are co-resident by the cooperative
+// launch); a barrier that gives up raises the status word and every CTA
+// returns.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kCoopThreads = 256;
+constexpr int kCoopNb = 16;
+constexpr long long kCoopSpin = 1LL << 22;
+
+// bar[0] arrivals, bar[1] generation, bar[2] abort; zeroed before the launch
+__device__ bool coop_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, int* flags) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    if (atomicAdd(&bar[0], 1u) == nblocks - 1) {
+      atomicExch(&bar[0], 0u);
+      __threadfence();
+      atomicExch(&bar[1], gen + 1);
+    } else {
+      volatile unsigned* g = &bar[1];
+      long long it = 0;
+      while (*g == gen) {
+        if (++it > kCoopSpin || *(volatile unsigned*)&bar[2]) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (!ok || *(volatile unsigned*)&bar[2]) {
+      if (!*(volatile unsigned*)&bar[2]) atomicOr(flags, DEV_WAIT_TIMEOUT);
+      atomicExch(&bar[2], 1u);
+      ok = 0;
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  ++gen;
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// 1 / sqrt(d) for a positive normal d: an FP32 seed refined by two
+// Newton-Raphson steps for the reciprocal square root, y <- y (3 - d y^2) / 2
+// (each step doubles the correct bits: 2^-22 -> 2^-44 -> FP64 rounding).
+// About 8 instructions on the FP64 pipe, against several times that for an
+// FP64 square root followed by a division; outside the FP32 exponent range
+// the library routines are used.
+__device__ __forceinline__ double rsqrt_newton(double d) {
+  if (!(d > 1.0e-30 && d < 1.0e30)) return 1.0 / sqrt(d);
+  double y = double(rsqrtf(float(d)));
+  const double h = 0.5 * d;
+  y = y * fma(-h, y * y, 1.5);
+  y = y * fma(-h, y * y, 1.5);
+  return y;
+}
+
+// Unblocked Cholesky of the nb x nb diagonal block at (j0, j0) of S by one
+// warp: lane i holds row i of the block in registers, each pivot is one
+// lane's value broadcast by a shuffle, the column is scaled by the pivot's
+// reciprocal (as DPBTF2 does).  The reciprocals go to rd[j0 ..] for the
+// solves.  An FP64 warp instruction occupies the SM's FP64 pipe for about 16
+// cycles on this part, so the block stays in one warp (no CTA barriers, no
+// redundant arithmetic).  Elements written by other CTAs are read through L2.
+__device__ bool coop_factor_diag_warp(int n, double* S, double* rd, int j0, int nb) {
+  const int lane = threadIdx.x & 31;
+  double li[kCoopNb];
+#pragma unroll
+  for (int j = 0; j < kCoopNb; ++j)
+    li[j] = (lane < nb && j <= lane && j < nb) ? __ldcg(&S[(j0 + lane) + size_t(j0 + j) * n]) : 0.0;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < kCoopNb; ++k) {
+    if (k >= nb) break;
+    const double d = __shfl_sync(0xffffffffu, li[k], k);
+    if (!(d > 0.0)) {
+      ok = false;  // uniform: every lane holds the same pivot
+      break;
+    }
+    const double y = rsqrt_newton(d);
+    if (lane == k) li[k] = d * y;
+    if (lane > k) li[k] *= y;
+    if (lane == 0) rd[j0 + k] = y;
+#pragma unroll
+    for (int j = k + 1; j < kCoopNb; ++j) {
+      if (j >= nb) break;
+      const double ljk = __shfl_sync(0xffffffffu, li[k], j);
+      if (lane >= j) li[j] = fma(-li[k], ljk, li[j]);
+    }
+  }
+  if (!ok) return false;
+#pragma unroll
+  for (int j = 0; j < kCoopNb; ++j)
+    if (lane < nb && j <= lane && j < nb) S[(j0 + lane) + size_t(j0 + j) * n] = li[j];
+  return true;
+}
+
+__global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, double* S, const double* A,
+                                                                       long long a_stride, double* X,
+                                                                       long long x_stride, unsigned* bar,
+                                                                       int* flags) {
+  extern __shared__ double coop_smem[];  // the panel rows; then L (n x n) and 1 / L_jj in the solve phase
+  __shared__ double L11[kCoopNb][kCoopNb + 1];
+  __shared__ double rdiag[kCoopNb];
+  __shared__ unsigned gen_s;
+  const int t = threadIdx.x, G = gridDim.x, cta = blockIdx.x;
+  if (t == 0) gen_s = *(volatile unsigned*)&bar[1];
+  __syncthreads();
+  unsigned gen = gen_s;  // every thread keeps its own copy of the generation
+  double* rd = S + size_t(n) * n;  // 1 / L_jj
+  if (cta == 0 && t < 32 && !coop_factor_diag_warp(n, S, rd, 0, min(kCoopNb, n))) {
+    if (t == 0) {
+      atomicOr(flags, DEV_CHOLESKY);
+      atomicExch(&bar[2], 1u);
+    }
+  }
+  if (!coop_barrier(bar, G, gen, flags)) return;
+  for (int j0 = 0;;) {
+    const int j1 = min(j0 + kCoopNb, n);
+    if (j1 >= n) break;
+    const int nbp = j1 - j0, j2 = min(j1 + kCoopNb, n);
+    // panel rows below the diagonal block: L21 = S21 L11^{-T}, one warp per
+    // row (lane k holds x_k), rows spread over the CTAs so that their FP64
+    // work runs on different SMs
+    if (j1 + cta < n) {
+      for (int idx = t; idx < nbp * nbp; idx += blockDim.x) {
+        const int i = idx % nbp, j = idx / nbp;
+        if (i >= j) L11[i][j] = __ldcg(&S[(j0 + i) + size_t(j0 + j) * n]);
+      }
+      if (t < nbp) rdiag[t] = __ldcg(&rd[j0 + t]);
+      __syncthreads();
+      const int warp = t >> 5, lane = t & 31, warps = blockDim.x >> 5;
+      for (int i = j1 + cta + G * warp; i < n; i += G * warps) {
+        double xk = (lane < nbp) ? __ldcg(&S[i + size_t(j0 + lane) * n]) : 0.0;
+        for (int m = 0; m < nbp; ++m) {
+          if (lane == m) xk *= rdiag[m];
+          const double xm = __shfl_sync(0xffffffffu, xk, m);
+          if (lane > m && lane < nbp) xk = fma(-xm, L11[lane][m], xk);
+        }
+        if (lane < nbp) S[i + size_t(j0 + lane) * n] = xk;
+      }
+    }
+    if (!coop_barrier(bar, G, gen, flags)) return;
+    // trailing update S22 -= L21 L21^T (lower triangle).  CTA 0 takes the
+    // next diagonal block (rows and columns j1 .. j2-1) and factors it; the
+    // other CTAs take the rest, one column at a time.  The panel rows j1..n-1
+    // are staged in shared memory first (independent loads: one L2 round
+    // trip instead of one per k).
+    double* P = coop_smem;  // (n - j1) x nbp, row-major
+    const int prow = n - j1;
+    if (cta == 0 || cta - 1 < prow) {
+#pragma unroll 4
+      for (int idx = t; idx < prow * nbp; idx += blockDim.x) {
+        const int k = idx / prow, i = idx - k * prow;
+        P[i * kCoopNb + k] = __ldcg(&S[(j1 + i) + size_t(j0 + k) * n]);
+      }
+      __syncthreads();
+    }
+    if (cta == 0) {
+      const int nb2 = j2 - j1;
+      for (int idx = t; idx < nb2 * nb2; idx += blockDim.x) {
+        const int i = idx % nb2, j = idx / nb2;
+        if (i < j) continue;
+        double v = __ldcg(&S[(j1 + i) + size_t(j1 + j) * n]);
+        for (int k = 0; k < nbp; ++k) v = fma(-P[i * kCoopNb + k], P[j * kCoopNb + k], v);
+        S[(j1 + i) + size_t(j1 + j) * n] = v;
+      }
+      __syncthreads();
+      if (t < 32 && !coop_factor_diag_warp(n, S, rd, j1, nb2) && t == 0) {
+        atomicOr(flags, DEV_CHOLESKY);
+        atomicExch(&bar[2], 1u);
+      }
+    }
+    if (cta > 0 || G == 1) {
+      const int workers = G > 1 ? G - 1 : 1, w = G > 1 ? cta - 1 : 0;
+      for (int j = j1 + w; j < n; j += workers) {
+        const double* pj = P + (j - j1) * kCoopNb;
+        const int i0 = (j < j2) ? j2 : j;
+        for (int i = i0 + t; i < n; i += blockDim.x) {
+          const double* pi = P + (i - j1) * kCoopNb;
+          double v = __ldcg(&S[i + size_t(j) * n]);
+          for (int k = 0; k < nbp; ++k) v = fma(-pi[k], pj[k], v);
+          S[i + size_t(j) * n] = v;
+        }
+      }
+    }
+    if (!coop_barrier(bar, G, gen, flags)) return;
+    j0 = j1;
+  }
+  // forward substitution L x = a for every row of A1 and A2: one warp per
+  // row, rows spread over all CTAs
+  const int warps = blockDim.x >> 5, warp = t >> 5, lane = t & 31;
+  const int rows = 2 * n;
+  if (cta >= rows) return;
+  double* Ls = coop_smem;
+  double* dinv = Ls + size_t(n) * n;
+#pragma unroll 8
+  for (int idx = t; idx < n * n; idx += blockDim.x) Ls[idx] = __ldcg(&S[idx]);
+  __syncthreads();
+  for (int j = t; j < n; j += blockDim.x) dinv[j] = __ldcg(&rd[j]);
+  __syncthreads();
+  constexpr int kMaxPerLane = 12;  // n <= 384
+  for (int r = cta + G * warp; r < rows; r += G * warps) {
+    const int mat = r >= n ? 1 : 0, row = r - mat * n;
+    const double* a = A + mat * a_stride;
+    double* x = X + mat * x_stride;
+    double v[kMaxPerLane];
+#pragma unroll
+    for (int q = 0; q < kMaxPerLane; ++q) {
+      const int j = lane + 32 * q;
+      v[q] = (j < n) ? a[row + size_t(j) * n] : 0.0;
+    }
+    for (int j = 0; j < n; ++j) {
+      const int owner = j & 31, qj = j >> 5;
+      double vj = v[0];
+#pragma unroll
+      for (int q = 1; q < kMaxPerLane; ++q)
+        if (q == qj) vj = v[q];
+      const double xj = __shfl_sync(0xffffffffu, vj, owner) * dinv[j];
+      if (lane == owner) {
+#pragma unroll
+        for (int q = 0; q < kMaxPerLane; ++q)
+          if (q == qj) v[q] = xj;
+      }
+      const double* lc = Ls + size_t(j) * n;
+#pragma unroll
+      for (int q = 0; q < kMaxPerLane; ++q) {
+        const int jj = lane + 32 * q;
+        if (32 * q + 31 > j && 32 * q < n && jj > j && jj < n) v[q] = fma(-xj, lc[jj], v[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxPerLane; ++q) {
+      const int j = lane + 32 * q;
+      if (j < n) x[row + size_t(j) * n] = v[q];
+    }
+  }
+}
+
+}  // namespace
+
+int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, double* X, long long x_stride,
+                         unsigned* bar, int* flags, cudaStream_t s) {
+  const size_t shm = sizeof(double) * (size_t(n) * n + n);
+  if (n > 384 || shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
+  static int grid = 0;
+  static size_t attr_shm = 0;
+  if (shm > attr_shm) {
+    TVAP_CUDA(cudaFuncSetAttribute(cholesky_evolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    attr_shm = shm;
+    int per_sm = 0, sms = 0;
+    TVAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cholesky_evolve_kernel, kCoopThreads, shm));
+    TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+    grid = std::min(per_sm * sms, 128);
+  }
+  if (grid < 1) return TVAP_ERR_ARG;
+  TVAP_CUDA(cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned), s));
+  void* args[] = {&n, &S, &A, &a_stride, &X, &x_stride, &bar, &flags};
+  TVAP_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_evolve_kernel, dim3(grid), dim3(kCoopThreads), args,
+                                        shm, s));
+  return TVAP_OK;
+}
+
 }  // namespace tvap

@@ -81,8 +81,10 @@ struct EvolveBuf {
   double *Z = nullptr, *L = nullptr, *A1 = nullptr, *A2 = nullptr, *U0 = nullptr, *V0 = nullptr;
 };
 
-// U1 = (U0 + V0 Z) L^{-T}, V1 = (V0 + U0 Z) L^{-T}; L^{-1} left in b.L
-int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1) {
+// U1 = (U0 + V0 Z) L^{-T}, V1 = (V0 + U0 Z) L^{-T} with L L^T = 1 + Z^T Z.
+// With want_linv, L^{-1} is left in b.L (cholesky_inverse and two products);
+// otherwise one cooperative launch factorises and solves when n allows it.
+int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1, bool want_linv) {
   cudaStream_t s = c->stream;
   const size_t nn = size_t(n) * n;
   int rc;
@@ -90,9 +92,10 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1) {
   sec_begin(c, SEC_EVOLVE);
   if ((rc = rgemm(n, n, n, view_t(Zv), Zv, b.L, n, 1.0, 0.0, s))) return rc;
   add_identity_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, b.L);
-  if ((rc = cholesky_inverse(n, b.L, c->d_flags, s))) return rc;
   TVAP_CUDA(cudaMemcpyAsync(b.A1, b.U0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   TVAP_CUDA(cudaMemcpyAsync(b.A2, b.V0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+  const bool coop = !want_linv && c->d_bar;
+  if (!coop && (rc = cholesky_inverse(n, b.L, c->d_flags, s))) return rc;
   const View LinvT = view_t(view_cm(b.L, n, 0));
   // A1 = U0 + V0 Z, A2 = V0 + U0 Z as one batch of two when A2 follows A1
   // (then U1 = A1 L^-T, V1 = A2 L^-T likewise when V1 follows U1)
@@ -115,6 +118,17 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1) {
   } else {
     if ((rc = rgemm(n, n, n, view_cm(b.V0, n, 0), Zv, b.A1, n, 1.0, 1.0, s))) return rc;
     if ((rc = rgemm(n, n, n, view_cm(b.U0, n, 0), Zv, b.A2, n, 1.0, 1.0, s))) return rc;
+  }
+  if (coop) {
+    rc = cholesky_evolve_coop(n, b.L, b.A1, (long long)(b.A2 - b.A1), U1, (long long)(V1 - U1), c->d_bar,
+                              c->d_flags, s);
+    if (rc == TVAP_OK) {
+      sec_end(c, SEC_EVOLVE);
+      c->kernel_launches += 5;
+      return TVAP_OK;
+    }
+    if (rc != TVAP_ERR_ARG) return rc;
+    if ((rc = cholesky_inverse(n, b.L, c->d_flags, s))) return rc;
   }
   if (pair_u) {
     GemmArgs g{};
@@ -255,7 +269,7 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   int rc = upload_matrix(Z, b.Z, sizeof(double) * nn, s);
   if (!rc) rc = upload_matrix(U0, b.U0, sizeof(double) * nn, s);
   if (!rc) rc = upload_matrix(V0, b.V0, sizeof(double) * nn, s);
-  if (!rc) rc = evolve_device(c, b, n, dU1, dV1);
+  if (!rc) rc = evolve_device(c, b, n, dU1, dV1, false);
   if (!rc) rc = download_matrix(dU1, U1, sizeof(double) * nn, s);
   if (!rc) rc = download_matrix(dV1, V1, sizeof(double) * nn, s);
   if (!rc) rc = check_flags(c);
@@ -342,7 +356,7 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
   rc = upload_matrix(Z, b.Z, sizeof(double) * nn, s);
   if (!rc) rc = upload_matrix(U0, b.U0, sizeof(double) * nn, s);
   if (!rc) rc = upload_matrix(V0, b.V0, sizeof(double) * nn, s);
-  if (!rc) rc = evolve_device(c, b, n, ws_U(c), ws_V(c));
+  if (!rc) rc = evolve_device(c, b, n, ws_U(c), ws_V(c), true);
   if (!rc) rc = check_flags(c);
   tvap_pnp p{};
   if (!rc) rc = project_device(c, *opts, &p);

@@ -746,15 +746,21 @@ __global__ void refine_update_kernel(int n, const double* __restrict__ XtX, cons
   const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (e >= size_t(n) * n) return;
   const int i = int(e % n), j = int(e / n);
-  const double r = ((i == j) ? 1.0 : 0.0) - XtX[e];
+  const size_t et = j + size_t(i) * n;
+  // E = R/2 + F with R = I - X^T X and F antisymmetric (Ogita & Aishima's
+  // correction E_ij = (S_ij + l_j R_ij)/(l_j - l_i) split into its symmetric
+  // and antisymmetric parts).  Both parts are formed from the symmetrised S
+  // and R, so F_ji = -F_ij holds exactly and the orthonormality update R/2
+  // carries no rounding amplified by small gaps l_j - l_i.
+  const double rb = 0.5 * ((((i == j) ? 1.0 : 0.0) - XtX[e]) + (((i == j) ? 1.0 : 0.0) - XtX[et]));
+  const double sb = 0.5 * (S[e] + S[et]);
   const double dl = lam[j] - lam[i];
-  // Newton correction where the gap dominates the coupling; pairs that are
+  // the rotation only where the gap dominates the coupling; pairs that are
   // (nearly) degenerate relative to their coupling are only re-orthonormalised
   // and diagonalised exactly at the end
-  const double sij = fmax(fabs(S[e]), fabs(S[j + size_t(i) * n]));
-  const bool newton = (i != j) && fabs(dl) > 4.0 * sij + 1.0e-13 * rscal[1];
-  const double E = newton ? (S[e] + lam[j] * r) / dl : 0.5 * r;
-  M[e] = ((i == j) ? 1.0 : 0.0) + E;
+  const bool newton = (i != j) && fabs(dl) > 4.0 * fabs(sb) + 1.0e-13 * rscal[1];
+  const double F = newton ? (sb + 0.5 * (lam[i] + lam[j]) * rb) / dl : 0.0;
+  M[e] = ((i == j) ? 1.0 : 0.0) + 0.5 * rb + F;
 }
 
 // Sort by eigenvalue, diagonalise clusters of (near-)degenerate eigenvalues
@@ -886,6 +892,15 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
       }
     }
     __syncwarp();
+    if (c < ncl && m > CM) {
+      // too large to diagonalise here (the attempt fails): the refined
+      // columns go to D unrotated, so that D stays an orthonormal basis to
+      // start the next attempt from
+      for (int r = 0; r < m; ++r) {
+        if (lane == 0) evals[k0 + r] = S[perm[k0 + r] + size_t(perm[k0 + r]) * n];
+        for (int row = lane; row < n; row += 32) D[row + size_t(k0 + r) * n] = X[row + size_t(perm[k0 + r]) * n];
+      }
+    }
     if (c < ncl && m <= CM) {
       for (int r = 0; r < m; ++r) {
         const int src = osh[warp][r];
@@ -1436,6 +1451,8 @@ int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, c
   TVAP_CUDA(cudaStreamSynchronize(s));
   *fail = hr[0];
   c->canon_attempts[3] += hr[1];
+  for (int b = 0; b < 3; ++b)
+    if (hr[0] & (1 << b)) ++c->canon_attempts[4 + b];
   return TVAP_OK;
 }
 
@@ -1458,18 +1475,24 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
     double* X = w->Xr;
     double* Xn = w->Xn;
     const View Rho = view_cm(w->rho, n, 0);
-    if (w->have_basis) {
-      // warm start: rotate rho into the previous canonical basis (FP64 GEMMs)
-      const View Dp = view_cm(w->D, n, 0);
-      if ((rc = real_gemm(n, n, n, Rho, Dp, w->Br, n, 1.0, 0.0, s))) return rc;
-      if ((rc = real_gemm(n, n, n, view_t(Dp), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
-      if ((rc = jacobi32_smem(n, w->Sr, w->D, X, w->rflag + 1, s))) return rc;
-    } else {
-      if ((rc = jacobi32_smem(n, w->rho, nullptr, X, w->rflag + 1, s))) return rc;
+    // a second attempt starts from the basis the first one refined (left in
+    // w->D): the FP32 Jacobi then works on a nearly diagonal matrix whose
+    // small entries keep their relative precision, which resolves the pairs
+    // whose gaps were too small for the Newton steps
+    for (int attempt = 0; attempt < 2 && fail; ++attempt) {
+      if (w->have_basis || attempt > 0) {
+        // warm start: rotate rho into the previous canonical basis
+        const View Dp = view_cm(w->D, n, 0);
+        if ((rc = real_gemm(n, n, n, Rho, Dp, w->Br, n, 1.0, 0.0, s))) return rc;
+        if ((rc = real_gemm(n, n, n, view_t(Dp), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+        if ((rc = jacobi32_smem(n, w->Sr, w->D, X, w->rflag + 1, s))) return rc;
+      } else {
+        if ((rc = jacobi32_smem(n, w->rho, nullptr, X, w->rflag + 1, s))) return rc;
+      }
+      c->kernel_launches += 1;
+      ++c->canon_attempts[0];
+      if ((rc = refine_canonical(c, X, Xn, 3, &fail, s))) return rc;
     }
-    c->kernel_launches += 1;
-    ++c->canon_attempts[0];
-    if ((rc = refine_canonical(c, X, Xn, 3, &fail, s))) return rc;
     if (!fail) {
       ++c->canon_attempts[1];
       w->have_basis = true;
@@ -1806,8 +1829,8 @@ int check_flags(tvap_ctx* c) {
   if (f & DEV_CHOLESKY) return TVAP_ERR_CHOLESKY;
   if (f & DEV_TRTRI) return TVAP_ERR_TRTRI;
   if (f & DEV_IMAG_GRAD) return TVAP_ERR_IMAG_GRADIENT;
-  if (f & DEV_TC_TIMEOUT) {
-    set_last_error("a tensor-core kernel ran out of its bounded wait", __FILE__, __LINE__);
+  if (f & DEV_WAIT_TIMEOUT) {
+    set_last_error("a device kernel ran out of its bounded wait", __FILE__, __LINE__);
     return TVAP_ERR_DEVICE_TIMEOUT;
   }
   return TVAP_OK;

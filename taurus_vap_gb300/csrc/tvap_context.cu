@@ -153,7 +153,7 @@ int tvap_get_timing(tvap_ctx* c, double* ms, long long* calls, int nsec) {
 
 int tvap_get_counters(tvap_ctx* c, long long* out, int nout) {
   if (!c || !out) return TVAP_ERR_ARG;
-  for (int i = 0; i < nout && i < 4; ++i) out[i] = c->canon_attempts[i];
+  for (int i = 0; i < nout && i < 7; ++i) out[i] = c->canon_attempts[i];
   return TVAP_OK;
 }
 
@@ -205,6 +205,8 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
   if ((e = cudaMalloc(&c->d_sp_tr, sizeof(int) * n)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_l, sizeof(int) * n)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_flags, sizeof(int))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->d_bar, 4 * sizeof(unsigned))) != cudaSuccess) return fail(e);
+  cudaMemset(c->d_bar, 0, 4 * sizeof(unsigned));
   cudaMemcpy(c->d_sp_2mj, sp_2mj, sizeof(int) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_sp_tr, sp_tr, sizeof(int) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_sp_l, sp_l, sizeof(int) * n, cudaMemcpyHostToDevice);
@@ -230,6 +232,7 @@ void tvap_destroy(tvap_ctx* c) {
   cudaFree(c->d_trperm);
   cudaFree(c->d_H1);
   cudaFree(c->d_flags);
+  cudaFree(c->d_bar);
   for (auto& e : c->ev_open) {
     cudaEventDestroy(e.second.first);
     cudaEventDestroy(e.second.second);

@@ -68,7 +68,8 @@ enum DevFlag : int {
   DEV_CHOLESKY = 32,
   DEV_TRTRI = 64,
   DEV_IMAG_GRAD = 128,
-  DEV_TC_TIMEOUT = 256,
+  DEV_TC_TIMEOUT = 256,  // a bounded device wait gave up (tensor-core pipeline, grid barrier)
+  DEV_WAIT_TIMEOUT = 256,
 };
 
 // ---------------------------------------------------------------------------
@@ -175,6 +176,7 @@ struct tvap_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_canon = nullptr;
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
+  unsigned* d_bar = nullptr;  // grid-barrier state of the cooperative kernels (3 words)
   int kernel_launches = 0;  // launches issued by the last top-level call
   int gemm_mode = 2;        // 0: FP64 pipe, 1/2: FP64 emulated on the bf16 tensor cores (mma.sync / tcgen05)
   // optional section timing with CUDA events on the context's stream
@@ -189,7 +191,7 @@ struct tvap_ctx {
   size_t scratch_count = 0;
   // canonical bases: [0] FP32 Jacobi + refinement attempts, [1] of them
   // accepted, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in total
-  long long canon_attempts[4] = {0, 0, 0, 0};
+  long long canon_attempts[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace tvap {
@@ -240,5 +242,11 @@ size_t jacobi32_smem_limit();
 int jacobi32_smem(int n, const double* A64, const double* W0, double* W64, int* sweeps_out, cudaStream_t s);
 // Cholesky L L^T = A (lower), then L^{-1} in place
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
+// Cholesky L L^T = S (S overwritten by L, lower) and X_m = A_m L^{-T} for
+// m = 0, 1 (A_1 at A + a_stride, X_1 at X + x_stride) in one cooperative
+// launch; TVAP_ERR_ARG when n is outside its range (the caller then uses
+// cholesky_inverse and two products)
+int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, double* X, long long x_stride,
+                         unsigned* bar, int* flags, cudaStream_t s);
 
 }  // namespace tvap

@@ -158,9 +158,11 @@ class Context:
 
     def canonical_paths(self):
         """Canonical-basis counters since the last set_timing: (FP32 Jacobi +
-        refinement attempts, accepted, exact FP64 Jacobi runs, FP32 sweeps)."""
-        out = np.zeros(4, dtype=np.int64)
-        _check(lib().tvap_get_counters(self.h, _p(out), 4), "tvap_get_counters")
+        refinement attempts, accepted, exact FP64 Jacobi runs, FP32 sweeps,
+        rejections for coupled clusters, for lost orthonormality, for too
+        large clusters)."""
+        out = np.zeros(7, dtype=np.int64)
+        _check(lib().tvap_get_counters(self.h, _p(out), 7), "tvap_get_counters")
         return tuple(int(v) for v in out)
 
     GEMM_FP64, GEMM_MMA_SYNC, GEMM_TCGEN05 = 0, 1, 2
