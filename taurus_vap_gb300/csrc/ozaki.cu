@@ -339,6 +339,9 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
     B = reinterpret_cast<const unsigned char*>(Bs) + (size_t(bz) * b_tiles + nt) * nks * size_t(oztc::kBBytes);
   };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // The stores of a tile overlap the MMAs of the next one: exponents, values
+  // and (with beta) the old outputs are fetched with independent loads, all
+  // issued before the first store (C is not known not to alias them).
   auto store = [&](int tile, const oztc::Acc& acc) {
     const int nt = tile % b_tiles, rest = tile / b_tiles;
     const int mt = rest % a_tiles, z = rest / a_tiles;
@@ -353,21 +356,46 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
       comp_a = 1;
     }
     const int eai = ea[size_t(z) * a_rows_pad + q] - 57;
-    double* C = static_cast<double*>(o.C);
+    double* __restrict__ C = static_cast<double*>(o.C);
     const int cw = o.c_real ? 1 : 2;  // doubles per element
-#pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      const int col = nt * oztc::kN + 16 * (warp >> 2) + c;
-      if (col >= o.b_rows) continue;
+    const int col0 = nt * oztc::kN + 16 * (warp >> 2);
+    const int* __restrict__ ebz = eb + size_t(bz) * b_rows_pad;
+    // element index of column c, or -1 (padding, or the imaginary part of a
+    // real output)
+    auto idx_of = [&](int c) -> long long {
+      const int col = col0 + c;
       int j = col, comp = comp_a;
       if (j >= o.b_split) {
         j -= o.b_split;
         comp += 1;
       }
-      if (comp > 0 && o.c_real) continue;
-      const double v = oztc::value(acc, c) * (o.alpha * oz::pow2(eai + eb[size_t(bz) * b_rows_pad + col]));
-      const long long idx = (i * o.crs + j * o.ccs + b * o.cbs) * cw + comp;
-      C[idx] = (o.beta == 0.0) ? v : fma(o.beta, C[idx], v);
+      if (col >= o.b_rows || (comp > 0 && o.c_real)) return -1;
+      return (i * o.crs + j * o.ccs + b * o.cbs) * cw + comp;
+    };
+    double v[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int e = (col0 + c < o.b_rows) ? ebz[col0 + c] : 0;
+      v[c] = oztc::value(acc, c) * (o.alpha * oz::pow2(eai + e));
+    }
+    // two groups of 8: the loads of a group are in flight together
+#pragma unroll
+    for (int c0 = 0; c0 < 16; c0 += 8) {
+      if (o.beta != 0.0) {
+        double old[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const long long k = idx_of(c0 + c);
+          old[c] = k >= 0 ? C[k] : 0.0;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) v[c0 + c] = fma(o.beta, old[c], v[c0 + c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const long long k = idx_of(c0 + c);
+        if (k >= 0) C[k] = v[c0 + c];
+      }
     }
   };
   if (!oztc::run_tiles(blockIdx.x, gridDim.x, ntiles, nks, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)

@@ -76,6 +76,9 @@ struct Workspace {
   double2 *OW = nullptr, *OX = nullptr, *OY = nullptr;
   int* rflag = nullptr;
   int* piv = nullptr;  // [G][n] row interchanges of the Thouless LU
+  // [G][panel][L11^-1, U11^-1] (kPanelMax^2 each) of the Thouless LU
+  double2* Tinv = nullptr;
+  double2* tpart = nullptr;  // [kTraceChunks][G][9] partial traces
   bool have_basis = false;
   size_t bytes = 0;
 };
@@ -90,6 +93,11 @@ int dalloc(T** p, size_t count, size_t& total) {
   return TVAP_OK;
 }
 
+constexpr int kPanelMax = 32;  // columns per panel of the Thouless LU
+
+// double2 entries per angle of Workspace::Tinv
+size_t tinv_stride(int n) { return size_t((n + kPanelMax - 1) / kPanelMax) * 2 * kPanelMax * kPanelMax; }
+
 void ws_free(Workspace* w) {
   void* ptrs[] = {w->VU,  w->rho,    w->kap,   w->jac,    w->D,     w->evals,  w->jwork, w->rhoc,
                   w->kapc, w->tmp,  w->blocks, w->canon_i, w->canon_d, w->Uphi, w->Vphi,   w->W,     w->A,
@@ -97,7 +105,7 @@ void ws_free(Workspace* w) {
                   w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
                   w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
                   w->H20v,  w->XB,    w->RS,     w->Br,    w->Mr,     w->lam,   w->rscal,
-                  w->rflag, w->OW,    w->OX,     w->OY,     w->piv};
+                  w->rflag, w->OW,    w->OX,     w->OY,     w->piv, w->Tinv, w->tpart};
   for (void* p : ptrs) cudaFree(p);
   *w = Workspace();
 }
@@ -127,6 +135,7 @@ int ws_ensure(tvap_ctx* c, int G) {
   A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
   A_(XB, 4 * nn) A_(RS, 2 * nn) A_(Br, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
   A_(OW, nG) A_(OX, nG) A_(OY, nG) A_(piv, size_t(n) * G)
+  A_(Tinv, size_t(G) * tinv_stride(n)) A_(tpart, size_t(G) * 9 * 256)
 #undef A_
   w->V = w->VU;
   w->U = w->VU + nn;
@@ -356,57 +365,80 @@ __global__ void overlap_prep_kernel(int n, int G, const int* __restrict__ canon_
 // per-angle traces: particle numbers (calculate_particle_number io=0,
 // module_particlenumber.f90:78-143) and energy (calculate_expectval_energy,
 // module_hamiltonian.f90:1098-1126), from angle-innermost arrays.
-__global__ void traces_kernel(int n, int G, const double2* __restrict__ rho, const double2* __restrict__ kLR,
-                              const double2* __restrict__ kRL, const double2* __restrict__ gam,
-                              const double2* __restrict__ dLR, const double2* __restrict__ H1, double2 H0,
-                              double2* __restrict__ obs) {
-  const int b = blockIdx.x;
+// Traces of the densities and fields per angle (particle numbers, their
+// squares, energy).  Threads run over the angles -- the contiguous index of
+// the angle-innermost arrays, so every load is coalesced -- and a CTA over a
+// chunk of the n^2 elements; the partial sums of the chunks are reduced in a
+// fixed order by traces_finish_kernel.  Partial layout:
+// part[((chunk * G + b) * 9 + q)], q = prot, neut, tr rho_p^2, tr kRL kLR (p),
+// tr rho_n^2, tr kRL kLR (n), tr H1 rho, tr gamma rho, tr Delta kRL.
+constexpr int kTraceChunks = 256;
+static_assert(kTraceChunks == 256, "Workspace::tpart is allocated for 256 chunks");
+constexpr int kTraceThreads = 128;
+__global__ void __launch_bounds__(kTraceThreads)
+    traces_partial_kernel(int n, int G, const double2* __restrict__ rho, const double2* __restrict__ kLR,
+                          const double2* __restrict__ kRL, const double2* __restrict__ gam,
+                          const double2* __restrict__ dLR, const double2* __restrict__ H1,
+                          double2* __restrict__ part) {
   const int h = n / 2;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  // accumulators: prot, neut, tr1, tr2, tr3, tr4, e1, e2, e3
-  double2 a[9];
-  for (int q = 0; q < 9; ++q) a[q] = make_double2(0.0, 0.0);
-  auto at = [G, n, b](const double2* X, int i, int j) { return X[(size_t(i) + size_t(j) * n) * G + b]; };
-  for (int e = tid; e < n * n; e += nt) {
-    const int j = e / n, i = e - j * n;
-    const double2 rij = at(rho, i, j), rji = at(rho, j, i);
-    if (i == j) {
-      if (i < h)
-        a[0] = cadd(a[0], rij);
-      else
-        a[1] = cadd(a[1], rij);
+  const long long nn = (long long)n * n;
+  const int chunk = blockIdx.x;
+  const int e0 = int(nn * chunk / kTraceChunks), e1 = int(nn * (chunk + 1) / kTraceChunks);
+  for (int b = threadIdx.x; b < G; b += blockDim.x) {
+    double2 a[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) a[q] = make_double2(0.0, 0.0);
+    auto at = [G, n, b](const double2* X, int i, int j) { return X[(size_t(i) + size_t(j) * n) * G + b]; };
+    for (int e = e0; e < e1; ++e) {
+      const int j = e / n, i = e - j * n;
+      const double2 rij = at(rho, i, j), rji = at(rho, j, i);
+      if (i == j) {
+        if (i < h)
+          a[0] = cadd(a[0], rij);
+        else
+          a[1] = cadd(a[1], rij);
+      }
+      const bool pblk = (i < h && j < h), nblk = (i >= h && j >= h);
+      if (pblk) {
+        cfma(a[2], rij, rji);
+        cfma(a[3], at(kRL, i, j), at(kLR, i, j));
+      } else if (nblk) {
+        cfma(a[4], rij, rji);
+        cfma(a[5], at(kRL, i, j), at(kLR, i, j));
+      }
+      cfma(a[6], H1[i + size_t(j) * n], rji);
+      cfma(a[7], at(gam, i, j), rji);
+      cfma(a[8], at(dLR, i, j), at(kRL, i, j));
     }
-    const bool pblk = (i < h && j < h), nblk = (i >= h && j >= h);
-    if (pblk) {
-      cfma(a[2], rij, rji);
-      cfma(a[3], at(kRL, i, j), at(kLR, i, j));
-    } else if (nblk) {
-      cfma(a[4], rij, rji);
-      cfma(a[5], at(kRL, i, j), at(kLR, i, j));
-    }
-    cfma(a[6], H1[i + size_t(j) * n], rji);
-    cfma(a[7], at(gam, i, j), rji);
-    cfma(a[8], at(dLR, i, j), at(kRL, i, j));
+#pragma unroll
+    for (int q = 0; q < 9; ++q) part[(size_t(chunk) * G + b) * 9 + q] = a[q];
   }
-  __shared__ double2 red[9][256];
-  for (int q = 0; q < 9; ++q) red[q][tid] = a[q];
+}
+
+// one CTA per angle, warp q sums partial q over the chunks (lanes over
+// chunks, then a shuffle tree: a fixed order)
+__global__ void __launch_bounds__(9 * 32) traces_finish_kernel(int G, const double2* __restrict__ part, double2 H0,
+                                                               double2* __restrict__ obs) {
+  __shared__ double2 r[9];
+  const int b = blockIdx.x, q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double2 s = make_double2(0.0, 0.0);
+  for (int c = lane; c < kTraceChunks; c += 32) s = cadd(s, part[(size_t(c) * G + b) * 9 + q]);
+  for (int off = 16; off > 0; off >>= 1) {
+    s.x += __shfl_down_sync(0xffffffffu, s.x, off);
+    s.y += __shfl_down_sync(0xffffffffu, s.y, off);
+  }
+  if (lane == 0) r[q] = s;
   __syncthreads();
-  for (int s = nt / 2; s > 0; s >>= 1) {
-    if (tid < s)
-      for (int q = 0; q < 9; ++q) red[q][tid] = cadd(red[q][tid], red[q][tid + s]);
-    __syncthreads();
-  }
-  if (tid == 0) {
-    const double2 prot = red[0][0], neut = red[1][0];
-    const double2 prot2 = cadd(csub(cadd(prot, cmul(prot, prot)), red[2][0]), red[3][0]);
-    const double2 neut2 = cadd(csub(cadd(neut, cmul(neut, neut)), red[4][0]), red[5][0]);
-    const double2 ener = cadd(cadd(H0, red[6][0]), cscale(cadd(red[7][0], red[8][0]), 0.5));
-    obs[8 * b + 1] = ener;
-    obs[8 * b + 2] = prot;
-    obs[8 * b + 3] = neut;
-    obs[8 * b + 4] = prot2;
-    obs[8 * b + 5] = neut2;
-  }
+  if (threadIdx.x != 0) return;
+  const double2 prot = r[0], neut = r[1];
+  const double2 prot2 = cadd(csub(cadd(prot, cmul(prot, prot)), r[2]), r[3]);
+  const double2 neut2 = cadd(csub(cadd(neut, cmul(neut, neut)), r[4]), r[5]);
+  const double2 ener = cadd(cadd(H0, r[6]), cscale(cadd(r[7], r[8]), 0.5));
+  obs[8 * b + 1] = ener;
+  obs[8 * b + 2] = prot;
+  obs[8 * b + 3] = neut;
+  obs[8 * b + 4] = prot2;
+  obs[8 * b + 5] = neut2;
 }
 
 // overlap per angle and the sum_gauge coefficients
@@ -475,36 +507,57 @@ __global__ void sum_scalars_kernel(int G, const double2* __restrict__ obs, const
   if (lane == 0)
     for (int q = 0; q < 6; ++q) pscal[q] = accumulate ? cadd(pscal[q], s[q]) : s[q];
 }
-__global__ void sum_matrices_kernel(int n, int G, const double2* __restrict__ A, const double2* __restrict__ T,
-                                    const double2* __restrict__ coefA, const double2* __restrict__ coefAE,
-                                    const double* __restrict__ mult, double2* __restrict__ pA, double2* __restrict__ pH,
-                                    double2* __restrict__ pAH, int accumulate) {
-  const size_t nn = size_t(n) * n;
-  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
-  if (e >= nn) return;
-  double2 sa = accumulate ? pA[e] : make_double2(0.0, 0.0);
-  double2 sh = accumulate ? pH[e] : make_double2(0.0, 0.0);
-  double2 sah = accumulate ? pAH[e] : make_double2(0.0, 0.0);
+// sum_gauge of the matrices: pA = sum_b c_b A_b, pH = sum_b c_b 2 T_b,
+// pAH = sum_b c_b E_b A_b.  A warp covers 32 consecutive elements (coalesced
+// loads), the warps of a CTA split the angles and are reduced in shared
+// memory; a folded angle (multiplicity 2) contributes 2 Re(c_b X_b) only, so
+// it costs two FMAs per sum (FP64 throughput is the bound on this part).
+constexpr int kSumWarps = 8;
+__global__ void __launch_bounds__(32 * kSumWarps)
+    sum_matrices_kernel(int n, int G, const double2* __restrict__ A, const double2* __restrict__ T,
+                        const double2* __restrict__ coefA, const double2* __restrict__ coefAE,
+                        const double* __restrict__ mult, double2* __restrict__ pA, double2* __restrict__ pH,
+                        double2* __restrict__ pAH, int accumulate) {
   // H20_b = T_b - T_b^T enters as 2 T_b: the sum is antisymmetrised once, in
   // projected_h20_kernel (1/2 (X - X^T)), which gives sum c_b (T_b - T_b^T)
-#pragma unroll 4
-  for (int b = 0; b < G; ++b) {
-    const double2 a = A[size_t(b) * nn + e];
-    const double2 h = cscale(T[size_t(b) * nn + e], 2.0);
-    const double2 t1 = cmul(a, coefA[b]), t2 = cmul(h, coefA[b]), t3 = cmul(a, coefAE[b]);
-    if (mult[b] == 2.0) {
-      sa.x += 2.0 * t1.x;
-      sh.x += 2.0 * t2.x;
-      sah.x += 2.0 * t3.x;
-    } else {
-      sa = cadd(sa, t1);
-      sh = cadd(sh, t2);
-      sah = cadd(sah, t3);
+  extern __shared__ double2 sc[];  // per angle: c_b m_b, 2 c_b m_b, c_b E_b m_b (m_b folded into the scale)
+  __shared__ double2 red[3][kSumWarps][32];
+  const size_t nn = size_t(n) * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = threadIdx.x; b < G; b += blockDim.x) {
+    const double f = mult[b] == 2.0 ? 2.0 : 1.0;
+    sc[3 * b] = cscale(coefA[b], f);
+    sc[3 * b + 1] = cscale(coefA[b], 2.0 * f);
+    sc[3 * b + 2] = cscale(coefAE[b], f);
+  }
+  __syncthreads();
+  const size_t e = blockIdx.x * size_t(32) + lane;
+  double2 sa = make_double2(0.0, 0.0), sh = sa, sah = sa;
+  if (e < nn) {
+    for (int b = warp; b < G; b += kSumWarps) {
+      const double2 a = A[size_t(b) * nn + e], tv = T[size_t(b) * nn + e];
+      const double2 c1 = sc[3 * b], c2 = sc[3 * b + 1], c3 = sc[3 * b + 2];
+      if (mult[b] == 2.0) {
+        sa.x = fma(a.x, c1.x, fma(-a.y, c1.y, sa.x));
+        sh.x = fma(tv.x, c2.x, fma(-tv.y, c2.y, sh.x));
+        sah.x = fma(a.x, c3.x, fma(-a.y, c3.y, sah.x));
+      } else {
+        sa = cadd(sa, cmul(a, c1));
+        sh = cadd(sh, cmul(tv, c2));
+        sah = cadd(sah, cmul(a, c3));
+      }
     }
   }
-  pA[e] = sa;
-  pH[e] = sh;
-  pAH[e] = sah;
+  red[0][warp][lane] = sa;
+  red[1][warp][lane] = sh;
+  red[2][warp][lane] = sah;
+  __syncthreads();
+  if (warp < 3 && e < nn) {
+    double2 s = accumulate ? (warp == 0 ? pA[e] : (warp == 1 ? pH[e] : pAH[e])) : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int w = 0; w < kSumWarps; ++w) s = cadd(s, red[warp][w][lane]);
+    (warp == 0 ? pA : (warp == 1 ? pH : pAH))[e] = s;
+  }
 }
 
 // calculate_projected_H20 (module_projection.f90:729-759)
@@ -935,6 +988,20 @@ __global__ void copy_kernel(size_t m, const double* __restrict__ a, double* __re
 // ---------------------------------------------------------------------------
 constexpr int kPanelThreads = 512;
 
+// argmax over a warp on integer keys: for non-negative doubles the bit
+// pattern orders like the value, and an integer compare avoids the FP64 pipe
+// (a dependent FP64 operation takes about 64 cycles on this part)
+__device__ __forceinline__ void warp_argmax_key(long long& v, int& i) {
+  for (int off = 16; off > 0; off >>= 1) {
+    const long long v2 = __shfl_down_sync(0xffffffffu, v, off);
+    const int i2 = __shfl_down_sync(0xffffffffu, i, off);
+    if (v2 > v || (v2 == v && i2 < i)) {
+      v = v2;
+      i = i2;
+    }
+  }
+}
+
 __device__ __forceinline__ void warp_argmax(double& v, int& i) {
   for (int off = 16; off > 0; off >>= 1) {
     const double v2 = __shfl_down_sync(0xffffffffu, v, off);
@@ -1085,16 +1152,22 @@ __global__ void __launch_bounds__(kPanelThreads)
 // angle): partial pivoting by max |re| + |im| (first row on ties, as izamax),
 // multipliers and the updated panel written back, pivots (absolute rows) to
 // piv[b * n + j].  The interchanges of the other columns and the block row
-// U12 are left to panel_apply_kernel.
-constexpr int kPanelMax = 32;
+// U12 are left to panel_apply_kernel (or panel_swap_kernel and a product with
+// L11^{-1}).  With Tinv non-null the inverses of the unit lower L11 and of
+// U11 are written to Tinv + b * tstride (nbp x nbp each, column-major, the
+// second at + kPanelMax^2), computed right-looking in shared memory: every
+// step updates all remaining entries at once, so the dependent FP64 chain is
+// one complex update per step.
 constexpr int kFactorThreads = 256;
 constexpr int kApplyThreads = 32;  // one warp: L11 + the column buffers stay under 48 KB
 
 __global__ void __launch_bounds__(kFactorThreads)
-    panel_factor_kernel(int n, int j0, int nbp, double2* __restrict__ Wall, int* __restrict__ piv, int* flags) {
-  extern __shared__ double2 P[];  // rows j0..n-1 of the panel, column-major, ld m
+    panel_factor_kernel(int n, int j0, int nbp, double2* __restrict__ Wall, int* __restrict__ piv, int* flags,
+                        double2* __restrict__ Tinv, long long tstride) {
+  extern __shared__ double2 P[];  // rows j0..n-1 of the panel, column-major, ld m; then L11^-1, U11^-1
   __shared__ int s_piv;
   __shared__ double s_pv;
+  __shared__ double2 s_rp;
   const int b = blockIdx.x;
   double2* W = Wall + size_t(b) * 2 * n * n;
   const int m = n - j0;
@@ -1107,19 +1180,22 @@ __global__ void __launch_bounds__(kFactorThreads)
   bool singular = false;
   for (int jj = 0; jj < nbp; ++jj) {
     if (warp == 0) {
-      double best = -1.0;
+      long long best = -1;
       int bi = m;
       for (int r = jj + lane; r < m; r += 32) {
-        const double v = cabs1(P[jj * m + r]);
+        const long long v = __double_as_longlong(cabs1(P[jj * m + r]));
         if (v > best) {
           best = v;
           bi = r;
         }
       }
-      warp_argmax(best, bi);
+      warp_argmax_key(best, bi);
       if (lane == 0) {
         s_piv = bi;
-        s_pv = best;
+        s_pv = __longlong_as_double(best);
+        // the pivot's reciprocal, once (an FP64 division costs ~1000 cycles)
+        const double2 pe = P[jj * m + bi];
+        s_rp = (s_pv == 0.0) ? make_double2(0.0, 0.0) : crcp(pe);
       }
     }
     __syncthreads();
@@ -1137,7 +1213,7 @@ __global__ void __launch_bounds__(kFactorThreads)
         P[c * m + p] = t;
       }
     __syncthreads();
-    const double2 rp = (pv == 0.0) ? make_double2(0.0, 0.0) : crcp(P[jj * m + jj]);
+    const double2 rp = s_rp;
     for (int r = jj + 1 + tid; r < m; r += blockDim.x) {
       const double2 mu = cmul(P[jj * m + r], rp);
       P[jj * m + r] = mu;
@@ -1158,6 +1234,74 @@ __global__ void __launch_bounds__(kFactorThreads)
     W[(j0 + r) + size_t(j0 + c) * n] = P[c * m + r];
   }
   if (singular && tid == 0) atomicOr(flags, DEV_SINGULAR_UPHI);
+  if (!Tinv) return;
+  // X = L11^{-1}: X = I; step k: X[i][j] -= L[i][k] X[k][j] for i > k >= j
+  double2* X = P + size_t(m) * nbp;
+  double2* Y = X + nbp * nbp;
+  __shared__ double2 rdu[kPanelMax];
+  for (int idx = tid; idx < nbp * nbp; idx += blockDim.x) {
+    const int i = idx % nbp, j = idx / nbp;
+    X[idx] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    Y[idx] = X[idx];
+  }
+  if (tid < nbp) rdu[tid] = singular ? make_double2(0.0, 0.0) : crcp(P[tid * m + tid]);
+  __syncthreads();
+  for (int k = 0; k + 1 < nbp; ++k) {
+    const int rows = nbp - 1 - k;
+    for (int idx = tid; idx < rows * (k + 1); idx += blockDim.x) {
+      const int i = k + 1 + idx % rows, j = idx / rows;
+      const double2 l = P[k * m + i], x = X[k + j * nbp];
+      double2 v = X[i + j * nbp];
+      v.x = fma(-l.x, x.x, v.x);
+      v.x = fma(l.y, x.y, v.x);
+      v.y = fma(-l.x, x.y, v.y);
+      v.y = fma(-l.y, x.x, v.y);
+      X[i + j * nbp] = v;
+    }
+    __syncthreads();
+  }
+  // Y = U11^{-1}: Y = I; step k (last to first): row k scaled by 1/U_kk, then
+  // Y[i][j] -= U[i][k] Y[k][j] for i < k <= j
+  for (int k = nbp - 1; k >= 0; --k) {
+    for (int j = k + tid; j < nbp; j += blockDim.x) Y[k + j * nbp] = cmul(Y[k + j * nbp], rdu[k]);
+    __syncthreads();
+    const int cols = nbp - k;
+    for (int idx = tid; idx < k * cols; idx += blockDim.x) {
+      const int i = idx % k, j = k + idx / k;
+      const double2 u = P[k * m + i], y = Y[k + j * nbp];
+      double2 v = Y[i + j * nbp];
+      v.x = fma(-u.x, y.x, v.x);
+      v.x = fma(u.y, y.y, v.x);
+      v.y = fma(-u.x, y.y, v.y);
+      v.y = fma(-u.y, y.x, v.y);
+      Y[i + j * nbp] = v;
+    }
+    __syncthreads();
+  }
+  double2* T = Tinv + size_t(b) * tstride;
+  for (int idx = tid; idx < nbp * nbp; idx += blockDim.x) {
+    T[idx] = X[idx];
+    T[kPanelMax * kPanelMax + idx] = Y[idx];
+  }
+}
+
+// Row interchanges of a factored panel applied to columns j1 .. 2n-1 (one
+// thread per column, in the order of the pivots)
+__global__ void __launch_bounds__(kApplyThreads)
+    panel_swap_kernel(int n, int j0, int nbp, double2* __restrict__ Wall, const int* __restrict__ piv) {
+  const int b = blockIdx.y;
+  const int j1 = j0 + nbp;
+  const int c = j1 + blockIdx.x * kApplyThreads + threadIdx.x;
+  if (c >= 2 * n) return;
+  double2* col = Wall + size_t(b) * 2 * n * n + size_t(c) * n;
+  const int* pv = piv + size_t(b) * n + j0;
+  for (int jj = 0; jj < nbp; ++jj) {
+    const int p = pv[jj];
+    if (p == j0 + jj) continue;
+    const double2 tmp = col[j0 + jj];
+    col[j0 + jj] = col[p];
+    col[p] = tmp;
+  }
 }
 
 // Columns j1 .. 2n-1 (one thread each): the panel's row interchanges, then
@@ -1321,9 +1465,17 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
   // (n x nb complex) must fit, else the former wider kernels run from global
   const int npanels = (n + kPanelMax - 1) / kPanelMax;
   const int nb_smem = (n + npanels - 1) / npanels;
-  const size_t panel_bytes = sizeof(double2) * size_t(n) * nb_smem;
+  // with the emulated products, the triangular solves of the block rows and
+  // of the back substitution run as products with the inverted diagonal
+  // blocks (computed by the panel kernel) on the tensor cores; on the FP64
+  // pipe they stay one-thread-per-column substitutions
+  const bool inv_path = g_gemm_mode >= 1;
+  const size_t panel_bytes =
+      sizeof(double2) * (size_t(n) * nb_smem + (inv_path ? 2 * size_t(nb_smem) * nb_smem : 0));
   const bool smem_path = panel_bytes <= size_t(jacobi32_smem_limit());
+  const bool use_inv = inv_path && smem_path;
   const int nb = smem_path ? nb_smem : ((n <= 64) ? n : 28);
+  const long long tstride = (long long)tinv_stride(n);
   int rc;
   if (smem_path && panel_bytes > 48 * 1024) {
     static bool attr = false;
@@ -1338,14 +1490,43 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     build_augmented_kernel<<<grid, kPanelThreads, 0, s>>>(n, w->Uphi, w->Vphi, w->W);
   }
   int launches = 1;
-  for (int j0 = 0; j0 < n; j0 += nb) {
+  // product with an inverted diagonal block, in place on a block row:
+  // rows r0 .. r0+nbp-1 of columns c0 .. 2n-1 <- T (nbp x nbp) times them
+  // (the operands are split into digit planes before the product is formed,
+  // so the output may overwrite its input)
+  auto block_row_product = [&](int blk, int which, int r0, int nbp, int c0) -> int {
+    GemmArgs g{};
+    g.M = nbp;
+    g.N = 2 * n - c0;
+    g.K = nbp;
+    g.batch = G;
+    g.A = View{w->Tinv + (size_t(blk) * 2 + which) * kPanelMax * kPanelMax, 1, nbp, tstride};
+    g.B = View{w->W + r0 + size_t(c0) * n, 1, n, bsW};
+    g.C = w->W + r0 + size_t(c0) * n;
+    g.crs = 1;
+    g.ccs = n;
+    g.cbs = bsW;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    ++launches;
+    return gemm_ozaki(g, s);
+  };
+  int blk = 0;
+  for (int j0 = 0; j0 < n; j0 += nb, ++blk) {
     const int nbp = std::min(nb, n - j0);
     const int j1 = j0 + nbp;
     if (smem_path) {
-      panel_factor_kernel<<<G, kFactorThreads, sizeof(double2) * size_t(n - j0) * nbp, s>>>(n, j0, nbp, w->W, w->piv,
-                                                                                             c->d_flags);
+      const size_t fac_bytes = sizeof(double2) * (size_t(n - j0) * nbp + (use_inv ? 2 * size_t(nbp) * nbp : 0));
+      panel_factor_kernel<<<G, kFactorThreads, fac_bytes, s>>>(
+          n, j0, nbp, w->W, w->piv, c->d_flags,
+          use_inv ? w->Tinv + size_t(blk) * 2 * kPanelMax * kPanelMax : nullptr, tstride);
       dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, G);
-      panel_apply_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
+      if (use_inv) {
+        panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
+        if ((rc = block_row_product(blk, 0, j0, nbp, j1))) return rc;
+      } else {
+        panel_apply_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
+      }
       launches += 2;
     } else {
       panel_kernel<<<G, kPanelThreads, 0, s>>>(n, j0, nbp, w->W, c->d_flags);
@@ -1394,13 +1575,17 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
       if ((rc = gemm(g, s))) return rc;
       ++launches;
     }
-    if (smem_path) {
+    if (use_inv) {
+      // X_i = U_ii^{-1} Y_i
+      if ((rc = block_row_product(bi, 1, i0, nbp, n))) return rc;
+    } else if (smem_path) {
       dim3 gb((n + kApplyThreads - 1) / kApplyThreads, G);
       backsolve_apply_kernel<<<gb, kApplyThreads, 0, s>>>(n, i0, nbp, w->W);
+      ++launches;
     } else {
       block_backsolve_kernel<<<G, kPanelThreads, 0, s>>>(n, i0, nbp, w->W);
+      ++launches;
     }
-    ++launches;
   }
   const size_t tot = size_t(n) * n * G;
   thouless_out_kernel<<<nblk(tot, 256), 256, 0, s>>>(n, G, w->W, w->A);
@@ -1714,7 +1899,9 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
   sec_end_on(c, SEC_DENSITIES, s);
   if ((rc = fields_batched(c, G, G, w->rhoL, w->kLR, w->kRL, w->gam, w->hsp, w->dLR, w->dRL, s))) return rc;
   sec_begin_on(c, SEC_TRACES, s);
-  traces_kernel<<<G, 256, 0, s>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR, c->d_H1, c->H0, w->obs);
+  traces_partial_kernel<<<kTraceChunks, kTraceThreads, 0, s>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR,
+                                                               c->d_H1, w->tpart);
+  traces_finish_kernel<<<G, 9 * 32, 0, s>>>(G, w->tpart, c->H0, w->obs);
   TVAP_CUDA(cudaGetLastError());
   sec_end_on(c, SEC_TRACES, s);
   sec_begin_on(c, SEC_H20, s);
@@ -1758,7 +1945,7 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
     if ((rc = gemm(g, s))) return rc;
   }
   sec_end_on(c, SEC_H20, s);
-  c->kernel_launches += 1 + 2 + 2 + 3 + 1 + 5;
+  c->kernel_launches += 1 + 2 + 2 + 3 + 2 + 5;
   return TVAP_OK;
 }
 
@@ -1774,8 +1961,8 @@ int angles_sums(tvap_ctx* c, int G, const double2* d_weight, const double* d_mul
   overlap_finish_kernel<<<nblk(G, tb), tb, 0, s>>>(n, G, have_overlap ? 1 : 0, w->canon_i, w->canon_d, w->pf,
                                                     w->detR22, d_weight, d_mult, w->obs, w->coefA, w->coefAE);
   sum_scalars_kernel<<<1, 32, 0, s>>>(G, w->obs, d_mult, d_weight, w->pscal, accumulate);
-  sum_matrices_kernel<<<nblk(nn, tb), tb, 0, s>>>(n, G, w->A, w->T, w->coefA, w->coefAE, d_mult, w->pA, w->pH,
-                                                  w->pAH, accumulate);
+  sum_matrices_kernel<<<unsigned((nn + 31) / 32), 32 * kSumWarps, sizeof(double2) * 3 * size_t(G), s>>>(
+      n, G, w->A, w->T, w->coefA, w->coefAE, d_mult, w->pA, w->pH, w->pAH, accumulate);
   TVAP_CUDA(cudaGetLastError());
   sec_end_on(c, SEC_SUMS, s);
   c->kernel_launches += 3;
