@@ -156,9 +156,9 @@ def host_iteration(ctx, state, mode):
     return (U1, V1, Zi), (pnp.c("ener") / pnp.c("over")).real
 
 
-# DRAM bytes (read + write) of one H20-shaped ozaki_mma_kernel<2,2> launch at
-# n = 140, G = 113, from `ncu --set full` (profiles/ozaki_mma_h20_emax4.md)
-H20_TRAFFIC_PER_LAUNCH = 191.9e6
+# DRAM bytes (read + write) of one H20-shaped ozaki_tc_kernel launch at
+# n = 140, G = 113, from `ncu --set full` (profiles/ozaki_tc_h20_emax4.md)
+H20_TRAFFIC_PER_LAUNCH = 325.4e6
 
 
 def fp64_flops_per_iteration(n, G):
@@ -281,11 +281,12 @@ def run_ours(args):
     e2e = {"value": world * 1000.0 / e_ms, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     # ---- roofline of the dominant kernel, from the live section timings.
-    # The dominant kernel (launch list in profiles/) is the emulated complex
-    # GEMM ozaki_mma_kernel<2,2>; its largest use is H20: 5 products of
-    # n x n x n complex per angle (3M: 3 real products per digit pair, 36 digit
-    # pairs, bf16 m16n8k16 on the tensor cores).  The H20 section also holds
-    # the 10 operand-splitting launches (about 15 % of it in the launch list).
+    # The dominant kernel (launch list in profiles/) is the tcgen05 product
+    # ozaki_tc_kernel; its largest use is H20: 5 complex products of n x n x n
+    # per angle, each formed as the real product [[Ar,-Ai],[Ai,Ar]] [Br;Bi]
+    # (2n x n x 2n) of digit planes, 36 digit pairs, bf16 MMAs with FP32
+    # accumulation in tensor memory.  The h20_tc section times exactly those
+    # 5 launches per step with CUDA events on the main stream.
     G_total = MPHI * MPHI
     G = (G_total + 1) // 2  # folded angle pairs computed
     S = mdl.ham.S
@@ -304,12 +305,12 @@ def run_ours(args):
                 fp64_peak = float(line.split(":")[1])
     except OSError:
         pass
-    h20_launch_ms = sections["h20"][0] / sec_steps / 5.0
-    h20_flops = 2.0 * n ** 3 * 36 * 3 * G  # bf16 tensor flops per launch (unpadded)
-    h20_tflops = h20_flops / (h20_launch_ms / 1000.0) / 1e12
+    tc_launch_ms = sections["h20_tc"][0] / sec_steps / 5.0
+    h20_flops = 2.0 * (2 * n) * n * (2 * n) * 36 * G  # bf16 tensor flops per launch (unpadded)
+    h20_tflops = h20_flops / (tc_launch_ms / 1000.0) / 1e12
     roofline = {
-        "kernel": "ozaki_mma_kernel<2,2>: H20 complex GEMM n x n x n x G, FP64 emulated on bf16 mma (per launch, "
-                  "incl. operand splitting)",
+        "kernel": "ozaki_tc_kernel (tcgen05): H20 complex GEMM n x n x n x G as the real product 2n x n x 2n of "
+                  "bf16 digit planes, 36 digit pairs, per launch",
         "bound": "tensor",
         "achieved": h20_tflops,
         "peak": bf16_peak,
@@ -317,9 +318,10 @@ def run_ours(args):
         "frac": h20_tflops / bf16_peak,
         "traffic": H20_TRAFFIC_PER_LAUNCH,
         "algorithmic_flops_per_launch": h20_flops,
-        "ms_per_launch": h20_launch_ms,
+        "ms_per_launch": tc_launch_ms,
         "peak_source": f"{peak_src} bf16_tflops (burst, of measured)",
-        "fp64_equivalent_tflops": 2.0 * 3 * n ** 3 * G / (h20_launch_ms / 1000.0) / 1e12,
+        "fp64_equivalent_tflops": 8.0 * n ** 3 * G / (tc_launch_ms / 1000.0) / 1e12,
+        "h20_section_ms_per_product": sections["h20"][0] / sec_steps / 5.0,
     }
     fld_ms = (sections["fields_gamma"][0] + sections["fields_delta"][0]) / sec_steps
     fld_bytes = 13 * S + 16 * n * n * 7 * G
@@ -357,7 +359,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "n": n, "elements": S, "angle_pairs": G_total, "angle_pairs_computed": G,
                    "form": "batched (all angles per launch, conjugate folding)",
                    "parallelism": f"replicas x{world}", "l2": "working set > L2 (per-angle arrays ~0.7 GB)",
-                   "dense_products": "FP64 emulated on the bf16 tensor cores (exact integer splitting)",
+                   "dense_products": "FP64 emulated on the bf16 tensor cores (exact integer splitting; tcgen05)",
                    "eta": ETA, "mu": MU},
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "roofline_fp64": roofline_fp64,
         "roofline_fields": roofline_fields,

@@ -255,6 +255,8 @@ int pick_tile(int M, int N) {
 
 int g_gemm_mode = 2;
 int* g_dev_flags = nullptr;
+tvap_ctx* g_tc_timing_ctx = nullptr;
+int g_tc_timing_sec = -1;
 
 int gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return TVAP_OK;

@@ -580,8 +580,10 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
   const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / oztc::kN) * a_slots;
   const int grid = int(std::min<long long>(ntiles, sms));
+  if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   ozaki_tc_kernel<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
                                                                   b_slots == 1 ? 1 : 0, a_slots, nks, o, g_dev_flags);
+  if (g_tc_timing_ctx) sec_end_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }

@@ -1907,6 +1907,7 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
   sec_begin_on(c, SEC_H20, s);
   // H20: T = U~^T (h V~ + fd/2 DeltaLR U~) - fd/2 V~^T DeltaRL V~, H20 = T - T^T
   {
+    TcTimingScope tc_timing(c, SEC_H20_TC);
     const View hv{w->hsp, (long long)G, (long long)n * G, 1};
     const View dl{w->dLR, (long long)G, (long long)n * G, 1};
     const View dr{w->dRL, (long long)G, (long long)n * G, 1};

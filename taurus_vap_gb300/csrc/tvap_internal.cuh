@@ -109,6 +109,20 @@ int oz_scratch(cudaStream_t s, size_t bytes, size_t ex_count, __nv_bfloat16** bu
 // context), and the status word of that context
 extern int g_gemm_mode;
 extern int* g_dev_flags;
+// when set, the tensor-memory product launches are timed into this section
+// of this context (the H20 products; the host issues them one after the other)
+extern tvap_ctx* g_tc_timing_ctx;
+extern int g_tc_timing_sec;
+struct TcTimingScope {
+  TcTimingScope(tvap_ctx* c, int sec) {
+    g_tc_timing_ctx = c;
+    g_tc_timing_sec = sec;
+  }
+  ~TcTimingScope() {
+    g_tc_timing_ctx = nullptr;
+    g_tc_timing_sec = -1;
+  }
+};
 
 // ---------------------------------------------------------------------------
 // Hamiltonian in gather form (built once from the reference's element list)
@@ -197,7 +211,7 @@ struct tvap_ctx {
 namespace tvap {
 enum Section : int {
   SEC_CANONICAL = 0, SEC_BLOCKS, SEC_SOLVE, SEC_UV, SEC_DENSITIES, SEC_FIELDS_GAMMA, SEC_FIELDS_DELTA, SEC_TRACES,
-  SEC_H20, SEC_OVERLAP, SEC_PFAFFIAN, SEC_SUMS, SEC_GRADIENT, SEC_EVOLVE, SEC_COUNT
+  SEC_H20, SEC_OVERLAP, SEC_PFAFFIAN, SEC_SUMS, SEC_GRADIENT, SEC_EVOLVE, SEC_H20_TC, SEC_COUNT
 };
 // brackets a section with events when timing is on (no-ops otherwise)
 void sec_begin(tvap_ctx* c, int sec);

@@ -145,7 +145,7 @@ class Context:
         return lib().tvap_kernel_launches(self.h)
 
     SECTIONS = ("canonical", "blocks", "solve", "uv", "densities", "fields_gamma", "fields_delta", "traces",
-                "h20", "overlap", "pfaffian", "sums", "gradient", "evolve")
+                "h20", "overlap", "pfaffian", "sums", "gradient", "evolve", "h20_tc")
 
     def set_timing(self, on: bool):
         _check(lib().tvap_set_timing(self.h, 1 if on else 0), "tvap_set_timing")
