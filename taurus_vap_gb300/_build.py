@@ -30,6 +30,7 @@ GPU_SOURCES = [
     "projection.cu",
     "gradient.cu",
     "ozaki.cu",
+    "jacobi_cluster.cu",
     "field_blocks.cu",
 ]
 

@@ -1,0 +1,252 @@
+// Block one-sided (Hestenes) Jacobi in FP32 on a thread-block cluster: the
+// first stage of the canonical basis (eigenvectors of rho = V V^T).
+//
+// With the previous canonical basis D (or the identity), M = V^T D satisfies
+// M^T M = D^T rho D; rotating column pairs of M until they are orthogonal and
+// applying the same rotations to D gives the eigenvectors of rho (the column
+// norms^2 are the eigenvalues).  One-sided Jacobi works on V, not on its
+// square rho, so small eigenvalues keep their relative precision.
+//
+// The 16 column blocks (width bw = ceil(n / 16), padded with zero columns)
+// live two per CTA in a cluster of 8.  A sweep is 15 rounds of the circle
+// method over the blocks (block 0 fixed, the others move one position per
+// round): in each round a CTA rotates all pairs between its two blocks (bw
+// sub-rounds of bw disjoint pairs, one warp per pair), and in the first round
+// also the pairs inside each block.  Between rounds the blocks move to their
+// next CTA through distributed shared memory (double buffered: compute,
+// cluster barrier, pull, cluster barrier).  The sweep's largest |cos| of a
+// pair, reduced over the cluster, decides convergence.
+//
+// The hardware cluster barrier is the only wait: all CTAs of a cluster are
+// co-scheduled, and every CTA takes the same number of rounds and sweeps
+// (the convergence flag is read from the same cluster-wide value).
+#include <cooperative_groups.h>
+
+#include "tvap_internal.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace tvap {
+
+namespace {
+
+constexpr int kJcCtas = 8;
+constexpr int kJcBlocks = 2 * kJcCtas;
+constexpr int kJcThreads = 512;  // 16 warps: one per pair of a sub-round
+constexpr int kJcMaxBw = 16;     // n <= 256
+constexpr int kJcMaxSweeps = 30;
+constexpr float kJcTol = 2.0e-6f;  // |cos| of every pair: the FP64 refinement takes it from there
+
+// block at position p of round r (circle method, block 0 fixed)
+__device__ __forceinline__ int jc_block(int r, int p) {
+  return p == 0 ? 0 : 1 + ((p - 1 - r) % 15 + 15) % 15;
+}
+
+// one-sided rotation of columns a and b (M and W), one warp; returns |cos|
+__device__ __forceinline__ float jc_rotate(float* Ma, float* Mb, float* Wa, float* Wb, int n, int lane) {
+  float aa = 0.f, bb = 0.f, ab = 0.f;
+  for (int r = lane; r < n; r += 32) {
+    const float x = Ma[r], y = Mb[r];
+    aa = fmaf(x, x, aa);
+    bb = fmaf(y, y, bb);
+    ab = fmaf(x, y, ab);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    aa += __shfl_xor_sync(0xffffffffu, aa, off);
+    bb += __shfl_xor_sync(0xffffffffu, bb, off);
+    ab += __shfl_xor_sync(0xffffffffu, ab, off);
+  }
+  if (!(aa > 0.f && bb > 0.f) || ab == 0.f) return 0.f;
+  const float cosab = fabsf(ab) * rsqrtf(aa) * rsqrtf(bb);
+  if (cosab < 1.0e-8f) return cosab;
+  const float zeta = (bb - aa) / (2.f * ab);
+  const float t = fabsf(zeta) > 1.0e18f ? 0.5f / zeta
+                                        : copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
+  const float c = rsqrtf(fmaf(t, t, 1.f)), s = c * t;
+  for (int r = lane; r < n; r += 32) {
+    const float x = Ma[r], y = Mb[r];
+    Ma[r] = c * x - s * y;
+    Mb[r] = s * x + c * y;
+    const float u = Wa[r], v = Wb[r];
+    Wa[r] = c * u - s * v;
+    Wb[r] = s * u + c * v;
+  }
+  return cosab;
+}
+
+// M64: rho = M64 M64^T columns source: column j of M = M64[j * n ..] (mt = 0)
+// or row j of M64 (mt = 1, M = M64^T); W0: the basis the rotations apply to
+// (identity when null); W64 receives the rotated basis.
+__global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const double* __restrict__ M64, int mt,
+                                                                    const double* __restrict__ W0,
+                                                                    double* __restrict__ W64, int* sweeps_out) {
+  extern __shared__ float jc[];  // [buf 2][slot 2][mat 2][bw][n]
+  __shared__ float wmax[kJcThreads / 32];
+  __shared__ float cl_max[kJcCtas];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int c = int(cluster.block_rank());
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int bw = (n + kJcBlocks - 1) / kJcBlocks;
+  const size_t colsz = size_t(n);
+  auto col = [&](int buf, int slot, int mat, int k) -> float* {
+    return jc + ((size_t(buf * 2 + slot) * 2 + mat) * bw + k) * colsz;
+  };
+  // initial blocks: slot 0 = position c, slot 1 = position 15 - c of round 0
+  for (int slot = 0; slot < 2; ++slot) {
+    const int blk = jc_block(0, slot == 0 ? c : kJcBlocks - 1 - c);
+    for (int idx = tid; idx < bw * n; idx += blockDim.x) {
+      const int k = idx / n, r = idx - k * n;
+      const int j = blk * bw + k;  // global column
+      float m = 0.f, w = 0.f;
+      if (j < n) {
+        m = float(mt ? M64[j + size_t(r) * n] : M64[r + size_t(j) * n]);
+        w = W0 ? float(W0[r + size_t(j) * n]) : (r == j ? 1.f : 0.f);
+      }
+      col(0, slot, 0, k)[r] = m;
+      col(0, slot, 1, k)[r] = w;
+    }
+  }
+  __syncthreads();
+  int cur = 0, sweep = 0;
+  for (; sweep < kJcMaxSweeps; ++sweep) {
+    float mx = 0.f;
+    for (int round = 0; round < kJcBlocks - 1; ++round) {
+      if (round == 0) {
+        // pairs inside each block: round robin over bwe = bw rounded up to
+        // even (the odd one out sits out), both slots at once
+        const int bwe = (bw + 1) & ~1;
+        for (int sr = 0; sr < bwe - 1; ++sr) {
+          const int half = bwe / 2;
+          if (warp < 2 * half) {
+            const int slot = warp / half, k = warp - slot * half;
+            int p, q;
+            if (k == 0) {
+              p = sr;
+              q = bwe - 1;
+            } else {
+              p = (sr + k) % (bwe - 1);
+              q = (sr - k + (bwe - 1)) % (bwe - 1);
+            }
+            if (p < bw && q < bw)
+              mx = fmaxf(mx, jc_rotate(col(cur, slot, 0, p), col(cur, slot, 0, q), col(cur, slot, 1, p),
+                                       col(cur, slot, 1, q), n, lane));
+          }
+          __syncthreads();
+        }
+      }
+      // pairs between the two blocks: sub-round sr pairs column k of slot 0
+      // with column (k + sr) % bw of slot 1
+      for (int sr = 0; sr < bw; ++sr) {
+        if (warp < bw) {
+          const int k = warp, k2 = (warp + sr) % bw;
+          mx = fmaxf(mx, jc_rotate(col(cur, 0, 0, k), col(cur, 1, 0, k2), col(cur, 0, 1, k), col(cur, 1, 1, k2), n,
+                                   lane));
+        }
+        __syncthreads();
+      }
+      // move the blocks to their positions of the next round (after the last
+      // round of a sweep too: the sweep restarts from round 0's layout
+      // shifted, which the circle method allows -- positions are reassigned
+      // below from the pull map, not from the round number)
+      cluster.sync();
+      const int nxt = cur ^ 1;
+      // new position p pulls from old position p - 1 (1 -> 15); position 0 stays
+      for (int slot = 0; slot < 2; ++slot) {
+        int src_cta, src_slot;
+        if (slot == 0) {
+          if (c == 0) {
+            src_cta = 0;
+            src_slot = 0;
+          } else if (c == 1) {
+            src_cta = 0;
+            src_slot = 1;
+          } else {
+            src_cta = c - 1;
+            src_slot = 0;
+          }
+        } else {
+          if (c == kJcCtas - 1) {
+            src_cta = c;
+            src_slot = 0;
+          } else {
+            src_cta = c + 1;
+            src_slot = 1;
+          }
+        }
+        const float* src = cluster.map_shared_rank(col(cur, src_slot, 0, 0), src_cta);
+        float* dst = col(nxt, slot, 0, 0);
+        // M and W of a slot are contiguous: 2 bw n floats
+        const int cnt = 2 * bw * n;
+        for (int idx = tid; idx < cnt; idx += blockDim.x) dst[idx] = src[idx];
+      }
+      cluster.sync();
+      cur = nxt;
+    }
+    // cluster-wide largest |cos| of the sweep
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    if (lane == 0) wmax[warp] = mx;
+    __syncthreads();
+    if (tid == 0) {
+      float m = 0.f;
+      for (int w = 0; w < kJcThreads / 32; ++w) m = fmaxf(m, wmax[w]);
+      float* dst = cluster.map_shared_rank(cl_max, 0);
+      dst[c] = m;
+    }
+    cluster.sync();
+    float gm = 0.f;
+    {
+      const float* src = cluster.map_shared_rank(cl_max, 0);
+      for (int k = 0; k < kJcCtas; ++k) gm = fmaxf(gm, src[k]);
+    }
+    cluster.sync();  // cl_max of CTA 0 is rewritten by the next sweep
+    if (gm <= kJcTol) {
+      ++sweep;
+      break;
+    }
+  }
+  // after 15 rounds per sweep the blocks sit at round 15 == round 0 of the
+  // circle (the rotation period is 15): slot s of CTA c holds block
+  // jc_block(0, position)
+  for (int slot = 0; slot < 2; ++slot) {
+    const int blk = jc_block(0, slot == 0 ? c : kJcBlocks - 1 - c);
+    for (int idx = tid; idx < bw * n; idx += blockDim.x) {
+      const int k = idx / n, r = idx - k * n;
+      const int j = blk * bw + k;
+      if (j < n) W64[r + size_t(j) * n] = double(col(cur, slot, 1, k)[r]);
+    }
+  }
+  if (c == 0 && tid == 0 && sweeps_out) *sweeps_out = sweep;
+}
+
+}  // namespace
+
+int jacobi_cluster(int n, const double* M, int m_transposed, const double* W0, double* W, int* sweeps_out,
+                   cudaStream_t s) {
+  const int bw = (n + kJcBlocks - 1) / kJcBlocks;
+  if (bw > kJcMaxBw) return TVAP_ERR_ARG;
+  const size_t shm = sizeof(float) * 8 * size_t(bw) * n;
+  if (shm > size_t(200) * 1024) return TVAP_ERR_ARG;
+  static size_t granted = 48 * 1024;
+  if (shm > granted) {
+    TVAP_CUDA(cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    granted = shm;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kJcCtas);
+  cfg.blockDim = dim3(kJcThreads);
+  cfg.dynamicSmemBytes = shm;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kJcCtas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  TVAP_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_kernel, n, M, m_transposed, W0, W, sweeps_out));
+  return TVAP_OK;
+}
+
+}  // namespace tvap

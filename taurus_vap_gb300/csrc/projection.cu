@@ -1664,15 +1664,30 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
     // w->D): the FP32 Jacobi then works on a nearly diagonal matrix whose
     // small entries keep their relative precision, which resolves the pairs
     // whose gaps were too small for the Newton steps
+    const View Vn = view_cm(w->V, n, 0);
     for (int attempt = 0; attempt < 2 && fail; ++attempt) {
-      if (w->have_basis || attempt > 0) {
-        // warm start: rotate rho into the previous canonical basis
+      const bool warm = w->have_basis || attempt > 0;
+      // one-sided Jacobi on M = V^T D (M^T M = D^T rho D) over a cluster of
+      // 8 CTAs; the two-sided single-CTA kernel on D^T rho D when n is too
+      // large for it
+      if (warm) {
         const View Dp = view_cm(w->D, n, 0);
-        if ((rc = real_gemm(n, n, n, Rho, Dp, w->Br, n, 1.0, 0.0, s))) return rc;
-        if ((rc = real_gemm(n, n, n, view_t(Dp), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
-        if ((rc = jacobi32_smem(n, w->Sr, w->D, X, w->rflag + 1, s))) return rc;
+        if ((rc = real_gemm(n, n, n, view_t(Vn), Dp, w->Br, n, 1.0, 0.0, s))) return rc;
+        rc = jacobi_cluster(n, w->Br, 0, w->D, X, w->rflag + 1, s);
       } else {
-        if ((rc = jacobi32_smem(n, w->rho, nullptr, X, w->rflag + 1, s))) return rc;
+        rc = jacobi_cluster(n, w->V, 1, nullptr, X, w->rflag + 1, s);
+      }
+      if (rc == TVAP_ERR_ARG) {
+        if (warm) {
+          const View Dp = view_cm(w->D, n, 0);
+          if ((rc = real_gemm(n, n, n, Rho, Dp, w->Br, n, 1.0, 0.0, s))) return rc;
+          if ((rc = real_gemm(n, n, n, view_t(Dp), view_cm(w->Br, n, 0), w->Sr, n, 1.0, 0.0, s))) return rc;
+          if ((rc = jacobi32_smem(n, w->Sr, w->D, X, w->rflag + 1, s))) return rc;
+        } else {
+          if ((rc = jacobi32_smem(n, w->rho, nullptr, X, w->rflag + 1, s))) return rc;
+        }
+      } else if (rc) {
+        return rc;
       }
       c->kernel_launches += 1;
       ++c->canon_attempts[0];

@@ -254,6 +254,12 @@ size_t jacobi32_smem_bytes(int n);
 size_t jacobi32_smem_limit();
 // FP32 Jacobi in shared memory (one CTA); the number of sweeps goes to *sweeps_out (may be null)
 int jacobi32_smem(int n, const double* A64, const double* W0, double* W64, int* sweeps_out, cudaStream_t s);
+// block one-sided FP32 Jacobi on a cluster of 8 CTAs: the columns of M (of
+// M^T when m_transposed) orthogonalised, the rotations applied to W0 (the
+// identity when null) and written to W (FP64): the eigenvectors of M^T M.
+// TVAP_ERR_ARG when n > 256 (the caller then uses jacobi32_smem).
+int jacobi_cluster(int n, const double* M, int m_transposed, const double* W0, double* W, int* sweeps_out,
+                   cudaStream_t s);
 // Cholesky L L^T = A (lower), then L^{-1} in place
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
 // Cholesky L L^T = S (S overwritten by L, lower) and X_m = A_m L^{-T} for
