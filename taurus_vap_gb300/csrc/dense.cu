@@ -419,16 +419,24 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_kernel(int N, double2* Aa
 // pivot search is a warp reduction plus one block step, and the already
 // eliminated columns (which no longer enter the Pfaffian) are neither
 // exchanged nor scaled.
+// The same elimination with the packed upper triangle in shared memory.  Per
+// step only the pivot's reciprocal is needed by every thread: one thread
+// forms it (an FP64 division costs ~1000 cycles and an FP64 warp instruction
+// ~16 cycles of the SM's FP64 pipe, so redundant scalar work in every thread
+// costs as much as the rank-2 update), the pivot search compares integer keys,
+// and the pivots are kept in shared memory and folded into log|Pf| and its
+// phase once, at the end, by a fixed-order warp reduction.
 __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const double2* __restrict__ Aall,
                                                                    double2* pf, int batch, int* flags) {
   extern __shared__ double2 pf_smem[];
   double2* pk = pf_smem;
   double2* xcol = pk + size_t(N) * (N + 1) / 2;  // 1-based, N + 1 entries
   double2* ycol = xcol + N + 1;
-  __shared__ double wv[kPfThreads / 32];
+  double2* pivs = ycol + N + 1;                  // N / 2 pivots, then N / 2 signs in .x of the next slots
+  __shared__ long long wv[kPfThreads / 32];
   __shared__ int wi[kPfThreads / 32];
   __shared__ int s_kp;
-  __shared__ double s_pv;
+  __shared__ double2 s_alpha;
   const int b = blockIdx.x;
   const double2* A = Aall + size_t(b) * N * N;
   auto a = [pk](int i, int j) -> double2& { return pk[(i - 1) + (size_t(j) * (j - 1)) / 2]; };  // 1 <= i <= j
@@ -436,21 +444,21 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
   for (int j = 1 + warp; j <= N; j += nw)
     for (int i = 1 + lane; i <= j; i += 32) a(i, j) = A[(i - 1) + size_t(j - 1) * N];
   __syncthreads();
-  double logmag = 0.0;
-  double2 phase = make_double2(1.0, 0.0);
   bool zero = false;
-  for (int K = N; K >= 2; K -= 2) {
-    double best = -1.0;
+  int steps = 0;
+  for (int K = N; K >= 2; K -= 2, ++steps) {
+    // |re| + |im| >= 0: its bit pattern orders like its value
+    long long best = -1;
     int bi = N + 1;
     for (int i = 1 + tid; i <= K - 1; i += nt) {
-      const double v = cabs1(a(i, K));
+      const long long v = __double_as_longlong(cabs1(a(i, K)));
       if (v > best) {
         best = v;
         bi = i;
       }
     }
     for (int off = 16; off > 0; off >>= 1) {
-      const double v2 = __shfl_down_sync(0xffffffffu, best, off);
+      const long long v2 = __shfl_down_sync(0xffffffffu, best, off);
       const int i2 = __shfl_down_sync(0xffffffffu, bi, off);
       if (v2 > best || (v2 == best && i2 < bi)) {
         best = v2;
@@ -463,26 +471,22 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
     }
     __syncthreads();
     if (warp == 0) {
-      double v = (lane < nw) ? wv[lane] : -1.0;
+      long long v = (lane < nw) ? wv[lane] : -1;
       int i = (lane < nw) ? wi[lane] : N + 1;
       for (int off = 16; off > 0; off >>= 1) {
-        const double v2 = __shfl_down_sync(0xffffffffu, v, off);
+        const long long v2 = __shfl_down_sync(0xffffffffu, v, off);
         const int i2 = __shfl_down_sync(0xffffffffu, i, off);
         if (v2 > v || (v2 == v && i2 < i)) {
           v = v2;
           i = i2;
         }
       }
-      if (lane == 0) {
-        s_kp = i;
-        s_pv = v;
-      }
+      if (lane == 0) s_kp = (v <= 0) ? -1 : i;  // -1: the column is zero
     }
     __syncthreads();
     int KP = s_kp;
-    const double pv = s_pv;
     const int KK = K - 1;
-    if (pv == 0.0) {
+    if (KP < 0) {
       zero = true;
       KP = KK;
     }
@@ -508,18 +512,19 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
       __syncthreads();
     }
     if (zero) break;
-    const double2 piv = a(K - 1, K);
-    const double m = hypot(piv.x, piv.y);
-    logmag += log(m);
-    phase = cmul(phase, make_double2(piv.x / m, piv.y / m));
-    if (KP != KK) phase = cneg(phase);
-    const double2 alpha = crcp(piv);
     const int nn = K - 2;
+    if (tid == 0) {
+      const double2 piv = a(K - 1, K);
+      pivs[steps] = piv;
+      pivs[N / 2 + steps] = make_double2(KP != KK ? -1.0 : 1.0, 0.0);
+      s_alpha = crcp(piv);
+    }
     for (int i = 1 + tid; i <= nn; i += nt) {
       xcol[i] = a(i, K);
       ycol[i] = a(i, K - 1);
     }
     __syncthreads();
+    const double2 alpha = s_alpha;
     // A(I,J) += X(I) (alpha Y(J)) - Y(I) (alpha X(J)), I < J <= nn
     for (int J = 2 + warp; J <= nn; J += nw) {
       const double2 xj = xcol[J], yj = ycol[J];
@@ -535,10 +540,31 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
     }
     __syncthreads();
   }
-  if (tid == 0) {
-    pf[b] = make_double2(zero ? -INFINITY : logmag, 0.0);
-    pf[batch + b] = zero ? make_double2(0.0, 0.0) : phase;
-    if (zero) atomicOr(flags, DEV_PFAFF_ZERO);
+  // Pf = prod_k piv_k (times -1 per interchange), as log|Pf| and a unit phase:
+  // warp 0, lanes over the pivots, then a fixed shuffle tree
+  if (warp == 0) {
+    double lm = 0.0;
+    double2 ph = make_double2(1.0, 0.0);
+    if (!zero) {
+      for (int k = lane; k < steps; k += 32) {
+        const double2 piv = pivs[k];
+        const double m = hypot(piv.x, piv.y);
+        lm += log(m);
+        ph = cmul(ph, make_double2(piv.x / m, piv.y / m));
+        if (pivs[N / 2 + k].x < 0.0) ph = cneg(ph);
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const double lm2 = __shfl_down_sync(0xffffffffu, lm, off);
+      const double2 ph2 = make_double2(__shfl_down_sync(0xffffffffu, ph.x, off), __shfl_down_sync(0xffffffffu, ph.y, off));
+      lm += lm2;
+      ph = cmul(ph, ph2);
+    }
+    if (lane == 0) {
+      pf[b] = make_double2(zero ? -INFINITY : lm, 0.0);
+      pf[batch + b] = zero ? make_double2(0.0, 0.0) : ph;
+      if (zero) atomicOr(flags, DEV_PFAFF_ZERO);
+    }
   }
 }
 
@@ -546,7 +572,7 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
 
 int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s) {
   if (n > 512 || (n & 1)) return TVAP_ERR_ARG;
-  const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 2 * size_t(n + 1));
+  const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 2 * size_t(n + 1) + size_t(n));
   if (shm <= jacobi32_smem_limit()) {
     static bool attr = false;
     if (!attr) {
