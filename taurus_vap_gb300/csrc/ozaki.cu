@@ -320,13 +320,14 @@ struct TcOut {
   int a_rows, a_split, b_rows, b_split, nstack;
 };
 
-// Persistent CTAs over the (128 x 64 tile of A' B'^T, slot) tiles; tile
-// numbers run over the N tiles fastest, then the M tiles, then the slots, so
-// that the CTAs working at one time share their A and B tiles through L2.
+// Persistent CTAs over the (128 x 64 tile of A' B'^T, slot) tiles, claimed in
+// order from *counter; tile numbers run over the N tiles fastest, then the M
+// tiles, then the slots, so that the CTAs working at one time share their A
+// and B tiles through L2.
 __global__ void __launch_bounds__(oztc::kThreads, 1)
     ozaki_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ ea, int a_rows_pad,
                     const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb, int b_rows_pad, int b_shared,
-                    int nslots, int nks, TcOut o, int* flags) {
+                    int nslots, int nks, TcOut o, int* counter, int* flags) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ oztc::Ctl ctl;
   const int a_tiles = a_rows_pad / oztc::kM, b_tiles = b_rows_pad / oztc::kN;
@@ -398,7 +399,7 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
       }
     }
   };
-  if (!oztc::run_tiles(blockIdx.x, gridDim.x, ntiles, nks, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
+  if (!oztc::run_tiles(counter, ntiles, nks, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
     atomicOr(flags, DEV_TC_TIMEOUT);
 }
 
@@ -408,6 +409,7 @@ struct OzScratch {
   size_t bytes = 0;
   int* ex = nullptr;
   size_t ex_count = 0;
+  int* counter = nullptr;  // tile counter of the tcgen05 kernel
 };
 constexpr int kMaxScratch = 16;
 OzScratch g_oz[kMaxScratch];
@@ -429,6 +431,7 @@ int oz_reserve(cudaStream_t s, size_t bytes, size_t ex_count, OzScratch** out) {
     set_last_error("too many streams use the emulated GEMM", __FILE__, __LINE__);
     return TVAP_ERR_ARG;
   }
+  if (!sc->counter) TVAP_CUDA(cudaMalloc(&sc->counter, sizeof(int)));
   if (bytes > sc->bytes) {
     if (sc->buf) {
       cudaStreamSynchronize(s);
@@ -471,6 +474,7 @@ void oz_release(cudaStream_t s) {
       cudaStreamSynchronize(s);
       cudaFree(e.buf);
       cudaFree(e.ex);
+      cudaFree(e.counter);
       e = OzScratch();
     }
 }
@@ -580,9 +584,11 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
   const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / oztc::kN) * a_slots;
   const int grid = int(std::min<long long>(ntiles, sms));
+  TVAP_CUDA(cudaMemsetAsync(sc->counter, 0, sizeof(int), s));
   if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   ozaki_tc_kernel<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
-                                                                  b_slots == 1 ? 1 : 0, a_slots, nks, o, g_dev_flags);
+                                                                  b_slots == 1 ? 1 : 0, a_slots, nks, o, sc->counter,
+                                                                  g_dev_flags);
   if (g_tc_timing_ctx) sec_end_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;

@@ -17,7 +17,7 @@
 // k % 8.  Descriptor LBO = 128 B (next k-block), SBO = 256 B (next row group).
 // The tiles of one operand are ordered [slot][row tile][k-step][digit].
 //
-// Persistent CTAs (one per SM) loop over output tiles.  Roles (576 threads):
+// Persistent CTAs (one per SM) claim output tiles dynamically.  Roles (576 threads):
 // warps 0-15 read the accumulators (warp w: TMEM lanes
 // 32 (w % 4) .. + 32 = tile rows, columns 16 (w / 4) .. + 16), warp 16 issues
 // the copies, warp 17 allocates tensor memory and one of its threads issues
@@ -164,10 +164,14 @@ struct Acc {
   long long h[16], l[16];
 };
 
+constexpr int kRing = 4;  // tile numbers handed from the copy thread to the others
+
 // shared control block
 struct Ctl {
   uint64_t full[kStages], empty[kStages];
   uint64_t acc_full, acc_empty, mma_done;
+  uint64_t tile_full[kRing], tile_empty[kRing];
+  int tile_id[kRing];
   uint32_t tmem;
   int abort;
 };
@@ -221,23 +225,31 @@ __device__ __forceinline__ void fold(uint32_t tmem, Acc& o) {
   }
 }
 
-// Persistent driver, called by every thread of the CTA: the CTA runs the
-// tiles first, first + step, ... below ntiles.  tile_ptrs(tile, A, B) gives
-// the tile's first k-step blocks (digit 0; nks k-steps of kABytes / kBBytes
-// each follow contiguously); store(tile, acc) is called by the epilogue
-// threads with the tile's integer accumulators, after the tensor memory has
-// been handed back to the MMA thread, so that the stores of one tile overlap
-// the MMAs of the next.  The producer runs ahead across tile boundaries.
-// Returns false on a timeout (the CTA's remaining outputs are then missing).
+// Persistent driver, called by every thread of the CTA.  Tiles are claimed
+// dynamically: the copy thread takes the next tile number from *counter
+// (zero before the launch) and hands it to the MMA thread and the epilogue
+// through a ring of kRing entries (mbarriers tile_full / tile_empty), so that
+// CTAs that start late -- their SMs held by kernels of other streams -- take
+// fewer tiles instead of delaying the product.  A number >= ntiles ends the
+// CTA.  tile_ptrs(tile, A, B) gives the tile's first k-step blocks (digit 0;
+// nks k-steps of kABytes / kBBytes each follow contiguously); store(tile, acc)
+// is called by the epilogue threads with the tile's integer accumulators,
+// after the tensor memory has been handed back to the MMA thread, so that the
+// stores of one tile overlap the MMAs of the next.  The copy thread runs
+// ahead across tile boundaries.  Returns false on a timeout.
 template <class TilePtrs, class Store>
-__device__ bool run_tiles(int first, int step, int ntiles, int nks, unsigned char* smem, Ctl& ctl,
-                          TilePtrs tile_ptrs, Store store) {
+__device__ bool run_tiles(int* counter, int ntiles, int nks, unsigned char* smem, Ctl& ctl, TilePtrs tile_ptrs,
+                          Store store) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int* abort = &ctl.abort;
   if (threadIdx.x == 0) {
     for (int q = 0; q < kStages; ++q) {
       mbar_init(&ctl.full[q], 1);
       mbar_init(&ctl.empty[q], 1);
+    }
+    for (int q = 0; q < kRing; ++q) {
+      mbar_init(&ctl.tile_full[q], 1);
+      mbar_init(&ctl.tile_empty[q], 32 * kEpiWarps + 1);
     }
     mbar_init(&ctl.acc_full, 1);
     mbar_init(&ctl.acc_empty, 32 * kEpiWarps);
@@ -256,11 +268,21 @@ __device__ bool run_tiles(int first, int step, int ntiles, int nks, unsigned cha
   const uint32_t tmem = ctl.tmem;
   const int nfold = (nks + kFoldKs - 1) / kFoldKs;  // fold intervals per tile
   bool ok = true;
-  long long issued = 0;  // copies issued (producer thread)
+  long long issued = 0;  // copies issued (copy thread)
   if (warp == kProducerWarp) {
     if (lane == 0) {
       long long it = 0;  // k-steps over all tiles of the CTA
-      for (int tile = first; tile < ntiles && ok; tile += step) {
+      for (int tt = 0; ok; ++tt) {
+        const int slot = tt % kRing;
+        if (tt >= kRing && !wait_parity(&ctl.tile_empty[slot], uint32_t((tt / kRing - 1) & 1), abort, false)) {
+          ok = false;
+          break;
+        }
+        int tile = atomicAdd(counter, 1);
+        if (tile >= ntiles) tile = -1;
+        ctl.tile_id[slot] = tile;
+        mbar_arrive(&ctl.tile_full[slot]);
+        if (tile < 0) break;
         const unsigned char *A, *B;
         tile_ptrs(tile, A, B);
         for (int ks = 0; ks < nks; ++ks, ++it) {
@@ -280,7 +302,15 @@ __device__ bool run_tiles(int first, int step, int ntiles, int nks, unsigned cha
   } else if (warp == kMmaWarp) {
     if (lane == 0) {
       long long it = 0, fc = 0;  // k-steps and fold intervals over all tiles
-      for (int tile = first; tile < ntiles && ok; tile += step) {
+      for (int tt = 0; ok; ++tt) {
+        const int slot = tt % kRing;
+        if (!wait_parity(&ctl.tile_full[slot], uint32_t((tt / kRing) & 1), abort, false)) {
+          ok = false;
+          break;
+        }
+        const int tile = ctl.tile_id[slot];
+        mbar_arrive(&ctl.tile_empty[slot]);
+        if (tile < 0) break;
         for (int ks = 0; ks < nks; ++ks, ++it) {
           const int st = int(it % kStages);
           if (!wait_parity(&ctl.full[st], uint32_t((it / kStages) & 1), abort, false)) {
@@ -313,7 +343,15 @@ __device__ bool run_tiles(int first, int step, int ntiles, int nks, unsigned cha
     }
   } else {
     long long fc = 0;
-    for (int tile = first; tile < ntiles && ok; tile += step) {
+    for (int tt = 0; ok; ++tt) {
+      const int slot = tt % kRing;
+      if (!wait_parity(&ctl.tile_full[slot], uint32_t((tt / kRing) & 1), abort, true)) {
+        ok = false;
+        break;
+      }
+      const int tile = ctl.tile_id[slot];
+      mbar_arrive(&ctl.tile_empty[slot]);
+      if (tile < 0) break;
       Acc o;
 #pragma unroll
       for (int c = 0; c < 16; ++c) o.h[c] = o.l[c] = 0;
