@@ -367,12 +367,12 @@ void free_field_dense(FieldDense& f) {
 int fields_dense(tvap_ctx* c, int ncol, int ldc, const double2* rho, const double2* kLR, const double2* kRL,
                  double2* gamma, double2* hsp, double2* dLR, double2* dRL, cudaStream_t s) {
   int rc;
-  sec_begin(c, SEC_FIELDS_GAMMA);
+  sec_begin_on(c, SEC_FIELDS_GAMMA, s);
   if ((rc = apply_one<false>(c, c->csr.dense_g, ncol, ldc, rho, rho, gamma, hsp, s))) return rc;
-  sec_end(c, SEC_FIELDS_GAMMA);
-  sec_begin(c, SEC_FIELDS_DELTA);
+  sec_end_on(c, SEC_FIELDS_GAMMA, s);
+  sec_begin_on(c, SEC_FIELDS_DELTA, s);
   if ((rc = apply_one<true>(c, c->csr.dense_d, ncol, ldc, kLR, kRL, dLR, dRL, s))) return rc;
-  sec_end(c, SEC_FIELDS_DELTA);
+  sec_end_on(c, SEC_FIELDS_DELTA, s);
   return TVAP_OK;
 }
 

@@ -385,15 +385,15 @@ void launch_fields(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
                    double2* gamma, double2* hsp, double2* dLR, double2* dRL, cudaStream_t s) {
   const int n = c->n;
   const long long rows = (long long)n * n;
-  sec_begin(c, SEC_FIELDS_GAMMA);
+  sec_begin_on(c, SEC_FIELDS_GAMMA, s);
   gamma_gather_kernel<CPL><<<(rows + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, s>>>(
       n, ncol, ldc, c->csr.g_rowptr, c->csr.g_src, c->csr.g_coef, rho, c->d_H1, gamma, hsp);
-  sec_end(c, SEC_FIELDS_GAMMA);
-  sec_begin(c, SEC_FIELDS_DELTA);
+  sec_end_on(c, SEC_FIELDS_GAMMA, s);
+  sec_begin_on(c, SEC_FIELDS_DELTA, s);
   const long long tri = (long long)n * (n + 1) / 2;
   delta_gather_kernel<CPL><<<(tri + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, s>>>(
       n, ncol, ldc, c->csr.d_rowptr, c->csr.d_src, c->csr.d_coef, kLR, kRL, dLR, dRL);
-  sec_end(c, SEC_FIELDS_DELTA);
+  sec_end_on(c, SEC_FIELDS_DELTA, s);
 }
 
 }  // namespace

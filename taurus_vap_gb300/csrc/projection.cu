@@ -2070,22 +2070,28 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
     return TVAP_ERR_CANONICAL;
   };
   if (o.mode == 0) {
-    // The Thouless chain needs only U and V: it is queued first on the main
-    // stream; the canonical basis (with its host-side checks) and the
-    // overlap chain follow on the second stream and run concurrently.
+    // The Thouless chain needs only U and V: it is queued first, on streamM
+    // (priority between those of the second and third streams); the
+    // canonical basis (with its host-side checks) follows on the second
+    // stream and the overlap chain on the third, concurrently; the sums join
+    // all three on the caller's stream.
+    cudaStream_t sm = c->streamM;
     TVAP_CUDA(cudaEventRecord(c->ev_fork, s));
     TVAP_CUDA(cudaStreamWaitEvent(s2, c->ev_fork, 0));
-    if ((rc = prepare_uv_blocks(c, s))) return rc;
-    if ((rc = angles_thouless(c, G, w->ephase, o.factor_delta, s))) return rc;
+    TVAP_CUDA(cudaStreamWaitEvent(sm, c->ev_fork, 0));
+    if ((rc = prepare_uv_blocks(c, sm))) return rc;
+    if ((rc = angles_thouless(c, G, w->ephase, o.factor_delta, sm))) return rc;
+    TVAP_CUDA(cudaEventRecord(c->ev_main, sm));
     if ((rc = prepare_canonical(c, o.seed_occeps, o.seed_allemp, canon, s2))) return rc;
     if (canon[2] && have_overlap) return canon_error();
-    // the overlap chain (wide kernels) runs at the main stream's priority
+    // the overlap chain (wide kernels) at the lowest priority
     cudaStream_t s3 = c->stream3;
     TVAP_CUDA(cudaEventRecord(c->ev_canon, s2));
     TVAP_CUDA(cudaStreamWaitEvent(s3, c->ev_canon, 0));
     if (have_overlap && (rc = angles_overlap(c, G, w->ephase, canon[0], canon[1], s3))) return rc;
     TVAP_CUDA(cudaEventRecord(c->ev_join, s3));
     TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+    TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_main, 0));
     if ((rc = angles_sums(c, G, w->weight, w->mult, have_overlap, 0, s))) return rc;
   } else {
     // plain form: one angle per launch sequence

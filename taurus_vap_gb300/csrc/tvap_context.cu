@@ -198,6 +198,12 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
   if ((e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithPriority(&c->stream2, cudaStreamNonBlocking, prio_hi)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithPriority(&c->stream3, cudaStreamNonBlocking, prio_lo)) != cudaSuccess) return fail(e);
+  // the Thouless chain ahead of the overlap chain when they share the SMs
+  // (the caller's stream usually has the lowest priority)
+  const int prio_mid = prio_hi + (prio_lo - prio_hi) / 2;
+  if ((e = cudaStreamCreateWithPriority(&c->streamM, cudaStreamNonBlocking, prio_mid)) != cudaSuccess)
+    return fail(e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_canon, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
@@ -221,6 +227,7 @@ void tvap_destroy(tvap_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->stream2) cudaStreamSynchronize(c->stream2);
   if (c->stream3) cudaStreamSynchronize(c->stream3);
+  if (c->streamM) cudaStreamSynchronize(c->streamM);
   cudaFree(c->scratch);
   destroy_workspace(c);
   free_field_csr(c->csr);
@@ -241,11 +248,14 @@ void tvap_destroy(tvap_ctx* c) {
   if (c->stream) oz_release(c->stream);
   if (c->stream2) oz_release(c->stream2);
   if (c->stream3) oz_release(c->stream3);
+  if (c->streamM) oz_release(c->streamM);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->stream3) cudaStreamDestroy(c->stream3);
+  if (c->streamM) cudaStreamDestroy(c->streamM);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_main) cudaEventDestroy(c->ev_main);
   if (c->ev_canon) cudaEventDestroy(c->ev_canon);
   delete c;
 }

@@ -186,8 +186,9 @@ struct tvap_ctx {
   bool have_ham = false;
   tvap::FieldCSR csr;
   cudaStream_t stream2 = nullptr;  // canonical basis (high priority), concurrent with the Thouless chain
-  cudaStream_t stream3 = nullptr;  // overlap chain and Pfaffians (normal priority)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_canon = nullptr;
+  cudaStream_t stream3 = nullptr;  // overlap chain and Pfaffians (lowest priority)
+  cudaStream_t streamM = nullptr;  // Thouless chain of the projection (priority between the two)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_canon = nullptr, ev_main = nullptr;
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
   unsigned* d_bar = nullptr;  // grid-barrier state of the cooperative kernels (3 words)
