@@ -33,7 +33,7 @@ namespace {
 constexpr int kJcCtas = 8;
 constexpr int kJcBlocks = 2 * kJcCtas;
 constexpr int kJcThreads = 512;  // 16 warps: one per pair of a sub-round
-constexpr int kJcMaxBw = 16;     // n <= 256
+constexpr int kJcMaxBw = 16;     // n <= 256 (and at most 8 rows per lane in jc_rotate)
 constexpr int kJcMaxSweeps = 30;
 constexpr float kJcTol = 2.0e-6f;  // |cos| of every pair: the FP64 refinement takes it from there
 
@@ -42,14 +42,40 @@ __device__ __forceinline__ int jc_block(int r, int p) {
   return p == 0 ? 0 : 1 + ((p - 1 - r) % 15 + 15) % 15;
 }
 
-// one-sided rotation of columns a and b (M and W), one warp; returns |cos|
-__device__ __forceinline__ float jc_rotate(float* Ma, float* Mb, float* Wa, float* Wb, int n, int lane) {
+// one-sided rotation of columns a and b (M and W), one warp; returns |cos|.
+// The rows stay in registers (n <= 256: at most 8 per lane) between the dot
+// products and the update, the W columns are fetched while the dot products
+// are reduced, and the rotation uses the fast reciprocal / reciprocal square
+// root: this stage only has to reach FP32 accuracy (the FP64 refinement
+// follows), and every step of the per-pair chain is latency.
+constexpr int kJcRows = 8;
+__device__ __forceinline__ float jc_rotate(int ma, int mb, int wa, int wb, int n, int lane) {
+  extern __shared__ float jc[];  // the kernel's dynamic shared memory: offsets keep the accesses in LDS/STS
+  float* Ma = jc + ma;
+  float* Mb = jc + mb;
+  float* Wa = jc + wa;
+  float* Wb = jc + wb;
+  float x[kJcRows], y[kJcRows], u[kJcRows], v[kJcRows];
   float aa = 0.f, bb = 0.f, ab = 0.f;
-  for (int r = lane; r < n; r += 32) {
-    const float x = Ma[r], y = Mb[r];
-    aa = fmaf(x, x, aa);
-    bb = fmaf(y, y, bb);
-    ab = fmaf(x, y, ab);
+#pragma unroll
+  for (int j = 0; j < kJcRows; ++j) {
+    const int r = lane + 32 * j;
+    const bool ok = r < n;
+    x[j] = ok ? Ma[r] : 0.f;
+    y[j] = ok ? Mb[r] : 0.f;
+  }
+#pragma unroll
+  for (int j = 0; j < kJcRows; ++j) {
+    const int r = lane + 32 * j;
+    const bool ok = r < n;
+    u[j] = ok ? Wa[r] : 0.f;
+    v[j] = ok ? Wb[r] : 0.f;
+  }
+#pragma unroll
+  for (int j = 0; j < kJcRows; ++j) {
+    aa = fmaf(x[j], x[j], aa);
+    bb = fmaf(y[j], y[j], bb);
+    ab = fmaf(x[j], y[j], ab);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -58,19 +84,27 @@ __device__ __forceinline__ float jc_rotate(float* Ma, float* Mb, float* Wa, floa
     ab += __shfl_xor_sync(0xffffffffu, ab, off);
   }
   if (!(aa > 0.f && bb > 0.f) || ab == 0.f) return 0.f;
-  const float cosab = fabsf(ab) * rsqrtf(aa) * rsqrtf(bb);
+  const float cosab = fabsf(ab) * rsqrtf(aa * bb);
   if (cosab < 1.0e-8f) return cosab;
-  const float zeta = (bb - aa) / (2.f * ab);
-  const float t = fabsf(zeta) > 1.0e18f ? 0.5f / zeta
-                                        : copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
+  const float zeta = __fdividef(bb - aa, 2.f * ab);
+  const float az = fabsf(zeta);
+  float t;
+  if (az > 1.0e18f) {
+    t = __fdividef(0.5f, zeta);
+  } else {
+    const float q = fmaf(zeta, zeta, 1.f);
+    t = copysignf(__frcp_rn(az + q * rsqrtf(q)), zeta);
+  }
   const float c = rsqrtf(fmaf(t, t, 1.f)), s = c * t;
-  for (int r = lane; r < n; r += 32) {
-    const float x = Ma[r], y = Mb[r];
-    Ma[r] = c * x - s * y;
-    Mb[r] = s * x + c * y;
-    const float u = Wa[r], v = Wb[r];
-    Wa[r] = c * u - s * v;
-    Wb[r] = s * u + c * v;
+#pragma unroll
+  for (int j = 0; j < kJcRows; ++j) {
+    const int r = lane + 32 * j;
+    if (r < n) {
+      Ma[r] = c * x[j] - s * y[j];
+      Mb[r] = s * x[j] + c * y[j];
+      Wa[r] = c * u[j] - s * v[j];
+      Wb[r] = s * u[j] + c * v[j];
+    }
   }
   return cosab;
 }
@@ -92,6 +126,7 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
   auto col = [&](int buf, int slot, int mat, int k) -> float* {
     return jc + ((size_t(buf * 2 + slot) * 2 + mat) * bw + k) * colsz;
   };
+  auto off = [&](int buf, int slot, int mat, int k) -> int { return ((buf * 2 + slot) * 2 + mat) * bw * n + k * n; };
   // initial blocks: slot 0 = position c, slot 1 = position 15 - c of round 0
   for (int slot = 0; slot < 2; ++slot) {
     const int blk = jc_block(0, slot == 0 ? c : kJcBlocks - 1 - c);
@@ -129,8 +164,8 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
               q = (sr - k + (bwe - 1)) % (bwe - 1);
             }
             if (p < bw && q < bw)
-              mx = fmaxf(mx, jc_rotate(col(cur, slot, 0, p), col(cur, slot, 0, q), col(cur, slot, 1, p),
-                                       col(cur, slot, 1, q), n, lane));
+              mx = fmaxf(mx, jc_rotate(off(cur, slot, 0, p), off(cur, slot, 0, q), off(cur, slot, 1, p),
+                                       off(cur, slot, 1, q), n, lane));
           }
           __syncthreads();
         }
@@ -140,15 +175,14 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
       for (int sr = 0; sr < bw; ++sr) {
         if (warp < bw) {
           const int k = warp, k2 = (warp + sr) % bw;
-          mx = fmaxf(mx, jc_rotate(col(cur, 0, 0, k), col(cur, 1, 0, k2), col(cur, 0, 1, k), col(cur, 1, 1, k2), n,
+          mx = fmaxf(mx, jc_rotate(off(cur, 0, 0, k), off(cur, 1, 0, k2), off(cur, 0, 1, k), off(cur, 1, 1, k2), n,
                                    lane));
         }
         __syncthreads();
       }
       // move the blocks to their positions of the next round (after the last
-      // round of a sweep too: the sweep restarts from round 0's layout
-      // shifted, which the circle method allows -- positions are reassigned
-      // below from the pull map, not from the round number)
+      // round of a sweep too: the 15 moves of a sweep bring every block back
+      // to its position of round 0)
       cluster.sync();
       const int nxt = cur ^ 1;
       // new position p pulls from old position p - 1 (1 -> 15); position 0 stays
