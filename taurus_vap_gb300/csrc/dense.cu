@@ -258,8 +258,28 @@ int* g_dev_flags = nullptr;
 tvap_ctx* g_tc_timing_ctx = nullptr;
 int g_tc_timing_sec = -1;
 
+int gemm_split_k2(const GemmArgs& g, cudaStream_t s) {
+  GemmArgs g1 = g;
+  g1.K2 = 0;
+  int rc;
+  if ((rc = gemm(g1, s))) return rc;
+  GemmArgs g2 = g;
+  g2.K2 = 0;
+  g2.A = g.A2;
+  g2.B = g.B2;
+  g2.K = g.K2;
+  g2.alpha = cscale(g.alpha, g.s2);
+  g2.beta = make_double2(1.0, 0.0);
+  return gemm(g2, s);
+}
+
 int gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return TVAP_OK;
+  if (g.K2 > 0) {
+    const double kk = double(g.K) + g.K2;
+    if (g_gemm_mode == 2 && double(g.M) * g.N * kk * g.batch >= 1.0e6) return gemm_ozaki(g, s);
+    return gemm_split_k2(g, s);
+  }
   // every product of at least 10^6 multiply-adds runs emulated on the tensor
   // cores; the smaller ones (few-column blocks, short K) stay on the FP64 pipe
   if (g_gemm_mode >= 1 && g.K >= 16 && double(g.M) * g.N * g.K * g.batch >= 1.0e6) return gemm_ozaki(g, s);

@@ -177,6 +177,11 @@ struct TcSrc {
   int rows, K, form;
   bool conj;
   int xrows, xk, nstack, kp;
+  // k >= K1 comes from the second source (k - K1), scaled by scale2
+  const void* p2;
+  long long sr2, sk2, bs2;
+  int K1;
+  double scale2;
 };
 
 // Digit planes of X' in the tiled layout of ozaki_tc.cuh.  One CTA per 8
@@ -218,12 +223,18 @@ __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int ti
     if (sq0 + row < nsrc) {
       int b, i;
       src_row(row, b, i);
-      const long long off = b * x.bs + i * x.sr + k * x.sk;
+      const bool second = k >= x.K1;
+      const long long off = second ? b * x.bs2 + i * x.sr2 + (k - x.K1) * x.sk2 : b * x.bs + i * x.sr + k * x.sk;
+      const void* P = second ? x.p2 : x.p;
       if (cplx) {
-        v = static_cast<const double2*>(x.p)[off];
+        v = static_cast<const double2*>(P)[off];
         if (x.conj) v.y = -v.y;
       } else {
-        v.x = static_cast<const double*>(x.p)[off];
+        v.x = static_cast<const double*>(P)[off];
+      }
+      if (second) {
+        v.x *= x.scale2;
+        v.y *= x.scale2;
       }
     }
     xs[row * K + k] = v;
@@ -499,17 +510,26 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
     long long sr, sk, bs;
     int rows;
     bool real, conj;
+    const void* p2;
+    long long sr2, sk2, bs2;
   };
-  Side L{g.A.p, g.A.rs, g.A.cs, g.A.bs, g.M, g.a_real, g.conj_a};
-  Side R{g.B.p, g.B.cs, g.B.rs, g.B.bs, g.N, g.b_real, g.conj_b};
+  if (g.K2 > 0 && ((g.A2.bs == 0) != (g.A.bs == 0) || (g.B2.bs == 0) != (g.B.bs == 0))) return TVAP_ERR_ARG;
+  Side L{g.A.p, g.A.rs, g.A.cs, g.A.bs, g.M, g.a_real, g.conj_a, g.A2.p, g.A2.rs, g.A2.cs, g.A2.bs};
+  Side R{g.B.p, g.B.cs, g.B.rs, g.B.bs, g.N, g.b_real, g.conj_b, g.B2.p, g.B2.cs, g.B2.rs, g.B2.bs};
   long long crs = g.crs, ccs = g.ccs;
   if (a_sh) {
     std::swap(L, R);
     std::swap(crs, ccs);
   }
-  const int K = g.K, kp = (K + 15) / 16 * 16;
-  TcSrc xa{L.p, L.sr, L.sk, L.bs, L.rows, K, 0, L.conj, L.rows, K, 1, K};
-  TcSrc xb{R.p, R.sr, R.sk, R.bs, R.rows, K, 0, R.conj, R.rows, K, 1, K};
+  // the second term (K2 > 0) continues the contraction: k >= g.K reads A2 /
+  // B2, the B side scaled by s2
+  const int K = g.K + (g.K2 > 0 ? g.K2 : 0), kp = (K + 15) / 16 * 16;
+  const int K1 = g.K2 > 0 ? g.K : K;
+  const bool scale_left = a_sh;  // after the swap the B side is on the left
+  TcSrc xa{L.p, L.sr, L.sk, L.bs, L.rows, K, 0, L.conj, L.rows, K, 1, K, L.p2, L.sr2, L.sk2, L.bs2, K1,
+           scale_left ? g.s2 : 1.0};
+  TcSrc xb{R.p, R.sr, R.sk, R.bs, R.rows, K, 0, R.conj, R.rows, K, 1, K, R.p2, R.sr2, R.sk2, R.bs2, K1,
+           scale_left ? 1.0 : g.s2};
   TcOut o{};
   o.a_split = o.b_split = INT_MAX;
   if (!L.real && !R.real) {
@@ -601,6 +621,7 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
 int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.batch <= 0) return TVAP_OK;
   if (g_gemm_mode == 2 && gemm_tc(g, s) == TVAP_OK) return TVAP_OK;
+  if (g.K2 > 0) return gemm_split_k2(g, s);
   const int PA = g.a_real ? 1 : 2, PB = g.b_real ? 1 : 2;
   const int mpad = (g.M + 31) / 32 * 32, npad = (g.N + 31) / 32 * 32, kpad = (g.K + 15) / 16 * 16;
   // operands with batch stride 0 are split once for the whole batch

@@ -1920,7 +1920,9 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
   TVAP_CUDA(cudaGetLastError());
   sec_end_on(c, SEC_TRACES, s);
   sec_begin_on(c, SEC_H20, s);
-  // H20: T = U~^T (h V~ + fd/2 DeltaLR U~) - fd/2 V~^T DeltaRL V~, H20 = T - T^T
+  // H20: T = U~^T (h V~ + fd/2 DeltaLR U~) - fd/2 V~^T DeltaRL V~, H20 = T - T^T,
+  // as three products: X = [h | DeltaLR] [V~; fd/2 U~], Y = DeltaRL V~ and
+  // T = [U~^T | V~^T] [X; -fd/2 Y] (the first and the last stacked along K)
   {
     TcTimingScope tc_timing(c, SEC_H20_TC);
     const View hv{w->hsp, (long long)G, (long long)n * G, 1};
@@ -1933,31 +1935,28 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
     g.ccs = n;
     g.cbs = (long long)nn;
     g.three_m = true;
-    g.A = hv;
-    g.B = view_cm(w->Vt, n, (long long)nn);
-    g.C = w->X;
     g.alpha = make_double2(1.0, 0.0);
     g.beta = make_double2(0.0, 0.0);
+    g.A = hv;
+    g.B = view_cm(w->Vt, n, (long long)nn);
+    g.K2 = n;
+    g.A2 = dl;
+    g.B2 = view_cm(w->Ut, n, (long long)nn);
+    g.s2 = 0.5 * factor_delta;
+    g.C = w->X;
     if ((rc = gemm(g, s))) return rc;
-    g.A = dl;
-    g.B = view_cm(w->Ut, n, (long long)nn);
-    g.alpha = make_double2(0.5 * factor_delta, 0.0);
-    g.beta = make_double2(1.0, 0.0);
-    if ((rc = gemm(g, s))) return rc;
+    g.K2 = 0;
     g.A = dr;
     g.B = view_cm(w->Vt, n, (long long)nn);
     g.C = w->Y;
-    g.alpha = make_double2(1.0, 0.0);
-    g.beta = make_double2(0.0, 0.0);
     if ((rc = gemm(g, s))) return rc;
     g.A = view_t(view_cm(w->Ut, n, (long long)nn));
     g.B = view_cm(w->X, n, (long long)nn);
+    g.K2 = n;
+    g.A2 = view_t(view_cm(w->Vt, n, (long long)nn));
+    g.B2 = view_cm(w->Y, n, (long long)nn);
+    g.s2 = -0.5 * factor_delta;
     g.C = w->T;
-    if ((rc = gemm(g, s))) return rc;
-    g.A = view_t(view_cm(w->Vt, n, (long long)nn));
-    g.B = view_cm(w->Y, n, (long long)nn);
-    g.alpha = make_double2(-0.5 * factor_delta, 0.0);
-    g.beta = make_double2(1.0, 0.0);
     if ((rc = gemm(g, s))) return rc;
   }
   sec_end_on(c, SEC_H20, s);

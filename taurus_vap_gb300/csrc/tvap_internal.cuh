@@ -97,8 +97,17 @@ struct GemmArgs {
   bool conj_a, conj_b;
   bool three_m;     // complex x complex with three real products (3M)
   bool upper_only;  // square tiles strictly below the diagonal are skipped
+  // optional second term along K: C = alpha (op(A) op(B) + s2 op(A2) op(B2))
+  // + beta C with A2 (M x K2) and B2 (K2 x N) of the types and conjugations
+  // of A and B.  The tcgen05 path forms it as one product over K + K2 (the
+  // operands stacked along K); elsewhere it is split into two products.
+  int K2;
+  View A2, B2;
+  double s2;
 };
 int gemm(const GemmArgs& g, cudaStream_t s);
+// the two terms of a product with K2 > 0 as two products
+int gemm_split_k2(const GemmArgs& g, cudaStream_t s);
 // the same product with the FP64 arithmetic emulated on the bf16 tensor cores
 int gemm_ozaki(const GemmArgs& g, cudaStream_t s);
 void oz_release(cudaStream_t s);
