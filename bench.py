@@ -330,7 +330,7 @@ def run_ours(args):
     fld_ms = (sections["fields_gamma"][0] + sections["fields_delta"][0]) / sec_steps
     fld_bytes = 13 * S + 16 * n * n * 7 * G
     roofline_fields = {
-        "kernel": "calculate_fields (Gamma + Delta, all angles): dense symmetry blocks, FP64 emulated on bf16 mma",
+        "kernel": "calculate_fields (Gamma + Delta, all angles): dense symmetry blocks, FP64 emulated on the bf16 tensor cores (tcgen05 in GEMM mode 2, mma.sync in mode 1)",
         "bound": "tensor",
         "algorithmic_bytes": fld_bytes,
         "achieved_gbs": fld_bytes / (fld_ms / 1000.0) / 1e9,

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "ozaki_core.cuh"
+#include "ozaki_tc.cuh"
 #include "tvap_internal.cuh"
 
 namespace tvap {
@@ -152,6 +153,150 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
 }
 
 // ---------------------------------------------------------------------------
+// tcgen05 form (GEMM mode 2): per block, C_b = W_b X_b with W_b in 128-row
+// tiles (planes tiled once per Hamiltonian) and X_b' = [Re X_b; Im X_b]^T
+// (B' rows: the real parts of the ncols_tot columns, then the imaginary
+// parts) sliced per call into 64-row tiles, on the persistent kernel of
+// ozaki_tc.cuh with one k-step count per block.
+// ---------------------------------------------------------------------------
+
+// X' planes: one warp per 8-entry chunk of a block's inputs, lanes over the
+// columns (coalesced reads of the angle-innermost densities).  The warps
+// after the chunks write the rows without gather entries (zero field; for
+// Gamma h = H1), which the products do not cover.
+template <bool DELTA>
+__global__ void __launch_bounds__(128)
+    slice_fields_tc_kernel(int n, int ncol, int ncols_tot, int ntn, int ldc, const double2* __restrict__ X0,
+                           const double2* __restrict__ X1, const int* __restrict__ colperm,
+                           const FieldBlockDesc* __restrict__ blocks, const FieldTcBlock* __restrict__ tcb,
+                           const int2* __restrict__ chunks, int nchunks, const int* __restrict__ empty_rows,
+                           int nempty, const int* __restrict__ eb_enc, __nv_bfloat16* __restrict__ xt,
+                           const double2* __restrict__ H1, double2* __restrict__ out0, double2* __restrict__ out1) {
+  const int lane = threadIdx.x & 31;
+  const int ch = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (ch >= nchunks) {
+    if (ch - nchunks >= nempty) return;
+    const int p = empty_rows[ch - nchunks];
+    const double2 z = make_double2(0.0, 0.0);
+    if (!DELTA) {
+      const double2 h = H1[p];
+      for (int j = lane; j < ncols_tot; j += 32) {
+        out0[(long long)p * ldc + j] = z;
+        out1[(long long)p * ldc + j] = h;
+      }
+    } else {
+      const int pt = p / n + (p % n) * n;
+      for (int j = lane; j < ncols_tot; j += 32) {
+        const int g = j < ncol ? j : j - ncol;
+        double2* out = j < ncol ? out0 : out1;
+        out[(long long)p * ldc + g] = z;
+        if (pt != p) out[(long long)pt * ldc + g] = z;
+      }
+    }
+    return;
+  }
+  const int2 c = chunks[ch];
+  const FieldBlockDesc d = blocks[c.x];
+  const FieldTcBlock q = tcb[c.x];
+  const int k0 = c.y;
+  int ent[8];
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) ent[kk] = colperm[d.kbeg + k0 + kk];
+  for (int j = lane; j < ncols_tot; j += 32) {
+    const double2* X = j < ncol ? X0 : X1;
+    const int jj = j < ncol ? j : j - ncol;
+    const int e = col_exp(eb_enc, j);
+    double2 v[8];
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) v[kk] = ent[kk] >= 0 ? X[(long long)ent[kk] * ldc + jj] : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      uint32_t w[kDigits][4];
+#pragma unroll
+      for (int kk = 0; kk < 8; kk += 2) {
+        int d0[kDigits], d1[kDigits];
+        oz::to_digits(oz::to_fixed(part ? v[kk].y : v[kk].x, e), d0);
+        oz::to_digits(oz::to_fixed(part ? v[kk + 1].y : v[kk + 1].x, e), d1);
+#pragma unroll
+        for (int s = 0; s < kDigits; ++s) w[s][kk >> 1] = oz::bf16x2_of_ints(d0[s], d1[s]);
+      }
+      const int jr = part * ncols_tot + j;
+      const size_t tb = (size_t(q.kboff) * ntn + size_t(jr / oztc::kN) * q.nks + k0 / 16) * kDigits;
+      const int toff = oztc::tile_offset(jr % oztc::kN, k0 % 16);
+#pragma unroll
+      for (int s = 0; s < kDigits; ++s)
+        *reinterpret_cast<uint4*>(xt + (tb + s) * oztc::kBTileElems + toff) =
+            make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+    }
+  }
+}
+
+// One persistent CTA per SM over the (block, 128-row tile, 64-column tile)
+// tiles.  DELTA = false: Gamma and h = Gamma + H1; DELTA = true: Delta^LR
+// (columns < ncol) and Delta^RL, each written with its skew image.  Every
+// thread stores one real or imaginary part per column.
+template <bool DELTA>
+__global__ void __launch_bounds__(oztc::kThreads, 1)
+    field_tc_kernel(int n, int ncol, int ncols_tot, int ntn, int ldc, const FieldBlockDesc* __restrict__ blocks,
+                    const FieldTcBlock* __restrict__ tcb, const int2* __restrict__ bm, int nbm,
+                    const __nv_bfloat16* __restrict__ wt, const __nv_bfloat16* __restrict__ xt,
+                    const int* __restrict__ ea, const int* __restrict__ rowperm, const int* __restrict__ eb_enc,
+                    const double2* __restrict__ H1, double2* __restrict__ out0, double2* __restrict__ out1,
+                    int* counter, int* flags) {
+  extern __shared__ __align__(1024) unsigned char fsm[];
+  __shared__ oztc::Ctl ctl;
+  const int ntiles = nbm * ntn;
+  auto tile_ptrs = [&](int tile, const unsigned char*& A, const unsigned char*& B) {
+    const int2 m = bm[tile / ntn];
+    const int nt = tile % ntn;
+    const FieldTcBlock q = tcb[m.x];
+    A = reinterpret_cast<const unsigned char*>(wt) +
+        (size_t(q.woff) + size_t(m.y) * q.nks * kDigits * oztc::kATileElems) * sizeof(__nv_bfloat16);
+    B = reinterpret_cast<const unsigned char*>(xt) + (size_t(q.kboff) * ntn + size_t(nt) * q.nks) * size_t(oztc::kBBytes);
+  };
+  auto nks_of = [&](int tile) { return tcb[bm[tile / ntn].x].nks; };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto store = [&](int tile, const oztc::Acc& acc) {
+    const int2 m = bm[tile / ntn];
+    const int nt = tile % ntn;
+    const FieldBlockDesc d = blocks[m.x];
+    const int i = m.y * oztc::kM + 32 * (warp & 3) + lane;
+    if (i >= d.r_pad) return;
+    const int rr = d.row_base + i;
+    const int p = rowperm[rr];
+    if (p < 0) return;
+    const int eai = ea[rr] - 57;
+    const int pt = p / n + (p % n) * n;
+    const int col0 = nt * oztc::kN + 16 * (warp >> 2);
+    double h1[2] = {0.0, 0.0};
+    if (!DELTA) {
+      const double2 hv = H1[p];
+      h1[0] = hv.x;
+      h1[1] = hv.y;
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int jr = col0 + c;
+      if (jr >= 2 * ncols_tot) break;
+      const int comp = jr >= ncols_tot ? 1 : 0;
+      const int j = jr - comp * ncols_tot;
+      const double v = oztc::value(acc, c) * oz::pow2(eai + col_exp(eb_enc, j));
+      if (!DELTA) {
+        reinterpret_cast<double*>(out0)[((long long)p * ldc + j) * 2 + comp] = v;
+        reinterpret_cast<double*>(out1)[((long long)p * ldc + j) * 2 + comp] = v + h1[comp];
+      } else {
+        const int g = j < ncol ? j : j - ncol;
+        double* out = reinterpret_cast<double*>(j < ncol ? out0 : out1);
+        out[((long long)p * ldc + g) * 2 + comp] = v;
+        if (pt != p) out[((long long)pt * ldc + g) * 2 + comp] = -v;
+      }
+    }
+  };
+  if (!oztc::run_tiles(counter, ntiles, nks_of, fsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
+    atomicOr(flags, DEV_TC_TIMEOUT);
+}
+
+// ---------------------------------------------------------------------------
 // host: blocks from the gather form
 // ---------------------------------------------------------------------------
 struct Dsu {
@@ -241,6 +386,28 @@ int build_one(int n, bool delta, const std::vector<int>& rowptr, const std::vect
   std::vector<int> ea(nrows, 0), rowperm(nrows, -1), colperm(ktot, -1);
   std::vector<int2> tiles;
   std::vector<double> wblk;
+  // tcgen05 form of the same planes
+  std::vector<FieldTcBlock> tcb(nb + 1);
+  long long woff = 0;
+  int kboff = 0;
+  for (int b = 0; b <= nb; ++b) {
+    const FieldBlockDesc& d = desc[b];
+    FieldTcBlock& q = tcb[b];
+    const int rows = b < nb ? int(brow[b].size()) : int(empty_rows.size());
+    q.mtiles = b < nb ? (rows + oztc::kM - 1) / oztc::kM : 0;  // the empty rows need no product
+    q.nks = d.kb_pad / 16;
+    q.kboff = kboff;
+    q.pad = 0;
+    q.woff = woff;
+    woff += (long long)q.mtiles * q.nks * kDigits * oztc::kATileElems;
+    kboff += q.nks;
+  }
+  std::vector<uint16_t> wt(size_t(std::max<long long>(woff, 1)), 0);
+  std::vector<int2> tc_bm, tc_chunks;
+  for (int b = 0; b < nb; ++b) {
+    for (int mt = 0; mt < tcb[b].mtiles; ++mt) tc_bm.push_back(make_int2(b, mt));
+    for (int k0 = 0; k0 < desc[b].kb_pad; k0 += 8) tc_chunks.push_back(make_int2(b, k0));
+  }
   for (int b = 0; b <= nb; ++b) {
     const FieldBlockDesc& d = desc[b];
     const std::vector<int>& rows = b < nb ? brow[b] : empty_rows;
@@ -260,11 +427,18 @@ int build_one(int n, bool delta, const std::vector<int>& rowptr, const std::vect
         if (wr[k] != 0.0) emax = std::max(emax, oz::dexp(wr[k]));
       if (emax == oz::kExpZero) emax = 0;
       ea[d.row_base + i] = emax;
+      const FieldTcBlock& q = tcb[b];
+      const int mt = i / oztc::kM, ri = i % oztc::kM;
       for (int k = 0; k < d.kb_pad; ++k) {
         int dg[kDigits];
         oz::to_digits(oz::to_fixed(wr[k], emax), dg);
-        for (int s = 0; s < kDigits; ++s)
-          wd[size_t(d.aoff) + (size_t(s) * d.r_pad + i) * d.kb_pad + k] = oz::bf16_bits_of_int(dg[s]);
+        for (int s = 0; s < kDigits; ++s) {
+          const uint16_t bits = oz::bf16_bits_of_int(dg[s]);
+          wd[size_t(d.aoff) + (size_t(s) * d.r_pad + i) * d.kb_pad + k] = bits;
+          if (mt < q.mtiles)
+            wt[size_t(q.woff) + ((size_t(mt) * q.nks + k / 16) * kDigits + s) * oztc::kATileElems +
+               oztc::tile_offset(ri, k % 16)] = bits;
+        }
       }
     }
   }
@@ -284,6 +458,21 @@ int build_one(int n, bool delta, const std::vector<int>& rowptr, const std::vect
   TVAP_CUDA(cudaMemcpy(f->colperm, colperm.data(), sizeof(int) * ktot, cudaMemcpyHostToDevice));
   TVAP_CUDA(cudaMemcpy(f->tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
   TVAP_CUDA(cudaMemcpy(f->blocks, desc.data(), sizeof(FieldBlockDesc) * desc.size(), cudaMemcpyHostToDevice));
+  TVAP_CUDA(cudaMalloc(&f->wt, sizeof(uint16_t) * wt.size()));
+  TVAP_CUDA(cudaMalloc(&f->tcb, sizeof(FieldTcBlock) * tcb.size()));
+  TVAP_CUDA(cudaMalloc(&f->tc_bm, sizeof(int2) * std::max<size_t>(tc_bm.size(), 1)));
+  TVAP_CUDA(cudaMalloc(&f->tc_chunks, sizeof(int2) * std::max<size_t>(tc_chunks.size(), 1)));
+  TVAP_CUDA(cudaMemcpy(f->wt, wt.data(), sizeof(uint16_t) * wt.size(), cudaMemcpyHostToDevice));
+  TVAP_CUDA(cudaMemcpy(f->tcb, tcb.data(), sizeof(FieldTcBlock) * tcb.size(), cudaMemcpyHostToDevice));
+  if (!tc_bm.empty())
+    TVAP_CUDA(cudaMemcpy(f->tc_bm, tc_bm.data(), sizeof(int2) * tc_bm.size(), cudaMemcpyHostToDevice));
+  if (!tc_chunks.empty())
+    TVAP_CUDA(cudaMemcpy(f->tc_chunks, tc_chunks.data(), sizeof(int2) * tc_chunks.size(), cudaMemcpyHostToDevice));
+  f->tc_nbm = int(tc_bm.size());
+  f->tc_ksteps = kboff;
+  f->tc_nchunks = int(tc_chunks.size());
+  f->tc_empty_base = desc[nb].row_base;
+  f->tc_nempty = int(empty_rows.size());
   *dense = true;
   return TVAP_OK;
 }
@@ -302,8 +491,46 @@ int download_csr(int nrows, const int* d_rowptr, const int* d_src, const double*
 }
 
 template <bool DELTA>
+int apply_one_tc(tvap_ctx* c, const FieldDense& f, int ncol, int ldc, const double2* X0, const double2* X1,
+                 double2* out0, double2* out1, cudaStream_t s) {
+  const int n = c->n, nent = n * n;
+  const int ncols_tot = DELTA ? 2 * ncol : ncol;
+  const int ntn = (2 * ncols_tot + oztc::kN - 1) / oztc::kN;
+  const int npad = (ncols_tot + 31) / 32 * 32;
+  __nv_bfloat16* xt = nullptr;
+  int* eb = nullptr;
+  int rc;
+  const size_t xt_elems = size_t(f.tc_ksteps) * ntn * kDigits * oztc::kBTileElems;
+  if ((rc = oz_scratch(s, sizeof(__nv_bfloat16) * xt_elems + sizeof(int) * 64, size_t(npad), &xt, &eb))) return rc;
+  // the tile counter sits after the planes (256-byte aligned: the planes are multiples of 2 KB)
+  int* counter = reinterpret_cast<int*>(xt + xt_elems);
+  TVAP_CUDA(cudaMemsetAsync(eb, 0, sizeof(int) * npad, s));
+  TVAP_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s));
+  colexp_kernel<<<dim3(npad / 32, 64), 256, 0, s>>>(nent, ncol, ncols_tot, ldc, X0, X1, eb);
+  slice_fields_tc_kernel<DELTA><<<(f.tc_nchunks + f.tc_nempty + 3) / 4, 128, 0, s>>>(
+      n, ncol, ncols_tot, ntn, ldc, X0, X1, f.colperm, f.blocks, f.tcb, f.tc_chunks, f.tc_nchunks,
+      f.rowperm + f.tc_empty_base, f.tc_nempty, eb, xt, c->d_H1, out0, out1);
+  static bool attr = false;
+  if (!attr) {
+    TVAP_CUDA(cudaFuncSetAttribute(field_tc_kernel<DELTA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(oztc::kSmemBytes)));
+    attr = true;
+  }
+  static int sms = 0;
+  if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+  const int grid = std::min(f.tc_nbm * ntn, sms);
+  field_tc_kernel<DELTA><<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(
+      n, ncol, ncols_tot, ntn, ldc, f.blocks, f.tcb, f.tc_bm, f.tc_nbm, static_cast<const __nv_bfloat16*>(f.wt), xt,
+      f.ea, f.rowperm, eb, c->d_H1, out0, out1, counter, g_dev_flags);
+  TVAP_CUDA(cudaGetLastError());
+  c->kernel_launches += 3;
+  return TVAP_OK;
+}
+
+template <bool DELTA>
 int apply_one(tvap_ctx* c, const FieldDense& f, int ncol, int ldc, const double2* X0, const double2* X1,
               double2* out0, double2* out1, cudaStream_t s) {
+  if (c->gemm_mode == 2 && f.tc_nbm > 0) return apply_one_tc<DELTA>(c, f, ncol, ldc, X0, X1, out0, out1, s);
   const int n = c->n, nent = n * n;
   const int ncols_tot = DELTA ? 2 * ncol : ncol;
   const int npad = (ncols_tot + kTile - 1) / kTile * kTile;
@@ -355,6 +582,10 @@ int build_field_dense(tvap_ctx* c) {
 }
 
 void free_field_dense(FieldDense& f) {
+  cudaFree(f.wt);
+  cudaFree(f.tcb);
+  cudaFree(f.tc_bm);
+  cudaFree(f.tc_chunks);
   cudaFree(f.wd);
   cudaFree(f.ea);
   cudaFree(f.rowperm);

@@ -410,7 +410,8 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
       }
     }
   };
-  if (!oztc::run_tiles(counter, ntiles, nks, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
+  auto nks_of = [nks](int) { return nks; };
+  if (!oztc::run_tiles(counter, ntiles, nks_of, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
     atomicOr(flags, DEV_TC_TIMEOUT);
 }
 

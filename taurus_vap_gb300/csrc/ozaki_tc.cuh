@@ -232,13 +232,13 @@ __device__ __forceinline__ void fold(uint32_t tmem, Acc& o) {
 // CTAs that start late -- their SMs held by kernels of other streams -- take
 // fewer tiles instead of delaying the product.  A number >= ntiles ends the
 // CTA.  tile_ptrs(tile, A, B) gives the tile's first k-step blocks (digit 0;
-// nks k-steps of kABytes / kBBytes each follow contiguously); store(tile, acc)
+// nks_of(tile) k-steps of kABytes / kBBytes each follow contiguously); store(tile, acc)
 // is called by the epilogue threads with the tile's integer accumulators,
 // after the tensor memory has been handed back to the MMA thread, so that the
 // stores of one tile overlap the MMAs of the next.  The copy thread runs
 // ahead across tile boundaries.  Returns false on a timeout.
-template <class TilePtrs, class Store>
-__device__ bool run_tiles(int* counter, int ntiles, int nks, unsigned char* smem, Ctl& ctl, TilePtrs tile_ptrs,
+template <class TilePtrs, class NksOf, class Store>
+__device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char* smem, Ctl& ctl, TilePtrs tile_ptrs,
                           Store store) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int* abort = &ctl.abort;
@@ -266,7 +266,6 @@ __device__ bool run_tiles(int* counter, int ntiles, int nks, unsigned char* smem
   __syncthreads();
   fence_after();
   const uint32_t tmem = ctl.tmem;
-  const int nfold = (nks + kFoldKs - 1) / kFoldKs;  // fold intervals per tile
   bool ok = true;
   long long issued = 0;  // copies issued (copy thread)
   if (warp == kProducerWarp) {
@@ -285,6 +284,7 @@ __device__ bool run_tiles(int* counter, int ntiles, int nks, unsigned char* smem
         if (tile < 0) break;
         const unsigned char *A, *B;
         tile_ptrs(tile, A, B);
+        const int nks = nks_of(tile);
         for (int ks = 0; ks < nks; ++ks, ++it) {
           const int st = int(it % kStages);
           if (it >= kStages && !wait_parity(&ctl.empty[st], uint32_t((it / kStages - 1) & 1), abort, false)) {
@@ -311,6 +311,7 @@ __device__ bool run_tiles(int* counter, int ntiles, int nks, unsigned char* smem
         const int tile = ctl.tile_id[slot];
         mbar_arrive(&ctl.tile_empty[slot]);
         if (tile < 0) break;
+        const int nks = nks_of(tile);
         for (int ks = 0; ks < nks; ++ks, ++it) {
           const int st = int(it % kStages);
           if (!wait_parity(&ctl.full[st], uint32_t((it / kStages) & 1), abort, false)) {
@@ -352,6 +353,7 @@ __device__ bool run_tiles(int* counter, int ntiles, int nks, unsigned char* smem
       const int tile = ctl.tile_id[slot];
       mbar_arrive(&ctl.tile_empty[slot]);
       if (tile < 0) break;
+      const int nfold = (nks_of(tile) + kFoldKs - 1) / kFoldKs;  // fold intervals of the tile
       Acc o;
 #pragma unroll
       for (int c = 0; c < 16; ++c) o.h[c] = o.l[c] = 0;

@@ -141,8 +141,22 @@ struct FieldBlockDesc {
   long long aoff;  // first digit-plane element of the block
   int r_pad, kb_pad, kbeg, row_base;
 };
+// per block of the tcgen05 form: 128-row tiles of W, k-steps of 16, first
+// k-step of the block (prefix over the blocks), first element of its W planes
+struct FieldTcBlock {
+  int mtiles, nks, kboff, pad;
+  long long woff;
+};
 struct FieldDense {
   int nblk = 0, ntiles = 0, nrows = 0, ktot = 0;
+  // tcgen05 form: W planes tiled [block][m tile][k-step][digit][128 x 16],
+  // (block, m tile) list, 8-entry chunks of the blocks' inputs (block, k0)
+  void* wt = nullptr;
+  FieldTcBlock* tcb = nullptr;
+  int2* tc_bm = nullptr;
+  int2* tc_chunks = nullptr;
+  int tc_nbm = 0, tc_ksteps = 0, tc_nchunks = 0;
+  int tc_empty_base = 0, tc_nempty = 0;  // permuted rows of the rows without entries (zero fields)
   void* wd = nullptr;       // bf16 digit planes of W, block by block
   int* ea = nullptr;        // exponent per permuted output row
   int* rowperm = nullptr;   // permuted row -> output entry (-1: padding)
