@@ -219,6 +219,7 @@ def run_ours(args):
     ms = t0.elapsed_time(t1)
     launches = it.launches
     sections = ctx.get_timing()
+    timeline = ctx.get_timeline()
     canon_paths = ctx.canonical_paths()
     sec_steps = args.steps
     ctx.set_timing(False)
@@ -368,6 +369,7 @@ def run_ours(args):
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "roofline_fp64": roofline_fp64,
         "roofline_fields": roofline_fields,
         "sections_ms_per_step": {k: round(v, 4) for k, v in sec_ms.items()},
+        "timeline_ms": {k: [round(a, 3), round(b, 3)] for k, (a, b) in timeline.items() if sections[k][1]},
         "dominant_section": dom[0], "canonical_paths": canon_paths, "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
         "final_energy": it.energy,
     }

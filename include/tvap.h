@@ -106,6 +106,10 @@ int tvap_set_timing(tvap_ctx* ctx, int on);
  * all reductions run on the FP64 pipe in every mode. */
 int tvap_set_gemm_mode(tvap_ctx* ctx, int mode);
 int tvap_get_timing(tvap_ctx* ctx, double* ms, long long* calls, int nsec);
+/* Mean start and end of every timed section in milliseconds from the start
+ * of the projection it belongs to (the gradient and the evolution count
+ * from the projection before them).  No reference counterpart. */
+int tvap_get_timeline(tvap_ctx* ctx, double* start_ms, double* end_ms, int nsec);
 /* Diagnostic counters since the last tvap_set_timing, for the canonical
  * basis: [0] FP32 Jacobi + FP64 refinement attempts, [1] of them accepted by
  * the final check, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in

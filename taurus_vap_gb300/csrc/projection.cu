@@ -971,11 +971,6 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
   if (tid == 0) rflag[0] = fail;
 }
 
-__global__ void copy_kernel(size_t m, const double* __restrict__ a, double* __restrict__ b) {
-  const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
-  if (i < m) b[i] = a[i];
-}
-
 // ---------------------------------------------------------------------------
 // Blocked Thouless solve.  X = V_phi U_phi^{-1} is obtained from the
 // augmented system W = [U_phi^T | V_phi^T] (n x 2n, one per angle) by a
@@ -985,6 +980,10 @@ __global__ void copy_kernel(size_t m, const double* __restrict__ a, double* __re
 // GEMM over all SMs.  The blocked back substitution with U alternates GEMM
 // updates and small per-block triangular solves.  Same pivots as the
 // unblocked elimination; 10.7 n^3 FP64 flops per angle, mostly in GEMMs.
+// With the emulated products the solve is a blocked Gauss-Jordan elimination
+// instead (panel_gj_kernel): the same partial pivoting per panel, the block
+// row scaled by the inverse of its diagonal block and every other row
+// eliminated by one product, so that no back substitution is needed.
 // ---------------------------------------------------------------------------
 constexpr int kPanelThreads = 512;
 
@@ -1285,6 +1284,267 @@ __global__ void __launch_bounds__(kFactorThreads)
   }
 }
 
+// Panel of the blocked Gauss-Jordan solve (GEMM modes 1 and 2), one CTA per
+// angle.  The pivot rows are chosen by a single-precision Crout elimination
+// of the panel rows j0 .. n-1 with partial pivoting (first maximum of
+// |re| + |im|, as izamax): warp w holds columns w, w + 8, w + 16, w + 24,
+// lane l rows l, l + 32, ... (SLOTS rows a lane); one barrier per column
+// (before it the pivot column's warp finds and swaps the pivot row and forms
+// its reciprocal; after it the other warps swap the rows, every warp scales
+// its entries of the pivot row and updates its columns).  Only the choice of
+// rows comes from single precision: the block A11 of the chosen rows is then
+// inverted in FP64 from the original values by Gauss-Jordan elimination
+// without further interchanges (its pivots are the partial-pivoting pivots),
+// T = A11^{-1} written to Tinv + b * tstride (nbp x nbp, column-major).  The
+// panel columns of W are rewritten for the elimination product: the block
+// rows j0 .. j0+nbp-1 as zeros, the rows below with their original values in
+// the pivoted order.  The other columns' interchanges are left to
+// panel_swap_kernel.
+__device__ __forceinline__ float2 shfl_f2(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// first maximum over the warp, the result in every lane
+__device__ __forceinline__ void warp_argmax_key_all(int& v, int& i) {
+  for (int off = 16; off > 0; off >>= 1) {
+    const int v2 = __shfl_xor_sync(0xffffffffu, v, off);
+    const int i2 = __shfl_xor_sync(0xffffffffu, i, off);
+    if (v2 > v || (v2 == v && i2 < i)) {
+      v = v2;
+      i = i2;
+    }
+  }
+}
+
+// 1/z = conj(z) / |z|^2 with |z|^2 inverted by two Newton steps from the
+// single-precision reciprocal (relative error a few units of the last
+// place); outside the safe range the scaled division (crcp)
+__device__ __forceinline__ double2 crcp_newton(double2 z) {
+  const double d = fma(z.x, z.x, z.y * z.y);
+  if (!(d > 1.0e-30 && d < 1.0e30)) return crcp(z);
+  double y = double(__frcp_rn(float(d)));
+  double e = fma(-d, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-d, y, 1.0);
+  y = fma(y, e, y);
+  return make_double2(z.x * y, -z.y * y);
+}
+
+template <int SLOTS>
+__device__ __forceinline__ float2 slot_get(const float2 (&a)[SLOTS], int s) {
+  float2 v = a[0];
+#pragma unroll
+  for (int k = 1; k < SLOTS; ++k)
+    if (k == s) v = a[k];
+  return v;
+}
+
+template <int SLOTS>
+__device__ __forceinline__ void slot_set(float2 (&a)[SLOTS], int s, float2 v) {
+#pragma unroll
+  for (int k = 0; k < SLOTS; ++k)
+    if (k == s) a[k] = v;
+}
+
+// exchange rows r1 != r2 of a column held as a[slot] in lanes
+template <int SLOTS>
+__device__ __forceinline__ void swap_rows(float2 (&a)[SLOTS], int r1, int r2, int lane) {
+  const float2 v1 = shfl_f2(slot_get(a, r1 >> 5), r1 & 31);
+  const float2 v2 = shfl_f2(slot_get(a, r2 >> 5), r2 & 31);
+  if (lane == (r1 & 31)) slot_set(a, r1 >> 5, v2);
+  if (lane == (r2 & 31)) slot_set(a, r2 >> 5, v1);
+}
+
+__device__ __forceinline__ float2 fcmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+constexpr int kGjMaxSlots = 6;  // panels of up to 192 rows
+constexpr int kGjEntries = kPanelMax * kPanelMax / kFactorThreads;  // block entries per thread
+
+template <int SLOTS>
+__global__ void __launch_bounds__(kFactorThreads)
+    panel_gj_kernel(int n, int j0, int nbp, double2* __restrict__ Wall, int* __restrict__ piv, int* flags,
+                    double2* __restrict__ Tinv, long long tstride) {
+  constexpr int kQ = kPanelMax / 8;
+  constexpr int kP = kPanelMax + 1;
+  static_assert(kFactorThreads == 256 && kGjEntries * kFactorThreads == kPanelMax * kPanelMax,
+                "eight warps hold the panel's columns; the block's entries divide evenly");
+  __shared__ float2 scol[2][32 * SLOTS];
+  __shared__ float2 s_rp[2];
+  __shared__ int s_piv[2];
+  __shared__ int s_sing;
+  __shared__ int srow[32 * SLOTS];
+  __shared__ double2 A11[kPanelMax * kP];
+  __shared__ double2 smu[kPanelMax], srk[kPanelMax];
+  __shared__ double2 s_rd[2];
+  const int b = blockIdx.x;
+  double2* W = Wall + size_t(b) * 2 * n * n;
+  const int m = n - j0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_sing = 0;
+  for (int r = tid; r < 32 * SLOTS; r += kFactorThreads) srow[r] = r;
+  float2 a[kQ][SLOTS];
+#pragma unroll
+  for (int q = 0; q < kQ; ++q) {
+    const int c = warp + 8 * q;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+      const int r = lane + 32 * s;
+      double2 v = make_double2(0.0, 0.0);
+      if (c < nbp && r < m) v = W[(j0 + r) + size_t(j0 + c) * n];
+      a[q][s] = make_float2(float(v.x), float(v.y));
+    }
+  }
+  __syncthreads();
+  for (int jj = 0; jj < nbp; ++jj) {
+    const int buf = jj & 1, wj = jj & 7, qj = jj >> 3;
+    if (warp == wj) {
+      int best = -1, bi = m;
+#pragma unroll
+      for (int q = 0; q < kQ; ++q)
+        if (q == qj) {
+#pragma unroll
+          for (int s = 0; s < SLOTS; ++s) {
+            const int r = lane + 32 * s;
+            if (r >= jj && r < m) {
+              const int v = __float_as_int(fabsf(a[q][s].x) + fabsf(a[q][s].y));
+              if (v > best) {
+                best = v;
+                bi = r;
+              }
+            }
+          }
+        }
+      warp_argmax_key_all(best, bi);
+      const bool zero = best <= 0;
+      const int p = zero ? jj : bi;
+      if (p != jj) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) swap_rows(a[q], jj, p, lane);
+      }
+      float2 pv = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < kQ; ++q)
+        if (q == qj) {
+          pv = shfl_f2(slot_get(a[q], jj >> 5), jj & 31);
+#pragma unroll
+          for (int s = 0; s < SLOTS; ++s) {
+            const int r = lane + 32 * s;
+            if (r > jj && r < m) scol[buf][r] = a[q][s];
+          }
+        }
+      if (lane == 0) {
+        const float d = fmaf(pv.x, pv.x, pv.y * pv.y);
+        const float rd = (zero || !(d > 0.f)) ? 0.f : __frcp_rn(d);
+        s_rp[buf] = make_float2(pv.x * rd, -pv.y * rd);
+        s_piv[buf] = p;
+        piv[size_t(b) * n + j0 + jj] = j0 + p;
+        const int t0 = srow[jj];
+        srow[jj] = srow[p];
+        srow[p] = t0;
+        if (zero) s_sing = 1;
+      }
+    }
+    __syncthreads();
+    if (warp != wj) {
+      const int p = s_piv[buf];
+      if (p != jj) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) swap_rows(a[q], jj, p, lane);
+      }
+    }
+    const float2 rp = s_rp[buf];
+    float2 mu[SLOTS];
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+      const int r = lane + 32 * s;
+      mu[s] = (r > jj && r < m) ? scol[buf][r] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+      const int c = warp + 8 * q;
+      if (c <= jj || c >= nbp) continue;
+      // U' entry of the pivot row, then the column update
+      const float2 u = fcmul(shfl_f2(slot_get(a[q], jj >> 5), jj & 31), rp);
+      if (lane == (jj & 31)) slot_set(a[q], jj >> 5, u);
+#pragma unroll
+      for (int s = 0; s < SLOTS; ++s)
+        if (32 * s + 31 > jj) {
+          a[q][s].x = fmaf(-mu[s].x, u.x, fmaf(mu[s].y, u.y, a[q][s].x));
+          a[q][s].y = fmaf(-mu[s].x, u.y, fmaf(-mu[s].y, u.x, a[q][s].y));
+        }
+    }
+  }
+  // the original rows in the pivoted order: the block to shared memory, the
+  // rows below back to the panel (the block rows as zeros)
+  double2 raw[kQ][SLOTS];
+#pragma unroll
+  for (int q = 0; q < kQ; ++q) {
+    const int c = warp + 8 * q;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+      const int r = lane + 32 * s;
+      raw[q][s] = (c < nbp && r < m) ? W[(j0 + srow[r]) + size_t(j0 + c) * n] : make_double2(0.0, 0.0);
+      if (c < nbp && r < nbp) A11[r + c * kP] = raw[q][s];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < kQ; ++q) {
+    const int c = warp + 8 * q;
+    if (c >= nbp) continue;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+      const int r = lane + 32 * s;
+      if (r < m) W[(j0 + r) + size_t(j0 + c) * n] = (r < nbp) ? make_double2(0.0, 0.0) : raw[q][s];
+    }
+  }
+  if (s_sing && tid == 0) atomicOr(flags, DEV_SINGULAR_UPHI);
+  // Gauss-Jordan inverse of the block in place: step k with the reciprocal
+  // of the pivot (formed by the owner of that entry at the end of the step
+  // before), multipliers and the pivot row staged, then every entry at once
+  if (tid == 0) s_rd[0] = crcp_newton(A11[0]);
+  int ei[kGjEntries], ej[kGjEntries];
+#pragma unroll
+  for (int e = 0; e < kGjEntries; ++e) {
+    const int idx = tid + e * kFactorThreads;
+    ei[e] = idx % kPanelMax;
+    ej[e] = idx / kPanelMax;
+  }
+  __syncthreads();
+  for (int k = 0; k < nbp; ++k) {
+    const double2 rd = s_rd[k & 1];
+    if (tid < nbp) {
+      smu[tid] = (tid == k) ? make_double2(0.0, 0.0) : cmul(A11[tid + k * kP], rd);
+      srk[tid] = A11[k + tid * kP];
+    }
+    __syncthreads();
+    double2 v[kGjEntries];
+#pragma unroll
+    for (int e = 0; e < kGjEntries; ++e) v[e] = A11[ei[e] + ej[e] * kP];
+#pragma unroll
+    for (int e = 0; e < kGjEntries; ++e) {
+      const int i = ei[e], j = ej[e];
+      if (i >= nbp || j >= nbp) continue;
+      if (i != k && j != k) {
+        cfma(v[e], cneg(smu[i]), srk[j]);
+      } else if (i == k && j != k) {
+        v[e] = cmul(srk[j], rd);
+      } else if (i != k) {
+        v[e] = cneg(smu[i]);
+      } else {
+        v[e] = rd;
+      }
+      A11[i + j * kP] = v[e];
+      if (i == k + 1 && j == k + 1) s_rd[(k + 1) & 1] = crcp_newton(v[e]);
+    }
+    __syncthreads();
+  }
+  double2* T = Tinv + size_t(b) * tstride;
+  for (int idx = tid; idx < nbp * nbp; idx += kFactorThreads) T[idx] = A11[(idx % nbp) + (idx / nbp) * kP];
+}
+
 // Row interchanges of a factored panel applied to columns j1 .. 2n-1 (one
 // thread per column, in the order of the pivots)
 __global__ void __launch_bounds__(kApplyThreads)
@@ -1511,15 +1771,70 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     ++launches;
     return gemm_ozaki(g, s);
   };
+  // Blocked Gauss-Jordan (the emulated products, panels of up to 192 rows):
+  // per panel the factor kernel chooses the pivots and forms T = A11^{-1},
+  // the block row becomes T [A12 | B1] and one product eliminates the panel
+  // columns from all other rows; no back substitution follows.
+  if (use_inv && (n + 31) / 32 <= kGjMaxSlots && nb <= kPanelMax) {
+    int blk = 0;
+    for (int j0 = 0; j0 < n; j0 += nb, ++blk) {
+      const int nbp = std::min(nb, n - j0);
+      const int j1 = j0 + nbp;
+      double2* tinv = w->Tinv + size_t(blk) * 2 * kPanelMax * kPanelMax;
+      switch ((n - j0 + 31) / 32) {
+#define TVAP_PANEL_GJ(S)                                                                                      \
+  case S:                                                                                                     \
+    panel_gj_kernel<S><<<G, kFactorThreads, 0, s>>>(n, j0, nbp, w->W, w->piv, c->d_flags, tinv, tstride);   \
+    break;
+        TVAP_PANEL_GJ(1)
+        TVAP_PANEL_GJ(2)
+        TVAP_PANEL_GJ(3)
+        TVAP_PANEL_GJ(4)
+        TVAP_PANEL_GJ(5)
+        TVAP_PANEL_GJ(6)
+#undef TVAP_PANEL_GJ
+        default:
+          return TVAP_ERR_ARG;
+      }
+      if (j1 < 2 * n) {
+        dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, G);
+        panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
+      }
+      launches += 2;
+      if ((rc = block_row_product(blk, 0, j0, nbp, j1))) return rc;
+      // all other rows: W[:, j1:] -= W[:, j0:j1] R (the block rows' panel
+      // entries are zero, so they keep R)
+      GemmArgs g{};
+      g.M = n;
+      g.N = 2 * n - j1;
+      g.K = nbp;
+      g.batch = G;
+      g.A = View{w->W + size_t(j0) * n, 1, n, bsW};
+      g.B = View{w->W + j0 + size_t(j1) * n, 1, n, bsW};
+      g.C = w->W + size_t(j1) * n;
+      g.crs = 1;
+      g.ccs = n;
+      g.cbs = bsW;
+      g.alpha = make_double2(-1.0, 0.0);
+      g.beta = make_double2(1.0, 0.0);
+      g.three_m = true;
+      if ((rc = gemm(g, s))) return rc;
+      ++launches;
+    }
+    const size_t tot = size_t(n) * n * G;
+    thouless_out_kernel<<<nblk(tot, 256), 256, 0, s>>>(n, G, w->W, w->A);
+    TVAP_CUDA(cudaGetLastError());
+    c->kernel_launches += launches + 1;
+    return TVAP_OK;
+  }
   int blk = 0;
   for (int j0 = 0; j0 < n; j0 += nb, ++blk) {
     const int nbp = std::min(nb, n - j0);
     const int j1 = j0 + nbp;
     if (smem_path) {
       const size_t fac_bytes = sizeof(double2) * (size_t(n - j0) * nbp + (use_inv ? 2 * size_t(nbp) * nbp : 0));
-      panel_factor_kernel<<<G, kFactorThreads, fac_bytes, s>>>(
-          n, j0, nbp, w->W, w->piv, c->d_flags,
-          use_inv ? w->Tinv + size_t(blk) * 2 * kPanelMax * kPanelMax : nullptr, tstride);
+      double2* tinv = use_inv ? w->Tinv + size_t(blk) * 2 * kPanelMax * kPanelMax : nullptr;
+      panel_factor_kernel<<<G, kFactorThreads, fac_bytes, s>>>(n, j0, nbp, w->W, w->piv, c->d_flags, tinv, tstride);
       dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, G);
       if (use_inv) {
         panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
@@ -2075,6 +2390,7 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
     // stream and the overlap chain on the third, concurrently; the sums join
     // all three on the caller's stream.
     cudaStream_t sm = c->streamM;
+    sec_mark(c, s);
     TVAP_CUDA(cudaEventRecord(c->ev_fork, s));
     TVAP_CUDA(cudaStreamWaitEvent(s2, c->ev_fork, 0));
     TVAP_CUDA(cudaStreamWaitEvent(sm, c->ev_fork, 0));
@@ -2094,6 +2410,7 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
     if ((rc = angles_sums(c, G, w->weight, w->mult, have_overlap, 0, s))) return rc;
   } else {
     // plain form: one angle per launch sequence
+    sec_mark(c, s);
     if ((rc = prepare_uv_blocks(c, s))) return rc;
     if ((rc = prepare_canonical(c, o.seed_occeps, o.seed_allemp, canon, s))) return rc;
     if (canon[2] && have_overlap) return canon_error();

@@ -55,21 +55,38 @@ void sec_end_on(tvap_ctx* c, int sec, cudaStream_t s) {
     }
 }
 
+void sec_mark(tvap_ctx* c, cudaStream_t s) {
+  if (!c->timing) return;
+  cudaEvent_t a = take_event(c);
+  cudaEventRecord(a, s);
+  c->ev_open.push_back({-1, {a, nullptr}});
+}
+
 void sec_begin(tvap_ctx* c, int sec) { sec_begin_on(c, sec, c->stream); }
 void sec_end(tvap_ctx* c, int sec) { sec_end_on(c, sec, c->stream); }
 
 static void collect_sections(tvap_ctx* c) {
   if (c->ev_open.empty()) return;
   cudaStreamSynchronize(c->stream);
+  cudaEvent_t mark = nullptr;
   for (auto& e : c->ev_open) {
-    if (e.first >= 1000) {
+    if (e.first == -1) {
+      mark = e.second.first;
+    } else if (e.first >= 1000) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e.second.first, e.second.second);
       c->section_ms[e.first - 1000] += ms;
       c->section_calls[e.first - 1000] += 1;
+      if (mark) {
+        float t0 = 0.f, t1 = 0.f;
+        cudaEventElapsedTime(&t0, mark, e.second.first);
+        cudaEventElapsedTime(&t1, mark, e.second.second);
+        c->section_t0[e.first - 1000] += t0;
+        c->section_t1[e.first - 1000] += t1;
+      }
     }
     c->ev_pool.push_back(e.second.first);
-    c->ev_pool.push_back(e.second.second);
+    if (e.second.second) c->ev_pool.push_back(e.second.second);
   }
   c->ev_open.clear();
 }
@@ -130,6 +147,7 @@ int tvap_set_timing(tvap_ctx* c, int on) {
   for (int i = 0; i < 16; ++i) {
     c->section_ms[i] = 0.0;
     c->section_calls[i] = 0;
+    c->section_t0[i] = c->section_t1[i] = 0.0;
   }
   for (long long& v : c->canon_attempts) v = 0;
   return TVAP_OK;
@@ -147,6 +165,17 @@ int tvap_get_timing(tvap_ctx* c, double* ms, long long* calls, int nsec) {
   for (int i = 0; i < nsec && i < 16; ++i) {
     ms[i] = c->section_ms[i];
     if (calls) calls[i] = c->section_calls[i];
+  }
+  return TVAP_OK;
+}
+
+int tvap_get_timeline(tvap_ctx* c, double* t0, double* t1, int nsec) {
+  if (!c || !t0 || !t1) return TVAP_ERR_ARG;
+  collect_sections(c);
+  for (int i = 0; i < nsec && i < 16; ++i) {
+    const double k = c->section_calls[i] ? double(c->section_calls[i]) : 1.0;
+    t0[i] = c->section_t0[i] / k;
+    t1[i] = c->section_t1[i] / k;
   }
   return TVAP_OK;
 }

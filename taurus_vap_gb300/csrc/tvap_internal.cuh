@@ -223,6 +223,8 @@ struct tvap_ctx {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_open;
   double section_ms[16] = {0};
   long long section_calls[16] = {0};
+  // summed start and end offsets of the sections from the last timeline mark
+  double section_t0[16] = {0}, section_t1[16] = {0};
   // work buffer of the per-call entry points (gradient, evolution), grown on
   // demand and reused: no allocation (and no device-wide cudaFree) per call
   double* scratch = nullptr;
@@ -242,6 +244,8 @@ void sec_begin(tvap_ctx* c, int sec);
 void sec_end(tvap_ctx* c, int sec);
 void sec_begin_on(tvap_ctx* c, int sec, cudaStream_t s);
 void sec_end_on(tvap_ctx* c, int sec, cudaStream_t s);
+// origin of the section offsets that follow (the start of a projection)
+void sec_mark(tvap_ctx* c, cudaStream_t s);
 }  // namespace tvap
 
 namespace tvap {

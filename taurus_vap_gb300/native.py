@@ -76,6 +76,8 @@ def lib():
         L.tvap_set_timing.restype = ci
         L.tvap_get_timing.argtypes = [vp, vp, vp, ci]
         L.tvap_get_timing.restype = ci
+        L.tvap_get_timeline.argtypes = [vp, vp, vp, ci]
+        L.tvap_get_timeline.restype = ci
         L.tvap_get_counters.argtypes = [vp, vp, ci]
         L.tvap_get_counters.restype = ci
         L.tvap_set_gemm_mode.argtypes = [vp, ci]
@@ -155,6 +157,14 @@ class Context:
         calls = np.zeros(16, dtype=np.int64)
         _check(lib().tvap_get_timing(self.h, _p(ms), _p(calls), 16), "tvap_get_timing")
         return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(self.SECTIONS)}
+
+    def get_timeline(self):
+        """Mean (start, end) in ms of every timed section from the start of
+        its projection (gradient and evolution: from the projection before)."""
+        t0 = np.zeros(16)
+        t1 = np.zeros(16)
+        _check(lib().tvap_get_timeline(self.h, _p(t0), _p(t1), 16), "tvap_get_timeline")
+        return {k: (float(t0[i]), float(t1[i])) for i, k in enumerate(self.SECTIONS)}
 
     def canonical_paths(self):
         """Canonical-basis counters since the last set_timing: (FP32 Jacobi +
