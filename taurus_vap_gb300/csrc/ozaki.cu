@@ -497,9 +497,11 @@ constexpr int kTcMinTiles = 152;
 
 // The tensor-memory path for one product (mode 2).  Returns TVAP_ERR_ARG
 // without launching anything when the product is not of a supported kind.
+// With upper_only the whole product is formed (the lower triangle is
+// written too; its readers ignore it).
 int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const bool real_scalars = g.alpha.y == 0.0 && g.beta.y == 0.0 && !g.alpha_vec;
-  if (!real_scalars || g.upper_only || (g.a_real && g.b_real && !g.c_real)) return TVAP_ERR_ARG;
+  if (!real_scalars || (g.a_real && g.b_real && !g.c_real)) return TVAP_ERR_ARG;
   const bool a_sh = g.A.bs == 0 && g.batch > 1, b_sh = g.B.bs == 0 && g.batch > 1;
   if (a_sh && b_sh) return TVAP_ERR_ARG;
   // rows of op(A): element (i, k) at A.p[i rs + k cs]; rows of op(B)^T:

@@ -759,33 +759,59 @@ __global__ void schur_kernel(int n2, int nb, int G, const double2* __restrict__ 
 // a serial Jacobi sweep on one SM.  Near-degenerate clusters are
 // diagonalised exactly afterwards (cluster_finish_kernel).
 // ---------------------------------------------------------------------------
-__global__ void refine_lambda_kernel(int n, const double* __restrict__ XtX, const double* __restrict__ S,
-                                     const double* __restrict__ A, double* __restrict__ lam,
-                                     double* __restrict__ rscal) {
-  __shared__ double red[3][256];
-  const int tid = threadIdx.x, nt = blockDim.x;
+constexpr int kRlThreads = 1024;
+__global__ void __launch_bounds__(kRlThreads)
+    refine_lambda_kernel(int n, const double* __restrict__ XtX, const double* __restrict__ S,
+                         const double* __restrict__ A, double* __restrict__ lam, double* __restrict__ rscal) {
+  __shared__ double red[3][kRlThreads / 32];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < n; i += nt) lam[i] = S[i + size_t(i) * n] / XtX[i + size_t(i) * n];
-  __syncthreads();
   double s_off = 0.0, s_r = 0.0, s_a = 0.0;
-  for (size_t e = tid; e < size_t(n) * n; e += nt) {
-    const int i = int(e % n), j = int(e / n);
-    const double r = ((i == j) ? 1.0 : 0.0) - XtX[e];
-    const double so = S[e] - ((i == j) ? lam[i] : 0.0);
-    s_off += so * so;
-    s_r += r * r;
-    s_a += A[e] * A[e];
+  const size_t nn = size_t(n) * n;
+  // four elements in flight per thread
+  for (size_t e0 = tid; e0 < nn; e0 += 4 * size_t(nt)) {
+    double xv[4], sv[4], av[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const size_t e = e0 + size_t(u) * nt;
+      xv[u] = e < nn ? XtX[e] : 0.0;
+      sv[u] = e < nn ? S[e] : 0.0;
+      av[u] = e < nn ? A[e] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const size_t e = e0 + size_t(u) * nt;
+      if (e >= nn) continue;
+      const int i = int(e % n), j = int(e / n);
+      const bool d = (i == j);
+      const double r = (d ? 1.0 : 0.0) - xv[u];
+      // the diagonal of S - diag(l) with l = S_ii / XtX_ii, formed here from
+      // the same operands as lam
+      const double so = d ? sv[u] - sv[u] / xv[u] : sv[u];
+      s_off += so * so;
+      s_r += r * r;
+      s_a += av[u] * av[u];
+    }
   }
-  red[0][tid] = s_off;
-  red[1][tid] = s_r;
-  red[2][tid] = s_a;
+  for (int o = 16; o > 0; o >>= 1) {
+    s_off += __shfl_xor_sync(0xffffffffu, s_off, o);
+    s_r += __shfl_xor_sync(0xffffffffu, s_r, o);
+    s_a += __shfl_xor_sync(0xffffffffu, s_a, o);
+  }
+  if (lane == 0) {
+    red[0][warp] = s_off;
+    red[1][warp] = s_r;
+    red[2][warp] = s_a;
+  }
   __syncthreads();
-  for (int s = nt / 2; s > 0; s >>= 1) {
-    if (tid < s)
-      for (int q = 0; q < 3; ++q) red[q][tid] += red[q][tid + s];
-    __syncthreads();
-  }
   if (tid == 0) {
-    const double nS = sqrt(red[0][0]), nR = sqrt(red[1][0]), nA = sqrt(red[2][0]);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int w2 = 0; w2 < nt / 32; ++w2) {
+      a0 += red[0][w2];
+      a1 += red[1][w2];
+      a2 += red[2][w2];
+    }
+    const double nS = sqrt(a0), nR = sqrt(a1), nA = sqrt(a2);
     rscal[0] = 2.0 * (nS + nA * nR);  // delta
     rscal[1] = nA;
     rscal[2] = nS;
@@ -816,25 +842,99 @@ __global__ void refine_update_kernel(int n, const double* __restrict__ XtX, cons
   M[e] = ((i == j) ? 1.0 : 0.0) + 0.5 * rb + F;
 }
 
+// Cyclic Jacobi of one cluster block a (m x m, m <= M) with its rotations
+// accumulated in q, by one thread: sweeps until the off-diagonal part is at
+// rounding level (at most 30)
+template <int M>
+__device__ void cluster_jacobi(int m, double (&a)[M][M], double (&q)[M][M]) {
+  for (int sweep = 0; sweep < 30 && m > 1; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (int r = 0; r < m; ++r) {
+      dia += a[r][r] * a[r][r];
+      for (int t = r + 1; t < m; ++t) off += a[r][t] * a[r][t];
+    }
+    // converged to rounding: further rotations only move noise
+    if (off <= 1.0e-32 * dia) break;
+    for (int pp = 0; pp < m; ++pp)
+      for (int qq = pp + 1; qq < m; ++qq) {
+        if (a[pp][qq] == 0.0) continue;
+        const double theta = (a[qq][qq] - a[pp][pp]) / (2.0 * a[pp][qq]);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int r = 0; r < m; ++r) {
+          const double ap = a[r][pp], aq = a[r][qq];
+          a[r][pp] = cs * ap - sn * aq;
+          a[r][qq] = sn * ap + cs * aq;
+        }
+        for (int r = 0; r < m; ++r) {
+          const double ap = a[pp][r], aq = a[qq][r];
+          a[pp][r] = cs * ap - sn * aq;
+          a[qq][r] = sn * ap + cs * aq;
+        }
+        for (int r = 0; r < m; ++r) {
+          const double qp = q[r][pp], qv = q[r][qq];
+          q[r][pp] = cs * qp - sn * qv;
+          q[r][qq] = sn * qp + cs * qv;
+        }
+      }
+  }
+}
+
+// One cluster (positions k0 .. k0+m-1 of the sorted order): its block of S,
+// Jacobi, the eigenvalues in ascending order to lsh / the source column of
+// each to osh, the rotation to qb (m x m, column t of the block at t * m)
+template <int M>
+__device__ void cluster_solve(int n, int m, int k0, const double* __restrict__ S, const int* perm, double* lsh,
+                              int* osh, double* qb) {
+  double a[M][M], q[M][M];
+  for (int r = 0; r < m; ++r)
+    for (int t = 0; t < m; ++t) {
+      a[r][t] = S[perm[k0 + r] + size_t(perm[k0 + t]) * n];
+      q[r][t] = (r == t) ? 1.0 : 0.0;
+    }
+  cluster_jacobi<M>(m, a, q);
+  int ord[M];
+  for (int r = 0; r < m; ++r) ord[r] = r;
+  for (int r = 1; r < m; ++r)
+    for (int t = r; t > 0 && a[ord[t]][ord[t]] < a[ord[t - 1]][ord[t - 1]]; --t) {
+      const int x = ord[t];
+      ord[t] = ord[t - 1];
+      ord[t - 1] = x;
+    }
+  for (int r = 0; r < m; ++r) {
+    osh[k0 + r] = ord[r];
+    lsh[k0 + r] = a[ord[r]][ord[r]];
+    for (int t = 0; t < m; ++t) qb[t * m + r] = q[t][r];
+  }
+}
+
 // Sort by eigenvalue, diagonalise clusters of (near-)degenerate eigenvalues
 // exactly with a small Jacobi, verify the off-diagonal coupling between
-// clusters, write D (ascending) and the eigenvalues.  One CTA.
-__global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const double* __restrict__ X,
-                                      const double* __restrict__ rscal, double* __restrict__ D,
-                                      double* __restrict__ evals, int* __restrict__ perm_ws, int* rflag) {
-  __shared__ int cl_start[513];
-  __shared__ int ncl;
-  __shared__ int fail;
-  __shared__ double red[256];
-  const int tid = threadIdx.x, nt = blockDim.x;
-  int* perm = perm_ws;        // sorted position -> original column
-  int* cid = perm_ws + n;     // original column -> cluster id
+// clusters, write D (ascending) and the eigenvalues.  One CTA: the diagonal,
+// the order and the clusters in shared memory, one thread per cluster for
+// the Jacobi, a warp per cluster for the rotation of its columns.
+constexpr int kCfThreads = 512;
+constexpr int kCfMaxN = 512;
+constexpr int kCfQ = 2048;  // rotation entries of all clusters (sum of m^2)
+__global__ void __launch_bounds__(kCfThreads)
+    cluster_finish_kernel(int n, const double* __restrict__ S, const double* __restrict__ X,
+                          const double* __restrict__ rscal, double* __restrict__ D, double* __restrict__ evals,
+                          int* rflag) {
+  constexpr int CM = 8;
+  __shared__ double sd[kCfMaxN], lsh[kCfMaxN];
+  __shared__ int perm[kCfMaxN], cid[kCfMaxN], osh[kCfMaxN], cl_start[kCfMaxN + 1], qoff[kCfMaxN + 1];
+  __shared__ double qbuf[kCfQ];
+  __shared__ int ncl, fail;
+  __shared__ double red[kCfThreads / 32];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
   if (tid == 0) fail = 0;
+  for (int i = tid; i < n; i += nt) sd[i] = S[i + size_t(i) * n];
+  __syncthreads();
   for (int i = tid; i < n; i += nt) {
-    const double v = S[i + size_t(i) * n];
+    const double v = sd[i];
     int rank = 0;
     for (int j = 0; j < n; ++j) {
-      const double u = S[j + size_t(j) * n];
+      const double u = sd[j];
       rank += (u < v || (u == v && j < i)) ? 1 : 0;
     }
     perm[rank] = i;
@@ -846,14 +946,19 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
     int c = 0;
     cl_start[0] = 0;
     for (int k = 0; k < n; ++k) {
-      if (k > 0) {
-        const double gap = S[perm[k] + size_t(perm[k]) * n] - S[perm[k - 1] + size_t(perm[k - 1]) * n];
-        if (gap > tau) cl_start[++c] = k;
-      }
+      if (k > 0 && sd[perm[k]] - sd[perm[k - 1]] > tau) cl_start[++c] = k;
       cid[perm[k]] = c;
     }
     ncl = c + 1;
     cl_start[ncl] = n;
+    int off = 0;
+    for (int q = 0; q < ncl; ++q) {
+      const int m = cl_start[q + 1] - cl_start[q];
+      qoff[q] = off;
+      if (m <= CM) off += m * m;
+    }
+    qoff[ncl] = off;
+    if (off > kCfQ) fail |= 4;
   }
   __syncthreads();
   // coupling between different clusters must be negligible
@@ -862,110 +967,59 @@ __global__ void cluster_finish_kernel(int n, const double* __restrict__ S, const
     const int i = int(e % n), j = int(e / n);
     if (cid[i] != cid[j]) mx = fmax(mx, fabs(S[e]));
   }
-  red[tid] = mx;
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) red[warp] = mx;
   __syncthreads();
-  for (int s = nt / 2; s > 0; s >>= 1) {
-    if (tid < s) red[tid] = fmax(red[tid], red[tid + s]);
-    __syncthreads();
-  }
   // X orthonormal and X^T A X block diagonal over clusters <=> invariant subspaces
   if (tid == 0) {
-    if (red[0] > 1.0e-12 * fmax(nA, 1e-300)) fail |= 1;  // clusters still coupled
+    double m2 = 0.0;
+    for (int w2 = 0; w2 < nwarp; ++w2) m2 = fmax(m2, red[w2]);
+    if (m2 > 1.0e-12 * fmax(nA, 1e-300)) fail |= 1;  // clusters still coupled
     if (rscal[3] > 1.0e-12 * sqrt(double(n))) fail |= 2;  // not orthonormal
   }
-  __syncthreads();
-  // per cluster: Jacobi on the cluster block (lane 0), then the warp rotates
-  // the cluster's columns of X into D
-  constexpr int CM = 8;
-  __shared__ double qsh[8][CM * CM];
-  __shared__ double lsh[8][CM];
-  __shared__ int osh[8][CM];
-  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  for (int cbase = 0; cbase < ncl; cbase += nwarp) {
-    const int c = cbase + warp;
-    int k0 = 0, m = 0;
-    if (c < ncl) {
-      k0 = cl_start[c];
-      m = cl_start[c + 1] - k0;
-    }
-    if (c < ncl && lane == 0) {
-      if (m > CM) {
-        atomicOr(&fail, 4);  // cluster too large
+  const bool qfit = qoff[ncl] <= kCfQ;
+  for (int c = tid; c < ncl; c += nt) {
+    const int k0 = cl_start[c], m = cl_start[c + 1] - k0;
+    if (m > CM) {
+      atomicOr(&fail, 4);  // cluster too large
+    } else if (qfit) {
+      double* qb = qbuf + qoff[c];
+      if (m == 1) {
+        osh[k0] = 0;
+        lsh[k0] = sd[perm[k0]];
+        qb[0] = 1.0;
+      } else if (m == 2) {
+        cluster_solve<2>(n, m, k0, S, perm, lsh, osh, qb);
+      } else if (m <= 4) {
+        cluster_solve<4>(n, m, k0, S, perm, lsh, osh, qb);
       } else {
-        double a[CM][CM], q[CM][CM];
-        for (int r = 0; r < m; ++r)
-          for (int t = 0; t < m; ++t) {
-            a[r][t] = S[perm[k0 + r] + size_t(perm[k0 + t]) * n];
-            q[r][t] = (r == t) ? 1.0 : 0.0;
-          }
-        for (int sweep = 0; sweep < 30 && m > 1; ++sweep) {
-          double off = 0.0, dia = 0.0;
-          for (int r = 0; r < m; ++r) {
-            dia += a[r][r] * a[r][r];
-            for (int t = r + 1; t < m; ++t) off += a[r][t] * a[r][t];
-          }
-          // converged to rounding: further rotations only move noise
-          if (off <= 1.0e-32 * dia) break;
-          for (int pp = 0; pp < m; ++pp)
-            for (int qq = pp + 1; qq < m; ++qq) {
-              if (a[pp][qq] == 0.0) continue;
-              const double theta = (a[qq][qq] - a[pp][pp]) / (2.0 * a[pp][qq]);
-              const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-              const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
-              for (int r = 0; r < m; ++r) {
-                const double ap = a[r][pp], aq = a[r][qq];
-                a[r][pp] = cs * ap - sn * aq;
-                a[r][qq] = sn * ap + cs * aq;
-              }
-              for (int r = 0; r < m; ++r) {
-                const double ap = a[pp][r], aq = a[qq][r];
-                a[pp][r] = cs * ap - sn * aq;
-                a[qq][r] = sn * ap + cs * aq;
-              }
-              for (int r = 0; r < m; ++r) {
-                const double qp = q[r][pp], qv = q[r][qq];
-                q[r][pp] = cs * qp - sn * qv;
-                q[r][qq] = sn * qp + cs * qv;
-              }
-            }
-        }
-        int ord[CM];
-        for (int r = 0; r < m; ++r) ord[r] = r;
-        for (int r = 1; r < m; ++r)
-          for (int t = r; t > 0 && a[ord[t]][ord[t]] < a[ord[t - 1]][ord[t - 1]]; --t) {
-            const int x = ord[t];
-            ord[t] = ord[t - 1];
-            ord[t - 1] = x;
-          }
-        for (int r = 0; r < m; ++r) {
-          osh[warp][r] = ord[r];
-          lsh[warp][r] = a[ord[r]][ord[r]];
-          for (int t = 0; t < m; ++t) qsh[warp][t * CM + r] = q[t][r];
-        }
+        cluster_solve<CM>(n, m, k0, S, perm, lsh, osh, qb);
       }
     }
-    __syncwarp();
-    if (c < ncl && m > CM) {
+  }
+  __syncthreads();
+  for (int c = warp; c < ncl; c += nwarp) {
+    const int k0 = cl_start[c], m = cl_start[c + 1] - k0;
+    if (m > CM || !qfit) {
       // too large to diagonalise here (the attempt fails): the refined
       // columns go to D unrotated, so that D stays an orthonormal basis to
       // start the next attempt from
       for (int r = 0; r < m; ++r) {
-        if (lane == 0) evals[k0 + r] = S[perm[k0 + r] + size_t(perm[k0 + r]) * n];
+        if (lane == 0) evals[k0 + r] = sd[perm[k0 + r]];
         for (int row = lane; row < n; row += 32) D[row + size_t(k0 + r) * n] = X[row + size_t(perm[k0 + r]) * n];
       }
-    }
-    if (c < ncl && m <= CM) {
+    } else {
+      const double* qb = qbuf + qoff[c];
       for (int r = 0; r < m; ++r) {
-        const int src = osh[warp][r];
-        if (lane == 0) evals[k0 + r] = lsh[warp][r];
+        const int src = osh[k0 + r];
+        if (lane == 0) evals[k0 + r] = lsh[k0 + r];
         for (int row = lane; row < n; row += 32) {
           double v = 0.0;
-          for (int t = 0; t < m; ++t) v = fma(X[row + size_t(perm[k0 + t]) * n], qsh[warp][t * CM + src], v);
+          for (int t = 0; t < m; ++t) v = fma(X[row + size_t(perm[k0 + t]) * n], qb[t * m + src], v);
           D[row + size_t(k0 + r) * n] = v;
         }
       }
     }
-    __syncwarp();
   }
   __syncthreads();
   if (tid == 0) rflag[0] = fail;
@@ -1935,15 +1989,14 @@ int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, c
   for (int step = 0; step < steps; ++step) {
     const View Xv = view_cm(X, n, 0);
     if ((rc = gram(X))) return rc;
-    refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+    refine_lambda_kernel<<<1, kRlThreads, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
     refine_update_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
     if ((rc = real_gemm(n, n, n, Xv, view_cm(w->Mr, n, 0), Xn, n, 1.0, 0.0, s))) return rc;
     std::swap(X, Xn);
   }
   if ((rc = gram(X))) return rc;
-  refine_lambda_kernel<<<1, 256, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
-  cluster_finish_kernel<<<1, 256, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals,
-                                          reinterpret_cast<int*>(w->jwork), w->rflag);
+  refine_lambda_kernel<<<1, kRlThreads, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+  cluster_finish_kernel<<<1, kCfThreads, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals, w->rflag);
   TVAP_CUDA(cudaGetLastError());
   c->kernel_launches += steps * 5 + 4;
   int hr[2] = {1, 0};
@@ -1971,7 +2024,7 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   int rc, fail = 1;
-  if (jacobi32_smem_bytes(n) <= jacobi32_smem_limit()) {
+  if (jacobi32_smem_bytes(n) <= jacobi32_smem_limit() && n <= kCfMaxN) {
     double* X = w->Xr;
     double* Xn = w->Xn;
     const View Rho = view_cm(w->rho, n, 0);

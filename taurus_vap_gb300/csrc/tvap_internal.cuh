@@ -96,7 +96,7 @@ struct GemmArgs {
   bool a_real, b_real, c_real;
   bool conj_a, conj_b;
   bool three_m;     // complex x complex with three real products (3M)
-  bool upper_only;  // square tiles strictly below the diagonal are skipped
+  bool upper_only;  // only the upper triangle is needed (the mma.sync path skips tiles below it)
   // optional second term along K: C = alpha (op(A) op(B) + s2 op(A2) op(B2))
   // + beta C with A2 (M x K2) and B2 (K2 x N) of the types and conjugations
   // of A and B.  The tcgen05 path forms it as one product over K + K2 (the
