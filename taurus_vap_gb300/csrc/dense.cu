@@ -453,6 +453,8 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
   double2* xcol = pk + size_t(N) * (N + 1) / 2;  // 1-based, N + 1 entries
   double2* ycol = xcol + N + 1;
   double2* pivs = ycol + N + 1;                  // N / 2 pivots, then N / 2 signs in .x of the next slots
+  double2* tt1 = pivs + N;                       // alpha y_J and alpha x_J, 1-based
+  double2* tt2 = tt1 + N + 1;
   __shared__ long long wv[kPfThreads / 32];
   __shared__ int wi[kPfThreads / 32];
   __shared__ int s_kp;
@@ -537,25 +539,59 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
       const double2 piv = a(K - 1, K);
       pivs[steps] = piv;
       pivs[N / 2 + steps] = make_double2(KP != KK ? -1.0 : 1.0, 0.0);
-      s_alpha = crcp(piv);
-    }
-    for (int i = 1 + tid; i <= nn; i += nt) {
-      xcol[i] = a(i, K);
-      ycol[i] = a(i, K - 1);
+      s_alpha = crcp_newton(piv);
     }
     __syncthreads();
-    const double2 alpha = s_alpha;
-    // A(I,J) += X(I) (alpha Y(J)) - Y(I) (alpha X(J)), I < J <= nn
-    for (int J = 2 + warp; J <= nn; J += nw) {
-      const double2 xj = xcol[J], yj = ycol[J];
-      if (xj.x == 0.0 && xj.y == 0.0 && yj.x == 0.0 && yj.y == 0.0) continue;
-      const double2 t1 = cmul(alpha, yj), t2 = cmul(alpha, xj);
-      double2* colJ = &a(1, J);
-      for (int I = 1 + lane; I <= J - 1; I += 32) {
-        double2 v = colJ[I - 1];
-        cfma(v, xcol[I], t1);
-        cfma(v, cneg(ycol[I]), t2);
-        colJ[I - 1] = v;
+    // the two columns and their products with alpha, once per step (threads
+    // over the entries: the FP64 pipe is the bottleneck of this kernel)
+    {
+      const double2 alpha = s_alpha;
+      for (int i = 1 + tid; i <= nn; i += nt) {
+        const double2 x = a(i, K), y = a(i, K - 1);
+        xcol[i] = x;
+        ycol[i] = y;
+        tt1[i] = cmul(alpha, y);
+        tt2[i] = cmul(alpha, x);
+      }
+    }
+    __syncthreads();
+    // A(I,J) += X(I) (alpha Y(J)) - Y(I) (alpha X(J)), I < J <= nn: a warp
+    // per pair of columns J1 = 2 + p and J2 = nn - p (about nn entries
+    // together), lanes over the pair's entries, two entries in flight
+    for (int p = warp; p < nn / 2; p += nw) {
+      const int J1 = 2 + p, J2 = nn - p;
+      const int L1 = J1 - 1, L = L1 + (J2 > J1 ? J2 - 1 : 0);
+      for (int f0 = lane; f0 < L; f0 += 64) {
+        int I[2], J[2];
+        double2 v[2], x[2], y[2], t1[2], t2[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int f = f0 + 32 * u;
+          const bool first = f < L1;
+          I[u] = first ? f + 1 : f - L1 + 1;
+          J[u] = first ? J1 : J2;
+          if (f < L) {
+            v[u] = a(I[u], J[u]);
+            x[u] = xcol[I[u]];
+            y[u] = ycol[I[u]];
+            t1[u] = tt1[J[u]];
+            t2[u] = tt2[J[u]];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (f0 + 32 * u >= L) continue;
+          double2 w = v[u];
+          w.x = fma(x[u].x, t1[u].x, w.x);
+          w.x = fma(-x[u].y, t1[u].y, w.x);
+          w.y = fma(x[u].x, t1[u].y, w.y);
+          w.y = fma(x[u].y, t1[u].x, w.y);
+          w.x = fma(-y[u].x, t2[u].x, w.x);
+          w.x = fma(y[u].y, t2[u].y, w.x);
+          w.y = fma(-y[u].x, t2[u].y, w.y);
+          w.y = fma(-y[u].y, t2[u].x, w.y);
+          a(I[u], J[u]) = w;
+        }
       }
     }
     __syncthreads();
@@ -592,7 +628,7 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
 
 int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s) {
   if (n > 512 || (n & 1)) return TVAP_ERR_ARG;
-  const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 2 * size_t(n + 1) + size_t(n));
+  const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 4 * size_t(n + 1) + size_t(n));
   if (shm <= jacobi32_smem_limit()) {
     static bool attr = false;
     if (!attr) {

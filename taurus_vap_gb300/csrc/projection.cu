@@ -1370,20 +1370,6 @@ __device__ __forceinline__ void warp_argmax_key_all(int& v, int& i) {
   }
 }
 
-// 1/z = conj(z) / |z|^2 with |z|^2 inverted by two Newton steps from the
-// single-precision reciprocal (relative error a few units of the last
-// place); outside the safe range the scaled division (crcp)
-__device__ __forceinline__ double2 crcp_newton(double2 z) {
-  const double d = fma(z.x, z.x, z.y * z.y);
-  if (!(d > 1.0e-30 && d < 1.0e30)) return crcp(z);
-  double y = double(__frcp_rn(float(d)));
-  double e = fma(-d, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-d, y, 1.0);
-  y = fma(y, e, y);
-  return make_double2(z.x * y, -z.y * y);
-}
-
 template <int SLOTS>
 __device__ __forceinline__ float2 slot_get(const float2 (&a)[SLOTS], int s) {
   float2 v = a[0];
