@@ -280,7 +280,9 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
       if (jr >= 2 * ncols_tot) break;
       const int comp = jr >= ncols_tot ? 1 : 0;
       const int j = jr - comp * ncols_tot;
-      const double v = oztc::value(acc, c) * oz::pow2(eai + col_exp(eb_enc, j));
+      double v;
+      if (!oztc::scaled(acc.h[c], acc.l[c], eai + col_exp(eb_enc, j), false, v))
+        v = oztc::value(acc, c) * oz::pow2(eai + col_exp(eb_enc, j));
       if (!DELTA) {
         reinterpret_cast<double*>(out0)[((long long)p * ldc + j) * 2 + comp] = v;
         reinterpret_cast<double*>(out1)[((long long)p * ldc + j) * 2 + comp] = v + h1[comp];

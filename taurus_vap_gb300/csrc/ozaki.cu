@@ -384,11 +384,19 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
       if (col >= o.b_rows || (comp > 0 && o.c_real)) return -1;
       return (i * o.crs + j * o.ccs + b * o.cbs) * cw + comp;
     };
+    // alpha = +-1 (nearly every product) is a sign of the integer
+    // conversion; any other alpha one product more
+    const bool unit = o.alpha == 1.0 || o.alpha == -1.0;
+    const bool neg = o.alpha < 0.0;
     double v[16];
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const int e = (col0 + c < o.b_rows) ? ebz[col0 + c] : 0;
-      v[c] = oztc::value(acc, c) * (o.alpha * oz::pow2(eai + e));
+      double x;
+      if (oztc::scaled(acc.h[c], acc.l[c], eai + e, unit && neg, x))
+        v[c] = unit ? x : x * o.alpha;
+      else
+        v[c] = oztc::value(acc, c) * (o.alpha * oz::pow2(eai + e));
     }
     // two groups of 8: the loads of a group are in flight together
 #pragma unroll

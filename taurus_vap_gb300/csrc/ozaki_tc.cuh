@@ -34,6 +34,7 @@
 // tensor memory; the kernel then reports through the status word.
 #pragma once
 
+#include "ozaki_scaled.h"
 #include "ozaki_core.cuh"
 
 namespace tvap {
@@ -389,6 +390,7 @@ __device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char*
 
 // value of column c (0..15 of the thread's quarter) before the exponent scale
 __device__ __forceinline__ double value(const Acc& o, int c) { return fma(double(o.h[c]), 0x1p28, double(o.l[c])); }
+
 
 #endif  // __CUDACC__
 
