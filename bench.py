@@ -156,13 +156,16 @@ def host_iteration(ctx, state, mode):
     return (U1, V1, Zi), (pnp.c("ener") / pnp.c("over")).real
 
 
-# DRAM bytes (read + write) of one H20-shaped ozaki_tc_kernel launch at
-# n = 140, G = 113, from `ncu --set full` (profiles/ozaki_tc_h20_emax4.md)
-H20_TRAFFIC_PER_LAUNCH = 325.4e6
+# DRAM bytes (read + write) per H20 ozaki_tc_kernel launch at n = 140,
+# G = 113: the mean of ncu's dram__bytes_read.sum + dram__bytes_write.sum over
+# the three launches of one projection (646.2, 325.3 and 642.6 MB)
+H20_TRAFFIC_PER_LAUNCH = 538.0e6
 
 
 def fp64_flops_per_iteration(n, G):
-    """Algorithmic FP64 flops of the reduced per-angle formulation."""
+    """Algorithmic FP64 flops of the reduced per-angle formulation: solve
+    10.7 n^3, U~/V~ 8 n^3, densities 12 n^3, H20 40 n^3, overlap product 4 n^3,
+    Pfaffian 1.4 n^3 per angle."""
     return G * (10.7 + 8 + 12 + 40 + 4 + 1.4) * n ** 3
 
 
