@@ -254,6 +254,7 @@ int pick_tile(int M, int N) {
 }  // namespace
 
 int g_gemm_mode = 2;
+int g_tc_grid_cap = 0;
 int* g_dev_flags = nullptr;
 tvap_ctx* g_tc_timing_ctx = nullptr;
 int g_tc_timing_sec = -1;

@@ -614,7 +614,7 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   static int sms = 0;
   if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
   const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / oztc::kN) * a_slots;
-  const int grid = int(std::min<long long>(ntiles, sms));
+  const int grid = int(std::min<long long>(ntiles, g_tc_grid_cap > 0 ? std::min(sms, g_tc_grid_cap) : sms));
   TVAP_CUDA(cudaMemsetAsync(sc->counter, 0, sizeof(int), s));
   if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   ozaki_tc_kernel<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,

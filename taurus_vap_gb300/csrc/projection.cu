@@ -93,7 +93,7 @@ int dalloc(T** p, size_t count, size_t& total) {
   return TVAP_OK;
 }
 
-constexpr int kPanelMax = 32;  // columns per panel of the Thouless LU
+constexpr int kPanelMax = 32;  // columns per panel of the Thouless solve
 
 // double2 entries per angle of Workspace::Tinv
 size_t tinv_stride(int n) { return size_t((n + kPanelMax - 1) / kPanelMax) * 2 * kPanelMax * kPanelMax; }
@@ -1400,7 +1400,7 @@ __device__ __forceinline__ float2 fcmul(float2 a, float2 b) {
 }
 
 constexpr int kGjMaxSlots = 6;  // panels of up to 192 rows
-constexpr int kGjEntries = kPanelMax * kPanelMax / kFactorThreads;  // block entries per thread
+constexpr int kGjEntries = (kPanelMax * kPanelMax + kFactorThreads - 1) / kFactorThreads;  // block entries per thread
 
 template <int SLOTS>
 __global__ void __launch_bounds__(kFactorThreads)
@@ -1408,8 +1408,7 @@ __global__ void __launch_bounds__(kFactorThreads)
                     double2* __restrict__ Tinv, long long tstride) {
   constexpr int kQ = kPanelMax / 8;
   constexpr int kP = kPanelMax + 1;
-  static_assert(kFactorThreads == 256 && kGjEntries * kFactorThreads == kPanelMax * kPanelMax,
-                "eight warps hold the panel's columns; the block's entries divide evenly");
+  static_assert(kFactorThreads == 256 && kPanelMax % 8 == 0, "eight warps hold the panel's columns");
   __shared__ float2 scol[2][32 * SLOTS];
   __shared__ float2 s_rp[2];
   __shared__ int s_piv[2];
@@ -1545,12 +1544,14 @@ __global__ void __launch_bounds__(kFactorThreads)
   // of the pivot (formed by the owner of that entry at the end of the step
   // before), multipliers and the pivot row staged, then every entry at once
   if (tid == 0) s_rd[0] = crcp_newton(A11[0]);
+  // entries of the nbp x nbp block, kGjEntries per thread (ei = nbp: none)
   int ei[kGjEntries], ej[kGjEntries];
 #pragma unroll
   for (int e = 0; e < kGjEntries; ++e) {
     const int idx = tid + e * kFactorThreads;
-    ei[e] = idx % kPanelMax;
-    ej[e] = idx / kPanelMax;
+    const bool in = idx < nbp * nbp;
+    ei[e] = in ? idx % nbp : nbp;
+    ej[e] = in ? idx / nbp : 0;
   }
   __syncthreads();
   for (int k = 0; k < nbp; ++k) {
@@ -1562,11 +1563,11 @@ __global__ void __launch_bounds__(kFactorThreads)
     __syncthreads();
     double2 v[kGjEntries];
 #pragma unroll
-    for (int e = 0; e < kGjEntries; ++e) v[e] = A11[ei[e] + ej[e] * kP];
+    for (int e = 0; e < kGjEntries; ++e) v[e] = (ei[e] < nbp) ? A11[ei[e] + ej[e] * kP] : make_double2(0.0, 0.0);
 #pragma unroll
     for (int e = 0; e < kGjEntries; ++e) {
       const int i = ei[e], j = ej[e];
-      if (i >= nbp || j >= nbp) continue;
+      if (i >= nbp) continue;
       if (i != k && j != k) {
         cfma(v[e], cneg(smu[i]), srk[j]);
       } else if (i == k && j != k) {
@@ -1757,6 +1758,89 @@ int real_gemm(int M, int N, int K, View A, View B, double* C, int ldc, double al
 }  // namespace
 
 
+// Gauss-Jordan solve of angles [g0, g0 + gc) on stream s (panels of nb
+// columns); ev_first, when given, is recorded after the first panel's
+// factorisation.  build_augmented_kernel has filled W.
+int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEvent_t ev_first) {
+  Workspace* w = c->ws;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  const long long bsW = 2LL * n * n;
+  const long long tstride = (long long)tinv_stride(n);
+  double2* W = w->W + size_t(g0) * 2 * nn;
+  int* piv = w->piv + size_t(g0) * n;
+  double2* Tinv = w->Tinv + size_t(g0) * tstride;
+  int rc, launches = 0, blk = 0;
+  for (int j0 = 0; j0 < n; j0 += nb, ++blk) {
+    const int nbp = std::min(nb, n - j0);
+    const int j1 = j0 + nbp;
+    double2* tinv = Tinv + size_t(blk) * 2 * kPanelMax * kPanelMax;
+    switch ((n - j0 + 31) / 32) {
+#define TVAP_PANEL_GJ(S)                                                                                 \
+  case S:                                                                                                \
+    panel_gj_kernel<S><<<gc, kFactorThreads, 0, s>>>(n, j0, nbp, W, piv, c->d_flags, tinv, tstride);    \
+    break;
+      TVAP_PANEL_GJ(1)
+      TVAP_PANEL_GJ(2)
+      TVAP_PANEL_GJ(3)
+      TVAP_PANEL_GJ(4)
+      TVAP_PANEL_GJ(5)
+      TVAP_PANEL_GJ(6)
+#undef TVAP_PANEL_GJ
+      default:
+        return TVAP_ERR_ARG;
+    }
+    if (j0 == 0 && ev_first) TVAP_CUDA(cudaEventRecord(ev_first, s));
+    if (j1 < 2 * n) {
+      dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, gc);
+      panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, W, piv);
+    }
+    launches += 2;
+    // the block row: R = T [A12 | B1] in place (the operands are split into
+    // digit planes before the product is formed)
+    {
+      GemmArgs g{};
+      g.M = nbp;
+      g.N = 2 * n - j1;
+      g.K = nbp;
+      g.batch = gc;
+      g.A = View{tinv, 1, nbp, tstride};
+      g.B = View{W + j0 + size_t(j1) * n, 1, n, bsW};
+      g.C = W + j0 + size_t(j1) * n;
+      g.crs = 1;
+      g.ccs = n;
+      g.cbs = bsW;
+      g.alpha = make_double2(1.0, 0.0);
+      g.beta = make_double2(0.0, 0.0);
+      if ((rc = gemm_ozaki(g, s))) return rc;
+      ++launches;
+    }
+    // all other rows: W[:, j1:] -= W[:, j0:j1] R (the block rows' panel
+    // entries are zero, so they keep R)
+    GemmArgs g{};
+    g.M = n;
+    g.N = 2 * n - j1;
+    g.K = nbp;
+    g.batch = gc;
+    g.A = View{W + size_t(j0) * n, 1, n, bsW};
+    g.B = View{W + j0 + size_t(j1) * n, 1, n, bsW};
+    g.C = W + size_t(j1) * n;
+    g.crs = 1;
+    g.ccs = n;
+    g.cbs = bsW;
+    g.alpha = make_double2(-1.0, 0.0);
+    g.beta = make_double2(1.0, 0.0);
+    g.three_m = true;
+    if ((rc = gemm(g, s))) return rc;
+    ++launches;
+  }
+  const size_t tot = nn * gc;
+  thouless_out_kernel<<<nblk(tot, 256), 256, 0, s>>>(n, gc, W, w->A + size_t(g0) * nn);
+  TVAP_CUDA(cudaGetLastError());
+  c->kernel_launches += launches + 1;
+  return TVAP_OK;
+}
+
 int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
   Workspace* w = c->ws;
   const int n = c->n;
@@ -1816,55 +1900,24 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
   // the block row becomes T [A12 | B1] and one product eliminates the panel
   // columns from all other rows; no back substitution follows.
   if (use_inv && (n + 31) / 32 <= kGjMaxSlots && nb <= kPanelMax) {
-    int blk = 0;
-    for (int j0 = 0; j0 < n; j0 += nb, ++blk) {
-      const int nbp = std::min(nb, n - j0);
-      const int j1 = j0 + nbp;
-      double2* tinv = w->Tinv + size_t(blk) * 2 * kPanelMax * kPanelMax;
-      switch ((n - j0 + 31) / 32) {
-#define TVAP_PANEL_GJ(S)                                                                                      \
-  case S:                                                                                                     \
-    panel_gj_kernel<S><<<G, kFactorThreads, 0, s>>>(n, j0, nbp, w->W, w->piv, c->d_flags, tinv, tstride);   \
-    break;
-        TVAP_PANEL_GJ(1)
-        TVAP_PANEL_GJ(2)
-        TVAP_PANEL_GJ(3)
-        TVAP_PANEL_GJ(4)
-        TVAP_PANEL_GJ(5)
-        TVAP_PANEL_GJ(6)
-#undef TVAP_PANEL_GJ
-        default:
-          return TVAP_ERR_ARG;
-      }
-      if (j1 < 2 * n) {
-        dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, G);
-        panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
-      }
-      launches += 2;
-      if ((rc = block_row_product(blk, 0, j0, nbp, j1))) return rc;
-      // all other rows: W[:, j1:] -= W[:, j0:j1] R (the block rows' panel
-      // entries are zero, so they keep R)
-      GemmArgs g{};
-      g.M = n;
-      g.N = 2 * n - j1;
-      g.K = nbp;
-      g.batch = G;
-      g.A = View{w->W + size_t(j0) * n, 1, n, bsW};
-      g.B = View{w->W + j0 + size_t(j1) * n, 1, n, bsW};
-      g.C = w->W + size_t(j1) * n;
-      g.crs = 1;
-      g.ccs = n;
-      g.cbs = bsW;
-      g.alpha = make_double2(-1.0, 0.0);
-      g.beta = make_double2(1.0, 0.0);
-      g.three_m = true;
-      if ((rc = gemm(g, s))) return rc;
-      ++launches;
-    }
-    const size_t tot = size_t(n) * n * G;
-    thouless_out_kernel<<<nblk(tot, 256), 256, 0, s>>>(n, G, w->W, w->A);
-    TVAP_CUDA(cudaGetLastError());
-    c->kernel_launches += launches + 1;
+    // Two halves of the angles on two streams, the second started after the
+    // first half's first panel: a panel factorisation takes the same time
+    // for any number of angles (one CTA each, latency-bound), so one half's
+    // factorisation runs beside the other half's products.  The products
+    // leave SMs for it (their CTAs are capped at the SMs the other half's
+    // panels do not hold: a panel CTA and a product CTA do not fit one SM).
+    c->kernel_launches += 1;  // build_augmented_kernel
+    const bool split = c->streamM2 && G >= 32;
+    if (!split) return gj_solve_range(c, 0, G, nb, s, nullptr);
+    static int sms = 0;
+    if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+    const int G1 = (G + 1) / 2, G2 = G - G1;
+    TcGridCap cap(std::max(sms - G1, sms / 2));
+    if ((rc = gj_solve_range(c, 0, G1, nb, s, c->ev_stagger))) return rc;
+    TVAP_CUDA(cudaStreamWaitEvent(c->streamM2, c->ev_stagger, 0));
+    if ((rc = gj_solve_range(c, G1, G2, nb, c->streamM2, nullptr))) return rc;
+    TVAP_CUDA(cudaEventRecord(c->ev_join2, c->streamM2));
+    TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join2, 0));
     return TVAP_OK;
   }
   int blk = 0;

@@ -232,7 +232,11 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
   const int prio_mid = prio_hi + (prio_lo - prio_hi) / 2;
   if ((e = cudaStreamCreateWithPriority(&c->streamM, cudaStreamNonBlocking, prio_mid)) != cudaSuccess)
     return fail(e);
+  if ((e = cudaStreamCreateWithPriority(&c->streamM2, cudaStreamNonBlocking, prio_mid)) != cudaSuccess)
+    return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_stagger, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_canon, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
@@ -257,6 +261,7 @@ void tvap_destroy(tvap_ctx* c) {
   if (c->stream2) cudaStreamSynchronize(c->stream2);
   if (c->stream3) cudaStreamSynchronize(c->stream3);
   if (c->streamM) cudaStreamSynchronize(c->streamM);
+  if (c->streamM2) cudaStreamSynchronize(c->streamM2);
   cudaFree(c->scratch);
   destroy_workspace(c);
   free_field_csr(c->csr);
@@ -271,18 +276,22 @@ void tvap_destroy(tvap_ctx* c) {
   cudaFree(c->d_bar);
   for (auto& e : c->ev_open) {
     cudaEventDestroy(e.second.first);
-    cudaEventDestroy(e.second.second);
+    if (e.second.second) cudaEventDestroy(e.second.second);
   }
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   if (c->stream) oz_release(c->stream);
   if (c->stream2) oz_release(c->stream2);
   if (c->stream3) oz_release(c->stream3);
   if (c->streamM) oz_release(c->streamM);
+  if (c->streamM2) oz_release(c->streamM2);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->stream3) cudaStreamDestroy(c->stream3);
   if (c->streamM) cudaStreamDestroy(c->streamM);
+  if (c->streamM2) cudaStreamDestroy(c->streamM2);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_stagger) cudaEventDestroy(c->ev_stagger);
+  if (c->ev_join2) cudaEventDestroy(c->ev_join2);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_main) cudaEventDestroy(c->ev_main);
   if (c->ev_canon) cudaEventDestroy(c->ev_canon);

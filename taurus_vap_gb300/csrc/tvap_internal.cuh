@@ -132,6 +132,14 @@ int oz_scratch(cudaStream_t s, size_t bytes, size_t ex_count, __nv_bfloat16** bu
 // mma.sync, 2 emulated with tcgen05 (set by every C-ABI entry point from its
 // context), and the status word of that context
 extern int g_gemm_mode;
+// upper bound on the CTAs of a tcgen05 product (0: one per SM), set while
+// two streams share the SMs with kernels that need their own
+extern int g_tc_grid_cap;
+struct TcGridCap {
+  int saved;
+  explicit TcGridCap(int cap) : saved(g_tc_grid_cap) { g_tc_grid_cap = cap; }
+  ~TcGridCap() { g_tc_grid_cap = saved; }
+};
 extern int* g_dev_flags;
 // when set, the tensor-memory product launches are timed into this section
 // of this context (the H20 products; the host issues them one after the other)
@@ -226,7 +234,9 @@ struct tvap_ctx {
   cudaStream_t stream2 = nullptr;  // canonical basis (high priority), concurrent with the Thouless chain
   cudaStream_t stream3 = nullptr;  // overlap chain and Pfaffians (lowest priority)
   cudaStream_t streamM = nullptr;  // Thouless chain of the projection (priority between the two)
+  cudaStream_t streamM2 = nullptr;  // second half of the angles in the Thouless solve (same priority)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_canon = nullptr, ev_main = nullptr;
+  cudaEvent_t ev_stagger = nullptr, ev_join2 = nullptr;  // the two halves of the Thouless solve
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
   unsigned* d_bar = nullptr;  // grid-barrier state of the cooperative kernels (3 words)
