@@ -335,6 +335,7 @@ struct TcOut {
 // order from *counter; tile numbers run over the N tiles fastest, then the M
 // tiles, then the slots, so that the CTAs working at one time share their A
 // and B tiles through L2.
+template <bool UNIT>
 __global__ void __launch_bounds__(oztc::kThreads, 1)
     ozaki_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ ea, int a_rows_pad,
                     const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb, int b_rows_pad, int b_shared,
@@ -386,15 +387,17 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
     };
     // alpha = +-1 (nearly every product) is a sign of the integer
     // conversion; any other alpha one product more
-    const bool unit = o.alpha == 1.0 || o.alpha == -1.0;
+    // UNIT: alpha = +-1 (every product of the path), a sign of the integer
+    // conversion; otherwise one product more (a separate instantiation, so
+    // that no FP64 multiply is predicated into the common case)
     const bool neg = o.alpha < 0.0;
     double v[16];
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const int e = (col0 + c < o.b_rows) ? ebz[col0 + c] : 0;
       double x;
-      if (oztc::scaled(acc.h[c], acc.l[c], eai + e, unit && neg, x))
-        v[c] = unit ? x : x * o.alpha;
+      if (oztc::scaled(acc.h[c], acc.l[c], eai + e, UNIT && neg, x))
+        v[c] = UNIT ? x : x * o.alpha;
       else
         v[c] = oztc::value(acc, c) * (o.alpha * oz::pow2(eai + e));
     }
@@ -503,6 +506,8 @@ namespace {
 
 constexpr int kTcMinTiles = 152;
 
+inline bool g_alpha_unit(double a) { return a == 1.0 || a == -1.0; }
+
 // The tensor-memory path for one product (mode 2).  Returns TVAP_ERR_ARG
 // without launching anything when the product is not of a supported kind.
 // With upper_only the whole product is formed (the lower triangle is
@@ -607,7 +612,9 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   o.nstack = xa.nstack;
   static bool attr = false;
   if (!attr) {
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(oztc::kSmemBytes)));
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    int(oztc::kSmemBytes)));
     attr = true;
   }
@@ -617,7 +624,13 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const int grid = int(std::min<long long>(ntiles, g_tc_grid_cap > 0 ? std::min(sms, g_tc_grid_cap) : sms));
   TVAP_CUDA(cudaMemsetAsync(sc->counter, 0, sizeof(int), s));
   if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);
-  ozaki_tc_kernel<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
+  const bool unit_alpha = g_alpha_unit(o.alpha);
+  if (unit_alpha)
+    ozaki_tc_kernel<true><<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
+                                                                  b_slots == 1 ? 1 : 0, a_slots, nks, o, sc->counter,
+                                                                  g_dev_flags);
+  else
+    ozaki_tc_kernel<false><<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
                                                                   b_slots == 1 ? 1 : 0, a_slots, nks, o, sc->counter,
                                                                   g_dev_flags);
   if (g_tc_timing_ctx) sec_end_on(g_tc_timing_ctx, g_tc_timing_sec, s);
