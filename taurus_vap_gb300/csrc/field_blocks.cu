@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
       }
     }
   };
-  if (!oztc::run_tiles(counter, ntiles, nks_of, fsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
+  if (!oztc::run_tiles<oztc::kN>(counter, ntiles, nks_of, fsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
     atomicOr(flags, DEV_TC_TIMEOUT);
 }
 

@@ -335,21 +335,21 @@ struct TcOut {
 // order from *counter; tile numbers run over the N tiles fastest, then the M
 // tiles, then the slots, so that the CTAs working at one time share their A
 // and B tiles through L2.
-template <bool UNIT>
+template <bool UNIT, int BN>
 __global__ void __launch_bounds__(oztc::kThreads, 1)
     ozaki_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ ea, int a_rows_pad,
                     const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb, int b_rows_pad, int b_shared,
                     int nslots, int nks, TcOut o, int* counter, int* flags) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ oztc::Ctl ctl;
-  const int a_tiles = a_rows_pad / oztc::kM, b_tiles = b_rows_pad / oztc::kN;
+  const int a_tiles = a_rows_pad / oztc::kM, b_tiles = b_rows_pad / BN;
   const int ntiles = a_tiles * b_tiles * nslots;
   auto tile_ptrs = [&](int tile, const unsigned char*& A, const unsigned char*& B) {
     const int nt = tile % b_tiles, rest = tile / b_tiles;
     const int mt = rest % a_tiles, z = rest / a_tiles;
     const int bz = b_shared ? 0 : z;
     A = reinterpret_cast<const unsigned char*>(As) + (size_t(z) * a_tiles + mt) * nks * size_t(oztc::kABytes);
-    B = reinterpret_cast<const unsigned char*>(Bs) + (size_t(bz) * b_tiles + nt) * nks * size_t(oztc::kBBytes);
+    B = reinterpret_cast<const unsigned char*>(Bs) + (size_t(bz) * b_tiles + nt) * nks * size_t(oztc::b_bytes(BN));
   };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // The stores of a tile overlap the MMAs of the next one: exponents, values
@@ -361,6 +361,9 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
     const int bz = b_shared ? 0 : z;
     const int q = mt * oztc::kM + 32 * (warp & 3) + lane;
     if (q >= o.nstack * o.a_rows) return;
+    if constexpr (BN < 64) {
+      if (16 * (warp >> 2) >= BN) return;  // these warps' columns belong to the next tile
+    }
     const int b = o.nstack > 1 ? q / o.a_rows : z;
     int i = o.nstack > 1 ? q - b * o.a_rows : q;
     int comp_a = 0;
@@ -371,7 +374,7 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
     const int eai = ea[size_t(z) * a_rows_pad + q] - 57;
     double* __restrict__ C = static_cast<double*>(o.C);
     const int cw = o.c_real ? 1 : 2;  // doubles per element
-    const int col0 = nt * oztc::kN + 16 * (warp >> 2);
+    const int col0 = nt * BN + 16 * (warp >> 2);
     const int* __restrict__ ebz = eb + size_t(bz) * b_rows_pad;
     // element index of column c, or -1 (padding, or the imaginary part of a
     // real output)
@@ -422,7 +425,7 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
     }
   };
   auto nks_of = [nks](int) { return nks; };
-  if (!oztc::run_tiles(counter, ntiles, nks_of, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
+  if (!oztc::run_tiles<BN>(counter, ntiles, nks_of, tsm, ctl, tile_ptrs, store) && threadIdx.x == 0 && flags)
     atomicOr(flags, DEV_TC_TIMEOUT);
 }
 
@@ -570,14 +573,18 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   xa.nstack = stack ? g.batch : 1;
   const int a_slots = stack ? 1 : g.batch, b_slots = stack ? 1 : g.batch;
   const int a_rows_pad = (xa.nstack * xa.xrows + oztc::kM - 1) / oztc::kM * oztc::kM;
-  const int b_rows_pad = (xb.xrows + oztc::kN - 1) / oztc::kN * oztc::kN;
+  // B' tiles of 48 or 64 rows, whichever pads the output columns less (140
+  // columns: 144 instead of 192)
+  const int pad48 = (xb.xrows + 47) / 48 * 48, pad64 = (xb.xrows + 63) / 64 * 64;
+  const int bn = pad48 < pad64 ? 48 : 64;
+  const int b_rows_pad = bn == 48 ? pad48 : pad64;
   const int nks = (xa.xk + 15) / 16;
   const size_t asz = size_t(a_slots) * (a_rows_pad / oztc::kM) * nks * (oztc::kABytes / 2);
-  const size_t bsz = size_t(b_slots) * (b_rows_pad / oztc::kN) * nks * (oztc::kBBytes / 2);
+  const size_t bsz = size_t(b_slots) * (b_rows_pad / bn) * nks * (oztc::b_bytes(bn) / 2);
   // products of few tiles (the single small products of the canonical basis
   // and the evolution) are latency-bound: the 32 x 32 mma.sync tiles spread
   // them over more SMs
-  if (size_t(a_rows_pad / oztc::kM) * (b_rows_pad / oztc::kN) * a_slots < size_t(kTcMinTiles)) return TVAP_ERR_ARG;
+  if (size_t(a_rows_pad / oztc::kM) * (b_rows_pad / bn) * a_slots < size_t(kTcMinTiles)) return TVAP_ERR_ARG;
   int rc;
   OzScratch* sc = nullptr;
   if ((rc = oz_reserve(s, sizeof(__nv_bfloat16) * (asz + bsz), size_t(a_slots) * a_rows_pad +
@@ -598,8 +605,8 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   }
   slice_tc_kernel<<<dim3((xa.nstack * xa.rows + 7) / 8, a_slots), kSliceThreads, slice_shm, s>>>(
       xa, oztc::kM, a_rows_pad, nks, As, ea);
-  slice_tc_kernel<<<dim3((xb.rows + 7) / 8, b_slots), kSliceThreads, slice_shm, s>>>(xb, oztc::kN, b_rows_pad, nks,
-                                                                                     Bs, eb);
+  slice_tc_kernel<<<dim3((xb.rows + 7) / 8, b_slots), kSliceThreads, slice_shm, s>>>(xb, bn, b_rows_pad, nks, Bs,
+                                                                                     eb);
   o.C = g.C;
   o.crs = crs;
   o.ccs = ccs;
@@ -612,27 +619,31 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   o.nstack = xa.nstack;
   static bool attr = false;
   if (!attr) {
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<true, 48>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    int(oztc::kSmemBytes)));
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(oztc::kSmemBytes)));
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<false, 48>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(oztc::kSmemBytes)));
+    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    int(oztc::kSmemBytes)));
     attr = true;
   }
   static int sms = 0;
   if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
-  const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / oztc::kN) * a_slots;
+  const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / bn) * a_slots;
   const int grid = int(std::min<long long>(ntiles, g_tc_grid_cap > 0 ? std::min(sms, g_tc_grid_cap) : sms));
   TVAP_CUDA(cudaMemsetAsync(sc->counter, 0, sizeof(int), s));
   if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   const bool unit_alpha = g_alpha_unit(o.alpha);
+  auto launch = [&](auto kern) {
+    kern<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad, b_slots == 1 ? 1 : 0,
+                                                        a_slots, nks, o, sc->counter, g_dev_flags);
+  };
   if (unit_alpha)
-    ozaki_tc_kernel<true><<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
-                                                                  b_slots == 1 ? 1 : 0, a_slots, nks, o, sc->counter,
-                                                                  g_dev_flags);
+    bn == 48 ? launch(ozaki_tc_kernel<true, 48>) : launch(ozaki_tc_kernel<true, 64>);
   else
-    ozaki_tc_kernel<false><<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad,
-                                                                  b_slots == 1 ? 1 : 0, a_slots, nks, o, sc->counter,
-                                                                  g_dev_flags);
+    bn == 48 ? launch(ozaki_tc_kernel<false, 48>) : launch(ozaki_tc_kernel<false, 64>);
   if (g_tc_timing_ctx) sec_end_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;

@@ -44,7 +44,7 @@ using oz::kDigits;
 using oz::kKeep;
 
 constexpr int kM = 128;                 // rows of A' per CTA (TMEM lanes)
-constexpr int kN = 64;                  // rows of B' (output columns) per CTA
+constexpr int kN = 64;                  // rows of B' (output columns) per tile, at most (48 or 64)
 constexpr int kEpiWarps = 16;           // accumulator readers
 constexpr int kProducerWarp = 16;       // bulk copies
 constexpr int kMmaWarp = 17;            // TMEM allocation + MMA issue
@@ -60,6 +60,9 @@ constexpr int kABytes = kDigits * kATileElems * 2;  // 32 KB per k-step
 constexpr int kBBytes = kDigits * kBTileElems * 2;  // 16 KB per k-step
 constexpr int kStageBytes = kABytes + kBBytes;
 constexpr size_t kSmemBytes = size_t(kStages) * kStageBytes;
+// B' tile of BN rows: elements of one digit plane of a k-step, bytes of a k-step
+__host__ __device__ constexpr int b_tile_elems(int bn) { return bn * 16; }
+__host__ __device__ constexpr int b_bytes(int bn) { return kDigits * bn * 16 * 2; }
 // one CTA per SM: two CTAs could never hold 512 TMEM columns each
 static_assert(2 * kSmemBytes > 228 * 1024, "the tcgen05 kernel must not share an SM with itself");
 
@@ -189,30 +192,33 @@ struct Ctl {
 // Every descriptor is the stage's base descriptor plus a constant (the
 // start-address field is the low 14 bits and shared addresses stay below
 // 2^18, so the addition never carries into the other fields).
-template <bool FIRST>
+template <int BN, bool FIRST>
 __device__ __forceinline__ void issue_kstep(uint32_t tmem, const unsigned char* st) {
   const uint64_t da = desc(smem_u32(st)), db = desc(smem_u32(st + kABytes));
-  constexpr uint32_t kAT = uint32_t(kATileElems * 2) >> 4, kBT = uint32_t(kBTileElems * 2) >> 4;
+  constexpr uint32_t kAT = uint32_t(kATileElems * 2) >> 4, kBT = uint32_t(b_tile_elems(BN) * 2) >> 4;
 #pragma unroll
   for (int s = 0; s < kDigits; ++s) {
 #pragma unroll
     for (int t0 = 0; t0 <= kKeep - s; t0 += 4) {
       const int c = (kKeep - s - t0 + 1) < 4 ? (kKeep - s - t0 + 1) : 4;
-      mma(tmem + uint32_t((s + t0) * kN), da + uint64_t(s * kAT), db + uint64_t(t0 * kBT), idesc(c * kN),
+      mma(tmem + uint32_t((s + t0) * BN), da + uint64_t(s * kAT), db + uint64_t(t0 * kBT), idesc(c * BN),
           (FIRST && s == 0) ? 0u : 1u);
     }
   }
 }
 
-// fold the accumulators of an interval into the integer accumulators
+// fold the accumulators of an interval into the integer accumulators (the
+// warps whose 16 columns lie beyond a tile of BN columns read the last 16
+// again, and store nothing)
+template <int BN>
 __device__ __forceinline__ void fold(uint32_t tmem, Acc& o) {
   const int warp = threadIdx.x >> 5;
   const uint32_t lane_base = uint32_t(32 * (warp & 3)) << 16;
-  const uint32_t c0 = uint32_t((warp >> 2) * 16);
+  const uint32_t c0 = uint32_t(min((warp >> 2) * 16, BN - 16));
 #pragma unroll
   for (int g = 0; g <= kKeep; ++g) {
     uint32_t r[16];
-    ld16(tmem + lane_base + uint32_t(g * kN) + c0, r);
+    ld16(tmem + lane_base + uint32_t(g * BN) + c0, r);
     ld_wait();
     const long long w = 1LL << (7 * (3 - (g & 3)));
 #pragma unroll
@@ -233,12 +239,12 @@ __device__ __forceinline__ void fold(uint32_t tmem, Acc& o) {
 // CTAs that start late -- their SMs held by kernels of other streams -- take
 // fewer tiles instead of delaying the product.  A number >= ntiles ends the
 // CTA.  tile_ptrs(tile, A, B) gives the tile's first k-step blocks (digit 0;
-// nks_of(tile) k-steps of kABytes / kBBytes each follow contiguously); store(tile, acc)
+// nks_of(tile) k-steps of kABytes / b_bytes(BN) each follow contiguously); store(tile, acc)
 // is called by the epilogue threads with the tile's integer accumulators,
 // after the tensor memory has been handed back to the MMA thread, so that the
 // stores of one tile overlap the MMAs of the next.  The copy thread runs
 // ahead across tile boundaries.  Returns false on a timeout.
-template <class TilePtrs, class NksOf, class Store>
+template <int BN, class TilePtrs, class NksOf, class Store>
 __device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char* smem, Ctl& ctl, TilePtrs tile_ptrs,
                           Store store) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -293,9 +299,9 @@ __device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char*
             break;
           }
           unsigned char* dst = smem + size_t(st) * kStageBytes;
-          mbar_expect_tx(&ctl.full[st], uint32_t(kStageBytes));
+          mbar_expect_tx(&ctl.full[st], uint32_t(kABytes + b_bytes(BN)));
           bulk_load(dst, A + size_t(ks) * kABytes, uint32_t(kABytes), &ctl.full[st]);
-          bulk_load(dst + kABytes, B + size_t(ks) * kBBytes, uint32_t(kBBytes), &ctl.full[st]);
+          bulk_load(dst + kABytes, B + size_t(ks) * b_bytes(BN), uint32_t(b_bytes(BN)), &ctl.full[st]);
           issued = it + 1;
         }
       }
@@ -329,9 +335,9 @@ __device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char*
           fence_after();
           const unsigned char* sb = smem + size_t(st) * kStageBytes;
           if (opens)
-            issue_kstep<true>(tmem, sb);
+            issue_kstep<BN, true>(tmem, sb);
           else
-            issue_kstep<false>(tmem, sb);
+            issue_kstep<BN, false>(tmem, sb);
           commit(&ctl.empty[st]);
           if ((ks + 1) % kFoldKs == 0 || ks + 1 == nks) {
             commit(&ctl.acc_full);
@@ -364,7 +370,7 @@ __device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char*
           break;
         }
         fence_after();
-        fold(tmem, o);
+        fold<BN>(tmem, o);
         fence_before();
         mbar_arrive(&ctl.acc_empty);
       }
