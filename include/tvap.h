@@ -142,7 +142,8 @@ int tvap_calculate_fields_batched(tvap_ctx* ctx, int ncol, const double* rhoLR, 
 /* project_wavefunction(iopt=0) + calculate_projected_H20
  * (src/module_projection.f90:201-373,729-759): from the real Bogoliubov
  * matrices U0, V0 (n x n) computes the projected sums and
- * field_H20v (n*n reals, may be NULL). */
+ * field_H20v (n*n reals, may be NULL).  A host H20v is complete on return; a
+ * device H20v is written in the order of the context's stream. */
 int tvap_project(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts, tvap_pnp* out,
                  double* H20v);
 

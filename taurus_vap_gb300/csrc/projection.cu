@@ -78,6 +78,10 @@ struct Workspace {
   int* piv = nullptr;  // [G][n] row interchanges of the Thouless LU
   // [G][panel][L11^-1, U11^-1] (kPanelMax^2 each) of the Thouless LU
   double2* Tinv = nullptr;
+  // the angle tables in ephase/weight/mult were made for these options
+  bool angles_valid = false;
+  int ang_Mp = 0, ang_Mn = 0, ang_mode = 0;
+  double ang_facpi = 0.0, ang_vz = 0.0, ang_vn = 0.0;
   double2* tpart = nullptr;  // [kTraceChunks][G][9] partial traces
   bool have_basis = false;
   size_t bytes = 0;
@@ -2409,6 +2413,13 @@ int project_angles(tvap_ctx* c, int G, const double2* d_ephase, const double2* d
   return angles_sums(c, G, d_weight, d_mult, have_overlap, accumulate, s);
 }
 
+bool is_device_pointer(const void* p) {
+  cudaPointerAttributes at{};
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) cudaGetLastError();
+  return e == cudaSuccess && (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
+}
+
 int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s) {
   cudaPointerAttributes at{};
   cudaError_t e = cudaPointerGetAttributes(&at, src);
@@ -2427,11 +2438,19 @@ int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s) {
   return TVAP_OK;
 }
 
-int check_flags(tvap_ctx* c) {
-  int f = 0;
-  TVAP_CUDA(cudaMemcpyAsync(&f, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+// Waits for the context's stream once, reading the status word and (when
+// bytes > 0) bytes of device data at src into dst through the pinned buffer;
+// then resets the status word and maps it to a code.
+int sync_with_flags(tvap_ctx* c, void* dst, const void* src, size_t bytes) {
+  if (bytes > kPinnedBytes - 16) return TVAP_ERR_ARG;
+  unsigned char* pin = static_cast<unsigned char*>(c->h_pin);
+  if (bytes) TVAP_CUDA(cudaMemcpyAsync(pin + 16, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+  TVAP_CUDA(cudaMemcpyAsync(pin, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   TVAP_CUDA(cudaStreamSynchronize(c->stream));
   TVAP_CUDA(cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
+  int f = 0;
+  std::memcpy(&f, pin, sizeof(int));
+  if (bytes) std::memcpy(dst, pin + 16, bytes);
   if (f & DEV_SINGULAR_RN) return TVAP_ERR_SINGULAR_RN;
   if (f & DEV_SINGULAR_UPHI) return TVAP_ERR_SINGULAR_UPHI;
   if (f & (DEV_EIGEN_NOCONV | DEV_CANON_BLOCK)) return TVAP_ERR_CANONICAL;
@@ -2444,6 +2463,8 @@ int check_flags(tvap_ctx* c) {
   }
   return TVAP_OK;
 }
+
+int check_flags(tvap_ctx* c) { return sync_with_flags(c, nullptr, nullptr, 0); }
 
 // Full projection of state (w->U, w->V) already on the device.  Leaves the
 // sums in w->pscal/pA/pH/pAH and the gradient in w->H20v.
@@ -2467,9 +2488,21 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
     eph[2 * b + 1] = make_double2(en.real(), en.imag());
     wt[b] = make_double2(t.w[b].real(), t.w[b].imag());
   }
-  TVAP_CUDA(cudaMemcpyAsync(w->ephase, eph.data(), sizeof(double2) * 2 * G, cudaMemcpyHostToDevice, s));
-  TVAP_CUDA(cudaMemcpyAsync(w->weight, wt.data(), sizeof(double2) * G, cudaMemcpyHostToDevice, s));
-  TVAP_CUDA(cudaMemcpyAsync(w->mult, t.mult.data(), sizeof(double) * G, cudaMemcpyHostToDevice, s));
+  // the tables stay on the device while the options do not change (three
+  // copies from pageable memory less per projection)
+  if (!(w->angles_valid && w->ang_Mp == o.Mphip && w->ang_Mn == o.Mphin && w->ang_mode == o.mode &&
+        w->ang_facpi == o.facpi && w->ang_vz == o.valence_Z && w->ang_vn == o.valence_N)) {
+    TVAP_CUDA(cudaMemcpyAsync(w->ephase, eph.data(), sizeof(double2) * 2 * G, cudaMemcpyHostToDevice, s));
+    TVAP_CUDA(cudaMemcpyAsync(w->weight, wt.data(), sizeof(double2) * G, cudaMemcpyHostToDevice, s));
+    TVAP_CUDA(cudaMemcpyAsync(w->mult, t.mult.data(), sizeof(double) * G, cudaMemcpyHostToDevice, s));
+    w->angles_valid = true;
+    w->ang_Mp = o.Mphip;
+    w->ang_Mn = o.Mphin;
+    w->ang_mode = o.mode;
+    w->ang_facpi = o.facpi;
+    w->ang_vz = o.valence_Z;
+    w->ang_vn = o.valence_N;
+  }
   auto canon_error = [&]() {
     set_last_error("canonical basis has a degenerate block larger than 2 or an odd paired block", __FILE__,
                    __LINE__);
@@ -2515,9 +2548,9 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
   TVAP_CUDA(cudaGetLastError());
   c->kernel_launches += 1;
   if (out) {
+    // the sums and the status word in one round trip
     double2 sc[6];
-    TVAP_CUDA(cudaMemcpyAsync(sc, w->pscal, sizeof(double2) * 6, cudaMemcpyDeviceToHost, s));
-    TVAP_CUDA(cudaStreamSynchronize(s));
+    rc = sync_with_flags(c, sc, w->pscal, sizeof(double2) * 6);
     double* dst[6] = {out->over, out->ener, out->prot, out->neut, out->prot2, out->neut2};
     for (int q = 0; q < 6; ++q) {
       dst[q][0] = sc[q].x;
@@ -2525,6 +2558,7 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
     }
     out->nocc = canon[0];
     out->nemp = canon[1];
+    return rc;
   }
   return check_flags(c);
 }

@@ -18,6 +18,7 @@ void set_last_error(const char* msg, const char* file, int line) {
 
 int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
 int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
+bool is_device_pointer(const void* p);
 int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out);
 int ensure_workspace(tvap_ctx* c, int G);
 void destroy_workspace(tvap_ctx* c);
@@ -236,6 +237,7 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
     return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_stagger, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  if ((e = cudaMallocHost(&c->h_pin, kPinnedBytes)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_canon, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
@@ -291,6 +293,7 @@ void tvap_destroy(tvap_ctx* c) {
   if (c->streamM2) cudaStreamDestroy(c->streamM2);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_stagger) cudaEventDestroy(c->ev_stagger);
+  if (c->h_pin) cudaFreeHost(c->h_pin);
   if (c->ev_join2) cudaEventDestroy(c->ev_join2);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_main) cudaEventDestroy(c->ev_main);
@@ -403,7 +406,9 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   if ((rc = project_device(c, *opts, out))) return rc;
   if (H20v) {
     if ((rc = download_matrix(ws_H20v(c), H20v, sizeof(double) * nn, c->stream))) return rc;
-    TVAP_CUDA(cudaStreamSynchronize(c->stream));
+    // a device destination is written in the order of the context's stream;
+    // a host one is complete on return
+    if (!is_device_pointer(H20v)) TVAP_CUDA(cudaStreamSynchronize(c->stream));
   }
   return TVAP_OK;
 }

@@ -213,6 +213,8 @@ struct Workspace;
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
+constexpr size_t kPinnedBytes = 256;
+
 struct tvap_ctx {
   int n = 0;
   int device = 0;
@@ -237,6 +239,7 @@ struct tvap_ctx {
   cudaStream_t streamM2 = nullptr;  // second half of the angles in the Thouless solve (same priority)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_canon = nullptr, ev_main = nullptr;
   cudaEvent_t ev_stagger = nullptr, ev_join2 = nullptr;  // the two halves of the Thouless solve
+  void* h_pin = nullptr;  // pinned host buffer (kPinnedBytes) for the status word and small results
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
   unsigned* d_bar = nullptr;  // grid-barrier state of the cooperative kernels (3 words)
