@@ -146,6 +146,15 @@ int tvap_calculate_fields_batched(tvap_ctx* ctx, int ncol, const double* rhoLR, 
  * device H20v is written in the order of the context's stream. */
 int tvap_project(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts, tvap_pnp* out,
                  double* H20v);
+/* tvap_project for nstates states of the same basis (multi-state batches:
+ * seeds, constraint points): state s reads U0s/V0s + s*n*n and opts[s], and
+ * writes outs[s] and H20vs + s*n*n (H20vs may be NULL).  The states run one
+ * after the other in the context, each on all of the device; the first
+ * failing state's code is returned (its outputs and the later ones are not
+ * written).  No reference counterpart (the reference projects one state per
+ * process). */
+int tvap_project_batched(tvap_ctx* ctx, int nstates, const double* U0s, const double* V0s,
+                         const tvap_proj_opts* opts, tvap_pnp* outs, double* H20vs);
 
 /* calculate_gradient with gradient_type 0 (src/module_gradient.f90:79-143):
  * Zi = -eta (H20v - sum_j lambda_j C20_j) + mu Zim1, and

@@ -413,4 +413,15 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   return TVAP_OK;
 }
 
+int tvap_project_batched(tvap_ctx* c, int nstates, const double* U0s, const double* V0s, const tvap_proj_opts* opts,
+                         tvap_pnp* outs, double* H20vs) {
+  if (!c || nstates < 0 || (nstates > 0 && (!U0s || !V0s || !opts || !outs))) return TVAP_ERR_ARG;
+  const size_t nn = size_t(c->n) * c->n;
+  for (int s = 0; s < nstates; ++s) {
+    int rc = tvap_project(c, U0s + s * nn, V0s + s * nn, opts + s, outs + s, H20vs ? H20vs + s * nn : nullptr);
+    if (rc) return rc;
+  }
+  return TVAP_OK;
+}
+
 }  // extern "C"

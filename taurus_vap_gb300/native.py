@@ -90,6 +90,8 @@ def lib():
         L.tvap_calculate_fields_batched.restype = ci
         L.tvap_project.argtypes = [vp, vp, vp, ctypes.POINTER(TvapProjOpts), ctypes.POINTER(TvapPnp), vp]
         L.tvap_project.restype = ci
+        L.tvap_project_batched.argtypes = [vp, ci, vp, vp, ctypes.POINTER(TvapProjOpts), ctypes.POINTER(TvapPnp), vp]
+        L.tvap_project_batched.restype = ci
         L.tvap_calculate_gradient.argtypes = [vp, vp, ci, vp, vp, vp, cd, cd, vp, vp]
         L.tvap_calculate_gradient.restype = ci
         L.tvap_evolve.argtypes = [vp] * 6
@@ -227,6 +229,24 @@ class Context:
         _check(lib().tvap_project(self.h, _p(U), _p(V), ctypes.byref(o), ctypes.byref(out), _p(H20v)),
                "tvap_project")
         return out, H20v
+
+    def project_batched(self, U0s, V0s, opts):
+        """tvap_project_batched: states U0s[s], V0s[s] (n x n each) with
+        options opts[s] = dict(Mphip=, Mphin=, facpi=, valence_Z=,
+        valence_N=, factor_delta=1.0, seed_occeps=0.0, seed_allemp=0,
+        mode=0); returns the list of (pnp, H20v)."""
+        n, ns = self.n, len(opts)
+        U = np.stack([_f(u, np.float64) for u in U0s]).transpose(0, 2, 1).copy()  # column-major per state
+        V = np.stack([_f(v, np.float64) for v in V0s]).transpose(0, 2, 1).copy()
+        O = (TvapProjOpts * ns)()
+        for s, d in enumerate(opts):
+            O[s] = TvapProjOpts(d["Mphip"], d["Mphin"], d["facpi"], d["valence_Z"], d["valence_N"],
+                                d.get("factor_delta", 1.0), d.get("seed_occeps", 0.0), d.get("seed_allemp", 0),
+                                d.get("mode", 0))
+        outs = (TvapPnp * ns)()
+        H20v = np.zeros(ns * n * n)
+        _check(lib().tvap_project_batched(self.h, ns, _p(U), _p(V), O, outs, _p(H20v)), "tvap_project_batched")
+        return [(outs[s], H20v[s * n * n:(s + 1) * n * n]) for s in range(ns)]
 
     # -- calculate_gradient (module_gradient.f90:79-143), gradient_type 0 -----
     def calculate_gradient(self, H20v, lambdas, C20, Zim1, eta, mu):

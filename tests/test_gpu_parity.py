@@ -268,3 +268,27 @@ def test_autograd_function_matches_finite_differences(sd):
     Em = projected_energy(torch.tensor(Z0 - h * D), ctx, U, V, 5, 5, 4, 4).item()
     fd = (Ep - Em) / (2 * h)
     assert abs(fd - float((Z.grad.numpy() * D).sum())) < 1e-6 * max(1.0, abs(fd))
+
+
+def test_project_batched_states(sd):
+    # several states of one basis in one call: each agrees with its own
+    # single projection (to rounding: the canonical basis is warm-started
+    # from the previous state's), and with the oracle for one of them
+    mdl, U, V = sd
+    states = [(U, V)] + [M.random_bogoliubov(mdl.basis, 4, 4, seed=s) for s in (11, 12)]
+    opts = [dict(Mphip=9, Mphin=9, facpi=2 * np.pi, valence_Z=4, valence_N=4),
+            dict(Mphip=7, Mphin=5, facpi=2 * np.pi, valence_Z=4, valence_N=4),
+            dict(Mphip=9, Mphin=9, facpi=2 * np.pi, valence_Z=4, valence_N=4, mode=1)]
+    ctx = Context(mdl.basis, mdl.ham)
+    got = ctx.project_batched([s[0] for s in states], [s[1] for s in states], opts)
+    for (Us, Vs), o, (pnp, H20v) in zip(states, opts, got):
+        p1, h1 = ctx.project(Us, Vs, o["Mphip"], o["Mphin"], o["facpi"], o["valence_Z"], o["valence_N"],
+                             mode=o.get("mode", 0))
+        assert abs(pnp.c("ener") / pnp.c("over") - p1.c("ener") / p1.c("over")) < 1e-12
+        assert abs(pnp.c("over") - p1.c("over")) < 1e-12 * abs(p1.c("over"))
+        assert relerr(H20v, h1) < 1e-12
+    om = O.OracleModel(mdl)
+    ref = om.project(states[1][0], states[1][1], 7, 5, 2 * np.pi, 4, 4)
+    e_ref = (ref["pnp"].c("ener") / ref["pnp"].c("over")).real
+    assert abs((got[1][0].c("ener") / got[1][0].c("over")).real - e_ref) < 1e-9
+    assert relerr(got[1][1], ref["H20v"]) < 1e-9
