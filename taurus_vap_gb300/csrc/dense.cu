@@ -266,6 +266,7 @@ int gemm_split_k2(const GemmArgs& g, cudaStream_t s) {
   if ((rc = gemm(g1, s))) return rc;
   GemmArgs g2 = g;
   g2.K2 = 0;
+  g2.reuse_left = false;  // another left operand
   g2.A = g.A2;
   g2.B = g.B2;
   g2.K = g.K2;

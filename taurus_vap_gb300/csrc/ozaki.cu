@@ -429,6 +429,24 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
     atomicOr(flags, DEV_TC_TIMEOUT);
 }
 
+// the left operand whose digit planes (at the start of buf) and exponents
+// (at the start of ex) the last tcgen05 product left
+struct LeftSlice {
+  bool valid = false;
+  const void* p = nullptr;
+  const void* p2 = nullptr;
+  long long sr = 0, sk = 0, bs = 0, sr2 = 0, sk2 = 0, bs2 = 0;
+  int rows = 0, K = 0, K1 = 0, form = 0, conj = 0, xrows = 0, xk = 0, kp = 0, nstack = 0, slots = 0, rows_pad = 0,
+      nks = 0;
+  double scale2 = 0.0;
+  bool operator==(const LeftSlice& o) const {
+    return valid && o.valid && p == o.p && p2 == o.p2 && sr == o.sr && sk == o.sk && bs == o.bs && sr2 == o.sr2 &&
+           sk2 == o.sk2 && bs2 == o.bs2 && rows == o.rows && K == o.K && K1 == o.K1 && form == o.form &&
+           conj == o.conj && xrows == o.xrows && xk == o.xk && kp == o.kp && nstack == o.nstack && slots == o.slots &&
+           rows_pad == o.rows_pad && nks == o.nks && scale2 == o.scale2;
+  }
+};
+
 struct OzScratch {
   cudaStream_t stream = nullptr;
   __nv_bfloat16* buf = nullptr;
@@ -436,6 +454,7 @@ struct OzScratch {
   int* ex = nullptr;
   size_t ex_count = 0;
   int* counter = nullptr;  // tile counter of the tcgen05 kernel
+  LeftSlice left;          // what buf / ex hold at their start
 };
 constexpr int kMaxScratch = 16;
 OzScratch g_oz[kMaxScratch];
@@ -466,6 +485,7 @@ int oz_reserve(cudaStream_t s, size_t bytes, size_t ex_count, OzScratch** out) {
     sc->buf = nullptr;
     TVAP_CUDA(cudaMalloc(&sc->buf, bytes));
     sc->bytes = bytes;
+    sc->left.valid = false;
   }
   if (ex_count > sc->ex_count) {
     if (sc->ex) {
@@ -475,6 +495,7 @@ int oz_reserve(cudaStream_t s, size_t bytes, size_t ex_count, OzScratch** out) {
     sc->ex = nullptr;
     TVAP_CUDA(cudaMalloc(&sc->ex, ex_count * sizeof(int)));
     sc->ex_count = ex_count;
+    sc->left.valid = false;
   }
   *out = sc;
   return TVAP_OK;
@@ -486,6 +507,7 @@ int oz_scratch(cudaStream_t s, size_t bytes, size_t ex_count, __nv_bfloat16** bu
   OzScratch* sc = nullptr;
   int rc;
   if ((rc = oz_reserve(s, bytes, ex_count, &sc))) return rc;
+  sc->left.valid = false;  // the caller overwrites the planes
   *buf = sc->buf;
   *ex = sc->ex;
   return TVAP_OK;
@@ -603,8 +625,34 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
       granted = slice_shm;
     }
   }
-  slice_tc_kernel<<<dim3((xa.nstack * xa.rows + 7) / 8, a_slots), kSliceThreads, slice_shm, s>>>(
-      xa, oztc::kM, a_rows_pad, nks, As, ea);
+  LeftSlice left;
+  left.valid = true;
+  left.p = xa.p;
+  left.p2 = xa.p2;
+  left.sr = xa.sr;
+  left.sk = xa.sk;
+  left.bs = xa.bs;
+  left.sr2 = xa.sr2;
+  left.sk2 = xa.sk2;
+  left.bs2 = xa.bs2;
+  left.rows = xa.rows;
+  left.K = xa.K;
+  left.K1 = xa.K1;
+  left.form = xa.form;
+  left.conj = xa.conj ? 1 : 0;
+  left.xrows = xa.xrows;
+  left.xk = xa.xk;
+  left.kp = xa.kp;
+  left.nstack = xa.nstack;
+  left.slots = a_slots;
+  left.rows_pad = a_rows_pad;
+  left.nks = nks;
+  left.scale2 = xa.scale2;
+  if (!(g.reuse_left && sc->left == left)) {
+    slice_tc_kernel<<<dim3((xa.nstack * xa.rows + 7) / 8, a_slots), kSliceThreads, slice_shm, s>>>(
+        xa, oztc::kM, a_rows_pad, nks, As, ea);
+    sc->left = left;
+  }
   slice_tc_kernel<<<dim3((xb.rows + 7) / 8, b_slots), kSliceThreads, slice_shm, s>>>(xb, bn, b_rows_pad, nks, Bs,
                                                                                      eb);
   o.C = g.C;
@@ -667,6 +715,7 @@ int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
   OzScratch* sc = nullptr;
   if ((rc = oz_reserve(s, sizeof(__nv_bfloat16) * (asz + bsz), size_t(abatch) * mpad + size_t(bbatch) * npad, &sc)))
     return rc;
+  sc->left.valid = false;  // the mma.sync planes overwrite the tcgen05 ones
   __nv_bfloat16* As = sc->buf;
   __nv_bfloat16* Bs = sc->buf + asz;
   int* ea = sc->ex;

@@ -2290,6 +2290,7 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
     if ((rc = gemm(g, s))) return rc;
     g.A = view_cm(w->U, n, 0);
     g.C = w->Vt;
+    g.reuse_left = true;  // A_phi, the per-angle operand of both products
     if ((rc = gemm(g, s))) return rc;
   }
   sec_end_on(c, SEC_UV, s);
@@ -2310,10 +2311,12 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
     g.b_real = true;
     g.C = w->rhoL;
     if ((rc = gemm(g, s))) return rc;
-    // kappaLR = V~ U^T
+    // kappaLR = V~ U^T (the digit planes of V~ from the product before)
     g.B = view_t(view_cm(w->U, n, 0));
     g.C = w->kLR;
+    g.reuse_left = true;
     if ((rc = gemm(g, s))) return rc;
+    g.reuse_left = false;
     // kappaRL = V U~^T
     g.A = view_cm(w->V, n, 0);
     g.a_real = true;

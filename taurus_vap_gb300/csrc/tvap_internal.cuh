@@ -119,6 +119,10 @@ struct GemmArgs {
   int K2;
   View A2, B2;
   double s2;
+  // the left operand (after a shared left operand is swapped to the right)
+  // is the previous tcgen05 product's on this stream, unchanged since: its
+  // digit planes are reused (checked against the recorded operand)
+  bool reuse_left;
 };
 int gemm(const GemmArgs& g, cudaStream_t s);
 // the two terms of a product with K2 > 0 as two products
