@@ -379,40 +379,74 @@ __global__ void overlap_prep_kernel(int n, int G, const int* __restrict__ canon_
 constexpr int kTraceChunks = 256;
 static_assert(kTraceChunks == 256, "Workspace::tpart is allocated for 256 chunks");
 constexpr int kTraceThreads = 128;
+// Partial traces over the pairs (i <= j) of chunk blockIdx.x, threads over the
+// angles (angle-innermost layout: coalesced).  A pair takes both entries
+// (i, j) and (j, i): Tr(H1 rho) and Tr(Gamma rho) need both products, while
+// rho_ij rho_ji, kappaRL kappaLR and Delta kappaRL are equal for the two
+// entries (Delta and the kappas are skew), so they are formed once and
+// doubled.  The diagonal adds the traces of rho.
 __global__ void __launch_bounds__(kTraceThreads)
     traces_partial_kernel(int n, int G, const double2* __restrict__ rho, const double2* __restrict__ kLR,
                           const double2* __restrict__ kRL, const double2* __restrict__ gam,
                           const double2* __restrict__ dLR, const double2* __restrict__ H1,
                           double2* __restrict__ part) {
   const int h = n / 2;
-  const long long nn = (long long)n * n;
+  const long long npairs = (long long)n * (n + 1) / 2;
   const int chunk = blockIdx.x;
-  const int e0 = int(nn * chunk / kTraceChunks), e1 = int(nn * (chunk + 1) / kTraceChunks);
+  const long long q0 = npairs * chunk / kTraceChunks, q1 = npairs * (chunk + 1) / kTraceChunks;
+  // pair q = j (j + 1) / 2 + i, 0 <= i <= j
+  int j0 = int((sqrt(8.0 * double(q0) + 1.0) - 1.0) * 0.5);
+  while ((long long)(j0 + 1) * (j0 + 2) / 2 <= q0) ++j0;
+  while ((long long)j0 * (j0 + 1) / 2 > q0) --j0;
+  const int i0 = int(q0 - (long long)j0 * (j0 + 1) / 2);
   for (int b = threadIdx.x; b < G; b += blockDim.x) {
     double2 a[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) a[q] = make_double2(0.0, 0.0);
     auto at = [G, n, b](const double2* X, int i, int j) { return X[(size_t(i) + size_t(j) * n) * G + b]; };
-    for (int e = e0; e < e1; ++e) {
-      const int j = e / n, i = e - j * n;
-      const double2 rij = at(rho, i, j), rji = at(rho, j, i);
+    int i = i0, j = j0;
+    for (long long q = q0; q < q1; ++q) {
+      const double2 rij = at(rho, i, j);
       if (i == j) {
         if (i < h)
           a[0] = cadd(a[0], rij);
         else
           a[1] = cadd(a[1], rij);
+        const double2 kri = at(kRL, i, i), kli = at(kLR, i, i);
+        if (i < h) {
+          cfma(a[2], rij, rij);
+          cfma(a[3], kri, kli);
+        } else {
+          cfma(a[4], rij, rij);
+          cfma(a[5], kri, kli);
+        }
+        cfma(a[6], H1[i + size_t(i) * n], rij);
+        cfma(a[7], at(gam, i, i), rij);
+        cfma(a[8], at(dLR, i, i), at(kRL, i, i));
+      } else {
+        const double2 rji = at(rho, j, i), kr = at(kRL, i, j);
+        const bool pblk = (i < h && j < h), nblk = (i >= h && j >= h);
+        if (pblk || nblk) {
+          const double2 rr = cmul(rij, rji), kk = cmul(kr, at(kLR, i, j));
+          if (pblk) {
+            a[2] = make_double2(fma(2.0, rr.x, a[2].x), fma(2.0, rr.y, a[2].y));
+            a[3] = make_double2(fma(2.0, kk.x, a[3].x), fma(2.0, kk.y, a[3].y));
+          } else {
+            a[4] = make_double2(fma(2.0, rr.x, a[4].x), fma(2.0, rr.y, a[4].y));
+            a[5] = make_double2(fma(2.0, kk.x, a[5].x), fma(2.0, kk.y, a[5].y));
+          }
+        }
+        cfma(a[6], H1[i + size_t(j) * n], rji);
+        cfma(a[6], H1[j + size_t(i) * n], rij);
+        cfma(a[7], at(gam, i, j), rji);
+        cfma(a[7], at(gam, j, i), rij);
+        const double2 dk = cmul(at(dLR, i, j), kr);
+        a[8] = make_double2(fma(2.0, dk.x, a[8].x), fma(2.0, dk.y, a[8].y));
       }
-      const bool pblk = (i < h && j < h), nblk = (i >= h && j >= h);
-      if (pblk) {
-        cfma(a[2], rij, rji);
-        cfma(a[3], at(kRL, i, j), at(kLR, i, j));
-      } else if (nblk) {
-        cfma(a[4], rij, rji);
-        cfma(a[5], at(kRL, i, j), at(kLR, i, j));
+      if (++i > j) {
+        ++j;
+        i = 0;
       }
-      cfma(a[6], H1[i + size_t(j) * n], rji);
-      cfma(a[7], at(gam, i, j), rji);
-      cfma(a[8], at(dLR, i, j), at(kRL, i, j));
     }
 #pragma unroll
     for (int q = 0; q < 9; ++q) part[(size_t(chunk) * G + b) * 9 + q] = a[q];
