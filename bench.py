@@ -158,8 +158,8 @@ def host_iteration(ctx, state, mode):
 
 # DRAM bytes (read + write) per H20 ozaki_tc_kernel launch at n = 140,
 # G = 113: the mean of ncu's dram__bytes_read.sum + dram__bytes_write.sum over
-# the three launches of one projection (646.2, 325.3 and 642.6 MB)
-H20_TRAFFIC_PER_LAUNCH = 538.0e6
+# the three launches of one projection (593.2, 299.4 and 590.5 MB)
+H20_TRAFFIC_PER_LAUNCH = 494.4e6
 
 
 def fp64_flops_per_iteration(n, G):
