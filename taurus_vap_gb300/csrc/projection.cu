@@ -1643,6 +1643,54 @@ __global__ void __launch_bounds__(kApplyThreads)
   }
 }
 
+// The same interchanges for 32 columns per CTA: the pivot sequence is first
+// composed into a permutation of rows j0 .. n-1 (row r after = row src[r]
+// before; at most 2 nbp rows move), then the moved rows are read with
+// independent loads and written back, instead of one dependent pair of
+// accesses per interchange and column.
+constexpr int kPermCols = 32;
+constexpr int kPermThreads = 256;
+constexpr int kPermMaxRows = 1024;
+__global__ void __launch_bounds__(kPermThreads)
+    panel_perm_kernel(int n, int j0, int nbp, double2* __restrict__ Wall, const int* __restrict__ piv) {
+  __shared__ int src[kPermMaxRows];
+  __shared__ int moved[2 * kPanelMax];
+  __shared__ int nmoved;
+  __shared__ double2 buf[2 * kPanelMax][kPermCols];
+  const int b = blockIdx.y, t = threadIdx.x;
+  const int m = n - j0, j1 = j0 + nbp;
+  double2* W = Wall + size_t(b) * 2 * n * n;
+  for (int r = t; r < m; r += kPermThreads) src[r] = r;
+  if (t == 0) nmoved = 0;
+  __syncthreads();
+  if (t == 0) {
+    const int* pv = piv + size_t(b) * n + j0;
+    for (int jj = 0; jj < nbp; ++jj) {
+      const int p = pv[jj] - j0;
+      if (p != jj) {
+        const int x = src[jj];
+        src[jj] = src[p];
+        src[p] = x;
+      }
+    }
+  }
+  __syncthreads();
+  for (int r = t; r < m; r += kPermThreads)
+    if (src[r] != r) moved[atomicAdd(&nmoved, 1)] = r;
+  __syncthreads();
+  const int nm = nmoved;
+  const int c0 = j1 + blockIdx.x * kPermCols;
+  for (int idx = t; idx < nm * kPermCols; idx += kPermThreads) {
+    const int k = idx / kPermCols, cc = idx - k * kPermCols, c = c0 + cc;
+    if (c < 2 * n) buf[k][cc] = W[(j0 + src[moved[k]]) + size_t(c) * n];
+  }
+  __syncthreads();
+  for (int idx = t; idx < nm * kPermCols; idx += kPermThreads) {
+    const int k = idx / kPermCols, cc = idx - k * kPermCols, c = c0 + cc;
+    if (c < 2 * n) W[(j0 + moved[k]) + size_t(c) * n] = buf[k][cc];
+  }
+}
+
 // Columns j1 .. 2n-1 (one thread each): the panel's row interchanges, then
 // U12 = L11^{-1} A12 on the block row j0 .. j1-1.
 __global__ void __launch_bounds__(kApplyThreads)
@@ -1745,7 +1793,30 @@ struct AngleTable {
   std::vector<std::complex<double>> w;
 };
 
-AngleTable make_angles(const tvap_proj_opts& o, bool fold) {
+AngleTable make_angles_uncached(const tvap_proj_opts& o, bool fold);
+
+// the last table per host thread (an iteration asks for the same one twice:
+// for the workspace size and for the projection)
+const AngleTable& make_angles(const tvap_proj_opts& o, bool fold) {
+  struct Key {
+    int Mp, Mn;
+    double facpi, vz, vn;
+    bool fold;
+    bool operator==(const Key& k) const {
+      return Mp == k.Mp && Mn == k.Mn && facpi == k.facpi && vz == k.vz && vn == k.vn && fold == k.fold;
+    }
+  };
+  static thread_local Key key{-1, -1, 0.0, 0.0, 0.0, false};
+  static thread_local AngleTable table;
+  const Key k{o.Mphip, o.Mphin, o.facpi, o.valence_Z, o.valence_N, fold};
+  if (!(k == key)) {
+    table = make_angles_uncached(o, fold);
+    key = k;
+  }
+  return table;
+}
+
+AngleTable make_angles_uncached(const tvap_proj_opts& o, bool fold) {
   AngleTable t;
   const int Mp = o.Mphip, Mn = o.Mphin;
   const std::complex<double> I(0.0, 1.0);
@@ -1830,8 +1901,13 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
     }
     if (j0 == 0 && ev_first) TVAP_CUDA(cudaEventRecord(ev_first, s));
     if (j1 < 2 * n) {
-      dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, gc);
-      panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, W, piv);
+      if (n - j0 <= kPermMaxRows) {
+        dim3 gp((2 * n - j1 + kPermCols - 1) / kPermCols, gc);
+        panel_perm_kernel<<<gp, kPermThreads, 0, s>>>(n, j0, nbp, W, piv);
+      } else {
+        dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, gc);
+        panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, W, piv);
+      }
     }
     launches += 2;
     // the block row: R = T [A12 | B1] in place (the operands are split into
@@ -2514,7 +2590,7 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
   const bool have_overlap = std::max(o.Mphip, o.Mphin) > 1;
   const bool fold = (o.mode == 0) && std::fabs(o.facpi - 2.0 * M_PI) < 1e-12 && is_integer(o.valence_Z) &&
                     is_integer(o.valence_N);
-  AngleTable t = make_angles(o, fold);
+  const AngleTable& t = make_angles(o, fold);
   const int G = int(t.php.size());
   Workspace* w = c->ws;
   std::vector<double2> eph(2 * G), wt(G);
