@@ -2437,12 +2437,19 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
   }
   sec_end_on(c, SEC_DENSITIES, s);
   if ((rc = fields_batched(c, G, G, w->rhoL, w->kLR, w->kRL, w->gam, w->hsp, w->dLR, w->dRL, s))) return rc;
-  sec_begin_on(c, SEC_TRACES, s);
-  traces_partial_kernel<<<kTraceChunks, kTraceThreads, 0, s>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR,
-                                                               c->d_H1, w->tpart);
-  traces_finish_kernel<<<G, 9 * 32, 0, s>>>(G, w->tpart, c->H0, w->obs);
+  // the traces feed only the sums: on the second stream of the chain, beside
+  // the H20 products, joined before the chain ends
+  cudaStream_t st = c->streamM2 ? c->streamM2 : s;
+  if (st != s) {
+    TVAP_CUDA(cudaEventRecord(c->ev_stagger, s));
+    TVAP_CUDA(cudaStreamWaitEvent(st, c->ev_stagger, 0));
+  }
+  sec_begin_on(c, SEC_TRACES, st);
+  traces_partial_kernel<<<kTraceChunks, kTraceThreads, 0, st>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR,
+                                                                c->d_H1, w->tpart);
+  traces_finish_kernel<<<G, 9 * 32, 0, st>>>(G, w->tpart, c->H0, w->obs);
   TVAP_CUDA(cudaGetLastError());
-  sec_end_on(c, SEC_TRACES, s);
+  sec_end_on(c, SEC_TRACES, st);
   sec_begin_on(c, SEC_H20, s);
   // H20: T = U~^T (h V~ + fd/2 DeltaLR U~) - fd/2 V~^T DeltaRL V~, H20 = T - T^T,
   // as three products: X = [h | DeltaLR] [V~; fd/2 U~], Y = DeltaRL V~ and
@@ -2484,6 +2491,10 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
     if ((rc = gemm(g, s))) return rc;
   }
   sec_end_on(c, SEC_H20, s);
+  if (st != s) {
+    TVAP_CUDA(cudaEventRecord(c->ev_join2, st));
+    TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join2, 0));
+  }
   c->kernel_launches += 1 + 2 + 2 + 3 + 2 + 5;
   return TVAP_OK;
 }
