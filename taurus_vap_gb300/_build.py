@@ -68,7 +68,8 @@ def build_setup(force: bool = False) -> str:
 
 def build_gpu(force: bool = False, verbose_ptxas: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in GPU_SOURCES]
-    deps = srcs + [os.path.join(CSRC, h) for h in ("tvap_internal.cuh", "ozaki_core.cuh", "ozaki_tc.cuh")] + [
+    deps = srcs + [os.path.join(CSRC, h) for h in ("tvap_internal.cuh", "ozaki_core.cuh", "ozaki_tc.cuh",
+                                                   "ozaki_scaled.h")] + [
         os.path.join(INCLUDE, "tvap.h")
     ]
     if not (force or _stale(GPU_LIB, deps)):
