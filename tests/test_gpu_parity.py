@@ -158,6 +158,14 @@ def test_project_emax4_small_grid(emax4, gemm_mode):
     check_projection(mdl, U, V, 3, 3, 8, 8, 0, gemm_mode=gemm_mode)
 
 
+def test_project_emax4_full_grid(emax4):
+    # the benchmark's workload (n = 140, 15 x 15 angles, 113 folded pairs): the
+    # staggered groups of the solve, the reused digit planes and the traces
+    # beside H20 all run here
+    mdl, U, V = emax4
+    check_projection(mdl, U, V, 15, 15, 8, 8, 0)
+
+
 def test_emulated_gemm_matches_fp64_pipe(emax4):
     # the two arithmetic modes of the dense products agree to FP64 rounding
     mdl, U, V = emax4
