@@ -27,7 +27,11 @@
  *     are handed over once through tvap_init / tvap_set_hamiltonian;
  *   - every call returns a status code; the Fortran shim turns a non-zero
  *     code into the reference's `stop` (the reference has no status codes).
- *   - one context per host thread; a context is not re-entrant.
+ *   - one context per host thread; a context is not re-entrant.  Contexts on
+ *     different threads (and devices) may run at the same time: the settings
+ *     a call takes from its context are kept per thread, and each kernel's
+ *     shared-memory limit is raised once per device; every call works on the
+ *     device that is current on its thread, which tvap_init selects.
  */
 #ifndef TVAP_H
 #define TVAP_H

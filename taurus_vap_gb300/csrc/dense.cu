@@ -9,6 +9,9 @@
 // of DFMAs; memory traffic is secondary.
 
 #include <algorithm>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 #include "tvap_internal.cuh"
 
@@ -253,11 +256,11 @@ int pick_tile(int M, int N) {
 
 }  // namespace
 
-int g_gemm_mode = 2;
-int g_tc_grid_cap = 0;
-int* g_dev_flags = nullptr;
-tvap_ctx* g_tc_timing_ctx = nullptr;
-int g_tc_timing_sec = -1;
+thread_local int g_gemm_mode = 2;
+thread_local int g_tc_grid_cap = 0;
+thread_local int* g_dev_flags = nullptr;
+thread_local tvap_ctx* g_tc_timing_ctx = nullptr;
+thread_local int g_tc_timing_sec = -1;
 
 int gemm_split_k2(const GemmArgs& g, cudaStream_t s) {
   GemmArgs g1 = g;
@@ -632,12 +635,7 @@ int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cuda
   if (n > 512 || (n & 1)) return TVAP_ERR_ARG;
   const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 4 * size_t(n + 1) + size_t(n));
   if (shm <= jacobi32_smem_limit()) {
-    static bool attr = false;
-    if (!attr) {
-      TVAP_CUDA(cudaFuncSetAttribute(pfaffian_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(jacobi32_smem_limit())));
-      attr = true;
-    }
+    if (int rc = smem_opt_in((const void*)pfaffian_smem_kernel, jacobi32_smem_limit())) return rc;
     pfaffian_smem_kernel<<<batch, kPfThreads, shm, s>>>(n, A, pf, batch, flags);
   } else {
     pfaffian_kernel<<<batch, kPfThreads, 0, s>>>(n, A, pf, batch, flags);
@@ -957,23 +955,30 @@ size_t jacobi32_smem_bytes(int n) {
   return sizeof(float) * (2 * size_t(n) * (n | 1) + 4) + 16 * size_t(m / 2) + 64;
 }
 
-// largest dynamic shared memory the FP32 Jacobi kernel may request on this device
+// largest dynamic shared memory the FP32 Jacobi kernel may request on the
+// current device (found once per device)
 size_t jacobi32_smem_limit() {
-  static size_t limit = 0;
-  if (limit == 0) {
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncAttributes fa{};
-    cudaFuncGetAttributes(&fa, jacobi32_smem_kernel);
-    const size_t lim = (size_t(optin) > fa.sharedSizeBytes) ? size_t(optin) - fa.sharedSizeBytes : 0;
-    if (cudaFuncSetAttribute(jacobi32_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lim)) ==
-        cudaSuccess)
-      limit = lim;
-    else
-      limit = 1;  // unusable: callers fall back to the FP64 solver
+  static std::mutex m;
+  static std::vector<std::pair<int, size_t>> limits;  // (device, bytes)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
+    return 1;
   }
+  std::lock_guard<std::mutex> lock(m);
+  for (const auto& e : limits)
+    if (e.first == dev) return e.second;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  cudaFuncGetAttributes(&fa, jacobi32_smem_kernel);
+  const size_t lim = (size_t(optin) > fa.sharedSizeBytes) ? size_t(optin) - fa.sharedSizeBytes : 0;
+  size_t limit = 1;  // unusable: callers fall back to the FP64 solver
+  if (cudaFuncSetAttribute(jacobi32_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lim)) ==
+      cudaSuccess)
+    limit = lim;
+  cudaGetLastError();
+  limits.emplace_back(dev, limit);
   return limit;
 }
 
@@ -1126,12 +1131,7 @@ __global__ void __launch_bounds__(kCholThreads) cholesky_inverse_smem_kernel(int
 int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s) {
   const size_t shm = sizeof(double) * (size_t(n) * n + n);
   if (shm <= jacobi32_smem_limit()) {
-    static bool attr = false;
-    if (!attr) {
-      TVAP_CUDA(cudaFuncSetAttribute(cholesky_inverse_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(jacobi32_smem_limit())));
-      attr = true;
-    }
+    if (int rc = smem_opt_in((const void*)cholesky_inverse_smem_kernel, jacobi32_smem_limit())) return rc;
     cholesky_inverse_smem_kernel<<<1, kCholThreads, shm, s>>>(n, A, flags);
   } else {
     cholesky_inverse_kernel<<<1, 1024, 0, s>>>(n, A, flags);
@@ -1399,15 +1399,23 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
                          unsigned* bar, int* flags, cudaStream_t s) {
   const size_t shm = sizeof(double) * (size_t(n) * n + n);
   if (n > 384 || shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
-  static int grid = 0;
-  static size_t attr_shm = 0;
-  if (shm > attr_shm) {
-    TVAP_CUDA(cudaFuncSetAttribute(cholesky_evolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
-    attr_shm = shm;
-    int per_sm = 0, sms = 0;
-    TVAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cholesky_evolve_kernel, kCoopThreads, shm));
-    TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
-    grid = std::min(per_sm * sms, 128);
+  // the co-resident grid for this shared-memory size, found once per device
+  static std::mutex m;
+  static std::vector<std::pair<std::pair<int, size_t>, int>> grids;  // ((device, bytes), grid)
+  int dev = 0;
+  TVAP_CUDA(cudaGetDevice(&dev));
+  int grid = 0;
+  {
+    std::lock_guard<std::mutex> lock(m);
+    for (const auto& e : grids)
+      if (e.first.first == dev && e.first.second == shm) grid = e.second;
+    if (grid == 0) {
+      if (int rc = smem_opt_in((const void*)cholesky_evolve_kernel, shm)) return rc;
+      int per_sm = 0;
+      TVAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cholesky_evolve_kernel, kCoopThreads, shm));
+      grid = std::min(per_sm * device_sms(), 128);
+      if (grid >= 1) grids.push_back({{dev, shm}, grid});
+    }
   }
   if (grid < 1) return TVAP_ERR_ARG;
   TVAP_CUDA(cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned), s));

@@ -512,15 +512,8 @@ int apply_one_tc(tvap_ctx* c, const FieldDense& f, int ncol, int ldc, const doub
   slice_fields_tc_kernel<DELTA><<<(f.tc_nchunks + f.tc_nempty + 3) / 4, 128, 0, s>>>(
       n, ncol, ncols_tot, ntn, ldc, X0, X1, f.colperm, f.blocks, f.tcb, f.tc_chunks, f.tc_nchunks,
       f.rowperm + f.tc_empty_base, f.tc_nempty, eb, xt, c->d_H1, out0, out1);
-  static bool attr = false;
-  if (!attr) {
-    TVAP_CUDA(cudaFuncSetAttribute(field_tc_kernel<DELTA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(oztc::kSmemBytes)));
-    attr = true;
-  }
-  static int sms = 0;
-  if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
-  const int grid = std::min(f.tc_nbm * ntn, sms);
+  if ((rc = smem_opt_in((const void*)field_tc_kernel<DELTA>, oztc::kSmemBytes))) return rc;
+  const int grid = std::min(f.tc_nbm * ntn, device_sms());
   field_tc_kernel<DELTA><<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(
       n, ncol, ncols_tot, ntn, ldc, f.blocks, f.tcb, f.tc_bm, f.tc_nbm, static_cast<const __nv_bfloat16*>(f.wt), xt,
       f.ea, f.rowperm, eb, c->d_H1, out0, out1, counter, g_dev_flags);
@@ -546,11 +539,7 @@ int apply_one(tvap_ctx* c, const FieldDense& f, int ncol, int ldc, const double2
   slice_cols_kernel<<<dim3(f.ktot / kTile, npad / kTile), 256, 0, s>>>(f.ktot, npad, ncol, ncols_tot, ldc, X0, X1,
                                                                        f.colperm, eb, bd);
   const size_t shm = oz::Shape<1, 2>::kSmemBytes;
-  static bool attr = false;
-  if (!attr) {
-    TVAP_CUDA(cudaFuncSetAttribute(field_mma_kernel<DELTA>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
-    attr = true;
-  }
+  if (int r = smem_opt_in((const void*)field_mma_kernel<DELTA>, shm)) return r;
   field_mma_kernel<DELTA><<<dim3(npad / kTile, f.ntiles), oz::kThreads, shm, s>>>(
       n, ncol, ncols_tot, ldc, npad, f.ktot, f.blocks, f.tiles, static_cast<const __nv_bfloat16*>(f.wd), f.ea, f.rowperm, bd, eb, c->d_H1, out0, out1);
   TVAP_CUDA(cudaGetLastError());

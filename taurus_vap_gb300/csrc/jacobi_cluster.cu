@@ -262,11 +262,8 @@ int jacobi_cluster(int n, const double* M, int m_transposed, const double* W0, d
   if (bw > kJcMaxBw) return TVAP_ERR_ARG;
   const size_t shm = sizeof(float) * 8 * size_t(bw) * n;
   if (shm > size_t(200) * 1024) return TVAP_ERR_ARG;
-  static size_t granted = 48 * 1024;
-  if (shm > granted) {
-    TVAP_CUDA(cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
-    granted = shm;
-  }
+  if (shm > 48 * 1024)
+    if (int rc = smem_opt_in((const void*)jacobi_cluster_kernel, shm)) return rc;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kJcCtas);
   cfg.blockDim = dim3(kJcThreads);

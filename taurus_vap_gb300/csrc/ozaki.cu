@@ -144,11 +144,7 @@ int launch_ozaki_mma(int M, int N, int mpad, int npad, int kpad, const __nv_bflo
                      const __nv_bfloat16* Bs, const int* eb, const GemmArgs& g, cudaStream_t s) {
   const int a_shared = g.A.bs == 0 ? 1 : 0, b_shared = g.B.bs == 0 ? 1 : 0;
   const size_t shm = oz::Shape<PA, PB>::kSmemBytes;
-  static bool attr = false;
-  if (!attr) {
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_mma_kernel<PA, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
-    attr = true;
-  }
+  if (int rc = smem_opt_in((const void*)ozaki_mma_kernel<PA, PB>, shm)) return rc;
   dim3 grid(npad / oz::kTile, mpad / oz::kTile, g.batch);
   ozaki_mma_kernel<PA, PB><<<grid, oz::kThreads, shm, s>>>(M, N, mpad, npad, kpad, As, ea, Bs, eb, g, a_shared,
                                                             b_shared);
@@ -618,12 +614,8 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   int* eb = sc->ex + size_t(a_slots) * a_rows_pad;
   const size_t slice_shm = sizeof(double2) * 8 * size_t(K);
   if (slice_shm > 48 * 1024) {
-    static size_t granted = 48 * 1024;
     if (slice_shm > size_t(227) * 1024) return TVAP_ERR_ARG;
-    if (slice_shm > granted) {
-      TVAP_CUDA(cudaFuncSetAttribute(slice_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(slice_shm)));
-      granted = slice_shm;
-    }
+    if ((rc = smem_opt_in((const void*)slice_tc_kernel, slice_shm))) return rc;
   }
   LeftSlice left;
   left.valid = true;
@@ -665,33 +657,19 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   o.a_rows = xa.xrows;
   o.b_rows = xb.xrows;
   o.nstack = xa.nstack;
-  static bool attr = false;
-  if (!attr) {
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<true, 48>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(oztc::kSmemBytes)));
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(oztc::kSmemBytes)));
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<false, 48>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(oztc::kSmemBytes)));
-    TVAP_CUDA(cudaFuncSetAttribute(ozaki_tc_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(oztc::kSmemBytes)));
-    attr = true;
-  }
-  static int sms = 0;
-  if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+  const int sms = device_sms();
   const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / bn) * a_slots;
   const int grid = int(std::min<long long>(ntiles, g_tc_grid_cap > 0 ? std::min(sms, g_tc_grid_cap) : sms));
+  // the instantiation: alpha = +-1 (a sign in the integer conversion) or
+  // general, and the B' tile width
+  const bool unit_alpha = g_alpha_unit(o.alpha);
+  auto kern = unit_alpha ? (bn == 48 ? ozaki_tc_kernel<true, 48> : ozaki_tc_kernel<true, 64>)
+                         : (bn == 48 ? ozaki_tc_kernel<false, 48> : ozaki_tc_kernel<false, 64>);
+  if ((rc = smem_opt_in((const void*)kern, oztc::kSmemBytes))) return rc;
   TVAP_CUDA(cudaMemsetAsync(sc->counter, 0, sizeof(int), s));
   if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);
-  const bool unit_alpha = g_alpha_unit(o.alpha);
-  auto launch = [&](auto kern) {
-    kern<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad, b_slots == 1 ? 1 : 0,
-                                                        a_slots, nks, o, sc->counter, g_dev_flags);
-  };
-  if (unit_alpha)
-    bn == 48 ? launch(ozaki_tc_kernel<true, 48>) : launch(ozaki_tc_kernel<true, 64>);
-  else
-    bn == 48 ? launch(ozaki_tc_kernel<false, 48>) : launch(ozaki_tc_kernel<false, 64>);
+  kern<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad, b_slots == 1 ? 1 : 0,
+                                                      a_slots, nks, o, sc->counter, g_dev_flags);
   if (g_tc_timing_ctx) sec_end_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;

@@ -1976,12 +1976,7 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
   const long long tstride = (long long)tinv_stride(n);
   int rc;
   if (smem_path && panel_bytes > 48 * 1024) {
-    static bool attr = false;
-    if (!attr) {
-      TVAP_CUDA(cudaFuncSetAttribute(panel_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(jacobi32_smem_limit())));
-      attr = true;
-    }
+    if (int r = smem_opt_in((const void*)panel_factor_kernel, jacobi32_smem_limit())) return r;
   }
   {
     dim3 grid(std::max(1, (2 * n + 15) / 16), G);
@@ -2023,8 +2018,7 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     c->kernel_launches += 1;  // build_augmented_kernel
     const bool split = c->streamM2 && G >= 32;
     if (!split) return gj_solve_range(c, 0, G, nb, s, nullptr);
-    static int sms = 0;
-    if (!sms) TVAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+    const int sms = device_sms();
     const int G1 = (G + 1) / 2, G2 = G - G1;
     TcGridCap cap(std::max(sms - G1, sms / 2));
     if ((rc = gj_solve_range(c, 0, G1, nb, s, c->ev_stagger))) return rc;

@@ -5,6 +5,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "tvap_internal.cuh"
 
@@ -14,6 +16,46 @@ static thread_local std::string g_last_error;
 
 void set_last_error(const char* msg, const char* file, int line) {
   g_last_error = std::string(msg) + " (" + file + ":" + std::to_string(line) + ")";
+}
+
+namespace {
+struct SmemGrant {
+  int device;
+  const void* func;
+  size_t bytes;
+};
+std::mutex g_smem_mutex;
+std::vector<SmemGrant> g_smem_grants;
+std::mutex g_sms_mutex;
+std::vector<std::pair<int, int>> g_sms;  // (device, SM count)
+}  // namespace
+
+int smem_opt_in(const void* func, size_t bytes) {
+  int dev = 0;
+  TVAP_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_smem_mutex);
+  SmemGrant* g = nullptr;
+  for (auto& e : g_smem_grants)
+    if (e.device == dev && e.func == func) g = &e;
+  if (g && g->bytes >= bytes) return TVAP_OK;
+  TVAP_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+  if (g)
+    g->bytes = bytes;
+  else
+    g_smem_grants.push_back({dev, func, bytes});
+  return TVAP_OK;
+}
+
+int device_sms() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lock(g_sms_mutex);
+  for (const auto& e : g_sms)
+    if (e.first == dev) return e.second;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  g_sms.emplace_back(dev, sms);
+  return sms;
 }
 
 int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
@@ -351,6 +393,8 @@ int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, cons
     return TVAP_ERR_ARG;
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   c->kernel_launches = 0;
+  g_gemm_mode = c->gemm_mode;
+  g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n, tot = nn * ncol;
   cudaStream_t s = c->stream;
@@ -382,6 +426,8 @@ int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, cons
   }
   c->kernel_launches += 7;
   cudaFree(buf);
+  // the status word: a bounded wait of the tensor-core field kernels that gave up
+  if (rc == TVAP_OK) rc = check_flags(c);
   return rc;
 }
 

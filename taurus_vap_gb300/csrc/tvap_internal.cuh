@@ -72,6 +72,12 @@ __host__ __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) +
   } while (0)
 
 void set_last_error(const char* msg, const char* file, int line);
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device (cudaFuncSetAttribute acts per device); once per device and
+// kernel, under a lock, so contexts on several threads and devices may call it.
+int smem_opt_in(const void* func, size_t bytes);
+// Streaming multiprocessors of the current device (cached per device).
+int device_sms();
 
 // device status word bits, written by kernels and read back by the host
 enum DevFlag : int {
@@ -134,21 +140,22 @@ void oz_release(cudaStream_t s);
 int oz_scratch(cudaStream_t s, size_t bytes, size_t ex_count, __nv_bfloat16** buf, int** ex);
 // GEMM arithmetic of the calls in flight: 0 FP64 pipe, 1 emulated with
 // mma.sync, 2 emulated with tcgen05 (set by every C-ABI entry point from its
-// context), and the status word of that context
-extern int g_gemm_mode;
+// context), and the status word of that context.  These call-scoped settings
+// are per host thread: each thread drives its own context.
+extern thread_local int g_gemm_mode;
 // upper bound on the CTAs of a tcgen05 product (0: one per SM), set while
 // two streams share the SMs with kernels that need their own
-extern int g_tc_grid_cap;
+extern thread_local int g_tc_grid_cap;
 struct TcGridCap {
   int saved;
   explicit TcGridCap(int cap) : saved(g_tc_grid_cap) { g_tc_grid_cap = cap; }
   ~TcGridCap() { g_tc_grid_cap = saved; }
 };
-extern int* g_dev_flags;
+extern thread_local int* g_dev_flags;
 // when set, the tensor-memory product launches are timed into this section
 // of this context (the H20 products; the host issues them one after the other)
-extern tvap_ctx* g_tc_timing_ctx;
-extern int g_tc_timing_sec;
+extern thread_local tvap_ctx* g_tc_timing_ctx;
+extern thread_local int g_tc_timing_sec;
 struct TcTimingScope {
   TcTimingScope(tvap_ctx* c, int sec) {
     g_tc_timing_ctx = c;
