@@ -26,6 +26,7 @@ ERRORS = {
     15: "error in the inverse of L (evolve_wavefunction)",
     16: "canonical basis: eigen solver did not converge or degenerate block > 2",
     18: "particle numbers wrong three times in the last five iterations",
+    19: "a bounded wait inside a device kernel ran out (the kernel stopped and released its resources)",
 }
 
 
@@ -72,6 +73,7 @@ def lib():
         L.tvap_kernel_launches.argtypes = [vp]
         L.tvap_kernel_launches.restype = ci
         L.tvap_set_stream.argtypes = [vp, vp]
+        L.tvap_set_stream.restype = ci
         L.tvap_set_timing.argtypes = [vp, ci]
         L.tvap_set_timing.restype = ci
         L.tvap_get_timing.argtypes = [vp, vp, vp, ci]
@@ -187,7 +189,9 @@ class Context:
         _check(lib().tvap_set_gemm_mode(self.h, int(mode)), "tvap_set_gemm_mode")
 
     def set_stream(self, stream_handle: int):
-        lib().tvap_set_stream(self.h, ctypes.c_void_p(stream_handle))
+        """Run the context's calls in order on this CUDA stream (a raw
+        cudaStream_t handle, e.g. torch.cuda.Stream.cuda_stream)."""
+        _check(lib().tvap_set_stream(self.h, ctypes.c_void_p(stream_handle)), "tvap_set_stream")
 
     def set_hamiltonian(self, ham):
         abcd = np.ascontiguousarray(ham.abcd, dtype=np.int16)

@@ -31,3 +31,15 @@ def test_setup_library_exports_header():
     L = ctypes.CDLL(_build.build_setup())
     for name in declared("tvap_setup.h"):
         assert hasattr(L, name), name
+
+
+def test_every_status_code_has_a_message():
+    """The binding names every status code the header declares."""
+    from taurus_vap_gb300 import native
+
+    text = open(os.path.join(ROOT, "include", "tvap.h")).read()
+    codes = {int(v) for v in re.findall(r"\bTVAP_ERR_[A-Z0-9_]+\s*=\s*(\d+)", text)}
+    assert codes and 19 in codes
+    assert codes <= set(native.ERRORS), sorted(codes - set(native.ERRORS))
+    err = native.TvapError(19, "tvap_project", "detail")
+    assert err.code == 19 and "bounded wait" in str(err) and "detail" in str(err)
