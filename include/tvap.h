@@ -93,11 +93,12 @@ int tvap_set_stream(tvap_ctx* ctx, void* cuda_stream);
 const char* tvap_last_error(void);
 /* Number of kernels the last top-level call launched. */
 int tvap_kernel_launches(const tvap_ctx* ctx);
-/* Optional per-section timing with CUDA events on the context's stream
- * (sections: canonical basis, angle-independent blocks, Thouless solve,
- * U~/V~, densities, Gamma gather, Delta gather, traces, H20, overlap,
- * Pfaffian, sums, gradient, evolve).  tvap_set_timing resets the totals;
- * tvap_get_timing returns milliseconds and call counts per section. */
+/* Optional per-section timing with CUDA events on the streams the sections
+ * run on (sections, in this order: canonical basis, angle-independent
+ * blocks, Thouless solve, U~/V~, densities, Gamma field, Delta field,
+ * traces, H20, overlap, Pfaffian, sums, gradient, evolve, and the tcgen05
+ * launches of H20).  tvap_set_timing resets the totals; tvap_get_timing
+ * returns milliseconds and call counts per section. */
 int tvap_set_timing(tvap_ctx* ctx, int on);
 /* Arithmetic of the dense products: 0 = the FP64 pipe (DFMA);
  * 1 = FP64 emulated on the bf16 tensor cores by exact integer splitting (8
@@ -137,8 +138,10 @@ int tvap_set_hamiltonian(tvap_ctx* ctx, int64_t S, const int16_t* abcd, const fl
 int tvap_calculate_fields(tvap_ctx* ctx, const double* rhoLR, const double* kappaLR, const double* kappaRL,
                           double* gammaLR, double* hspLR, double* deltaLR, double* deltaRL);
 
-/* calculate_fields for `ncol` independent density sets stored one after the
- * other (matrix c at offset c*n*n complex elements). */
+/* calculate_fields for `ncol` (1..256) independent density sets stored one
+ * after the other (matrix c at offset c*n*n complex elements).  The call
+ * allocates its staging buffers (8 ncol n^2 complex values) and frees them
+ * before it returns; cudaFree waits for the whole device. */
 int tvap_calculate_fields_batched(tvap_ctx* ctx, int ncol, const double* rhoLR, const double* kappaLR,
                                   const double* kappaRL, double* gammaLR, double* hspLR, double* deltaLR,
                                   double* deltaRL);
@@ -174,10 +177,11 @@ int tvap_evolve(tvap_ctx* ctx, const double* U0, const double* V0, const double*
 /* tvap_evolve for callers that cannot allocate device memory: the same
  * Thouless evolution, with every matrix (U0, V0, Z in; U1, V1 out) in device
  * memory and the work buffers taken from a fixed array inside the library
- * instead of cudaMalloc.  tvap_evolve allocates and frees its buffers on every
- * call, and cudaFree waits for the whole device; a caller that keeps other
- * work running on the GPU, or whose device memory is owned by its own pool
- * allocator, cannot accept that.  No counterpart in the reference.
+ * instead of cudaMalloc.  tvap_evolve keeps its work buffer in the context,
+ * allocated on first use and replaced when a larger one is needed (cudaFree
+ * of the old one waits for the whole device); a caller whose device memory
+ * is owned by its own pool allocator, or that cannot accept such a wait,
+ * uses this variant.  No counterpart in the reference.
  *   - limit: n <= 336 (the array holds 3 n^2 + n doubles for n = 336, about
  *     2.6 MB, kept on every GPU that loads the library until the process ends);
  *     larger n is rejected with TVAP_ERR_ARG;
