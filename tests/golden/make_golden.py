@@ -8,6 +8,7 @@ Sources (paths inside the reference project):
   examples/gradient_mg24/data/initial_wf.txt          deterministic seed
   examples/gradient_mg24/data/results_vap_benchmark   PNVAP M=5 table
   examples/gradient_mg24/data/results_hfb_benchmark   HFB table
+  examples/minima_usdb/data/results_benchmark         USDB minima (random seeds)
 """
 import os
 import shutil
@@ -19,6 +20,7 @@ FILES = {
     "examples/gradient_mg24/data/initial_wf.txt": "mg24_initial_wf.txt",
     "examples/gradient_mg24/data/results_vap_benchmark": "mg24_results_vap_benchmark",
     "examples/gradient_mg24/data/results_hfb_benchmark": "mg24_results_hfb_benchmark",
+    "examples/minima_usdb/data/results_benchmark": "usdb_minima_benchmark",
 }
 
 if __name__ == "__main__":
