@@ -464,31 +464,38 @@ def cpu_baseline(mdl, U, V, args):
                       f"warm-up, {cores} threads; median {med:.2f} s/iteration"}
 
 
+REFERENCE_WARMUP_BUDGET_S = 30.0
+REFERENCE_TIMED_BUDGET_S = 150.0
+
+
 def run_reference(args):
     """--impl reference: the oracle's gradient loop on the host cores, W
-    warm-up and K timed iterations of the full workload (rank 0 only)."""
+    warm-up and K timed iterations of the full workload (rank 0 only).  An
+    iteration takes seconds on the CPU, so the warm-up stops after 30 s and
+    the timed iterations after 150 s (at least one of each); `steps` reports
+    the iterations timed."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     mdl, U, V = build_workload()
     cores = os.cpu_count() or 1
     vap = _oracle_vap(mdl, U, V, cores)
-    for _ in range(args.warmup):
-        vap.iterate()
+    warm = _timed_iterations(vap, max(1, args.warmup), REFERENCE_WARMUP_BUDGET_S)
     t_start = time.perf_counter()
-    times = _timed_iterations(vap, max(1, args.steps), 1e30)
+    times = _timed_iterations(vap, max(1, args.steps), REFERENCE_TIMED_BUDGET_S)
     elapsed = time.perf_counter() - t_start
     value = len(times) / elapsed
     ms = 1000.0 * elapsed / len(times)
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": len(times), "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "steps": len(times), "warmup": len(warm), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": WORKLOAD, "form": "CPU restatement of the reference path (oracle/), OpenMP fields + "
                                                  "threaded BLAS/LAPACK"},
         "cpu_baseline": {"value": value, "unit": "iters/s", "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} oracle iterations of the full workload after {args.warmup} "
-                                   f"warm-up, {cores} threads"},
+                         "sample": f"{len(times)} oracle iterations of the full workload after {len(warm)} "
+                                   f"warm-up, {cores} threads (timed iterations stop after "
+                                   f"{REFERENCE_TIMED_BUDGET_S:.0f} s)"},
         "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
