@@ -143,7 +143,7 @@ class DeviceIteration:
         self.U, self.U1 = self.U1, self.U
         self.V, self.V1 = self.V1, self.V
         self.Zim1.copy_(self.Zi)
-        self.launches += k + 1  # + the Zim1 copy
+        self.launches += k  # this library's kernels (the Zim1 copy is torch's)
         self.energy = (self.pnp.c("ener") / self.pnp.c("over")).real
 
 

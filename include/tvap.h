@@ -91,7 +91,9 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
 void tvap_destroy(tvap_ctx* ctx);
 int tvap_set_stream(tvap_ctx* ctx, void* cuda_stream);
 const char* tvap_last_error(void);
-/* Number of kernels the last top-level call launched. */
+/* Number of kernels the last top-level call launched: every launch of this
+ * library (counted where it is issued); the CUB sort and scan inside
+ * tvap_set_hamiltonian launch kernels of their own that are not counted. */
 int tvap_kernel_launches(const tvap_ctx* ctx);
 /* Optional per-section timing with CUDA events on the streams the sections
  * run on (sections, in this order: canonical basis, angle-independent

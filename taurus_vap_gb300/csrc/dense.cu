@@ -219,7 +219,7 @@ __global__ void __launch_bounds__((TM / 2) * (TN / 2)) gemm3m_kernel(GemmArgs g)
 template <int T, typename TA, typename TB>
 void launch_gemm_t(const GemmArgs& g, cudaStream_t s) {
   dim3 grid((g.N + T - 1) / T, (g.M + T - 1) / T, g.batch);
-  gemm_kernel<T, T, TA, TB><<<grid, (T / 2) * (T / 2), 0, s>>>(g);
+  gemm_kernel<T, T, TA, TB><<<grid, (T / 2) * (T / 2), 0, tvap::counted(s)>>>(g);
 }
 
 template <int T>
@@ -232,7 +232,7 @@ void launch_gemm_tile(const GemmArgs& g, cudaStream_t s) {
     launch_gemm_t<T, double2, double>(g, s);
   else if (g.three_m) {
     dim3 grid((g.N + T - 1) / T, (g.M + T - 1) / T, g.batch);
-    gemm3m_kernel<T, T><<<grid, (T / 2) * (T / 2), 0, s>>>(g);
+    gemm3m_kernel<T, T><<<grid, (T / 2) * (T / 2), 0, tvap::counted(s)>>>(g);
   } else
     launch_gemm_t<T, double2, double2>(g, s);
 }
@@ -261,6 +261,7 @@ thread_local int g_tc_grid_cap = 0;
 thread_local int* g_dev_flags = nullptr;
 thread_local tvap_ctx* g_tc_timing_ctx = nullptr;
 thread_local int g_tc_timing_sec = -1;
+thread_local long long g_launch_count = 0;
 
 int gemm_split_k2(const GemmArgs& g, cudaStream_t s) {
   GemmArgs g1 = g;
@@ -636,9 +637,9 @@ int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cuda
   const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 4 * size_t(n + 1) + size_t(n));
   if (shm <= jacobi32_smem_limit()) {
     if (int rc = smem_opt_in((const void*)pfaffian_smem_kernel, jacobi32_smem_limit())) return rc;
-    pfaffian_smem_kernel<<<batch, kPfThreads, shm, s>>>(n, A, pf, batch, flags);
+    pfaffian_smem_kernel<<<batch, kPfThreads, shm, tvap::counted(s)>>>(n, A, pf, batch, flags);
   } else {
-    pfaffian_kernel<<<batch, kPfThreads, 0, s>>>(n, A, pf, batch, flags);
+    pfaffian_kernel<<<batch, kPfThreads, 0, tvap::counted(s)>>>(n, A, pf, batch, flags);
   }
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
@@ -791,7 +792,7 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
 int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s) {
   const int m = (n + 1) & ~1;
   const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
-  jacobi_kernel<double><<<1, kJacThreads, shm, s>>>(n, A, W, evals, work, flags, 1.0e-30);
+  jacobi_kernel<double><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-30);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }
@@ -799,7 +800,7 @@ int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* 
 int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s) {
   const int m = (n + 1) & ~1;
   const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
-  jacobi_kernel<float><<<1, kJacThreads, shm, s>>>(n, A, W, evals, work, flags, 1.0e-13);
+  jacobi_kernel<float><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-13);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }
@@ -985,7 +986,7 @@ size_t jacobi32_smem_limit() {
 int jacobi32_smem(int n, const double* A, const double* W0, double* W, int* sweeps_out, cudaStream_t s) {
   const size_t shm = jacobi32_smem_bytes(n);
   if (shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
-  jacobi32_smem_kernel<<<1, 1024, shm, s>>>(n, A, W0, W, sweeps_out);
+  jacobi32_smem_kernel<<<1, 1024, shm, tvap::counted(s)>>>(n, A, W0, W, sweeps_out);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }
@@ -1132,9 +1133,9 @@ int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s) {
   const size_t shm = sizeof(double) * (size_t(n) * n + n);
   if (shm <= jacobi32_smem_limit()) {
     if (int rc = smem_opt_in((const void*)cholesky_inverse_smem_kernel, jacobi32_smem_limit())) return rc;
-    cholesky_inverse_smem_kernel<<<1, kCholThreads, shm, s>>>(n, A, flags);
+    cholesky_inverse_smem_kernel<<<1, kCholThreads, shm, tvap::counted(s)>>>(n, A, flags);
   } else {
-    cholesky_inverse_kernel<<<1, 1024, 0, s>>>(n, A, flags);
+    cholesky_inverse_kernel<<<1, 1024, 0, tvap::counted(s)>>>(n, A, flags);
   }
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
@@ -1420,6 +1421,7 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
   if (grid < 1) return TVAP_ERR_ARG;
   TVAP_CUDA(cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned), s));
   void* args[] = {&n, &S, &A, &a_stride, &X, &x_stride, &bar, &flags};
+  ++g_launch_count;
   TVAP_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_evolve_kernel, dim3(grid), dim3(kCoopThreads), args,
                                         shm, s));
   return TVAP_OK;

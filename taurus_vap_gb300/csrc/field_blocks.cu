@@ -508,17 +508,16 @@ int apply_one_tc(tvap_ctx* c, const FieldDense& f, int ncol, int ldc, const doub
   int* counter = reinterpret_cast<int*>(xt + xt_elems);
   TVAP_CUDA(cudaMemsetAsync(eb, 0, sizeof(int) * npad, s));
   TVAP_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s));
-  colexp_kernel<<<dim3(npad / 32, 64), 256, 0, s>>>(nent, ncol, ncols_tot, ldc, X0, X1, eb);
-  slice_fields_tc_kernel<DELTA><<<(f.tc_nchunks + f.tc_nempty + 3) / 4, 128, 0, s>>>(
+  colexp_kernel<<<dim3(npad / 32, 64), 256, 0, tvap::counted(s)>>>(nent, ncol, ncols_tot, ldc, X0, X1, eb);
+  slice_fields_tc_kernel<DELTA><<<(f.tc_nchunks + f.tc_nempty + 3) / 4, 128, 0, tvap::counted(s)>>>(
       n, ncol, ncols_tot, ntn, ldc, X0, X1, f.colperm, f.blocks, f.tcb, f.tc_chunks, f.tc_nchunks,
       f.rowperm + f.tc_empty_base, f.tc_nempty, eb, xt, c->d_H1, out0, out1);
   if ((rc = smem_opt_in((const void*)field_tc_kernel<DELTA>, oztc::kSmemBytes))) return rc;
   const int grid = std::min(f.tc_nbm * ntn, device_sms());
-  field_tc_kernel<DELTA><<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(
+  field_tc_kernel<DELTA><<<grid, oztc::kThreads, oztc::kSmemBytes, tvap::counted(s)>>>(
       n, ncol, ncols_tot, ntn, ldc, f.blocks, f.tcb, f.tc_bm, f.tc_nbm, static_cast<const __nv_bfloat16*>(f.wt), xt,
       f.ea, f.rowperm, eb, c->d_H1, out0, out1, counter, g_dev_flags);
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += 3;
   return TVAP_OK;
 }
 
@@ -535,15 +534,14 @@ int apply_one(tvap_ctx* c, const FieldDense& f, int ncol, int ldc, const double2
   if ((rc = oz_scratch(s, sizeof(__nv_bfloat16) * size_t(kDigits) * 2 * npad * f.ktot, size_t(npad), &bd, &eb)))
     return rc;
   TVAP_CUDA(cudaMemsetAsync(eb, 0, sizeof(int) * npad, s));
-  colexp_kernel<<<dim3(npad / 32, 64), 256, 0, s>>>(nent, ncol, ncols_tot, ldc, X0, X1, eb);
-  slice_cols_kernel<<<dim3(f.ktot / kTile, npad / kTile), 256, 0, s>>>(f.ktot, npad, ncol, ncols_tot, ldc, X0, X1,
+  colexp_kernel<<<dim3(npad / 32, 64), 256, 0, tvap::counted(s)>>>(nent, ncol, ncols_tot, ldc, X0, X1, eb);
+  slice_cols_kernel<<<dim3(f.ktot / kTile, npad / kTile), 256, 0, tvap::counted(s)>>>(f.ktot, npad, ncol, ncols_tot, ldc, X0, X1,
                                                                        f.colperm, eb, bd);
   const size_t shm = oz::Shape<1, 2>::kSmemBytes;
   if (int r = smem_opt_in((const void*)field_mma_kernel<DELTA>, shm)) return r;
-  field_mma_kernel<DELTA><<<dim3(npad / kTile, f.ntiles), oz::kThreads, shm, s>>>(
+  field_mma_kernel<DELTA><<<dim3(npad / kTile, f.ntiles), oz::kThreads, shm, tvap::counted(s)>>>(
       n, ncol, ncols_tot, ldc, npad, f.ktot, f.blocks, f.tiles, static_cast<const __nv_bfloat16*>(f.wd), f.ea, f.rowperm, bd, eb, c->d_H1, out0, out1);
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += 3;
   return TVAP_OK;
 }
 

@@ -136,7 +136,7 @@ int sort_and_compress(long long m, int nrows, int* key, int* src, double* coef, 
   TVAP_CUDA(cudaMalloc(&key_out, sizeof(int) * m));
   const int tb = 256;
   const long long gb = (m + tb - 1) / tb;
-  iota_kernel<<<gb, tb, 0, s>>>(m, slot_in);
+  iota_kernel<<<gb, tb, 0, tvap::counted(s)>>>(m, slot_in);
   size_t tmp_bytes = 0;
   int end_bit = 1;
   while ((1LL << end_bit) <= (long long)kInvalid && end_bit < 31) ++end_bit;
@@ -148,7 +148,7 @@ int sort_and_compress(long long m, int nrows, int* key, int* src, double* coef, 
   long long* d_nnz = nullptr;
   TVAP_CUDA(cudaMalloc(&d_nnz, sizeof(long long)));
   TVAP_CUDA(cudaMemsetAsync(d_nnz, 0, sizeof(long long), s));
-  count_valid_kernel<<<gb, tb, 0, s>>>(m, key_out, d_nnz);
+  count_valid_kernel<<<gb, tb, 0, tvap::counted(s)>>>(m, key_out, d_nnz);
   long long nnz = 0;
   TVAP_CUDA(cudaMemcpyAsync(&nnz, d_nnz, sizeof(long long), cudaMemcpyDeviceToHost, s));
   TVAP_CUDA(cudaStreamSynchronize(s));
@@ -157,7 +157,7 @@ int sort_and_compress(long long m, int nrows, int* key, int* src, double* coef, 
   TVAP_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (nrows + 1), s));
   int* rowptr = nullptr;
   TVAP_CUDA(cudaMalloc(&rowptr, sizeof(int) * (nrows + 1)));
-  if (nnz > 0) count_rows_kernel<<<(nnz + tb - 1) / tb, tb, 0, s>>>(nnz, key_out, counts);
+  if (nnz > 0) count_rows_kernel<<<(nnz + tb - 1) / tb, tb, 0, tvap::counted(s)>>>(nnz, key_out, counts);
   size_t scan_bytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, counts, rowptr, nrows + 1, s);
   void* scan_tmp = nullptr;
@@ -167,7 +167,7 @@ int sort_and_compress(long long m, int nrows, int* key, int* src, double* coef, 
   double* coefs = nullptr;
   TVAP_CUDA(cudaMalloc(&srcs, sizeof(int) * std::max(1LL, nnz)));
   TVAP_CUDA(cudaMalloc(&coefs, sizeof(double) * std::max(1LL, nnz)));
-  if (nnz > 0) gather_sorted_kernel<<<(nnz + tb - 1) / tb, tb, 0, s>>>(nnz, slot_out, src, coef, srcs, coefs);
+  if (nnz > 0) gather_sorted_kernel<<<(nnz + tb - 1) / tb, tb, 0, tvap::counted(s)>>>(nnz, slot_out, src, coef, srcs, coefs);
   TVAP_CUDA(cudaGetLastError());
   TVAP_CUDA(cudaStreamSynchronize(s));
   cudaFree(slot_in);
@@ -204,7 +204,7 @@ int build_field_csr(tvap_ctx* c) {
   TVAP_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (S > 0) {
     const int tb = 256;
-    decode_kernel<<<(2 * S + tb - 1) / tb, tb, 0, s>>>(S, n, c->d_abcd, c->d_h2, c->d_trperm, c->d_sp_2mj,
+    decode_kernel<<<(2 * S + tb - 1) / tb, tb, 0, tvap::counted(s)>>>(S, n, c->d_abcd, c->d_h2, c->d_trperm, c->d_sp_2mj,
                                                        c->d_sp_tr, gkey, gsrc, gcoef, dkey, dsrc, dcoef, bad);
     TVAP_CUDA(cudaGetLastError());
   }
@@ -386,12 +386,12 @@ void launch_fields(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
   const int n = c->n;
   const long long rows = (long long)n * n;
   sec_begin_on(c, SEC_FIELDS_GAMMA, s);
-  gamma_gather_kernel<CPL><<<(rows + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, s>>>(
+  gamma_gather_kernel<CPL><<<(rows + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, tvap::counted(s)>>>(
       n, ncol, ldc, c->csr.g_rowptr, c->csr.g_src, c->csr.g_coef, rho, c->d_H1, gamma, hsp);
   sec_end_on(c, SEC_FIELDS_GAMMA, s);
   sec_begin_on(c, SEC_FIELDS_DELTA, s);
   const long long tri = (long long)n * (n + 1) / 2;
-  delta_gather_kernel<CPL><<<(tri + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, s>>>(
+  delta_gather_kernel<CPL><<<(tri + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, tvap::counted(s)>>>(
       n, ncol, ldc, c->csr.d_rowptr, c->csr.d_src, c->csr.d_coef, kLR, kRL, dLR, dRL);
   sec_end_on(c, SEC_FIELDS_DELTA, s);
 }
@@ -419,7 +419,6 @@ int fields_batched(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
   else
     return TVAP_ERR_ARG;
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += 2;
   return TVAP_OK;
 }
 

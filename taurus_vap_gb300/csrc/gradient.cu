@@ -91,7 +91,7 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1, bool
   const View Zv = view_cm(b.Z, n, 0);
   sec_begin(c, SEC_EVOLVE);
   if ((rc = rgemm(n, n, n, view_t(Zv), Zv, b.L, n, 1.0, 0.0, s))) return rc;
-  add_identity_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, b.L);
+  add_identity_kernel<<<(n + 255) / 256, 256, 0, tvap::counted(s)>>>(n, b.L);
   TVAP_CUDA(cudaMemcpyAsync(b.A1, b.U0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   TVAP_CUDA(cudaMemcpyAsync(b.A2, b.V0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   const bool coop = !want_linv && c->d_bar;
@@ -124,7 +124,6 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1, bool
                               c->d_flags, s);
     if (rc == TVAP_OK) {
       sec_end(c, SEC_EVOLVE);
-      c->kernel_launches += 5;
       return TVAP_OK;
     }
     if (rc != TVAP_ERR_ARG) return rc;
@@ -149,7 +148,6 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1, bool
     if ((rc = rgemm(n, n, n, view_cm(b.A2, n, 0), LinvT, V1, n, 1.0, 0.0, s))) return rc;
   }
   sec_end(c, SEC_EVOLVE);
-  c->kernel_launches += 8;
   return TVAP_OK;
 }
 
@@ -215,7 +213,7 @@ int tvap_calculate_gradient(tvap_ctx* c, const double* H20v, int cdim, const dou
                             const double* Zim1, double eta, double mu, double* Zi, double* gradient_norm) {
   if (!c || !H20v || !Zim1 || !Zi || !gradient_norm || cdim < 0 || (cdim > 0 && (!lambda || !C20)) || eta == 0.0)
     return TVAP_ERR_ARG;
-  c->kernel_launches = 0;
+  LaunchTally tally(c);
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;
@@ -232,10 +230,9 @@ int tvap_calculate_gradient(tvap_ctx* c, const double* H20v, int cdim, const dou
   if (!rc && cdim > 0) rc = upload_matrix(lambda, dl, sizeof(double) * cdim, s);
   if (!rc) {
     sec_begin(c, SEC_GRADIENT);
-    gradient_kernel<<<nblocks, tb, 0, s>>>(nn, cdim, dH, dl, dC, dZm, eta, mu, dZ, part);
-    sum_partials_kernel<<<1, 32, 0, s>>>(nblocks, part, sum);
+    gradient_kernel<<<nblocks, tb, 0, tvap::counted(s)>>>(nn, cdim, dH, dl, dC, dZm, eta, mu, dZ, part);
+    sum_partials_kernel<<<1, 32, 0, tvap::counted(s)>>>(nblocks, part, sum);
     sec_end(c, SEC_GRADIENT);
-    c->kernel_launches += 2;
     double h = 0.0;
     rc = download_matrix(dZ, Zi, sizeof(double) * nn, s);
     if (!rc) {
@@ -249,7 +246,7 @@ int tvap_calculate_gradient(tvap_ctx* c, const double* H20v, int cdim, const dou
 
 int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z, double* U1, double* V1) {
   if (!c || !U0 || !V0 || !Z || !U1 || !V1) return TVAP_ERR_ARG;
-  c->kernel_launches = 0;
+  LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_dev_flags = c->d_flags;
   const int n = c->n;
@@ -297,7 +294,7 @@ int tvap_evolve_noalloc(tvap_ctx* c, const double* U0, const double* V0, const d
   double* scratch = nullptr;
   int rc;
   if ((rc = noalloc_scratch(&scratch))) return rc;
-  c->kernel_launches = 0;
+  LaunchTally tally(c);
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;
   double* L = scratch;               // n*n + n
@@ -309,7 +306,7 @@ int tvap_evolve_noalloc(tvap_ctx* c, const double* U0, const double* V0, const d
   const View Zv = view_cm(Z, n, 0);
   rc = rgemm(n, n, n, view_t(Zv), Zv, L, n, 1.0, 0.0, s);  // Z^T Z (every entry written)
   if (!rc) {
-    add_identity_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, L);
+    add_identity_kernel<<<(n + 255) / 256, 256, 0, tvap::counted(s)>>>(n, L);
     rc = cholesky_inverse(n, L, c->d_flags, s);
   }
   if (!rc) {
@@ -327,7 +324,6 @@ int tvap_evolve_noalloc(tvap_ctx* c, const double* U0, const double* V0, const d
   if (!rc) rc = rgemm(n, n, n, view_cm(A2, n, 0), LinvT, V1, n, 1.0, 0.0, s);
   g_gemm_mode = saved_mode;
   if (rc) return rc;
-  c->kernel_launches += 8;
   return check_flags(c);
 }
 
@@ -340,7 +336,7 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
   cudaStream_t s = c->stream;
   int rc;
   if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
-  c->kernel_launches = 0;
+  LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_dev_flags = c->d_flags;
   double* buf = nullptr;

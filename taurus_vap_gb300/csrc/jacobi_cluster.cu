@@ -276,6 +276,7 @@ int jacobi_cluster(int n, const double* M, int m_transposed, const double* W0, d
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  ++g_launch_count;
   TVAP_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_kernel, n, M, m_transposed, W0, W, sweeps_out));
   return TVAP_OK;
 }

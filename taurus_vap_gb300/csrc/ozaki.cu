@@ -146,7 +146,7 @@ int launch_ozaki_mma(int M, int N, int mpad, int npad, int kpad, const __nv_bflo
   const size_t shm = oz::Shape<PA, PB>::kSmemBytes;
   if (int rc = smem_opt_in((const void*)ozaki_mma_kernel<PA, PB>, shm)) return rc;
   dim3 grid(npad / oz::kTile, mpad / oz::kTile, g.batch);
-  ozaki_mma_kernel<PA, PB><<<grid, oz::kThreads, shm, s>>>(M, N, mpad, npad, kpad, As, ea, Bs, eb, g, a_shared,
+  ozaki_mma_kernel<PA, PB><<<grid, oz::kThreads, shm, tvap::counted(s)>>>(M, N, mpad, npad, kpad, As, ea, Bs, eb, g, a_shared,
                                                             b_shared);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
@@ -641,11 +641,11 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   left.nks = nks;
   left.scale2 = xa.scale2;
   if (!(g.reuse_left && sc->left == left)) {
-    slice_tc_kernel<<<dim3((xa.nstack * xa.rows + 7) / 8, a_slots), kSliceThreads, slice_shm, s>>>(
+    slice_tc_kernel<<<dim3((xa.nstack * xa.rows + 7) / 8, a_slots), kSliceThreads, slice_shm, tvap::counted(s)>>>(
         xa, oztc::kM, a_rows_pad, nks, As, ea);
     sc->left = left;
   }
-  slice_tc_kernel<<<dim3((xb.rows + 7) / 8, b_slots), kSliceThreads, slice_shm, s>>>(xb, bn, b_rows_pad, nks, Bs,
+  slice_tc_kernel<<<dim3((xb.rows + 7) / 8, b_slots), kSliceThreads, slice_shm, tvap::counted(s)>>>(xb, bn, b_rows_pad, nks, Bs,
                                                                                      eb);
   o.C = g.C;
   o.crs = crs;
@@ -668,7 +668,7 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   if ((rc = smem_opt_in((const void*)kern, oztc::kSmemBytes))) return rc;
   TVAP_CUDA(cudaMemsetAsync(sc->counter, 0, sizeof(int), s));
   if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);
-  kern<<<grid, oztc::kThreads, oztc::kSmemBytes, s>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad, b_slots == 1 ? 1 : 0,
+  kern<<<grid, oztc::kThreads, oztc::kSmemBytes, tvap::counted(s)>>>(As, ea, a_rows_pad, Bs, eb, b_rows_pad, b_slots == 1 ? 1 : 0,
                                                       a_slots, nks, o, sc->counter, g_dev_flags);
   if (g_tc_timing_ctx) sec_end_on(g_tc_timing_ctx, g_tc_timing_sec, s);
   TVAP_CUDA(cudaGetLastError());
@@ -702,16 +702,16 @@ int gemm_ozaki(const GemmArgs& g, cudaStream_t s) {
   {
     dim3 grid((mpad + 7) / 8, abatch);
     if (PA == 2)
-      slice_kernel<true><<<grid, 256, 0, s>>>(g.M, g.K, mpad, kpad, g.A.p, g.A.rs, g.A.cs, g.A.bs, g.conj_a, As, ea);
+      slice_kernel<true><<<grid, 256, 0, tvap::counted(s)>>>(g.M, g.K, mpad, kpad, g.A.p, g.A.rs, g.A.cs, g.A.bs, g.conj_a, As, ea);
     else
-      slice_kernel<false><<<grid, 256, 0, s>>>(g.M, g.K, mpad, kpad, g.A.p, g.A.rs, g.A.cs, g.A.bs, false, As, ea);
+      slice_kernel<false><<<grid, 256, 0, tvap::counted(s)>>>(g.M, g.K, mpad, kpad, g.A.p, g.A.rs, g.A.cs, g.A.bs, false, As, ea);
   }
   {
     dim3 grid((npad + 7) / 8, bbatch);
     if (PB == 2)
-      slice_kernel<true><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, g.conj_b, Bs, eb);
+      slice_kernel<true><<<grid, 256, 0, tvap::counted(s)>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, g.conj_b, Bs, eb);
     else
-      slice_kernel<false><<<grid, 256, 0, s>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, false, Bs, eb);
+      slice_kernel<false><<<grid, 256, 0, tvap::counted(s)>>>(g.N, g.K, npad, kpad, g.B.p, g.B.cs, g.B.rs, g.B.bs, false, Bs, eb);
   }
   if (PA == 2 && PB == 2) return launch_ozaki_mma<2, 2>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);
   if (PA == 2) return launch_ozaki_mma<2, 1>(g.M, g.N, mpad, npad, kpad, As, ea, Bs, eb, g, s);

@@ -1879,7 +1879,7 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
   double2* W = w->W + size_t(g0) * 2 * nn;
   int* piv = w->piv + size_t(g0) * n;
   double2* Tinv = w->Tinv + size_t(g0) * tstride;
-  int rc, launches = 0, blk = 0;
+  int rc, blk = 0;
   for (int j0 = 0; j0 < n; j0 += nb, ++blk) {
     const int nbp = std::min(nb, n - j0);
     const int j1 = j0 + nbp;
@@ -1887,7 +1887,7 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
     switch ((n - j0 + 31) / 32) {
 #define TVAP_PANEL_GJ(S)                                                                                 \
   case S:                                                                                                \
-    panel_gj_kernel<S><<<gc, kFactorThreads, 0, s>>>(n, j0, nbp, W, piv, c->d_flags, tinv, tstride);    \
+    panel_gj_kernel<S><<<gc, kFactorThreads, 0, tvap::counted(s)>>>(n, j0, nbp, W, piv, c->d_flags, tinv, tstride);    \
     break;
       TVAP_PANEL_GJ(1)
       TVAP_PANEL_GJ(2)
@@ -1903,13 +1903,12 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
     if (j1 < 2 * n) {
       if (n - j0 <= kPermMaxRows) {
         dim3 gp((2 * n - j1 + kPermCols - 1) / kPermCols, gc);
-        panel_perm_kernel<<<gp, kPermThreads, 0, s>>>(n, j0, nbp, W, piv);
+        panel_perm_kernel<<<gp, kPermThreads, 0, tvap::counted(s)>>>(n, j0, nbp, W, piv);
       } else {
         dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, gc);
-        panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, W, piv);
+        panel_swap_kernel<<<ga, kApplyThreads, 0, tvap::counted(s)>>>(n, j0, nbp, W, piv);
       }
     }
-    launches += 2;
     // the block row: R = T [A12 | B1] in place (the operands are split into
     // digit planes before the product is formed)
     {
@@ -1927,7 +1926,6 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
       g.alpha = make_double2(1.0, 0.0);
       g.beta = make_double2(0.0, 0.0);
       if ((rc = gemm_ozaki(g, s))) return rc;
-      ++launches;
     }
     // all other rows: W[:, j1:] -= W[:, j0:j1] R (the block rows' panel
     // entries are zero, so they keep R)
@@ -1946,12 +1944,10 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
     g.beta = make_double2(1.0, 0.0);
     g.three_m = true;
     if ((rc = gemm(g, s))) return rc;
-    ++launches;
   }
   const size_t tot = nn * gc;
-  thouless_out_kernel<<<nblk(tot, 256), 256, 0, s>>>(n, gc, W, w->A + size_t(g0) * nn);
+  thouless_out_kernel<<<nblk(tot, 256), 256, 0, tvap::counted(s)>>>(n, gc, W, w->A + size_t(g0) * nn);
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += launches + 1;
   return TVAP_OK;
 }
 
@@ -1980,9 +1976,8 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
   }
   {
     dim3 grid(std::max(1, (2 * n + 15) / 16), G);
-    build_augmented_kernel<<<grid, kPanelThreads, 0, s>>>(n, w->Uphi, w->Vphi, w->W);
+    build_augmented_kernel<<<grid, kPanelThreads, 0, tvap::counted(s)>>>(n, w->Uphi, w->Vphi, w->W);
   }
-  int launches = 1;
   // product with an inverted diagonal block, in place on a block row:
   // rows r0 .. r0+nbp-1 of columns c0 .. 2n-1 <- T (nbp x nbp) times them
   // (the operands are split into digit planes before the product is formed,
@@ -2001,7 +1996,6 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     g.cbs = bsW;
     g.alpha = make_double2(1.0, 0.0);
     g.beta = make_double2(0.0, 0.0);
-    ++launches;
     return gemm_ozaki(g, s);
   };
   // Blocked Gauss-Jordan (the emulated products, panels of up to 192 rows):
@@ -2015,7 +2009,6 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     // factorisation runs beside the other half's products.  The products
     // leave SMs for it (their CTAs are capped at the SMs the other half's
     // panels do not hold: a panel CTA and a product CTA do not fit one SM).
-    c->kernel_launches += 1;  // build_augmented_kernel
     const bool split = c->streamM2 && G >= 32;
     if (!split) return gj_solve_range(c, 0, G, nb, s, nullptr);
     const int sms = device_sms();
@@ -2035,18 +2028,16 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     if (smem_path) {
       const size_t fac_bytes = sizeof(double2) * (size_t(n - j0) * nbp + (use_inv ? 2 * size_t(nbp) * nbp : 0));
       double2* tinv = use_inv ? w->Tinv + size_t(blk) * 2 * kPanelMax * kPanelMax : nullptr;
-      panel_factor_kernel<<<G, kFactorThreads, fac_bytes, s>>>(n, j0, nbp, w->W, w->piv, c->d_flags, tinv, tstride);
+      panel_factor_kernel<<<G, kFactorThreads, fac_bytes, tvap::counted(s)>>>(n, j0, nbp, w->W, w->piv, c->d_flags, tinv, tstride);
       dim3 ga((2 * n - j1 + kApplyThreads - 1) / kApplyThreads, G);
       if (use_inv) {
-        panel_swap_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
+        panel_swap_kernel<<<ga, kApplyThreads, 0, tvap::counted(s)>>>(n, j0, nbp, w->W, w->piv);
         if ((rc = block_row_product(blk, 0, j0, nbp, j1))) return rc;
       } else {
-        panel_apply_kernel<<<ga, kApplyThreads, 0, s>>>(n, j0, nbp, w->W, w->piv);
+        panel_apply_kernel<<<ga, kApplyThreads, 0, tvap::counted(s)>>>(n, j0, nbp, w->W, w->piv);
       }
-      launches += 2;
     } else {
-      panel_kernel<<<G, kPanelThreads, 0, s>>>(n, j0, nbp, w->W, c->d_flags);
-      ++launches;
+      panel_kernel<<<G, kPanelThreads, 0, tvap::counted(s)>>>(n, j0, nbp, w->W, c->d_flags);
     }
     if (j1 < n) {
       // A22 -= L21 U12 over columns j1 .. 2n-1
@@ -2065,7 +2056,6 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
       g.beta = make_double2(1.0, 0.0);
       g.three_m = true;
       if ((rc = gemm(g, s))) return rc;
-      ++launches;
     }
   }
   // back substitution, block rows from the last
@@ -2089,24 +2079,20 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
       g.beta = make_double2(1.0, 0.0);
       g.three_m = true;
       if ((rc = gemm(g, s))) return rc;
-      ++launches;
     }
     if (use_inv) {
       // X_i = U_ii^{-1} Y_i
       if ((rc = block_row_product(bi, 1, i0, nbp, n))) return rc;
     } else if (smem_path) {
       dim3 gb((n + kApplyThreads - 1) / kApplyThreads, G);
-      backsolve_apply_kernel<<<gb, kApplyThreads, 0, s>>>(n, i0, nbp, w->W);
-      ++launches;
+      backsolve_apply_kernel<<<gb, kApplyThreads, 0, tvap::counted(s)>>>(n, i0, nbp, w->W);
     } else {
-      block_backsolve_kernel<<<G, kPanelThreads, 0, s>>>(n, i0, nbp, w->W);
-      ++launches;
+      block_backsolve_kernel<<<G, kPanelThreads, 0, tvap::counted(s)>>>(n, i0, nbp, w->W);
     }
   }
   const size_t tot = size_t(n) * n * G;
-  thouless_out_kernel<<<nblk(tot, 256), 256, 0, s>>>(n, G, w->W, w->A);
+  thouless_out_kernel<<<nblk(tot, 256), 256, 0, tvap::counted(s)>>>(n, G, w->W, w->A);
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += launches + 1;
   return TVAP_OK;
 }
 
@@ -2136,16 +2122,15 @@ int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, c
   for (int step = 0; step < steps; ++step) {
     const View Xv = view_cm(X, n, 0);
     if ((rc = gram(X))) return rc;
-    refine_lambda_kernel<<<1, kRlThreads, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
-    refine_update_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
+    refine_lambda_kernel<<<1, kRlThreads, 0, tvap::counted(s)>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+    refine_update_kernel<<<nblk(nn, 256), 256, 0, tvap::counted(s)>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
     if ((rc = real_gemm(n, n, n, Xv, view_cm(w->Mr, n, 0), Xn, n, 1.0, 0.0, s))) return rc;
     std::swap(X, Xn);
   }
   if ((rc = gram(X))) return rc;
-  refine_lambda_kernel<<<1, kRlThreads, 0, s>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
-  cluster_finish_kernel<<<1, kCfThreads, 0, s>>>(n, w->Sr, X, w->rscal, w->D, w->evals, w->rflag);
+  refine_lambda_kernel<<<1, kRlThreads, 0, tvap::counted(s)>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
+  cluster_finish_kernel<<<1, kCfThreads, 0, tvap::counted(s)>>>(n, w->Sr, X, w->rscal, w->D, w->evals, w->rflag);
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += steps * 5 + 4;
   int hr[2] = {1, 0};
   TVAP_CUDA(cudaMemcpyAsync(hr, w->rflag, sizeof(hr), cudaMemcpyDeviceToHost, s));
   TVAP_CUDA(cudaStreamSynchronize(s));
@@ -2204,7 +2189,6 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
       } else if (rc) {
         return rc;
       }
-      c->kernel_launches += 1;
       ++c->canon_attempts[0];
       if ((rc = refine_canonical(c, X, Xn, 3, &fail, s))) return rc;
     }
@@ -2218,7 +2202,6 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
   ++c->canon_attempts[2];
   TVAP_CUDA(cudaMemcpyAsync(w->jac, w->rho, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
   if ((rc = jacobi_eigen(n, w->jac, w->D, w->evals, w->jwork, c->d_flags, s))) return rc;
-  c->kernel_launches += 1;
   w->have_basis = true;
   return TVAP_OK;
 }
@@ -2249,7 +2232,6 @@ int prepare_uv_blocks(tvap_ctx* c, cudaStream_t s) {
     if ((rc = gemm(g, s))) return rc;
   }
   sec_end_on(c, SEC_BLOCKS, s);
-  c->kernel_launches += 1;
   return TVAP_OK;
 }
 
@@ -2274,7 +2256,7 @@ int prepare_canonical(tvap_ctx* c, double occeps, double allemp_d, int* host_can
   if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->kap, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
   if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->kapc, n, 1.0, 0.0, s))) return rc;
   const double eps = (occeps < 2.2250738585072014e-308) ? 1.0e-8 : occeps;
-  canon_kernel<<<1, 256, 0, s>>>(n, w->rhoc, w->kapc, eps, int(allemp_d), w->canon_i, w->canon_d);
+  canon_kernel<<<1, 256, 0, tvap::counted(s)>>>(n, w->rhoc, w->kapc, eps, int(allemp_d), w->canon_i, w->canon_d);
   TVAP_CUDA(cudaGetLastError());
   {
     // D_t^T D_t over the rows of isospin t, batch t = p, n
@@ -2294,7 +2276,6 @@ int prepare_canonical(tvap_ctx* c, double occeps, double allemp_d, int* host_can
     if ((rc = gemm(g, s))) return rc;
   }
   sec_end_on(c, SEC_CANONICAL, s);
-  c->kernel_launches += 2 + 4 + 1 + 1;
   TVAP_CUDA(cudaMemcpyAsync(host_canon, w->canon_i, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
   TVAP_CUDA(cudaStreamSynchronize(s));
   return TVAP_OK;
@@ -2310,25 +2291,25 @@ int angles_overlap(tvap_ctx* c, int G, const double2* d_ephase, int nocc, int ne
   int rc;
   const int n2 = n - nemp, nb = n2 - nocc;
   sec_begin_on(c, SEC_OVERLAP, s2);
-  build_rn_kernel<<<nblk(size_t(n2) * n2 * G, tb), tb, 0, s2>>>(n, n2, G, w->blocks, d_ephase, w->Rn);
+  build_rn_kernel<<<nblk(size_t(n2) * n2 * G, tb), tb, 0, tvap::counted(s2)>>>(n, n2, G, w->blocks, d_ephase, w->Rn);
   const double2* S = w->Rn;
   int ldS = n2;
   long long bsS = (long long)n2 * n2;
   if (nocc > 0) {
     // Z = R22^{-1} R21 (nocc x nb), det(R22); S = R11 - R12 Z
-    left_solve_kernel<<<G, kLsThreads, 0, s2>>>(nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
+    left_solve_kernel<<<G, kLsThreads, 0, tvap::counted(s2)>>>(nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
                                                 View{w->Rn + nb, 1, n2, (long long)n2 * n2}, w->OW, w->OX, 1, nocc,
                                                 (long long)nocc * nb, 0, w->detR22, G, c->d_flags, DEV_SINGULAR_RN);
-    schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n2, nb, G, w->Rn, w->OX, w->SZ);
+    schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, tvap::counted(s2)>>>(n2, nb, G, w->Rn, w->OX, w->SZ);
     TVAP_CUDA(cudaGetLastError());
     S = w->SZ;
     ldS = nb;
     bsS = (long long)nb * nb;
   } else {
-    fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->detR22);
+    fill_det_one_kernel<<<nblk(G, tb), tb, 0, tvap::counted(s2)>>>(G, w->detR22);
   }
   if (nb > 0) {
-    overlap_prep_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, s2>>>(n, G, w->canon_i, w->canon_d, S, ldS, bsS,
+    overlap_prep_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, tvap::counted(s2)>>>(n, G, w->canon_i, w->canon_d, S, ldS, bsS,
                                                                       w->K, w->OY);
     TVAP_CUDA(cudaGetLastError());
     // K += S^T Y
@@ -2351,11 +2332,10 @@ int angles_overlap(tvap_ctx* c, int G, const double2* d_ephase, int nocc, int ne
     if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s2))) return rc;
     sec_end_on(c, SEC_PFAFFIAN, s2);
   } else {
-    fill_det_one_kernel<<<nblk(G, tb), tb, 0, s2>>>(G, w->pf);
+    fill_det_one_kernel<<<nblk(G, tb), tb, 0, tvap::counted(s2)>>>(G, w->pf);
     sec_end_on(c, SEC_OVERLAP, s2);
   }
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += 1 + (nocc > 0 ? 2 : 1) + (nb > 0 ? 3 : 1);
   return TVAP_OK;
 }
 
@@ -2369,15 +2349,15 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
   const int tb = 256;
   int rc;
   sec_begin_on(c, SEC_SOLVE, s);
-  build_uv_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(n, G, w->blocks, d_ephase, w->Uphi, w->Vphi);
+  build_uv_kernel<<<nblk(nn * G, tb), tb, 0, tvap::counted(s)>>>(n, G, w->blocks, d_ephase, w->Uphi, w->Vphi);
   TVAP_CUDA(cudaGetLastError());
   // A_phi = conj(V_phi U_phi^{-1}): solve U_phi^T Y = V_phi^T, A = conj(Y^T)
   if ((rc = blocked_thouless_solve(c, G, s))) return rc;
   sec_end_on(c, SEC_SOLVE, s);
   sec_begin_on(c, SEC_UV, s);
   // U~ = U + V A, V~ = V + U A
-  broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(nn, G, w->U, w->Ut);
-  broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, s>>>(nn, G, w->V, w->Vt);
+  broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, tvap::counted(s)>>>(nn, G, w->U, w->Ut);
+  broadcast_real_kernel<<<nblk(nn * G, tb), tb, 0, tvap::counted(s)>>>(nn, G, w->V, w->Vt);
   {
     GemmArgs g{};
     g.M = g.N = g.K = n;
@@ -2439,9 +2419,9 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
     TVAP_CUDA(cudaStreamWaitEvent(st, c->ev_stagger, 0));
   }
   sec_begin_on(c, SEC_TRACES, st);
-  traces_partial_kernel<<<kTraceChunks, kTraceThreads, 0, st>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR,
+  traces_partial_kernel<<<kTraceChunks, kTraceThreads, 0, tvap::counted(st)>>>(n, G, w->rhoL, w->kLR, w->kRL, w->gam, w->dLR,
                                                                 c->d_H1, w->tpart);
-  traces_finish_kernel<<<G, 9 * 32, 0, st>>>(G, w->tpart, c->H0, w->obs);
+  traces_finish_kernel<<<G, 9 * 32, 0, tvap::counted(st)>>>(G, w->tpart, c->H0, w->obs);
   TVAP_CUDA(cudaGetLastError());
   sec_end_on(c, SEC_TRACES, st);
   sec_begin_on(c, SEC_H20, s);
@@ -2489,7 +2469,6 @@ int angles_thouless(tvap_ctx* c, int G, const double2* d_ephase, double factor_d
     TVAP_CUDA(cudaEventRecord(c->ev_join2, st));
     TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join2, 0));
   }
-  c->kernel_launches += 1 + 2 + 2 + 3 + 2 + 5;
   return TVAP_OK;
 }
 
@@ -2502,14 +2481,13 @@ int angles_sums(tvap_ctx* c, int G, const double2* d_weight, const double* d_mul
   const size_t nn = size_t(n) * n;
   const int tb = 256;
   sec_begin_on(c, SEC_SUMS, s);
-  overlap_finish_kernel<<<nblk(G, tb), tb, 0, s>>>(n, G, have_overlap ? 1 : 0, w->canon_i, w->canon_d, w->pf,
+  overlap_finish_kernel<<<nblk(G, tb), tb, 0, tvap::counted(s)>>>(n, G, have_overlap ? 1 : 0, w->canon_i, w->canon_d, w->pf,
                                                     w->detR22, d_weight, d_mult, w->obs, w->coefA, w->coefAE);
-  sum_scalars_kernel<<<1, 32, 0, s>>>(G, w->obs, d_mult, d_weight, w->pscal, accumulate);
-  sum_matrices_kernel<<<unsigned((nn + 31) / 32), 32 * kSumWarps, sizeof(double2) * 3 * size_t(G), s>>>(
+  sum_scalars_kernel<<<1, 32, 0, tvap::counted(s)>>>(G, w->obs, d_mult, d_weight, w->pscal, accumulate);
+  sum_matrices_kernel<<<unsigned((nn + 31) / 32), 32 * kSumWarps, sizeof(double2) * 3 * size_t(G), tvap::counted(s)>>>(
       n, G, w->A, w->T, w->coefA, w->coefAE, d_mult, w->pA, w->pH, w->pAH, accumulate);
   TVAP_CUDA(cudaGetLastError());
   sec_end_on(c, SEC_SUMS, s);
-  c->kernel_launches += 3;
   return TVAP_OK;
 }
 
@@ -2662,9 +2640,8 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
                                canon[1], o.factor_delta, b > 0 ? 1 : 0)))
         return rc;
   }
-  projected_h20_kernel<<<nblk(nn, 256), 256, 0, s>>>(n, w->pA, w->pH, w->pAH, w->pscal, w->H20v, c->d_flags);
+  projected_h20_kernel<<<nblk(nn, 256), 256, 0, tvap::counted(s)>>>(n, w->pA, w->pH, w->pAH, w->pscal, w->H20v, c->d_flags);
   TVAP_CUDA(cudaGetLastError());
-  c->kernel_launches += 1;
   if (out) {
     // the sums and the status word in one round trip
     double2 sc[6];

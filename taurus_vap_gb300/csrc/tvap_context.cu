@@ -359,6 +359,7 @@ int tvap_set_hamiltonian(tvap_ctx* c, int64_t S, const int16_t* abcd, const floa
     g_last_error = "tvap_set_hamiltonian: element list too long (16 slots per element must fit int32)";
     return TVAP_ERR_ARG;
   }
+  LaunchTally tally(c);  // CUB's sort and scan of the element list launch kernels of their own, not counted
   const int n = c->n;
   cudaFree(c->d_abcd);
   cudaFree(c->d_h2);
@@ -392,7 +393,7 @@ int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, cons
   if (!c || ncol <= 0 || ncol > 256 || !rho || !kLR || !kRL || !gamma || !hsp || !dLR || !dRL)
     return TVAP_ERR_ARG;
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
-  c->kernel_launches = 0;
+  LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_dev_flags = c->d_flags;
   const int n = c->n;
@@ -410,11 +411,11 @@ int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, cons
   const unsigned nb = unsigned((tot + tb - 1) / tb);
   for (int q = 0; q < 3 && rc == TVAP_OK; ++q) {
     rc = upload_matrix(srcs[q], stage, sizeof(double2) * tot, s);
-    if (rc == TVAP_OK) to_inner_kernel<<<nb, tb, 0, s>>>(nn, ncol, stage, in[q]);
+    if (rc == TVAP_OK) to_inner_kernel<<<nb, tb, 0, tvap::counted(s)>>>(nn, ncol, stage, in[q]);
   }
   if (rc == TVAP_OK) rc = fields_batched(c, ncol, ncol, in[0], in[1], in[2], out[0], out[1], out[2], out[3], s);
   for (int q = 0; q < 4 && rc == TVAP_OK; ++q) {
-    from_inner_kernel<<<nb, tb, 0, s>>>(nn, ncol, out[q], stage);
+    from_inner_kernel<<<nb, tb, 0, tvap::counted(s)>>>(nn, ncol, out[q], stage);
     rc = download_matrix(stage, dsts[q], sizeof(double2) * tot, s);
     if (rc == TVAP_OK) {
       cudaError_t e = cudaStreamSynchronize(s);
@@ -424,7 +425,6 @@ int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, cons
       }
     }
   }
-  c->kernel_launches += 7;
   cudaFree(buf);
   // the status word: a bounded wait of the tensor-core field kernels that gave up
   if (rc == TVAP_OK) rc = check_flags(c);
@@ -440,7 +440,7 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
                  double* H20v) {
   if (!c || !U0 || !V0 || !opts || opts->Mphip < 1 || opts->Mphin < 1) return TVAP_ERR_ARG;
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
-  c->kernel_launches = 0;
+  LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_dev_flags = c->d_flags;
   const int n = c->n;
@@ -463,11 +463,14 @@ int tvap_project_batched(tvap_ctx* c, int nstates, const double* U0s, const doub
                          tvap_pnp* outs, double* H20vs) {
   if (!c || nstates < 0 || (nstates > 0 && (!U0s || !V0s || !opts || !outs))) return TVAP_ERR_ARG;
   const size_t nn = size_t(c->n) * c->n;
-  for (int s = 0; s < nstates; ++s) {
-    int rc = tvap_project(c, U0s + s * nn, V0s + s * nn, opts + s, outs + s, H20vs ? H20vs + s * nn : nullptr);
-    if (rc) return rc;
+  int launches = 0;  // each tvap_project records its own launches
+  int rc = TVAP_OK;
+  for (int s = 0; s < nstates && rc == TVAP_OK; ++s) {
+    rc = tvap_project(c, U0s + s * nn, V0s + s * nn, opts + s, outs + s, H20vs ? H20vs + s * nn : nullptr);
+    launches += c->kernel_launches;
   }
-  return TVAP_OK;
+  c->kernel_launches = launches;
+  return rc;
 }
 
 }  // extern "C"

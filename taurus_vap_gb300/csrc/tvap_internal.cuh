@@ -78,6 +78,14 @@ void set_last_error(const char* msg, const char* file, int line);
 int smem_opt_in(const void* func, size_t bytes);
 // Streaming multiprocessors of the current device (cached per device).
 int device_sms();
+// Kernels this thread launched since its current C-ABI call began.  Every
+// launch passes its stream through counted(); the launches that do not take
+// a stream argument count themselves.
+extern thread_local long long g_launch_count;
+inline cudaStream_t counted(cudaStream_t s) {
+  ++g_launch_count;
+  return s;
+}
 
 // device status word bits, written by kernels and read back by the host
 enum DevFlag : int {
@@ -274,6 +282,15 @@ struct tvap_ctx {
 };
 
 namespace tvap {
+// Scope of one C-ABI call: starts the launch count and, on every return,
+// records it as the context's tvap_kernel_launches.
+struct LaunchTally {
+  tvap_ctx* c;
+  explicit LaunchTally(tvap_ctx* ctx) : c(ctx) { g_launch_count = 0; }
+  ~LaunchTally() { c->kernel_launches = int(g_launch_count); }
+  LaunchTally(const LaunchTally&) = delete;
+  LaunchTally& operator=(const LaunchTally&) = delete;
+};
 enum Section : int {
   SEC_CANONICAL = 0, SEC_BLOCKS, SEC_SOLVE, SEC_UV, SEC_DENSITIES, SEC_FIELDS_GAMMA, SEC_FIELDS_DELTA, SEC_TRACES,
   SEC_H20, SEC_OVERLAP, SEC_PFAFFIAN, SEC_SUMS, SEC_GRADIENT, SEC_EVOLVE, SEC_H20_TC, SEC_COUNT
