@@ -13,8 +13,10 @@
 // vendored PFAPACK Pfaffian (subroutines_pfaffian.f) is restated here.
 //
 // Parity pin: tests/test_oracle_golden.py runs the Mg24 / USDB examples of the
-// reference (examples/gradient_mg24) and compares the converged projected
-// energies with the reference's stored tables.
+// reference (examples/gradient_mg24) and compares the iteration counts and the
+// converged projected energies with the reference's stored tables, and reaches
+// the HFB minimum of its USDB minima table (examples/minima_usdb) from random
+// seeds.
 
 #include <omp.h>
 
