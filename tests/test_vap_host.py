@@ -1,0 +1,78 @@
+"""The host side of the gradient loop (taurus_vap_gb300/vap.py: the constraint
+algebra, the Lagrange multipliers, the adjust_constraints Newton loop, the
+convergence test) on the CPU.
+
+vap.VAP drives a context object; here the context's three calls come from the
+oracle instead of the device library, so the loop's own logic is checked
+against the reference's Mg24 / USDB regression tables without a GPU.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import golden_table
+
+import oracle as O
+from taurus_vap_gb300.vap import VAP, Constraints
+
+
+class OracleBackedContext:
+    """The three calls vap.VAP makes, answered by the oracle: the projection
+    and the Thouless evolution from liboracle, the type-0 gradient step
+    Z_i = -eta (H20v - sum_j lambda_j C20_j) + mu Z_{i-1} with norm
+    |Z_i|_F / eta (module_gradient.f90:124-141)."""
+
+    def __init__(self, model):
+        self.n = model.n
+        self.om = O.OracleModel(model)
+
+    def project(self, U0, V0, Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta=1.0, seed_occeps=0.0,
+                seed_allemp=0, mode=0):
+        r = self.om.project(U0, V0, Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta=factor_delta,
+                            occeps=seed_occeps, allemp=seed_allemp, nthreads=1)
+        assert r["status"] == 0, r["status"]
+        return r["pnp"], r["H20v"]
+
+    def calculate_gradient(self, H20v, lambdas, C20, Zim1, eta, mu):
+        g = np.array(H20v, dtype=np.float64)
+        if lambdas is not None:
+            g -= np.asarray(lambdas) @ np.asarray(C20)
+        Zi = -eta * g + mu * np.asarray(Zim1, dtype=np.float64).reshape(-1)
+        return Zi, float(np.sqrt(np.sum(Zi * Zi)) / eta)
+
+    def evolve(self, U0, V0, Z):
+        st, U1, V1 = O.thouless_evolve(U0, V0, np.reshape(Z, (self.n, self.n), order="F"))
+        assert st == 0, st
+        return U1, V1
+
+
+@pytest.mark.parametrize("M,table,eta,mu", [(5, "mg24_results_vap_benchmark", 0.05, 0.6),
+                                            (1, "mg24_results_hfb_benchmark", 0.025, 0.6)])
+def test_host_loop_reproduces_mg24(usdb_model, mg24_seed, mg24_constraints, M, table, eta, mu):
+    it_ref, e_ref = golden_table(table)[(eta, mu)]
+    ops, vals = mg24_constraints
+    vap = VAP(OracleBackedContext(usdb_model), *mg24_seed, M, M, 4.0, 4.0, eta, mu,
+              constraints=Constraints(ops, vals))
+    it, info = vap.run(iter_max=3000)
+    assert abs(info[1] - e_ref) < 1e-6
+    assert it == it_ref
+
+
+def test_constraints_hold_after_adjustment(usdb_model, mg24_seed, mg24_constraints):
+    """After adjust_constraints the expectation values of the constraint
+    operators (Z, N, Q21) sit at their targets within the tolerance
+    (module_constraints.f90:270-373)."""
+    from taurus_vap_gb300.vap import expectval_obo
+
+    ops, vals = mg24_constraints
+    vap = VAP(OracleBackedContext(usdb_model), *mg24_seed, 5, 5, 4.0, 4.0, 0.05, 0.6,
+              constraints=Constraints(ops, vals))
+    vap.adjust_constraints()
+    for _ in range(3):
+        st, _ = vap.iterate()
+        assert st == 0
+    n = usdb_model.n
+    rho = vap.V0 @ vap.V0.T
+    for op, val in zip(ops, vals):
+        got = expectval_obo(rho, np.reshape(op, (n, n), order="F"))
+        assert abs(got - val) < 1e-6, (got, val)
