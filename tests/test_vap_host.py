@@ -76,3 +76,55 @@ def test_constraints_hold_after_adjustment(usdb_model, mg24_seed, mg24_constrain
     for op, val in zip(ops, vals):
         got = expectval_obo(rho, np.reshape(op, (n, n), order="F"))
         assert abs(got - val) < 1e-6, (got, val)
+
+
+class OracleAdjointContext:
+    """energy_adjoint answered by the oracle: E of the evolved state and
+    dE/dZ = L^-T H20v L^-1 with L L^T = 1 + Z^T Z, the relation the device
+    adjoint uses (checked against finite differences in
+    test_oracle_identities)."""
+
+    def __init__(self, model):
+        self.n = model.n
+        self.om = O.OracleModel(model)
+        self.calls = 0
+
+    def energy_adjoint(self, U0, V0, Z, Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta=1.0, mode=0):
+        self.calls += 1
+        n = self.n
+        Z = np.reshape(Z, (n, n), order="F")
+        st, U1, V1 = O.thouless_evolve(U0, V0, Z)
+        assert st == 0
+        r = self.om.project(U1, V1, Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta=factor_delta, nthreads=1)
+        p = r["pnp"]
+        H = r["H20v"].reshape(n, n, order="F")
+        Li = np.linalg.inv(np.linalg.cholesky(np.eye(n) + Z.T @ Z))
+        return (p.c("ener") / p.c("over")).real, np.asfortranarray(Li.T @ H @ Li)
+
+
+def test_autograd_function_on_the_cpu():
+    """taurus_vap_gb300.autograd: one adjoint call per forward, none in
+    backward, the gradient scaled by the incoming one, and central finite
+    differences of E(Z) matched."""
+    torch = pytest.importorskip("torch")
+    from taurus_vap_gb300 import model as M
+    from taurus_vap_gb300.autograd import projected_energy
+
+    mdl = M.sd_model(seed=3)
+    n = mdl.n
+    U, V = M.random_bogoliubov(mdl.basis, 4, 4, seed=7)
+    ctx = OracleAdjointContext(mdl)
+    rng = np.random.default_rng(4)
+    Z0 = 0.1 * rng.normal(size=(n, n))
+    Z0 = Z0 - Z0.T
+    Z = torch.tensor(Z0, dtype=torch.float64, requires_grad=True)
+    E = projected_energy(Z, ctx, U, V, 5, 5, 4, 4)
+    (3.0 * E).backward()
+    assert ctx.calls == 1
+    D = rng.normal(size=(n, n))
+    D = D - D.T
+    h = 1e-5
+    Ep = projected_energy(torch.tensor(Z0 + h * D), ctx, U, V, 5, 5, 4, 4).item()
+    Em = projected_energy(torch.tensor(Z0 - h * D), ctx, U, V, 5, 5, 4, 4).item()
+    fd = 3.0 * (Ep - Em) / (2 * h)
+    assert abs(fd - float((Z.grad.numpy() * D).sum())) < 1e-6 * max(1.0, abs(fd))
