@@ -43,3 +43,29 @@ def test_every_status_code_has_a_message():
     assert codes <= set(native.ERRORS), sorted(codes - set(native.ERRORS))
     err = native.TvapError(19, "tvap_project", "detail")
     assert err.code == 19 and "bounded wait" in str(err) and "detail" in str(err)
+
+
+def test_missing_library_raises(monkeypatch, tmp_path):
+    """No CPU fallback: without the built device library the binding raises."""
+    from taurus_vap_gb300 import native
+
+    monkeypatch.setattr(native._build, "GPU_LIB", str(tmp_path / "libtvap_gpu.so"))
+    monkeypatch.setattr(native, "_lib", None)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        native.lib()
+
+
+def test_context_without_a_device_raises():
+    """Without a CUDA device, creating a context is a CUDA status error, not
+    a silent fallback."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from taurus_vap_gb300 import model as M
+    from taurus_vap_gb300 import native
+
+    _build.build_gpu()
+    mdl = M.sd_model(seed=1)
+    with pytest.raises(native.TvapError) as e:
+        native.Context(mdl.basis, mdl.ham, device=0)
+    assert e.value.code == 2
