@@ -1887,7 +1887,8 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
     switch ((n - j0 + 31) / 32) {
 #define TVAP_PANEL_GJ(S)                                                                                 \
   case S:                                                                                                \
-    panel_gj_kernel<S><<<gc, kFactorThreads, 0, tvap::counted(s)>>>(n, j0, nbp, W, piv, c->d_flags, tinv, tstride);    \
+    panel_gj_kernel<S><<<gc, kFactorThreads, 0, tvap::counted(s)>>>(n, j0, nbp, W, piv, c->d_flags, tinv,\
+                                                                     tstride);                           \
     break;
       TVAP_PANEL_GJ(1)
       TVAP_PANEL_GJ(2)
