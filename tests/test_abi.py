@@ -69,3 +69,37 @@ def test_context_without_a_device_raises():
     with pytest.raises(native.TvapError) as e:
         native.Context(mdl.basis, mdl.ham, device=0)
     assert e.value.code == 2
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes structures of the binding have the sizes and field offsets
+    of the header's tvap_pnp and tvap_proj_opts (compiled with the host C
+    compiler)."""
+    import shutil
+    import subprocess
+
+    from taurus_vap_gb300 import native
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pnp = [f[0] for f in native.TvapPnp._fields_]
+    opts = [f[0] for f in native.TvapProjOpts._fields_]
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tvap.h"', "int main(void) {"]
+    lines.append('  printf("pnp %zu\\n", sizeof(tvap_pnp));')
+    lines += [f'  printf("pnp.{k} %zu\\n", offsetof(tvap_pnp, {k}));' for k in pnp]
+    lines.append('  printf("opts %zu\\n", sizeof(tvap_proj_opts));')
+    lines += [f'  printf("opts.{k} %zu\\n", offsetof(tvap_proj_opts, {k}));' for k in opts]
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    assert int(got["pnp"]) == ctypes.sizeof(native.TvapPnp)
+    assert int(got["opts"]) == ctypes.sizeof(native.TvapProjOpts)
+    for k in pnp:
+        assert int(got[f"pnp.{k}"]) == getattr(native.TvapPnp, k).offset, k
+    for k in opts:
+        assert int(got[f"opts.{k}"]) == getattr(native.TvapProjOpts, k).offset, k
