@@ -1,6 +1,6 @@
 """Device path (libtvap_gpu.so through the C ABI) against the oracle.
 
-Tolerances (the spec bar): fields 1e-12 relative to the largest entry;
+Tolerances (the FP64 accuracy the path must keep): fields 1e-12 relative to the largest entry;
 projected energy 1e-9 MeV; projected particle numbers 1e-10; the projected
 gradient field_H20v 1e-9 relative to its largest entry."""
 
