@@ -33,13 +33,15 @@ def set_operator_qpbasis(part: str, U, V, A):
 
 
 def expectval_obo(rho, B):
-    A1 = B @ rho
-    h = rho.shape[0] // 2
-    return np.trace(A1[:h, :h]) + np.trace(A1[h:, h:])
+    """<B> = Tr(B rho), the proton and neutron halves summed
+    (calculate_expectval_obo, module_operators.f90); formed as the sum of
+    B_ik rho_ki, without the n^3 product."""
+    return float(np.sum(B * rho.T))
 
 
 def expectval_pair(kappa, B):
-    return np.trace(B @ kappa.T)
+    """Tr(B kappa^T) (calculate_expectval_pair) as the sum of B_ik kappa_ik."""
+    return float(np.sum(B * kappa))
 
 
 @dataclass
@@ -93,11 +95,10 @@ class VAP:
         c = self.cons.dim
         if c == 0:
             return
-        n = self.n
-        Cm = [C.reshape((n, n), order="F") for C in self.C20]
-        H = H20v.reshape((n, n), order="F")
-        A = np.array([[np.trace(Cm[i] @ Cm[j].T) for j in range(c)] for i in range(c)])
-        B = np.array([np.trace(H @ Cm[i].T) for i in range(c)])
+        # Tr(C_i C_j^T) and Tr(H C_i^T) are dot products of the vectorised
+        # matrices (module_constraints.f90:413-484)
+        A = self.C20 @ self.C20.T
+        B = self.C20 @ np.asarray(H20v, dtype=np.float64).reshape(-1)
         try:
             self.lam1 = np.linalg.solve(A, B)
         except np.linalg.LinAlgError:
@@ -106,7 +107,7 @@ class VAP:
 
     def adjust_constraints(self):
         """module_constraints.f90:270-373; the Thouless evolution runs on the device."""
-        n, c = self.n, self.cons.dim
+        c = self.cons.dim
         U1, V1 = self.U0, self.V0
         for _ in range(100):
             U1, V1 = self.ctx.evolve(self.U0, self.V0, self.Zi)
@@ -119,8 +120,7 @@ class VAP:
             self.update_constraints_qpbasis(U1, V1)
             if ia == 0:
                 break
-            Cm = [C.reshape((n, n), order="F") for C in self.C20]
-            A = np.array([[np.trace(Cm[i].T @ Cm[j]) for j in range(c)] for i in range(c)])
+            A = self.C20 @ self.C20.T  # Tr(C_i^T C_j)
             B = np.linalg.solve(A, B)
             self.Zi = self.Zi + B @ self.C20
         self.U0, self.V0 = np.asfortranarray(U1), np.asfortranarray(V1)
