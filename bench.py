@@ -61,7 +61,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
@@ -317,7 +317,7 @@ def run_ours(args):
     state = (np.asfortranarray(U), np.asfortranarray(V), np.zeros(n * n))
     state, _ = host_iteration(ctx, state, 0)
     torch.cuda.synchronize()
-    e_steps = max(1, min(args.steps, 3))
+    e_steps = max(1, args.steps)
     barrier()
     tw = time.perf_counter()
     for _ in range(e_steps):
@@ -328,7 +328,12 @@ def run_ours(args):
     _, e_value = job_rate(e_ms_total, e_steps, world, "cuda")
     h2d = 8 * n * n * (2 + 2 + 3)
     d2h = 8 * n * n * (1 + 1 + 2)
-    e2e = {"value": e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    e2e = {"value": e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "steps": e_steps, "timer": "host perf_counter around the steps (copies and host work included)"}
+
+    # ---- the adjoint of E(Z) (tvap_energy_adjoint) at the workload's seed
+    # and a random skew Thouless matrix with entries ~ N(0, 0.1)
+    adjoint = adjoint_timing(ctx, U, V, torch, stream)
 
     # ---- roofline of the dominant kernel, from the live section timings.
     # The dominant kernel (launch list in profiles/) is the tcgen05 product
@@ -400,8 +405,10 @@ def run_ours(args):
 
     # ---- CPU baseline: the oracle on a bounded sample, rank 0 only
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(mdl, U, V, args)
+        cpu, oracle_energies = cpu_baseline(mdl, U, V, args)
+        parity = device_parity(ctx, U, V, torch, oracle_energies)
 
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
@@ -417,7 +424,8 @@ def run_ours(args):
         "sections_ms_per_step": {k: round(v, 4) for k, v in sec_ms.items()},
         "timeline_ms": {k: [round(a, 3), round(b, 3)] for k, (a, b) in timeline.items() if sections[k][1]},
         "longest_section": longest[0], "canonical_paths": canon_paths, "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
-        "final_energy": it.energy,
+        "final_energy": it.energy, "iterations_from_seed": args.warmup + args.steps,
+        "adjoint": adjoint, "parity": parity,
     }
     if rank == 0:
         print(json.dumps(out))
@@ -442,28 +450,102 @@ def _oracle_vap(mdl, U, V, nthreads):
                        np.zeros(0), nthreads=nthreads)
 
 
-def _timed_iterations(vap, count, budget_s):
+def _timed_iterations(vap, count, budget_s, energies=None):
+    """Up to `count` oracle iterations, stopping once `budget_s` seconds have
+    passed (at least one); the projected energy of each iterated state is
+    appended to `energies`."""
     times = []
     t_start = time.perf_counter()
     while len(times) < count and (not times or time.perf_counter() - t_start < budget_s):
         t = time.perf_counter()
-        vap.iterate()
+        st, info = vap.iterate()
         times.append(time.perf_counter() - t)
+        if energies is not None:
+            energies.append(float(info[1]))
+        if st != 0:
+            break
     return times
 
 
+CPU_BASELINE_BUDGET_S = 60.0
+
+
 def cpu_baseline(mdl, U, V, args):
-    """Oracle (CPU restatement of the reference path) on all host cores: one
-    warm-up iteration, then up to 3 timed iterations of the full workload
-    (stopping once 20 s have passed); the median is reported."""
+    """Oracle (CPU restatement of the reference path) on all host cores, from
+    the workload's seed: the first iteration is the warm-up, then up to
+    warmup + steps - 1 timed iterations of the full workload, stopping once
+    60 s have passed; the median is reported.  Returns the baseline and the
+    projected energy of every iterated state (for the parity block)."""
     cores = os.cpu_count() or 1
     vap = _oracle_vap(mdl, U, V, cores)
-    vap.iterate()
-    times = sorted(_timed_iterations(vap, 3, 20.0))
+    energies = []
+    _timed_iterations(vap, 1, 0.0, energies)
+    times = sorted(_timed_iterations(vap, max(1, args.warmup + args.steps - 1), CPU_BASELINE_BUDGET_S, energies))
     med = times[len(times) // 2]
-    return {"value": 1.0 / med, "unit": "iters/s", "cores": cores, "kind": "port",
-            "sample": f"{len(times)} oracle iterations of the full workload (15x15 angles, n = 140) after one "
-                      f"warm-up, {cores} threads; median {med:.2f} s/iteration"}
+    return ({"value": 1.0 / med, "unit": "iters/s", "cores": cores, "kind": "port",
+             "sample": f"{len(times)} oracle iterations of the full workload (15x15 angles, n = 140) after one "
+                       f"warm-up, {cores} threads, from the workload's seed; median {med:.2f} s/iteration"},
+            energies)
+
+
+def device_parity(ctx, U, V, torch, oracle_energies):
+    """The device loop from the same seed for as many iterations as the oracle
+    ran: projected energy of every iterated state against the oracle's
+    (|dE| in MeV; the acceptance bound is 1e-6 MeV)."""
+    it = DeviceIteration(ctx, U, V, 0, torch)
+    dev = []
+    for _ in oracle_energies:
+        it.step()
+        dev.append(it.energy)
+    torch.cuda.synchronize()
+    d = [abs(a - b) for a, b in zip(dev, oracle_energies)]
+    return {"iterations": len(dev), "dE_max": max(d), "dE_final": d[-1], "E_final_device": dev[-1],
+            "E_final_oracle": oracle_energies[-1], "bound": 1e-6, "unit": "MeV",
+            "what": "projected energy of each iterated state, device loop against the oracle's loop from the "
+                    "workload's seed (same eta, mu, 15x15 angles)"}
+
+
+def adjoint_timing(ctx, U, V, torch, stream, calls=5):
+    """tvap_energy_adjoint (Thouless evolution, projection with the per-angle
+    densities recomputed, dE/dZ = L^-T H20v L^-1) on device buffers at the
+    workload's seed and Z = skew(N(0, 0.1)), seed 40: one warm-up call, then
+    `calls` calls timed with CUDA events on the context's stream."""
+    import ctypes
+
+    import numpy as np
+
+    from taurus_vap_gb300 import native as N
+
+    n = ctx.n
+    rng = np.random.default_rng(40)
+    Z = 0.1 * rng.normal(size=(n, n))
+    Z = Z - Z.T
+    dev = torch.device("cuda")
+    f = lambda a: torch.tensor(np.asarray(a).reshape(-1, order="F"), dtype=torch.float64, device=dev)
+    dU, dV, dZ = f(U), f(V), f(Z)
+    G = torch.empty(n * n, dtype=torch.float64, device=dev)
+    E = ctypes.c_double()
+    opts = N.TvapProjOpts(MPHI, MPHI, 2 * math.pi, ZV, NV, 1.0, 0.0, 0, 0)
+    L, h = N.lib(), ctx.h
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def call():
+        N._check(L.tvap_energy_adjoint(h, p(dU), p(dV), p(dZ), ctypes.byref(opts), ctypes.byref(E), p(G)),
+                 "tvap_energy_adjoint")
+
+    call()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(calls):
+        call()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / calls
+    return {"ms_per_call": ms, "calls": calls, "energy": E.value,
+            "what": "tvap_energy_adjoint: E(Z) and dE/dZ (n x n) at the workload, Z = skew(N(0, 0.1)); one call = "
+                    "Thouless evolution + batched projection (densities recomputed) + 2 products"}
 
 
 REFERENCE_WARMUP_BUDGET_S = 30.0
@@ -482,9 +564,10 @@ def run_reference(args):
     mdl, U, V = build_workload()
     cores = os.cpu_count() or 1
     vap = _oracle_vap(mdl, U, V, cores)
-    warm = _timed_iterations(vap, max(1, args.warmup), REFERENCE_WARMUP_BUDGET_S)
+    energies = []
+    warm = _timed_iterations(vap, max(1, args.warmup), REFERENCE_WARMUP_BUDGET_S, energies)
     t_start = time.perf_counter()
-    times = _timed_iterations(vap, max(1, args.steps), REFERENCE_TIMED_BUDGET_S)
+    times = _timed_iterations(vap, max(1, args.steps), REFERENCE_TIMED_BUDGET_S, energies)
     elapsed = time.perf_counter() - t_start
     value = len(times) / elapsed
     ms = 1000.0 * elapsed / len(times)
@@ -499,6 +582,7 @@ def run_reference(args):
                                    f"warm-up, {cores} threads (timed iterations stop after "
                                    f"{REFERENCE_TIMED_BUDGET_S:.0f} s)"},
         "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "final_energy": energies[-1], "iterations_from_seed": len(energies),
     }
     print(json.dumps(out))
 
@@ -509,7 +593,7 @@ def main():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64-pipe comparison run")
     ap.add_argument("--gemm-mode", type=int, default=2,

@@ -192,7 +192,12 @@ int tvap_evolve(tvap_ctx* ctx, const double* U0, const double* V0, const double*
  *   - all calls share the array: calls that overlap on the GPU (from several
  *     contexts or streams at once) race on it;
  *   - the dense products run on the FP64 pipe in this variant;
- *   - the context's device must be the current device. */
+ *   - the context's device must be the current device, and all five
+ *     pointers must be device (or managed) memory of that device;
+ *   - the call works on the context's stream (tvap_set_stream): the inputs
+ *     must be complete in that stream's order when it is called, and the
+ *     outputs are complete when it returns (it ends with a synchronisation
+ *     of that stream). */
 int tvap_evolve_noalloc(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z, double* U1, double* V1);
 
 /* Adjoint of the projected energy E(Z) = <Phi(Z)|H P|Phi(Z)>/<Phi(Z)|P|Phi(Z)>

@@ -21,6 +21,7 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out);
 int ensure_workspace(tvap_ctx* c, int G);
 int angle_count(const tvap_proj_opts& o);
 int check_flags(tvap_ctx* c);
+bool is_device_pointer_on(const void* p, int device);
 
 namespace {
 
@@ -191,16 +192,6 @@ int noalloc_scratch(double** out) {
   return TVAP_OK;
 }
 
-bool is_device_pointer(const void* p) {
-  cudaPointerAttributes at{};
-  const cudaError_t e = cudaPointerGetAttributes(&at, p);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
 }  // namespace
 
 }  // namespace tvap
@@ -280,15 +271,17 @@ int tvap_evolve_noalloc(tvap_ctx* c, const double* U0, const double* V0, const d
     set_last_error("tvap_evolve_noalloc: basis larger than the static scratch (n > 336)", __FILE__, __LINE__);
     return TVAP_ERR_ARG;
   }
-  if (!is_device_pointer(U0) || !is_device_pointer(V0) || !is_device_pointer(Z) || !is_device_pointer(U1) ||
-      !is_device_pointer(V1)) {
-    set_last_error("tvap_evolve_noalloc: all matrices must be device memory", __FILE__, __LINE__);
-    return TVAP_ERR_ARG;
-  }
   int dev = 0;
   TVAP_CUDA(cudaGetDevice(&dev));
   if (dev != c->device) {
     set_last_error("tvap_evolve_noalloc: the context's device must be current", __FILE__, __LINE__);
+    return TVAP_ERR_ARG;
+  }
+  const int d = c->device;
+  if (!is_device_pointer_on(U0, d) || !is_device_pointer_on(V0, d) || !is_device_pointer_on(Z, d) ||
+      !is_device_pointer_on(U1, d) || !is_device_pointer_on(V1, d)) {
+    set_last_error("tvap_evolve_noalloc: all matrices must be device memory of the context's device", __FILE__,
+                   __LINE__);
     return TVAP_ERR_ARG;
   }
   double* scratch = nullptr;

@@ -2517,6 +2517,19 @@ bool is_device_pointer(const void* p) {
   return e == cudaSuccess && (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
 }
 
+// Device memory of `device` itself, or managed memory (reachable from every
+// device); memory of another GPU is refused.
+bool is_device_pointer_on(const void* p, int device) {
+  cudaPointerAttributes at{};
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == device;
+}
+
 int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s) {
   cudaPointerAttributes at{};
   cudaError_t e = cudaPointerGetAttributes(&at, src);
