@@ -103,9 +103,10 @@ int tvap_kernel_launches(const tvap_ctx* ctx);
  * returns milliseconds and call counts per section. */
 int tvap_set_timing(tvap_ctx* ctx, int on);
 /* Arithmetic of the dense products: 0 = the FP64 pipe (DFMA);
- * 1 = FP64 emulated on the bf16 tensor cores by exact integer splitting (8
- * balanced 7-bit digits per FP64 value, exact FP32 partial sums, integer
- * recombination) with warp-level mma.sync; 2 (default) = the same splitting
+ * 1 = FP64 emulated on the bf16 tensor cores by integer splitting (8
+ * balanced 7-bit digits per FP64 value under one power-of-two scale per row
+ * or column, exact FP32 partial sums, integer recombination; error bound at
+ * tvap_zgemm) with warp-level mma.sync; 2 (default) = the same splitting
  * with tcgen05 MMAs and tensor-memory accumulators for the batched products
  * (small single products keep the mma.sync kernel).  In modes 1 and 2 the
  * field contraction over 16 or more gauge angles also runs on the tensor
@@ -200,12 +201,58 @@ int tvap_evolve(tvap_ctx* ctx, const double* U0, const double* V0, const double*
  *     of that stream). */
 int tvap_evolve_noalloc(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z, double* U1, double* V1);
 
+/* Test hook, no counterpart in the reference: the next tvap_evolve on this
+ * context runs its cooperative launch with one CTA that leaves before the
+ * first grid-wide barrier, so that the other CTAs' bounded waits there run
+ * out (after about a second); they raise the status word and return, and
+ * that tvap_evolve returns TVAP_ERR_DEVICE_TIMEOUT.  Nothing faults or
+ * hangs, and the context stays usable.  It shows that a wait which is never
+ * released ends in a status the caller can read. */
+int tvap_test_wait_timeout(tvap_ctx* ctx);
+
 /* Adjoint of the projected energy E(Z) = <Phi(Z)|H P|Phi(Z)>/<Phi(Z)|P|Phi(Z)>
  * of the state Phi(Z) = evolve(U0, V0, Z) with respect to the real Thouless
  * matrix Z: writes E and dE/dZ (n*n reals).  The per-angle densities are
  * recomputed, not stored.  No counterpart in the reference. */
 int tvap_energy_adjoint(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z,
                         const tvap_proj_opts* opts, double* energy, double* dEdZ);
+
+/* ZSKPFA('U', 'P', n, A, n, PFAFF, ...) of PFAPACK
+ * (src/subroutines_pfaffian.f:12-258; called by calculate_overlap,
+ * src/module_projection.f90:921) for `batch` complex skew-symmetric n x n
+ * matrices stored one after the other (column-major, interleaved re/im; only
+ * the upper triangle is read).  pfaff receives batch complex values.  As in
+ * ZSKPFA: Pf = 1 for n = 0, Pf = 0 for odd n, and a zero pivot of the
+ * Parlett-Reid elimination gives Pf = 0 with a successful status.  A is not
+ * modified (ZSKPFA overwrites it).  n <= 512; host or device memory. */
+int tvap_zskpfa_batched(tvap_ctx* ctx, int batch, int64_t n, const double* A, double* pfaff);
+
+/* ZGEMM / DGEMM of BLAS (C = alpha op(A) op(B) + beta C, op = 'N', 'T' or
+ * 'C'; column-major with leading dimensions; alpha and beta are complex
+ * (2 doubles) for tvap_zgemm and real (1 double) for tvap_dgemm) in the
+ * arithmetic the context uses for the path's own products
+ * (tvap_set_gemm_mode).  Host or device memory; the call returns when C is
+ * written.  In modes 1 and 2 a product with K >= 16 and at least 10^6
+ * multiply-adds is emulated on the tensor cores: every row i of op(A) and
+ * column j of op(B) gets one power-of-two scale 2^e (2^e <= its largest
+ * entry), each entry is rounded to an integer multiple of 2^(e-53) (error
+ * <= 2^-54 of the row's or column's largest entry) and written as 8 balanced
+ * base-2^7 digits, and the digit pairs of total weight below the 8th are
+ * dropped.  With a_i = max_k max(|Re op(A)_ik|, |Im op(A)_ik|) and b_j the
+ * same over column j of op(B):
+ *   real:    |C_ij - (op(A) op(B))_ij| <= 2^-49 K a_i b_j
+ *   complex: |C_ij - (op(A) op(B))_ij| <= 2^-46 K a_i b_j
+ * before the final rounding of C_ij to FP64 and the scaling by alpha and
+ * beta.  The bound is relative to the largest entries of the row and the
+ * column, not to each term: an entry of C much smaller than K a_i b_j keeps
+ * fewer correct digits than a FP64 product (error <= ~2^-53 K sum_k |A_ik
+ * B_kj|) gives it.  Mode 0 runs on the FP64 pipe.  Replaces the BLAS calls
+ * of the reference (not a reference routine of
+ * its own). */
+int tvap_zgemm(tvap_ctx* ctx, char transa, char transb, int m, int n, int k, const double* alpha, const double* A,
+               int lda, const double* B, int ldb, const double* beta, double* C, int ldc);
+int tvap_dgemm(tvap_ctx* ctx, char transa, char transb, int m, int n, int k, const double* alpha, const double* A,
+               int lda, const double* B, int ldb, const double* beta, double* C, int ldc);
 
 #ifdef __cplusplus
 }

@@ -32,6 +32,7 @@ GPU_SOURCES = [
     "ozaki.cu",
     "jacobi_cluster.cu",
     "field_blocks.cu",
+    "linalg_abi.cu",
 ]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

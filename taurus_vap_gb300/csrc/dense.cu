@@ -1255,7 +1255,7 @@ __device__ bool coop_factor_diag_warp(int n, double* S, double* rd, int j0, int 
 __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, double* S, const double* A,
                                                                        long long a_stride, double* X,
                                                                        long long x_stride, unsigned* bar,
-                                                                       int* flags) {
+                                                                       int* flags, int skip_cta) {
   extern __shared__ double coop_smem[];  // the panel rows; then L (n x n) and 1 / L_jj in the solve phase
   __shared__ double L11[kCoopNb][kCoopNb + 1];
   __shared__ double rdiag[kCoopNb];
@@ -1271,6 +1271,9 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
       atomicExch(&bar[2], 1u);
     }
   }
+  // test hook: this CTA leaves without arriving, so that the others' bounded
+  // waits at the first barrier run out (status DEV_WAIT_TIMEOUT, abort)
+  if (cta == skip_cta) return;
   if (!coop_barrier(bar, G, gen, flags)) return;
   for (int j0 = 0;;) {
     const int j1 = min(j0 + kCoopNb, n);
@@ -1397,7 +1400,7 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
 }  // namespace
 
 int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, double* X, long long x_stride,
-                         unsigned* bar, int* flags, cudaStream_t s) {
+                         unsigned* bar, int* flags, cudaStream_t s, int skip_cta) {
   const size_t shm = sizeof(double) * (size_t(n) * n + n);
   if (n > 384 || shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
   // the co-resident grid for this shared-memory size, found once per device
@@ -1420,7 +1423,10 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
   }
   if (grid < 1) return TVAP_ERR_ARG;
   TVAP_CUDA(cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned), s));
-  void* args[] = {&n, &S, &A, &a_stride, &X, &x_stride, &bar, &flags};
+  // the hook names the grid's last CTA (never CTA 0, which factors the
+  // diagonal blocks); -1 leaves every CTA in
+  int skip = (skip_cta >= 0 && grid > 1) ? grid - 1 : -1;
+  void* args[] = {&n, &S, &A, &a_stride, &X, &x_stride, &bar, &flags, &skip};
   ++g_launch_count;
   TVAP_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_evolve_kernel, dim3(grid), dim3(kCoopThreads), args,
                                         shm, s));

@@ -121,8 +121,10 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1, bool
     if ((rc = rgemm(n, n, n, view_cm(b.U0, n, 0), Zv, b.A2, n, 1.0, 1.0, s))) return rc;
   }
   if (coop) {
+    const int skip = c->test_skip_arrival ? 1 : -1;
+    c->test_skip_arrival = false;
     rc = cholesky_evolve_coop(n, b.L, b.A1, (long long)(b.A2 - b.A1), U1, (long long)(V1 - U1), c->d_bar,
-                              c->d_flags, s);
+                              c->d_flags, s, skip);
     if (rc == TVAP_OK) {
       sec_end(c, SEC_EVOLVE);
       return TVAP_OK;
@@ -262,6 +264,12 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   if (!rc) rc = download_matrix(dV1, V1, sizeof(double) * nn, s);
   if (!rc) rc = check_flags(c);
   return rc;
+}
+
+int tvap_test_wait_timeout(tvap_ctx* c) {
+  if (!c) return TVAP_ERR_ARG;
+  c->test_skip_arrival = true;
+  return TVAP_OK;
 }
 
 int tvap_evolve_noalloc(tvap_ctx* c, const double* U0, const double* V0, const double* Z, double* U1, double* V1) {

@@ -7,7 +7,9 @@
 // written in balanced base 2^7 with 8 digits in [-64, 63] (most significant
 // first).  A digit is exact in bf16 and a digit product (<= 2^12) exact in
 // FP32.  The tensor cores sum the products of digit pairs (s, t) with
-// s + t <= 7 (the dropped pairs weigh < 2^-56 of the leading term) into one
+// s + t <= 7 (the dropped pairs sum to at most 7.05 * 2^54 units of
+// 2^(e_a + e_b - 106), i.e. 2^-49.2 of 2^(e_a + e_b), which is at most the
+// product of the row's and the column's largest entries) into one
 // FP32 accumulator per weight group g = s + t; over 64 consecutive k a group
 // sum stays below 2^21 (2^23 for the 3M sum products below), so it is an exact
 // integer.  Every 64 k the group sums are converted to integers and folded,

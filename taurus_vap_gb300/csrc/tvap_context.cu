@@ -61,6 +61,7 @@ int device_sms() {
 int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
 int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
 bool is_device_pointer(const void* p);
+int check_finite(tvap_ctx* c, const double* const* ptrs, const char* const* names, int count, size_t elems);
 int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out);
 int ensure_workspace(tvap_ctx* c, int G);
 void destroy_workspace(tvap_ctx* c);
@@ -287,13 +288,14 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
   if ((e = cudaMalloc(&c->d_sp_2mj, sizeof(int) * n)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_tr, sizeof(int) * n)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_sp_l, sizeof(int) * n)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&c->d_flags, sizeof(int))) != cudaSuccess) return fail(e);
+  // the status word, then words for the non-finite check of caller matrices
+  if ((e = cudaMalloc(&c->d_flags, 8 * sizeof(int))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->d_bar, 4 * sizeof(unsigned))) != cudaSuccess) return fail(e);
   cudaMemset(c->d_bar, 0, 4 * sizeof(unsigned));
   cudaMemcpy(c->d_sp_2mj, sp_2mj, sizeof(int) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_sp_tr, sp_tr, sizeof(int) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_sp_l, sp_l, sizeof(int) * n, cudaMemcpyHostToDevice);
-  cudaMemset(c->d_flags, 0, sizeof(int));
+  cudaMemset(c->d_flags, 0, 8 * sizeof(int));
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   *ctx = c;
   return TVAP_OK;
@@ -446,6 +448,11 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   int rc;
+  {
+    const double* mats[2] = {U0, V0};
+    const char* names[2] = {"U0", "V0"};
+    if ((rc = check_finite(c, mats, names, 2, nn))) return rc;
+  }
   if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
   if ((rc = upload_matrix(U0, ws_U(c), sizeof(double) * nn, c->stream))) return rc;
   if ((rc = upload_matrix(V0, ws_V(c), sizeof(double) * nn, c->stream))) return rc;

@@ -279,6 +279,9 @@ struct tvap_ctx {
   // canonical bases: [0] FP32 Jacobi + refinement attempts, [1] of them
   // accepted, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in total
   long long canon_attempts[7] = {0, 0, 0, 0, 0, 0, 0};
+  // test hook (tvap_test_wait_timeout): the next cooperative evolution has
+  // its last CTA leave before the first grid barrier; one-shot
+  bool test_skip_arrival = false;
 };
 
 namespace tvap {
@@ -351,6 +354,6 @@ int cholesky_inverse(int n, double* A, int* flags, cudaStream_t s);
 // launch; TVAP_ERR_ARG when n is outside its range (the caller then uses
 // cholesky_inverse and two products)
 int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, double* X, long long x_stride,
-                         unsigned* bar, int* flags, cudaStream_t s);
+                         unsigned* bar, int* flags, cudaStream_t s, int skip_cta = -1);
 
 }  // namespace tvap

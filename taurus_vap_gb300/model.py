@@ -227,13 +227,21 @@ def read_wavefunction_text(path: str, n: int):
 
 
 def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: int,
-                      block: int = 0):
+                      block: int = 0, mix_isospin: bool = True, zero_pair: int | None = None):
     """Random real Bogoliubov seed in the spirit of seed_type 0
     (module_wavefunctions.f90:134-204,250-354,442-547): BCS occupations drawn
     until the particle numbers are reached, then two random orthogonal
     transformations D (left) and C (right).  ``block`` > 0 exchanges the
     columns of U and V for that quasiparticle (block_quasiparticle,
-    :959-984).  The random stream is NumPy's, not the Fortran processor's."""
+    :959-984).  With ``mix_isospin`` false, D and C act on the proton and the
+    neutron states separately, so that the state has good proton and neutron
+    number parities (the states the half-circle projection, proj_facpi = pi,
+    is meant for).  ``zero_pair`` = k zeroes the columns of U and V of the
+    k-th canonical pair before the random transformations: the result is
+    not a Bogoliubov transformation (U^T U + V^T V is singular, and so is
+    U_phi at every gauge angle), while rho and kappa are those of a valid
+    state with that pair empty -- an input for the singular-U_phi failure
+    path.  The random stream is NumPy's, not the Fortran processor's."""
     rng = np.random.default_rng(seed)
     n = basis.n
     v2c = np.zeros(n // 2)
@@ -254,6 +262,7 @@ def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: in
     V = np.zeros((n, n))
     ipos = 0
     k = 0
+    pairs = []
     shells2j = [s % 100 for s in basis.shells]
     for j in shells2j:
         for m in range(1, (j + 1) // 2 + 1):
@@ -268,17 +277,30 @@ def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: in
             V[p2, p1] = -V[p1, p2]
             V[p3, p4] = np.sqrt(v2c[k + n // 4])
             V[p4, p3] = -V[p3, p4]
+            pairs += [(p1, p2), (p3, p4)]
             k += 1
         ipos += j + 1
+    if zero_pair is not None:
+        cols = list(pairs[zero_pair])
+        U[:, cols] = 0.0
+        V[:, cols] = 0.0
 
-    def unitary():
-        B = rng.random((n, n))
+    def unitary(m=n):
+        B = rng.random((m, m))
         B = np.triu(B) + np.triu(B, 1).T
         return np.linalg.eigh(B)[1]
 
-    D = unitary()
+    def transform():
+        if mix_isospin:
+            return unitary()
+        T = np.zeros((n, n))
+        T[: n // 2, : n // 2] = unitary(n // 2)
+        T[n // 2:, n // 2:] = unitary(n // 2)
+        return T
+
+    D = transform()
     U, V = D @ U, D @ V
-    C = unitary()
+    C = transform()
     U, V = U @ C, V @ C
     if block > 0:
         U[:, block - 1], V[:, block - 1] = V[:, block - 1].copy(), U[:, block - 1].copy()

@@ -102,6 +102,14 @@ def lib():
         L.tvap_evolve_noalloc.restype = ci
         L.tvap_energy_adjoint.argtypes = [vp, vp, vp, vp, ctypes.POINTER(TvapProjOpts), vp, vp]
         L.tvap_energy_adjoint.restype = ci
+        L.tvap_test_wait_timeout.argtypes = [vp]
+        L.tvap_test_wait_timeout.restype = ci
+        L.tvap_zskpfa_batched.argtypes = [vp, ci, ctypes.c_int64, vp, vp]
+        L.tvap_zskpfa_batched.restype = ci
+        cc = ctypes.c_char
+        for name in ("tvap_zgemm", "tvap_dgemm"):
+            getattr(L, name).argtypes = [vp, cc, cc, ci, ci, ci, vp, vp, ci, vp, ci, vp, vp, ci]
+            getattr(L, name).restype = ci
         _lib = L
     return _lib
 
@@ -285,6 +293,43 @@ class Context:
         _check(lib().tvap_energy_adjoint(self.h, _p(U), _p(V), _p(Zm), ctypes.byref(o), ctypes.byref(E), _p(G)),
                "tvap_energy_adjoint")
         return E.value, G
+
+    # -- ZSKPFA('U', 'P') of PFAPACK (subroutines_pfaffian.f:12-258) ------------
+    def zskpfa_batched(self, A):
+        """Pfaffians of a batch (b, m, m) of complex skew-symmetric matrices
+        (A[q] is matrix q, indexed [row, column]; only the upper triangle is
+        read)."""
+        A = np.asarray(A, dtype=np.complex128)
+        if A.ndim == 2:
+            A = A[None]
+        b, m = A.shape[0], A.shape[1]
+        cm = np.ascontiguousarray(np.transpose(A, (0, 2, 1)))  # column-major per matrix
+        pf = np.zeros(2 * b)
+        _check(lib().tvap_zskpfa_batched(self.h, b, m, _p(cm), _p(pf)), "tvap_zskpfa_batched")
+        return pf[0::2] + 1j * pf[1::2]
+
+    # -- ZGEMM / DGEMM in the context's arithmetic -----------------------------
+    def gemm(self, A, B, transa="N", transb="N", alpha=1.0, beta=0.0, C=None):
+        """C = alpha op(A) op(B) + beta C (complex when any operand is)."""
+        cplx = any(np.iscomplexobj(x) for x in (A, B, C) if x is not None) or isinstance(alpha, complex) or \
+            isinstance(beta, complex)
+        dt = np.complex128 if cplx else np.float64
+        A = np.asfortranarray(A, dtype=dt)
+        B = np.asfortranarray(B, dtype=dt)
+        m = A.shape[1] if transa.upper() != "N" else A.shape[0]
+        k = A.shape[0] if transa.upper() != "N" else A.shape[1]
+        n = B.shape[0] if transb.upper() != "N" else B.shape[1]
+        C = np.zeros((m, n), dtype=dt, order="F") if C is None else np.array(C, dtype=dt, order="F")
+        if cplx:
+            al = np.array([complex(alpha).real, complex(alpha).imag])
+            be = np.array([complex(beta).real, complex(beta).imag])
+            fn = lib().tvap_zgemm
+        else:
+            al, be = np.array([float(alpha)]), np.array([float(beta)])
+            fn = lib().tvap_dgemm
+        _check(fn(self.h, transa.encode(), transb.encode(), m, n, k, _p(al), _p(A), max(1, A.shape[0]), _p(B),
+                  max(1, B.shape[0]), _p(be), _p(C), max(1, m)), "tvap_gemm")
+        return C
 
 
 TWO_PI = 2.0 * math.pi
