@@ -56,8 +56,9 @@ enum {
   TVAP_ERR_IMAG_GRADIENT = 13,/* Im(gradient) > 1e-8 (module_projection.f90:751-755) */
   TVAP_ERR_CHOLESKY = 14,     /* dpbtrf failed (module_constraints.f90:528-531) */
   TVAP_ERR_TRTRI = 15,        /* dtrtri failed (module_constraints.f90:568-571) */
-  TVAP_ERR_CANONICAL = 16,    /* canonical basis: eigen solver did not converge or a
-                                 degenerate block larger than 2 (DGEES case) */
+  TVAP_ERR_CANONICAL = 16,    /* canonical basis: eigen solver did not converge, a
+                                 degenerate subspace larger than 64 or not reducible
+                                 to 2 x 2 blocks, or an odd number of paired states */
   TVAP_ERR_NUMBER_DRIFT = 18, /* particle numbers wrong 3 times in 5 iterations
                                  (module_gradient.f90:528-545) */
   TVAP_ERR_DEVICE_TIMEOUT = 19 /* a bounded wait inside a tensor-core kernel ran out

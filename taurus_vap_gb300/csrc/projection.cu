@@ -72,6 +72,9 @@ struct Workspace {
   // XB = [X0 | rho X0 | X1 | rho X1], RS = [X^T X | X^T rho X]
   double *XB = nullptr, *Xr = nullptr, *Xn = nullptr, *RS = nullptr, *Rr = nullptr, *Br = nullptr, *Sr = nullptr,
          *Mr = nullptr, *lam = nullptr, *rscal = nullptr;
+  // pairing bases of the degenerate subspaces of the canonical basis (Q, then
+  // Q^T kappa Q, kSubMax^2 each)
+  double* schq = nullptr;
   // overlap chain scratch (runs on the second stream)
   double2 *OW = nullptr, *OX = nullptr, *OY = nullptr;
   int* rflag = nullptr;
@@ -98,6 +101,7 @@ int dalloc(T** p, size_t count, size_t& total) {
 }
 
 constexpr int kPanelMax = 32;  // columns per panel of the Thouless solve
+constexpr int kSubMax = 64;    // largest degenerate subspace of the canonical basis
 
 // double2 entries per angle of Workspace::Tinv
 size_t tinv_stride(int n) { return size_t((n + kPanelMax - 1) / kPanelMax) * 2 * kPanelMax * kPanelMax; }
@@ -109,7 +113,7 @@ void ws_free(Workspace* w) {
                   w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
                   w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
                   w->H20v,  w->XB,    w->RS,     w->Br,    w->Mr,     w->lam,   w->rscal,
-                  w->rflag, w->OW,    w->OX,     w->OY,     w->piv, w->Tinv, w->tpart};
+                  w->rflag, w->OW,    w->OX,     w->OY,     w->piv, w->Tinv, w->tpart, w->schq};
   for (void* p : ptrs) cudaFree(p);
   *w = Workspace();
 }
@@ -139,7 +143,7 @@ int ws_ensure(tvap_ctx* c, int G) {
   A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
   A_(XB, 4 * nn) A_(RS, 2 * nn) A_(Br, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
   A_(OW, nG) A_(OX, nG) A_(OY, nG) A_(piv, size_t(n) * G)
-  A_(Tinv, size_t(G) * tinv_stride(n)) A_(tpart, size_t(G) * 9 * 256)
+  A_(Tinv, size_t(G) * tinv_stride(n)) A_(tpart, size_t(G) * 9 * 256) A_(schq, 2 * kSubMax * kSubMax)
 #undef A_
   w->V = w->VU;
   w->U = w->VU + nn;
@@ -154,15 +158,141 @@ int ws_ensure(tvap_ctx* c, int G) {
 // small kernels
 // ---------------------------------------------------------------------------
 
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// One warp: column c of Q (d x d, column-major) orthogonalised against
+// columns 0 .. c-1 (twice, classical Gram-Schmidt) and normalised; false if
+// nothing of it is left.
+__device__ bool pair_orthonormalise(int d, double* Q, int c) {
+  const int lane = threadIdx.x & 31;
+  for (int pass = 0; pass < 2; ++pass)
+    for (int cc = 0; cc < c; ++cc) {
+      double dot = 0.0;
+      for (int i = lane; i < d; i += 32) dot = fma(Q[i + cc * d], Q[i + c * d], dot);
+      dot = warp_sum_d(dot);
+      for (int i = lane; i < d; i += 32) Q[i + c * d] = fma(-dot, Q[i + cc * d], Q[i + c * d]);
+      __syncwarp();
+    }
+  double nrm = 0.0;
+  for (int i = lane; i < d; i += 32) nrm = fma(Q[i + c * d], Q[i + c * d], nrm);
+  nrm = warp_sum_d(nrm);
+  if (!(nrm > 1.0e-24)) return false;
+  const double r = 1.0 / sqrt(nrm);
+  for (int i = lane; i < d; i += 32) Q[i + c * d] *= r;
+  __syncwarp();
+  return true;
+}
+
+// Canonical form of kappa on a degenerate subspace of rho (rows and columns
+// k0 .. k0+d-1 of the basis; the reference Schur-reduces it with DGEES,
+// module_wavefunctions.f90:873-906).  On such a subspace rho = v^2 1 and, the
+// state being a quasiparticle vacuum, kappa^2 = -(v^2 - v^4) 1: kappa = b J
+// with J orthogonal and skew.  A pairing basis follows without an eigen
+// solver: q1 = a unit vector of the subspace (the basis vector least covered
+// by the columns so far), q2 = kappa q1 / |kappa q1|; kappa maps span{q1, q2}
+// onto itself, so the next pair starts orthogonal to both.  Q^T kappa Q is
+// then block diagonal with 2 x 2 blocks; any remaining coupling (a subspace
+// that is not exactly degenerate) larger than 1e-10 of the largest entry is
+// reported as a failure.  Kappa's subspace block is replaced by Q^T kappa Q
+// and D's columns by D Q (rho's diagonal is left as it is, as in the
+// reference).  Whole CTA; Q and T = kappa Q in global scratch (2 kSubMax^2).
+__device__ bool pair_subspace(int n, int k0, int d, double* kapc, double* D, double* Q, double* T) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+  __shared__ int s_ok;
+  __shared__ double s_kmax;
+  auto K = [&](int i, int j) -> double& { return kapc[(k0 + i) + size_t(k0 + j) * n]; };
+  if (tid < 32) {
+    bool ok = true;
+    for (int p = 0; p < d / 2 && ok; ++p) {
+      const int c0 = 2 * p;
+      // the basis vector with the largest part outside the columns so far
+      double best = -1.0;
+      int bi = d;
+      for (int i = lane; i < d; i += 32) {
+        double r = 1.0;
+        for (int c = 0; c < c0; ++c) r = fma(-Q[i + c * d], Q[i + c * d], r);
+        if (r > best) {
+          best = r;
+          bi = i;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      for (int i = lane; i < d; i += 32) Q[i + c0 * d] = (i == bi) ? 1.0 : 0.0;
+      __syncwarp();
+      ok = pair_orthonormalise(d, Q, c0);
+      if (!ok) break;
+      for (int i = lane; i < d; i += 32) {
+        double w = 0.0;
+        for (int j = 0; j < d; ++j) w = fma(K(i, j), Q[j + c0 * d], w);
+        Q[i + (c0 + 1) * d] = w;
+      }
+      __syncwarp();
+      ok = pair_orthonormalise(d, Q, c0 + 1);
+    }
+    if (lane == 0) s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  if (!s_ok) return false;
+  // T = kappa Q, then kappa <- Q^T T on the subspace
+  for (int e = tid; e < d * d; e += nt) {
+    const int i = e % d, c = e / d;
+    double v = 0.0;
+    for (int j = 0; j < d; ++j) v = fma(K(i, j), Q[j + c * d], v);
+    T[e] = v;
+  }
+  __syncthreads();
+  if (tid == 0) s_kmax = 0.0;
+  __syncthreads();
+  double kmax = 0.0;
+  for (int e = tid; e < d * d; e += nt) {
+    const int i = e % d, c = e / d;
+    double v = 0.0;
+    for (int j = 0; j < d; ++j) v = fma(Q[j + i * d], T[j + c * d], v);
+    K(i, c) = v;
+    kmax = fmax(kmax, fabs(v));
+  }
+  // the largest entry (non-negative doubles order as their bit patterns)
+  atomicMax(reinterpret_cast<unsigned long long*>(&s_kmax), __double_as_longlong(kmax));
+  __syncthreads();
+  const double tol = 1.0e-10 * s_kmax;
+  int bad = 0;
+  for (int e = tid; e < d * d; e += nt) {
+    const int i = e % d, c = e / d;
+    if ((i >> 1) != (c >> 1) && fabs(K(i, c)) > tol) bad = 1;
+  }
+  // D's subspace columns: D <- D Q, one row per thread
+  for (int r = tid; r < n; r += nt) {
+    double row[kSubMax];
+    for (int j = 0; j < d; ++j) row[j] = D[r + size_t(k0 + j) * n];
+    for (int c = 0; c < d; ++c) {
+      double v = 0.0;
+      for (int j = 0; j < d; ++j) v = fma(row[j], Q[j + c * d], v);
+      D[r + size_t(k0 + c) * n] = v;
+    }
+  }
+  return __syncthreads_or(bad) == 0;
+}
+
 // canonical-basis bookkeeping (construct_canonical_basis after the
 // diagonalisation, module_wavefunctions.f90:818-945, and the v/u extraction
 // of project_wavefunction, module_projection.f90:219-234).  One CTA.
-__global__ void canon_kernel(int n, const double* __restrict__ rhoc, const double* __restrict__ kapc, double eps,
-                             int allemp, int* canon_i, double* canon_d) {
+__global__ void canon_kernel(int n, const double* __restrict__ rhoc, double* __restrict__ kapc, double* D,
+                             double* sch, double eps, int allemp, int* canon_i, double* canon_d) {
   __shared__ int submax[1024];
   __shared__ double rd[256];
   __shared__ int ri[3][256];
-  __shared__ int s_nocc, s_nemp, s_nlow, s_bad;
+  __shared__ int s_nocc, s_nemp, s_nlow, s_bad, s_nsub;
+  __shared__ int s_sub[2][kSubMax];
   const int tid = threadIdx.x, nt = blockDim.x;
   // occupation counts and ovac = sum log u over paired states (parallel)
   double ov = 0.0;
@@ -217,14 +347,27 @@ __global__ void canon_kernel(int n, const double* __restrict__ rhoc, const doubl
       if (mx == j) k = j + 1;
     }
     k = 1 + nemp;
+    s_nsub = 0;
     while (k < n - nocc) {
       int d = submax[k] - k + 1;
-      if (d > 2 && (d % 2) != 0) d = 2;
-      if (d > 2) s_bad = 1;  // the reference would Schur-reduce this block (DGEES)
+      if (d > 2 && (d % 2) != 0) d = 2;  // as the reference does (with a warning)
+      if (d > 2) {
+        // a degenerate subspace: put into canonical form below
+        if (d <= kSubMax && s_nsub < kSubMax) {
+          s_sub[0][s_nsub] = k - 1;
+          s_sub[1][s_nsub] = d;
+          ++s_nsub;
+        } else {
+          s_bad = 1;
+        }
+      }
       k += d;
     }
     if ((n - nocc - nemp) % 2 != 0) s_bad = 1;
   }
+  __syncthreads();
+  for (int q = 0; q < s_nsub; ++q)
+    if (!pair_subspace(n, s_sub[0][q], s_sub[1][q], kapc, D, sch, sch + kSubMax * kSubMax) && tid == 0) s_bad = 1;
   __syncthreads();
   // v/u with the sign of kappa in the canonical basis; the paired states are
   // contiguous after the nlow states with v^2 <= eps, so the reference's
@@ -2257,7 +2400,8 @@ int prepare_canonical(tvap_ctx* c, double occeps, double allemp_d, int* host_can
   if ((rc = real_gemm(n, n, n, view_t(Dn), view_cm(w->kap, n, 0), w->tmp, n, 1.0, 0.0, s))) return rc;
   if ((rc = real_gemm(n, n, n, view_cm(w->tmp, n, 0), Dn, w->kapc, n, 1.0, 0.0, s))) return rc;
   const double eps = (occeps < 2.2250738585072014e-308) ? 1.0e-8 : occeps;
-  canon_kernel<<<1, 256, 0, tvap::counted(s)>>>(n, w->rhoc, w->kapc, eps, int(allemp_d), w->canon_i, w->canon_d);
+  canon_kernel<<<1, 256, 0, tvap::counted(s)>>>(n, w->rhoc, w->kapc, w->D, w->schq, eps, int(allemp_d), w->canon_i,
+                                                w->canon_d);
   TVAP_CUDA(cudaGetLastError());
   {
     // D_t^T D_t over the rows of isospin t, batch t = p, n
@@ -2301,7 +2445,10 @@ int angles_overlap(tvap_ctx* c, int G, const double2* d_ephase, int nocc, int ne
     left_solve_kernel<<<G, kLsThreads, 0, tvap::counted(s2)>>>(nocc, nb, View{w->Rn + nb + size_t(nb) * n2, 1, n2, (long long)n2 * n2},
                                                 View{w->Rn + nb, 1, n2, (long long)n2 * n2}, w->OW, w->OX, 1, nocc,
                                                 (long long)nocc * nb, 0, w->detR22, G, c->d_flags, DEV_SINGULAR_RN);
-    schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, tvap::counted(s2)>>>(n2, nb, G, w->Rn, w->OX, w->SZ);
+    // (nb = 0: every state occupied or empty, a Slater determinant; no
+    // Schur complement, only det R22)
+    if (nb > 0)
+      schur_kernel<<<nblk(size_t(nb) * nb * G, tb), tb, 0, tvap::counted(s2)>>>(n2, nb, G, w->Rn, w->OX, w->SZ);
     TVAP_CUDA(cudaGetLastError());
     S = w->SZ;
     ldS = nb;
@@ -2614,8 +2761,9 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
     w->ang_vn = o.valence_N;
   }
   auto canon_error = [&]() {
-    set_last_error("canonical basis has a degenerate block larger than 2 or an odd paired block", __FILE__,
-                   __LINE__);
+    set_last_error("canonical basis: a degenerate subspace larger than 64 or not reducible to 2 x 2 blocks, an "
+                   "odd number of paired states, or a zero v/u",
+                   __FILE__, __LINE__);
     return TVAP_ERR_CANONICAL;
   };
   if (o.mode == 0) {

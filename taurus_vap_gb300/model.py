@@ -237,11 +237,11 @@ def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: in
     neutron states separately, so that the state has good proton and neutron
     number parities (the states the half-circle projection, proj_facpi = pi,
     is meant for).  ``zero_pair`` = k zeroes the columns of U and V of the
-    k-th canonical pair before the random transformations: the result is
-    not a Bogoliubov transformation (U^T U + V^T V is singular, and so is
-    U_phi at every gauge angle), while rho and kappa are those of a valid
-    state with that pair empty -- an input for the singular-U_phi failure
-    path.  The random stream is NumPy's, not the Fortran processor's."""
+    k-th canonical pair and leaves out the right transformation C, so that
+    the two columns stay zero: the result is not a Bogoliubov transformation
+    (U_phi has two zero rows at every gauge angle), while rho and kappa are
+    those of a valid state with that pair empty -- an input for the
+    singular-U_phi failure path.  The random stream is NumPy's, not the Fortran processor's."""
     rng = np.random.default_rng(seed)
     n = basis.n
     v2c = np.zeros(n // 2)
@@ -301,7 +301,62 @@ def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: in
     D = transform()
     U, V = D @ U, D @ V
     C = transform()
-    U, V = U @ C, V @ C
+    if zero_pair is None:
+        U, V = U @ C, V @ C
     if block > 0:
         U[:, block - 1], V[:, block - 1] = V[:, block - 1].copy(), U[:, block - 1].copy()
+    return np.asfortranarray(U), np.asfortranarray(V)
+
+
+def spherical_seed(basis: Basis, valence_Z: float, valence_N: float, seed: int = 0, slater: bool = False,
+                   mix_quasiparticles: bool = True):
+    """Spherical real Bogoliubov state: one occupation v^2 per j-shell and
+    isospin for all its m-states, so that every shell is a (2j+1)-fold
+    degenerate level of the canonical basis (the case the reference
+    Schur-reduces with DGEES, module_wavefunctions.f90:873-906).  BCS
+    occupations are drawn from ``seed`` and scaled to the particle numbers;
+    with ``slater`` the lowest shells (in the basis order) are filled (v^2 = 1)
+    and the rest left empty, which needs closed-shell particle numbers.  A
+    random orthogonal mixing of the quasiparticles (right transformation)
+    leaves rho and kappa unchanged."""
+    rng = np.random.default_rng(seed)
+    n = basis.n
+    shells2j = [s % 100 for s in basis.shells]
+    v2 = np.zeros((2, len(shells2j)))
+    for t, target in enumerate((valence_Z, valence_N)):
+        if slater:
+            left = target
+            for k, j in enumerate(shells2j):
+                if left >= j + 1 - 1e-9:
+                    v2[t, k] = 1.0
+                    left -= j + 1
+            if abs(left) > 1e-9:
+                raise ValueError("a Slater determinant needs closed-shell particle numbers")
+        else:
+            w = rng.random(len(shells2j)) * np.exp(-0.3 * np.arange(len(shells2j)))
+            deg = np.array([j + 1 for j in shells2j], dtype=float)
+            # scale the occupations to the particle number, keeping 0 < v^2 < 1
+            lo, hi = 0.0, 1e6
+            for _ in range(200):
+                mid = 0.5 * (lo + hi)
+                num = float(np.sum(deg * (mid * w) / (1.0 + mid * w)))
+                lo, hi = (mid, hi) if num < target else (lo, mid)
+            v2[t] = (lo * w) / (1.0 + lo * w)
+    U = np.zeros((n, n))
+    V = np.zeros((n, n))
+    ipos = 0
+    for k, j in enumerate(shells2j):
+        for m in range(1, (j + 1) // 2 + 1):
+            p1 = ipos + m - 1
+            p2 = ipos + j + 2 - m - 1
+            for t in (0, 1):
+                a, b = p1 + t * (n // 2), p2 + t * (n // 2)
+                U[a, a] = U[b, b] = np.sqrt(1.0 - v2[t, k])
+                V[a, b] = np.sqrt(v2[t, k])
+                V[b, a] = -V[a, b]
+        ipos += j + 1
+    if mix_quasiparticles:
+        B = rng.random((n, n))
+        C = np.linalg.eigh(np.triu(B) + np.triu(B, 1).T)[1]
+        U, V = U @ C, V @ C
     return np.asfortranarray(U), np.asfortranarray(V)

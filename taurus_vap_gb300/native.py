@@ -24,7 +24,7 @@ ERRORS = {
     13: "the gradient has non-zero imaginary part (calculate_projected_H20)",
     14: "Cholesky factorization has failed (cholesky_factorization)",
     15: "error in the inverse of L (evolve_wavefunction)",
-    16: "canonical basis: eigen solver did not converge or degenerate block > 2",
+    16: "canonical basis: eigen solver did not converge or a degenerate subspace could not be reduced",
     18: "particle numbers wrong three times in the last five iterations",
     19: "a bounded wait inside a device kernel ran out (the kernel stopped and released its resources)",
 }

@@ -47,16 +47,17 @@ def energy(p):
 # failures
 # ---------------------------------------------------------------------------
 def test_singular_uphi_is_reported(sd):
-    # one canonical pair zeroed in U and V: rho and kappa are those of a valid
-    # state (the canonical basis and the overlap are regular) while U_phi has
-    # two zero rows at every angle.  The reference does not check zgetrf's
-    # info in calculate_thouless (module_projection.f90:700-702): it goes on
-    # with an undefined inverse and stops at the imaginary-gradient check
-    # (the oracle's status 30).  The device reports the singular U_phi itself.
+    # one canonical pair zeroed in U and V (no quasiparticle mixing after it):
+    # rho and kappa are those of a valid state with that pair empty, so the
+    # canonical basis and the overlap are regular, while U_phi has two zero
+    # rows at every angle.  The oracle's zgetrf in calculate_thouless
+    # (module_projection.f90:700-702) reports the zero pivot (its status 20;
+    # the reference itself does not check that info); the device reports the
+    # singular U_phi.
     mdl, U, V = sd
     U2, V2 = M.random_bogoliubov(mdl.basis, 4, 4, seed=3, zero_pair=3)
     ref = O.OracleModel(mdl).project(U2, V2, 9, 9, 2 * math.pi, 4, 4)
-    assert ref["status"] == 30
+    assert ref["status"] == 20
     ctx = Context(mdl.basis, mdl.ham)
     with pytest.raises(TvapError) as e:
         ctx.project(U2, V2, 9, 9, 2 * math.pi, 4, 4)
