@@ -8,7 +8,8 @@ angles per species (225 angle pairs), a random real Bogoliubov seed, FP64.
 One step = one gradient iteration of the reference's loop
 (taurus_vap.f90:77-123) without constraints (PNVAP lifts the N/Z ones):
 project_wavefunction + calculate_projected_H20, calculate_gradient
-(gradient_type 0), cholesky_factorization + evolve_wavefunction.
+(gradient_type 0), cholesky_factorization + evolve_wavefunction, made by one
+tvap_iterate call.
 
   --impl ours       (default) device path; `value` with the state resident in
                     HBM, `e2e` through the C ABI with host buffers.
@@ -128,31 +129,27 @@ class DeviceIteration:
         self.energy = None
 
     def step(self):
+        """tvap_iterate: projection, gradient and evolution with one host
+        round trip; the next step reads this step's outputs."""
         N, L, h = self.N, self.N.lib(), self.ctx.h
         import ctypes
 
         p = lambda t: ctypes.c_void_p(t.data_ptr())
-        N._check(L.tvap_project(h, p(self.U), p(self.V), ctypes.byref(self.opts), ctypes.byref(self.pnp), p(self.H)),
-                 "tvap_project")
-        k = L.tvap_kernel_launches(h)
-        N._check(L.tvap_calculate_gradient(h, p(self.H), 0, None, None, p(self.Zim1), ETA, MU, p(self.Zi),
-                                           ctypes.byref(self.norm)), "tvap_calculate_gradient")
-        k += L.tvap_kernel_launches(h)
-        N._check(L.tvap_evolve(h, p(self.U), p(self.V), p(self.Zi), p(self.U1), p(self.V1)), "tvap_evolve")
-        k += L.tvap_kernel_launches(h)
+        N._check(L.tvap_iterate(h, p(self.U), p(self.V), ctypes.byref(self.opts), ETA, MU, p(self.Zim1), p(self.Zi),
+                                p(self.U1), p(self.V1), ctypes.byref(self.pnp), p(self.H), ctypes.byref(self.norm)),
+                 "tvap_iterate")
+        self.launches += L.tvap_kernel_launches(h)  # this library's kernels
         self.U, self.U1 = self.U1, self.U
         self.V, self.V1 = self.V1, self.V
-        self.Zim1.copy_(self.Zi)
-        self.launches += k  # this library's kernels (the Zim1 copy is torch's)
+        self.Zim1, self.Zi = self.Zi, self.Zim1
         self.energy = (self.pnp.c("ener") / self.pnp.c("over")).real
 
 
-def host_iteration(ctx, state, mode):
-    """Same iteration through the C ABI with host buffers (copies inside)."""
+def host_iteration(ctx, state):
+    """Same iteration through the C ABI (tvap_iterate) with host buffers:
+    the state is copied in and the new state, the step and the sums out."""
     U, V, Zim1 = state
-    pnp, H20v = ctx.project(U, V, MPHI, MPHI, 2 * math.pi, ZV, NV, mode=mode)
-    Zi, norm = ctx.calculate_gradient(H20v, None, None, Zim1, ETA, MU)
-    U1, V1 = ctx.evolve(U, V, Zi)
+    pnp, Zi, norm, U1, V1 = ctx.iterate(U, V, Zim1, MPHI, MPHI, 2 * math.pi, ZV, NV, ETA, MU)
     return (U1, V1, Zi), (pnp.c("ener") / pnp.c("over")).real
 
 
@@ -315,19 +312,21 @@ def run_ours(args):
 
     # ---- end to end through the C ABI with host buffers
     state = (np.asfortranarray(U), np.asfortranarray(V), np.zeros(n * n))
-    state, _ = host_iteration(ctx, state, 0)
+    state, _ = host_iteration(ctx, state)
     torch.cuda.synchronize()
     e_steps = max(1, args.steps)
     barrier()
     tw = time.perf_counter()
     for _ in range(e_steps):
-        state, _ = host_iteration(ctx, state, 0)
+        state, _ = host_iteration(ctx, state)
     torch.cuda.synchronize()
     e_ms_total = (time.perf_counter() - tw) * 1000.0
     barrier()
     _, e_value = job_rate(e_ms_total, e_steps, world, "cuda")
-    h2d = 8 * n * n * (2 + 2 + 3)
-    d2h = 8 * n * n * (1 + 1 + 2)
+    h2d = 8 * n * n * 3  # U0, V0, Z_{i-1}
+    # Z_i, U1, V1; the sums and |Z_i|^2 (7 complex), the status word, and the
+    # canonical basis' nocc, nemp and check read in the middle of the projection
+    d2h = 8 * n * n * 3 + 16 * 7 + 4 + 12
     e2e = {"value": e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
            "steps": e_steps, "timer": "host perf_counter around the steps (copies and host work included)"}
 

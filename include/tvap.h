@@ -202,6 +202,22 @@ int tvap_evolve(tvap_ctx* ctx, const double* U0, const double* V0, const double*
  *     of that stream). */
 int tvap_evolve_noalloc(tvap_ctx* ctx, const double* U0, const double* V0, const double* Z, double* U1, double* V1);
 
+/* One gradient iteration of the reference's main loop for gradient_type 0
+ * without constraints (src/taurus_vap.f90:86-113: project_wavefunction +
+ * calculate_projected_H20, calculate_gradient, and the Thouless evolution
+ * that adjust_constraints applies when constraint_dim = 0 -- the PNVAP case,
+ * src/module_constraints.f90:84-100,270-373) in one call with a single host
+ * round trip at the end: out receives the projected sums of (U0, V0), H20v
+ * (may be NULL) field_H20v, Zi = -eta H20v + mu Zim1, gradient_norm =
+ * |Zi|_F / eta, and (U1, V1) = evolve(U0, V0, Zi).  The evolution is always
+ * computed: a caller whose convergence test (gradient_norm <= eps) stops
+ * the loop keeps (U0, V0), as the reference does.  Separate input and output
+ * buffers; host or device memory.  No single counterpart in the reference
+ * (it makes three calls). */
+int tvap_iterate(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts, double eta,
+                 double mu, const double* Zim1, double* Zi, double* U1, double* V1, tvap_pnp* out, double* H20v,
+                 double* gradient_norm);
+
 /* Test hook, no counterpart in the reference: the next tvap_evolve on this
  * context runs its cooperative launch with one CTA that leaves before the
  * first grid-wide barrier, so that the other CTAs' bounded waits there run

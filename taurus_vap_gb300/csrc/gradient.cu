@@ -17,7 +17,7 @@ namespace tvap {
 
 int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
 int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
-int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out);
+int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out, bool sync = true);
 int ensure_workspace(tvap_ctx* c, int G);
 int angle_count(const tvap_proj_opts& o);
 int check_flags(tvap_ctx* c);
@@ -159,6 +159,9 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1, bool
 double* ws_U(tvap_ctx* c);
 double* ws_V(tvap_ctx* c);
 double* ws_H20v(tvap_ctx* c);
+double2* ws_sums(tvap_ctx* c);
+int sync_with_flags(tvap_ctx* c, void* dst, const void* src, size_t bytes);
+int check_finite(tvap_ctx* c, const double* const* ptrs, const char* const* names, int count, size_t elems);
 
 // ---------------------------------------------------------------------------
 // Scratch of tvap_evolve_noalloc: a file-scope device array, so that the
@@ -263,6 +266,70 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   if (!rc) rc = download_matrix(dU1, U1, sizeof(double) * nn, s);
   if (!rc) rc = download_matrix(dV1, V1, sizeof(double) * nn, s);
   if (!rc) rc = check_flags(c);
+  return rc;
+}
+
+int tvap_iterate(tvap_ctx* c, const double* U0, const double* V0, const tvap_proj_opts* opts, double eta, double mu,
+                 const double* Zim1, double* Zi, double* U1, double* V1, tvap_pnp* out, double* H20v,
+                 double* gradient_norm) {
+  if (!c || !U0 || !V0 || !opts || !Zim1 || !Zi || !U1 || !V1 || !out || !gradient_norm || eta == 0.0 ||
+      opts->Mphip < 1 || opts->Mphin < 1)
+    return TVAP_ERR_ARG;
+  if (!c->have_ham) return TVAP_ERR_NOT_READY;
+  LaunchTally tally(c);
+  g_gemm_mode = c->gemm_mode;
+  g_dev_flags = c->d_flags;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  int rc;
+  if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
+  {
+    const double* mats[2] = {U0, V0};
+    const char* names[2] = {"U0", "V0"};
+    if ((rc = check_finite(c, mats, names, 2, nn))) return rc;
+  }
+  const int tb = 256;
+  const int nblocks = int((nn + tb - 1) / tb);
+  double* buf = nullptr;
+  // Z_{i-1}, Z_i, A1, A2, U1, V1 (adjacent pairs), L (n^2 + n), partial sums
+  if ((rc = ctx_scratch(c, 7 * nn + n + nblocks, &buf))) return rc;
+  double *dZm = buf, *dZ = buf + nn, *dU1 = buf + 4 * nn, *dV1 = buf + 5 * nn, *part = buf + 7 * nn + n;
+  if ((rc = upload_matrix(U0, ws_U(c), sizeof(double) * nn, s))) return rc;
+  if ((rc = upload_matrix(V0, ws_V(c), sizeof(double) * nn, s))) return rc;
+  if ((rc = upload_matrix(Zim1, dZm, sizeof(double) * nn, s))) return rc;
+  // project_wavefunction + calculate_projected_H20, without the final wait
+  if ((rc = project_device(c, *opts, out, false))) return rc;
+  // calculate_gradient (type 0, no constraints): Z_i = -eta H20v + mu Z_{i-1};
+  // |Z_i|^2 into the first free slot after the projected sums
+  double* norm2 = reinterpret_cast<double*>(ws_sums(c) + 6);
+  sec_begin(c, SEC_GRADIENT);
+  gradient_kernel<<<nblocks, tb, 0, tvap::counted(s)>>>(nn, 0, ws_H20v(c), nullptr, nullptr, dZm, eta, mu, dZ, part);
+  sum_partials_kernel<<<1, 32, 0, tvap::counted(s)>>>(nblocks, part, norm2);
+  TVAP_CUDA(cudaGetLastError());
+  sec_end(c, SEC_GRADIENT);
+  // cholesky_factorization + evolve_wavefunction of the projected state
+  EvolveBuf b;
+  b.Z = dZ;
+  b.U0 = ws_U(c);
+  b.V0 = ws_V(c);
+  b.A1 = buf + 2 * nn;
+  b.A2 = buf + 3 * nn;
+  b.L = buf + 6 * nn;
+  if ((rc = evolve_device(c, b, n, dU1, dV1, false))) return rc;
+  if ((rc = download_matrix(dZ, Zi, sizeof(double) * nn, s))) return rc;
+  if ((rc = download_matrix(dU1, U1, sizeof(double) * nn, s))) return rc;
+  if ((rc = download_matrix(dV1, V1, sizeof(double) * nn, s))) return rc;
+  if (H20v && (rc = download_matrix(ws_H20v(c), H20v, sizeof(double) * nn, s))) return rc;
+  // one round trip: the sums, |Z_i|^2 and the status word
+  double2 sc[7];
+  rc = sync_with_flags(c, sc, ws_sums(c), sizeof(sc));
+  double* dst[6] = {out->over, out->ener, out->prot, out->neut, out->prot2, out->neut2};
+  for (int q = 0; q < 6; ++q) {
+    dst[q][0] = sc[q].x;
+    dst[q][1] = sc[q].y;
+  }
+  *gradient_norm = std::sqrt(sc[6].x) / eta;
   return rc;
 }
 

@@ -2725,7 +2725,7 @@ int check_flags(tvap_ctx* c) { return sync_with_flags(c, nullptr, nullptr, 0); }
 
 // Full projection of state (w->U, w->V) already on the device.  Leaves the
 // sums in w->pscal/pA/pH/pAH and the gradient in w->H20v.
-int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
+int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out, bool sync) {
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream, s2 = c->stream2;
@@ -2804,6 +2804,15 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out) {
   }
   projected_h20_kernel<<<nblk(nn, 256), 256, 0, tvap::counted(s)>>>(n, w->pA, w->pH, w->pAH, w->pscal, w->H20v, c->d_flags);
   TVAP_CUDA(cudaGetLastError());
+  if (!sync) {
+    // the caller reads the sums (w->pscal) and the status word later, in
+    // its own round trip
+    if (out) {
+      out->nocc = canon[0];
+      out->nemp = canon[1];
+    }
+    return TVAP_OK;
+  }
   if (out) {
     // the sums and the status word in one round trip
     double2 sc[6];
@@ -2824,6 +2833,9 @@ int ensure_workspace(tvap_ctx* c, int G) { return ws_ensure(c, G); }
 double* ws_U(tvap_ctx* c) { return c->ws->U; }
 double* ws_V(tvap_ctx* c) { return c->ws->V; }
 double* ws_H20v(tvap_ctx* c) { return c->ws->H20v; }
+// the six projected sums (over, ener, prot, neut, prot2, neut2), then two
+// free complex slots
+double2* ws_sums(tvap_ctx* c) { return c->ws->pscal; }
 int angle_count(const tvap_proj_opts& o) {
   const bool fold = (o.mode == 0) && std::fabs(o.facpi - 2.0 * M_PI) < 1e-12 && is_integer(o.valence_Z) &&
                     is_integer(o.valence_N);

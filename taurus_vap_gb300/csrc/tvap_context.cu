@@ -62,7 +62,7 @@ int upload_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
 int download_matrix(const void* src, void* dst, size_t bytes, cudaStream_t s);
 bool is_device_pointer(const void* p);
 int check_finite(tvap_ctx* c, const double* const* ptrs, const char* const* names, int count, size_t elems);
-int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out);
+int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out, bool sync = true);
 int ensure_workspace(tvap_ctx* c, int G);
 void destroy_workspace(tvap_ctx* c);
 int angle_count(const tvap_proj_opts& o);

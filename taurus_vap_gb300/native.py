@@ -102,6 +102,9 @@ def lib():
         L.tvap_evolve_noalloc.restype = ci
         L.tvap_energy_adjoint.argtypes = [vp, vp, vp, vp, ctypes.POINTER(TvapProjOpts), vp, vp]
         L.tvap_energy_adjoint.restype = ci
+        L.tvap_iterate.argtypes = [vp, vp, vp, ctypes.POINTER(TvapProjOpts), cd, cd, vp, vp, vp, vp,
+                                   ctypes.POINTER(TvapPnp), vp, vp]
+        L.tvap_iterate.restype = ci
         L.tvap_test_wait_timeout.argtypes = [vp]
         L.tvap_test_wait_timeout.restype = ci
         L.tvap_zskpfa_batched.argtypes = [vp, ci, ctypes.c_int64, vp, vp]
@@ -282,6 +285,27 @@ class Context:
         V1 = np.zeros((n, n), order="F")
         _check(lib().tvap_evolve(self.h, _p(U), _p(V), _p(Zm), _p(U1), _p(V1)), "tvap_evolve")
         return U1, V1
+
+    # -- one gradient iteration (taurus_vap.f90:86-113), gradient_type 0 -------
+    def iterate(self, U0, V0, Zim1, Mphip, Mphin, facpi, valence_Z, valence_N, eta, mu, factor_delta=1.0,
+                seed_occeps=0.0, seed_allemp=0, want_H20v=False):
+        """Projection, gradient and Thouless evolution with one host round
+        trip: returns (pnp, Zi, gradient_norm, U1, V1[, H20v]).  A caller
+        whose convergence test stops the loop keeps (U0, V0)."""
+        n = self.n
+        U, V = _f(U0, np.float64), _f(V0, np.float64)
+        Zm = np.ascontiguousarray(Zim1, dtype=np.float64).reshape(-1)
+        o = TvapProjOpts(Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta, seed_occeps, seed_allemp, 0)
+        out = TvapPnp()
+        Zi = np.zeros(n * n)
+        U1 = np.zeros((n, n), order="F")
+        V1 = np.zeros((n, n), order="F")
+        H = np.zeros(n * n) if want_H20v else None
+        norm = ctypes.c_double()
+        _check(lib().tvap_iterate(self.h, _p(U), _p(V), ctypes.byref(o), eta, mu, _p(Zm), _p(Zi), _p(U1), _p(V1),
+                                  ctypes.byref(out), _p(H), ctypes.byref(norm)), "tvap_iterate")
+        res = (out, Zi, norm.value, U1, V1)
+        return res + (H,) if want_H20v else res
 
     # -- adjoint of E(Z) -------------------------------------------------------
     def energy_adjoint(self, U0, V0, Z, Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta=1.0, mode=0):

@@ -134,3 +134,32 @@ def test_adjoint_at_random_thouless_matrix(emax4):
     E0, G0 = ctx.energy_adjoint(U, V, np.zeros((n, n)), *args)
     ref0 = om.project(U, V, *args)
     assert relerr(G0.reshape(-1, order="F"), ref0["H20v"]) < 1e-9
+
+
+def test_iterate_matches_oracle_and_three_calls(emax4):
+    # tvap_iterate (one host round trip per iteration) against the oracle's
+    # loop, and against the same iteration made of tvap_project,
+    # tvap_calculate_gradient and tvap_evolve
+    mdl, U0, V0 = emax4
+    n = mdl.n
+    om = O.OracleModel(mdl)
+    ovap = O.OracleVAP(om, U0, V0, MPHI, MPHI, 2 * math.pi, 8, 8, ETA, MU, 0.0, np.zeros((0, n * n)), np.zeros(0))
+    ctx = Context(mdl.basis, mdl.ham)
+    U, V = np.asfortranarray(U0), np.asfortranarray(V0)
+    Zim1 = np.zeros(n * n)
+    for it in range(3):
+        st, info = ovap.iterate()
+        assert st == 0
+        Un, Vn, Zr, Hr = ovap.state()
+        pnp, Zi, gnorm, U1, V1, H = ctx.iterate(U, V, Zim1, MPHI, MPHI, 2 * math.pi, 8, 8, ETA, MU, want_H20v=True)
+        assert abs((pnp.c("ener") / pnp.c("over")).real - info[1]) < 1e-9, it
+        assert relerr(H, Hr) < 1e-9, it
+        assert abs(gnorm - info[0]) < 1e-9 * info[0], it
+        assert relerr(Zi, Zr) < 1e-9, it
+        assert np.abs(U1 - Un).max() < 1e-11 and np.abs(V1 - Vn).max() < 1e-11, it
+        p2, H2 = ctx.project(U, V, MPHI, MPHI, 2 * math.pi, 8, 8)
+        Zi2, g2 = ctx.calculate_gradient(H2, None, None, Zim1, ETA, MU)
+        U2, V2 = ctx.evolve(U, V, Zi2)
+        assert abs(p2.c("ener") - pnp.c("ener")) < 1e-12 * abs(pnp.c("ener"))
+        assert np.abs(U2 - U1).max() < 1e-13 and np.abs(V2 - V1).max() < 1e-13, it
+        U, V, Zim1 = U1, V1, Zi
