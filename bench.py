@@ -105,7 +105,7 @@ class ClockSampler:
 class DeviceIteration:
     """One gradient iteration with the state resident on the device."""
 
-    def __init__(self, ctx, U, V, mode, torch):
+    def __init__(self, ctx, U, V, mode, torch, zv=ZV, nv=NV):
         import ctypes
 
         from taurus_vap_gb300 import native as N
@@ -122,7 +122,7 @@ class DeviceIteration:
         self.H = torch.zeros(n * n, dtype=torch.float64, device=dev)
         self.Zi = torch.zeros_like(self.H)
         self.Zim1 = torch.zeros_like(self.H)
-        self.opts = N.TvapProjOpts(MPHI, MPHI, 2 * math.pi, ZV, NV, 1.0, 0.0, 0, mode)
+        self.opts = N.TvapProjOpts(MPHI, MPHI, 2 * math.pi, zv, nv, 1.0, 0.0, 0, mode)
         self.pnp = N.TvapPnp()
         self.norm = ctypes.c_double()
         self.launches = 0
@@ -409,6 +409,10 @@ def run_ours(args):
         cpu, oracle_energies = cpu_baseline(mdl, U, V, args)
         parity = device_parity(ctx, U, V, torch, oracle_energies)
 
+    emax6 = None
+    if rank == 0 and not args.no_emax6:
+        emax6 = emax6_leg(torch, peaks, hbm_peak)
+
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -424,7 +428,7 @@ def run_ours(args):
         "timeline_ms": {k: [round(a, 3), round(b, 3)] for k, (a, b) in timeline.items() if sections[k][1]},
         "longest_section": longest[0], "canonical_paths": canon_paths, "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
         "final_energy": it.energy, "iterations_from_seed": args.warmup + args.steps,
-        "adjoint": adjoint, "parity": parity,
+        "adjoint": adjoint, "parity": parity, "emax6": emax6,
     }
     if rank == 0:
         print(json.dumps(out))
@@ -502,6 +506,59 @@ def device_parity(ctx, U, V, torch, oracle_energies):
             "E_final_oracle": oracle_energies[-1], "bound": 1e-6, "unit": "MeV",
             "what": "projected energy of each iterated state, device loop against the oracle's loop from the "
                     "workload's seed (same eta, mu, 15x15 angles)"}
+
+
+def emax6_leg(torch, peaks, hbm_peak, steps=3):
+    """The same iteration on the emax=6 no-core basis (n = 336, 12.9 M stored
+    elements, a 52 MB element list that streams from HBM), Z = N = 10, 15 x 15
+    angles: one warm-up and `steps` timed tvap_iterate calls with the state
+    resident on the device, CUDA events on the context's stream, and the
+    field contraction's section time against HBM."""
+    from taurus_vap_gb300 import model as M
+    from taurus_vap_gb300 import native as N
+
+    t0 = time.perf_counter()
+    mdl = M.noncore_model(6, seed=1, valence_Z=10, valence_N=10)
+    U, V = M.random_bogoliubov(mdl.basis, 10, 10, seed=7)
+    ctx = N.Context(mdl.basis, mdl.ham)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    setup_s = time.perf_counter() - t0
+    it = DeviceIteration(ctx, U, V, 0, torch, zv=10.0, nv=10.0)
+    it.step()
+    torch.cuda.synchronize()
+    ctx.set_timing(True)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        it.step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / steps
+    sec = ctx.get_timing()
+    ctx.set_timing(False)
+    n, S = mdl.n, mdl.ham.S
+    G = (MPHI * MPHI + 1) // 2
+    fld_ms = (sec["fields_gamma"][0] + sec["fields_delta"][0]) / steps
+    list_bytes = 13 * S
+    fld_bytes = list_bytes + 16 * n * n * 7 * G
+    res = {
+        "workload": "emax=6 no-core SHO basis (n=336), synthetic JT interaction (seed 1), Z=N=10, random seed 7, "
+                    "15x15 angles, FP64",
+        "n": n, "elements": S, "ms_per_step": ms, "value": 1000.0 / ms, "unit": "iters/s", "steps": steps,
+        "setup_s": setup_s, "energy": it.energy,
+        "sections_ms_per_step": {k: round(v[0] / steps, 4) for k, v in sec.items()},
+        "roofline_fields": {
+            "algorithmic_bytes": fld_bytes, "element_list_bytes": list_bytes, "ms_per_step": fld_ms,
+            "achieved_gbs": fld_bytes / (fld_ms / 1000.0) / 1e9,
+            "hbm_frac": fld_bytes / (fld_ms / 1000.0) / 1e9 / hbm_peak,
+            "peak": hbm_peak, "unit": "GB/s",
+            "what": "Gamma + Delta for all 113 folded angle columns: the element list once (13 B per element) plus "
+                    "3 density and 4 field matrices per angle (16 B per complex entry)"},
+    }
+    ctx.close()
+    return res
 
 
 def adjoint_timing(ctx, U, V, torch, stream, calls=5):
@@ -595,6 +652,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64-pipe comparison run")
+    ap.add_argument("--no-emax6", action="store_true", help="skip the emax=6 (n = 336) iteration leg")
     ap.add_argument("--gemm-mode", type=int, default=2,
                     help="dense products: 2 emulated with tcgen05 (default), 1 emulated with mma.sync, 0 FP64 pipe")
     args = ap.parse_args()

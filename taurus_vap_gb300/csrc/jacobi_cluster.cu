@@ -7,15 +7,16 @@
 // norms^2 are the eigenvalues).  One-sided Jacobi works on V, not on its
 // square rho, so small eigenvalues keep their relative precision.
 //
-// The 16 column blocks (width bw = ceil(n / 16), padded with zero columns)
-// live two per CTA in a cluster of 8.  A sweep is 15 rounds of the circle
-// method over the blocks (block 0 fixed, the others move one position per
-// round): in each round a CTA rotates all pairs between its two blocks (bw
-// sub-rounds of bw disjoint pairs, one warp per pair), and in the first round
-// also the pairs inside each block.  Between rounds the blocks move to their
-// next CTA through distributed shared memory (double buffered: compute,
-// cluster barrier, pull, cluster barrier).  The sweep's largest |cos| of a
-// pair, reduced over the cluster, decides convergence.
+// The 2C column blocks (width bw = ceil(n / 2C), padded with zero columns)
+// live two per CTA in a cluster of C (8, or 16 above n = 256).  A sweep is
+// 2C - 1 rounds of the circle method over the blocks (block 0 fixed, the
+// others move one position per round): in each round a CTA rotates all pairs
+// between its two blocks (bw sub-rounds of bw disjoint pairs, one warp per
+// pair), and in the first round also the pairs inside each block.  Between
+// rounds the blocks move to their next CTA through distributed shared memory
+// (double buffered: compute, cluster barrier, pull, cluster barrier).  The
+// sweep's largest |cos| of a pair, reduced over the cluster, decides
+// convergence.
 //
 // The hardware cluster barrier is the only wait: all CTAs of a cluster are
 // co-scheduled, and every CTA takes the same number of rounds and sweeps
@@ -30,16 +31,16 @@ namespace tvap {
 
 namespace {
 
-constexpr int kJcCtas = 8;
-constexpr int kJcBlocks = 2 * kJcCtas;
 constexpr int kJcThreads = 512;  // 16 warps: one per pair of a sub-round
-constexpr int kJcMaxBw = 16;     // n <= 256 (and at most 8 rows per lane in jc_rotate)
+constexpr int kJcMaxBw = 16;     // column pairs of a sub-round, one per warp
 constexpr int kJcMaxSweeps = 30;
 constexpr float kJcTol = 2.0e-6f;  // |cos| of every pair: the FP64 refinement takes it from there
 
-// block at position p of round r (circle method, block 0 fixed)
-__device__ __forceinline__ int jc_block(int r, int p) {
-  return p == 0 ? 0 : 1 + ((p - 1 - r) % 15 + 15) % 15;
+// block at position p of round r (circle method over `nb` blocks, block 0
+// fixed, period nb - 1)
+__device__ __forceinline__ int jc_block(int r, int p, int nb) {
+  const int per = nb - 1;
+  return p == 0 ? 0 : 1 + ((p - 1 - r) % per + per) % per;
 }
 
 // one-sided rotation of columns a and b (M and W), one warp; returns |cos|.
@@ -48,7 +49,7 @@ __device__ __forceinline__ int jc_block(int r, int p) {
 // are reduced, and the rotation uses the fast reciprocal / reciprocal square
 // root: this stage only has to reach FP32 accuracy (the FP64 refinement
 // follows), and every step of the per-pair chain is latency.
-constexpr int kJcRows = 8;
+template <int kJcRows>
 __device__ __forceinline__ float jc_rotate(int ma, int mb, int wa, int wb, int n, int lane) {
   extern __shared__ float jc[];  // the kernel's dynamic shared memory: offsets keep the accesses in LDS/STS
   float* Ma = jc + ma;
@@ -112,9 +113,13 @@ __device__ __forceinline__ float jc_rotate(int ma, int mb, int wa, int wb, int n
 // M64: rho = M64 M64^T columns source: column j of M = M64[j * n ..] (mt = 0)
 // or row j of M64 (mt = 1, M = M64^T); W0: the basis the rotations apply to
 // (identity when null); W64 receives the rotated basis.
+// kJcCtas CTAs in the cluster (2 kJcCtas column blocks), kJcRows rows of a
+// column per lane (n <= 32 kJcRows)
+template <int kJcCtas, int kJcRows>
 __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const double* __restrict__ M64, int mt,
                                                                     const double* __restrict__ W0,
                                                                     double* __restrict__ W64, int* sweeps_out) {
+  constexpr int kJcBlocks = 2 * kJcCtas;
   extern __shared__ float jc[];  // [buf 2][slot 2][mat 2][bw][n]
   __shared__ float wmax[kJcThreads / 32];
   __shared__ float cl_max[kJcCtas];
@@ -127,9 +132,9 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
     return jc + ((size_t(buf * 2 + slot) * 2 + mat) * bw + k) * colsz;
   };
   auto off = [&](int buf, int slot, int mat, int k) -> int { return ((buf * 2 + slot) * 2 + mat) * bw * n + k * n; };
-  // initial blocks: slot 0 = position c, slot 1 = position 15 - c of round 0
+  // initial blocks: slot 0 = position c, slot 1 = position 2C - 1 - c of round 0
   for (int slot = 0; slot < 2; ++slot) {
-    const int blk = jc_block(0, slot == 0 ? c : kJcBlocks - 1 - c);
+    const int blk = jc_block(0, slot == 0 ? c : kJcBlocks - 1 - c, kJcBlocks);
     for (int idx = tid; idx < bw * n; idx += blockDim.x) {
       const int k = idx / n, r = idx - k * n;
       const int j = blk * bw + k;  // global column
@@ -164,8 +169,8 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
               q = (sr - k + (bwe - 1)) % (bwe - 1);
             }
             if (p < bw && q < bw)
-              mx = fmaxf(mx, jc_rotate(off(cur, slot, 0, p), off(cur, slot, 0, q), off(cur, slot, 1, p),
-                                       off(cur, slot, 1, q), n, lane));
+              mx = fmaxf(mx, jc_rotate<kJcRows>(off(cur, slot, 0, p), off(cur, slot, 0, q), off(cur, slot, 1, p),
+                                                 off(cur, slot, 1, q), n, lane));
           }
           __syncthreads();
         }
@@ -175,17 +180,18 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
       for (int sr = 0; sr < bw; ++sr) {
         if (warp < bw) {
           const int k = warp, k2 = (warp + sr) % bw;
-          mx = fmaxf(mx, jc_rotate(off(cur, 0, 0, k), off(cur, 1, 0, k2), off(cur, 0, 1, k), off(cur, 1, 1, k2), n,
-                                   lane));
+          mx = fmaxf(mx, jc_rotate<kJcRows>(off(cur, 0, 0, k), off(cur, 1, 0, k2), off(cur, 0, 1, k),
+                                             off(cur, 1, 1, k2), n, lane));
         }
         __syncthreads();
       }
       // move the blocks to their positions of the next round (after the last
-      // round of a sweep too: the 15 moves of a sweep bring every block back
-      // to its position of round 0)
+      // round of a sweep too: the kJcBlocks - 1 moves of a sweep bring every
+      // block back to its position of round 0)
       cluster.sync();
       const int nxt = cur ^ 1;
-      // new position p pulls from old position p - 1 (1 -> 15); position 0 stays
+      // new position p pulls from old position p - 1 (1 -> kJcBlocks - 1);
+      // position 0 stays
       for (int slot = 0; slot < 2; ++slot) {
         int src_cta, src_slot;
         if (slot == 0) {
@@ -240,11 +246,11 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
       break;
     }
   }
-  // after 15 rounds per sweep the blocks sit at round 15 == round 0 of the
-  // circle (the rotation period is 15): slot s of CTA c holds block
+  // after kJcBlocks - 1 rounds per sweep the blocks sit where round 0 put
+  // them (the rotation period): slot s of CTA c holds block
   // jc_block(0, position)
   for (int slot = 0; slot < 2; ++slot) {
-    const int blk = jc_block(0, slot == 0 ? c : kJcBlocks - 1 - c);
+    const int blk = jc_block(0, slot == 0 ? c : kJcBlocks - 1 - c, kJcBlocks);
     for (int idx = tid; idx < bw * n; idx += blockDim.x) {
       const int k = idx / n, r = idx - k * n;
       const int j = blk * bw + k;
@@ -256,29 +262,59 @@ __global__ void __launch_bounds__(kJcThreads) jacobi_cluster_kernel(int n, const
 
 }  // namespace
 
-int jacobi_cluster(int n, const double* M, int m_transposed, const double* W0, double* W, int* sweeps_out,
-                   cudaStream_t s) {
-  const int bw = (n + kJcBlocks - 1) / kJcBlocks;
-  if (bw > kJcMaxBw) return TVAP_ERR_ARG;
+namespace {
+
+template <int CT, int ROWS>
+int launch_jacobi_cluster(int n, const double* M, int m_transposed, const double* W0, double* W, int* sweeps_out,
+                          cudaStream_t s) {
+  const int bw = (n + 2 * CT - 1) / (2 * CT);
+  if (bw > kJcMaxBw || n > 32 * ROWS) return TVAP_ERR_ARG;
   const size_t shm = sizeof(float) * 8 * size_t(bw) * n;
   if (shm > size_t(200) * 1024) return TVAP_ERR_ARG;
+  auto kern = jacobi_cluster_kernel<CT, ROWS>;
   if (shm > 48 * 1024)
-    if (int rc = smem_opt_in((const void*)jacobi_cluster_kernel, shm)) return rc;
+    if (int rc = smem_opt_in((const void*)kern, shm)) return rc;
+  if (CT > 8) {
+    // a cluster of more than 8 CTAs is an opt-in size; refused or not
+    // schedulable here -> the caller takes another eigensolver
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      return TVAP_ERR_ARG;
+    }
+  }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kJcCtas);
+  cfg.gridDim = dim3(CT);
   cfg.blockDim = dim3(kJcThreads);
   cfg.dynamicSmemBytes = shm;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kJcCtas;
+  attr[0].val.clusterDim.x = CT;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (CT > 8) {
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)kern, &cfg) != cudaSuccess || clusters < 1) {
+      cudaGetLastError();
+      return TVAP_ERR_ARG;
+    }
+  }
   ++g_launch_count;
-  TVAP_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_kernel, n, M, m_transposed, W0, W, sweeps_out));
+  TVAP_CUDA(cudaLaunchKernelEx(&cfg, kern, n, M, m_transposed, W0, W, sweeps_out));
   return TVAP_OK;
+}
+
+}  // namespace
+
+// FP32 block one-sided Jacobi on a cluster: 8 CTAs (16 column blocks) up to
+// n = 256, 16 CTAs (32 column blocks, an opt-in cluster size) up to n = 384;
+// TVAP_ERR_ARG when neither fits (the caller then uses another eigensolver).
+int jacobi_cluster(int n, const double* M, int m_transposed, const double* W0, double* W, int* sweeps_out,
+                   cudaStream_t s) {
+  if (n <= 256) return launch_jacobi_cluster<8, 8>(n, M, m_transposed, W0, W, sweeps_out, s);
+  return launch_jacobi_cluster<16, 12>(n, M, m_transposed, W0, W, sweeps_out, s);
 }
 
 }  // namespace tvap

@@ -2300,7 +2300,9 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
   const int n = c->n;
   const size_t nn = size_t(n) * n;
   int rc, fail = 1;
-  if (jacobi32_smem_bytes(n) <= jacobi32_smem_limit() && n <= kCfMaxN) {
+  // the FP32 stage: the cluster Jacobi (n <= 384), else the single-CTA one
+  // when its matrices fit shared memory
+  if ((n <= 384 || jacobi32_smem_bytes(n) <= jacobi32_smem_limit()) && n <= kCfMaxN) {
     double* X = w->Xr;
     double* Xn = w->Xn;
     const View Rho = view_cm(w->rho, n, 0);
@@ -2322,6 +2324,10 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
         rc = jacobi_cluster(n, w->V, 1, nullptr, X, w->rflag + 1, s);
       }
       if (rc == TVAP_ERR_ARG) {
+        if (jacobi32_smem_bytes(n) > jacobi32_smem_limit()) {
+          fail = 1;  // neither FP32 stage runs here: the exact FP64 Jacobi below
+          break;
+        }
         if (warm) {
           const View Dp = view_cm(w->D, n, 0);
           if ((rc = real_gemm(n, n, n, Rho, Dp, w->Br, n, 1.0, 0.0, s))) return rc;
