@@ -218,6 +218,30 @@ int tvap_iterate(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_p
                  double mu, const double* Zim1, double* Zi, double* U1, double* V1, tvap_pnp* out, double* H20v,
                  double* gradient_norm);
 
+/* diagonalize_hsp_and_H11 with opt = 0 (src/module_gradient.f90:158-453):
+ * the eigenvalues (ascending) of h^RR - sum_m lambda_m C_m and of
+ * H11 - sum_m lambda_m C11_m for the state (U0, V0), where h and Delta are
+ * the fields of the real densities, H11 = U^T h U - V^T h^T V + (U^T Delta V
+ * + (U^T Delta V)^T) factor_delta (calculate_H11_real,
+ * src/module_fields.f90:327-354), C_m the cdim constraint operators
+ * constraint_HO (n*n reals each, the last cpair of them pair operators, whose
+ * C11 term is zero as in the reference) with multipliers lambda.  info[0],
+ * info[1] take the place of the DSYEV infos of the two (non-zero for a
+ * non-finite matrix).  Replaces the two DSYEV calls by an FP64 Householder
+ * reduction and Sturm multisection on the device; n <= 512. */
+int tvap_diagonalize_hsp_and_H11(tvap_ctx* ctx, const double* U0, const double* V0, int cdim, int cpair,
+                                 const double* lambda, const double* constraint_HO, double factor_delta,
+                                 double* eigen_hsp, double* eigen_H11, int* info);
+/* The step sizes of calculate_gradient (src/module_gradient.f90:86-119):
+ * gradient_type 0 returns eta_in, mu_in; 1 takes the H11 spectrum
+ * (eigen_max = 4 max|e|, eigen_min = 2 min|e|), 2 that of h (2 max|e|,
+ * 2 min|e|), with eta = (2 / (sqrt(eigen_max) + sqrt(eigen_min)))^2 and
+ * mu = ((sqrt(c) - 1) / (sqrt(c) + 1))^2, c = eigen_max / eigen_min; a failed
+ * diagonalisation (info) falls back to type 0, as in the reference.  Host
+ * arithmetic only. */
+int tvap_gradient_parameters(int gradient_type, int n, const double* eigen_hsp, const double* eigen_H11,
+                             const int* info, double eta_in, double mu_in, double* eta, double* mu);
+
 /* Test hook, no counterpart in the reference: the next tvap_evolve on this
  * context runs its cooperative launch with one CTA that leaves before the
  * first grid-wide barrier, so that the other CTAs' bounded waits there run
@@ -263,7 +287,9 @@ int tvap_zskpfa_batched(tvap_ctx* ctx, int batch, int64_t n, const double* A, do
  * beta.  The bound is relative to the largest entries of the row and the
  * column, not to each term: an entry of C much smaller than K a_i b_j keeps
  * fewer correct digits than a FP64 product (error <= ~2^-53 K sum_k |A_ik
- * B_kj|) gives it.  Mode 0 runs on the FP64 pipe.  Replaces the BLAS calls
+ * B_kj|) gives it.  The emulated modes do not carry NaN or infinity
+ * through: a non-finite operand gives undefined results.  Mode 0 runs on the
+ * FP64 pipe.  Replaces the BLAS calls
  * of the reference (not a reference routine of
  * its own). */
 int tvap_zgemm(tvap_ctx* ctx, char transa, char transb, int m, int n, int k, const double* alpha, const double* A,

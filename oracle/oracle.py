@@ -89,6 +89,9 @@ def lib():
         L.orc_vap_get_multipliers.argtypes = [vp, vp]
         L.orc_thouless_evolve.argtypes = [vp, vp, vp, ci, vp, vp]
         L.orc_thouless_evolve.restype = ci
+        L.orc_vap_get_step.argtypes = [vp] * 5
+        L.orc_diagonalize_hsp_and_H11.argtypes = [vp, vp, vp, ci, ci, ci, vp, vp, cd, vp, vp, vp, ci]
+        L.orc_diagonalize_hsp_and_H11.restype = ci
         _lib = L
     return _lib
 
@@ -201,7 +204,7 @@ class OracleVAP:
     """The reference's gradient loop (taurus_vap.f90:77-123), gradient_type 0."""
 
     def __init__(self, omodel: OracleModel, U, V, Mp, Mn, facpi, Z, N, eta, mu, geps, constraints_HO,
-                 constraint_vals, ceps=1e-6, cpair=0, factor_delta=1.0, nthreads=0):
+                 constraint_vals, ceps=1e-6, cpair=0, factor_delta=1.0, nthreads=0, gradient_type=0):
         n = omodel.n
         self.om = omodel
         self.n = n
@@ -210,7 +213,8 @@ class OracleVAP:
         cval = np.ascontiguousarray(np.asarray(constraint_vals, dtype=np.float64).reshape(-1))
         self.cdim = cval.size
         self._keep = [U, V, cHO, cval]
-        self.h = lib().orc_vap_new(omodel.h, _p(U), _p(V), Mp, Mn, facpi, Z, N, 0, eta, mu, geps, self.cdim, cpair,
+        self.h = lib().orc_vap_new(omodel.h, _p(U), _p(V), Mp, Mn, facpi, Z, N, gradient_type, eta, mu, geps,
+                                   self.cdim, cpair,
                                    _p(cHO) if cHO.size else None, _p(cval) if cval.size else None, ceps,
                                    factor_delta, nthreads)
 
@@ -227,6 +231,17 @@ class OracleVAP:
         st = lib().orc_vap_iterate(self.h, _p(info))
         return st, info
 
+    def step(self):
+        """Eigenvalues of h^RR and H11, their DSYEV infos and the (eta, mu) of
+        the last iteration."""
+        n = self.n
+        eh = np.zeros(n)
+        e11 = np.zeros(n)
+        infos = np.zeros(2, dtype=np.int32)
+        em = np.zeros(2)
+        lib().orc_vap_get_step(self.h, _p(eh), _p(e11), _p(infos), _p(em))
+        return eh, e11, (int(infos[0]), int(infos[1])), (float(em[0]), float(em[1]))
+
     def state(self):
         n = self.n
         U = np.zeros((n, n), order="F")
@@ -235,3 +250,23 @@ class OracleVAP:
         H = np.zeros(n * n)
         lib().orc_vap_get_state(self.h, _p(U), _p(V), _p(Zi), _p(H))
         return U, V, Zi, H
+
+
+def diagonalize_hsp_and_H11(om: OracleModel, U, V, lam=(), constraints_HO=None, cpair=0, factor_delta=1.0, Mphip=2,
+                            nthreads=0):
+    """diagonalize_hsp_and_H11(0) (module_gradient.f90:158-453): eigenvalues
+    of h^RR and of H11 for the state (U, V), with the constraint terms of the
+    multipliers lam; Mphip = 1 takes the fields of the phi = 0 transition
+    densities, as the reference does without projection.  Returns
+    (eigen_hsp, eigen_H11, (info_hsp, info_H11))."""
+    n = om.n
+    U, V = _cf(U, np.float64), _cf(V, np.float64)
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    cdim = lam.size
+    cHO = np.ascontiguousarray(np.zeros(1) if cdim == 0 else np.asarray(constraints_HO, dtype=np.float64).reshape(-1))
+    eh = np.zeros(n)
+    e11 = np.zeros(n)
+    infos = np.zeros(2, dtype=np.int32)
+    lib().orc_diagonalize_hsp_and_H11(om.h, _p(U), _p(V), Mphip, cdim, cpair, _p(lam) if cdim else None, _p(cHO),
+                                      factor_delta, _p(eh), _p(e11), _p(infos), nthreads)
+    return eh, e11, (int(infos[0]), int(infos[1]))

@@ -706,6 +706,10 @@ struct orc_vap {
   double ceps = 1e-6;
   std::vector<double> cHO, cval, c20, lam0, lam1;
   std::vector<double> Zi, Zim1, H20v, Lchol;
+  // diagonalize_hsp_and_H11 (gradient types 1 and 2)
+  std::vector<double> eig_hsp, eig_H11;
+  int info_hsp = 0, info_H11 = 0;
+  double eta_used = 0.0, mu_used = 0.0;
   double gnorm = 0.0;
   PNP pnp;
   std::vector<cplx> pnpA, pnpH20, pnpAH20;
@@ -1140,11 +1144,108 @@ static int adjust_constraints(orc_vap* s) {
   return 0;
 }
 
-// calculate_gradient type 0 (module_gradient.f90:79-143)
+int orc_angle_densities(const orc_model* m, const double* U0, const double* V0, double php, double phn, double* rho,
+                        double* kLR, double* kRL, double* Aphi);
+
+// diagonalize_hsp_and_H11 with opt = 0 (module_gradient.f90:158-453): the
+// eigenvalues of h^RR and of H11 that calculate_gradient's types 1 and 2
+// read.  The fields: for M = 1 those of the projection's single angle
+// phi = 0 (max(proj_Mphip, proj_Mphip) == 1, :177-179), else those of the
+// real densities rho^RR, kappa^RR (calculate_fields_diag, :181-185).  H11
+// (calculate_H11_real, module_fields.f90:327-354) = U^T h U - V^T h^T V +
+// (U^T Delta V + (U^T Delta V)^T) factor_delta; the constraint terms
+// lambda_m f11(C_m) (non-pair constraints only: the pair ones keep
+// constraint_11 = 0) and lambda_m C_m are subtracted (:189-218); DSYEV of both
+// (:297, :416).
+static void diagonalize_hsp_and_H11(orc_vap* s) {
+  const int n = s->n;
+  const size_t n2 = size_t(n) * n;
+  std::vector<cplx> rho(n2), kap(n2), kRL(n2), gam(n2), hsp(n2), dLR(n2);
+  if (s->Mp == 1) {
+    orc_angle_densities(s->m, s->U0.data(), s->V0.data(), 0.0, 0.0, reinterpret_cast<double*>(rho.data()),
+                        reinterpret_cast<double*>(kap.data()), reinterpret_cast<double*>(kRL.data()), nullptr);
+  } else {
+    for (size_t i = 0; i < n2; ++i) {
+      rho[i] = s->rhoRR[i] * zone;
+      kap[i] = s->kapRR[i] * zone;
+    }
+  }
+  calculate_fields_diag(s->m, rho.data(), kap.data(), gam.data(), hsp.data(), dLR.data(), nullptr, s->nthreads);
+  std::vector<double> h(n2), d(n2), A1(n2), A2(n2), A3(n2), A4(n2), H11(n2);
+  for (size_t i = 0; i < n2; ++i) {
+    h[i] = hsp[i].real();
+    d[i] = dLR[i].real();  // real(Delta^RL) = real(conj(Delta^LR))
+  }
+  const double* U = s->U0.data();
+  const double* V = s->V0.data();
+  dgemm('t', 'n', n, n, n, 1.0, U, n, h.data(), n, 0.0, A1.data(), n);
+  dgemm('n', 'n', n, n, n, 1.0, A1.data(), n, U, n, 0.0, A2.data(), n);
+  dgemm('t', 't', n, n, n, 1.0, V, n, h.data(), n, 0.0, A1.data(), n);
+  dgemm('n', 'n', n, n, n, 1.0, A1.data(), n, V, n, 0.0, A3.data(), n);
+  dgemm('t', 'n', n, n, n, 1.0, U, n, d.data(), n, 0.0, A1.data(), n);
+  dgemm('n', 'n', n, n, n, 1.0, A1.data(), n, V, n, 0.0, A4.data(), n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      const size_t ij = i + size_t(j) * n, ji = j + size_t(i) * n;
+      H11[ij] = A2[ij] - A3[ij] + (A4[ij] + A4[ji]) * s->factor_delta;
+    }
+  std::vector<double> c11(n2);
+  for (int m = 0; m < s->cdim; ++m) {
+    const double* cHO = s->cHO.data() + m * n2;
+    if (m < s->cdim - s->cpair) {
+      set_operator_qpbasis("f11", U, V, cHO, c11.data(), n);
+      for (size_t i = 0; i < n2; ++i) H11[i] -= s->lam1[m] * c11[i];
+    }
+    for (size_t i = 0; i < n2; ++i) h[i] -= s->lam1[m] * cHO[i];
+  }
+  s->eig_hsp.assign(n, 0.0);
+  s->eig_H11.assign(n, 0.0);
+  char jv = 'V', up = 'U';
+  int nn_ = n, lwork = 3 * n - 1, info = 0;
+  std::vector<double> work(lwork);
+  p_dsyev(&jv, &up, &nn_, h.data(), &nn_, s->eig_hsp.data(), work.data(), &lwork, &info);
+  s->info_hsp = info;
+  info = 0;
+  p_dsyev(&jv, &up, &nn_, H11.data(), &nn_, s->eig_H11.data(), work.data(), &lwork, &info);
+  s->info_H11 = info;
+}
+
+// the step sizes of calculate_gradient (module_gradient.f90:86-119): type 0
+// the input eta and mu; type 1 from the H11 eigenvalues, type 2 from those
+// of h^RR (heavy ball with approximate optimal parameters); a failed
+// diagonalisation falls back to type 0
+static void gradient_parameters(int type, const double* eig_hsp, const double* eig_H11, int info_hsp, int info_H11,
+                                int n, double eta_in, double mu_in, double& eta, double& mu) {
+  int opt = type;
+  if (info_H11 != 0 && type == 1) opt = 0;
+  if (info_hsp != 0 && type == 2) opt = 0;
+  eta = eta_in;
+  mu = mu_in;
+  if (opt == 0) return;
+  const double* e = (opt == 1) ? eig_H11 : eig_hsp;
+  double amax = 0.0, amin = 1.0e300;
+  for (int i = 0; i < n; ++i) {
+    amax = std::max(amax, std::fabs(e[i]));
+    amin = std::min(amin, std::fabs(e[i]));
+  }
+  const double emax = (opt == 1 ? 4.0 : 2.0) * amax, emin = 2.0 * amin;
+  const double cond = emax / emin;
+  const double t = 2.0 / (std::sqrt(emax) + std::sqrt(emin));
+  const double r = (std::sqrt(cond) - 1.0) / (std::sqrt(cond) + 1.0);
+  eta = t * t;
+  mu = r * r;
+}
+
+// calculate_gradient (module_gradient.f90:79-143)
 static void calculate_gradient(orc_vap* s) {
   const int n = s->n;
   const size_t n2 = size_t(n) * n;
-  const double eta = s->eta, mu = s->mu;
+  double eta = s->eta, mu = s->mu;
+  if (s->gtype > 0)
+    gradient_parameters(s->gtype, s->eig_hsp.data(), s->eig_H11.data(), s->info_hsp, s->info_H11, n, s->eta, s->mu,
+                        eta, mu);
+  s->eta_used = eta;
+  s->mu_used = mu;
   for (size_t i = 0; i < n2; ++i) {
     double sg = 0.0;
     for (int j = 0; j < s->cdim; ++j) sg += s->lam1[j] * s->c20[j * n2 + i];
@@ -1201,7 +1302,7 @@ void orc_vap_free(orc_vap* s) { delete s; }
 // The first adjust_constraints call before the loop (taurus_vap.f90:62-66).
 int orc_vap_initial_adjust(orc_vap* s) { return adjust_constraints(s); }
 
-// One gradient iteration (taurus_vap.f90:77-123) with gradient_type 0.
+// One gradient iteration (taurus_vap.f90:77-123) with gradient_type 0, 1 or 2.
 // Returns 0 (continue), 1 (converged), 2 (particle numbers wrong three times
 // in the last five iterations: the reference stops), or an error code.
 int orc_vap_iterate(orc_vap* s, double* info /* [gnorm, E, Z, varZ, N, varN] */) {
@@ -1214,6 +1315,7 @@ int orc_vap_iterate(orc_vap* s, double* info /* [gnorm, E, Z, varZ, N, varN] */)
                        s->occeps, s->allemp, &o, s->H20v.data(), nullptr, nullptr, nullptr, nullptr, s->nthreads);
   if (st) return 100 + st;
   calculate_lagrange_multipliers(s);
+  if (s->gtype > 0) diagonalize_hsp_and_H11(s);
   calculate_gradient(s);
   const cplx over(o.over[0], o.over[1]);
   const double ener = (cplx(o.ener[0], o.ener[1]) / over).real();
@@ -1251,6 +1353,50 @@ void orc_vap_get_state(const orc_vap* s, double* U, double* V, double* Zi, doubl
 
 void orc_vap_get_multipliers(const orc_vap* s, double* lam) {
   for (int i = 0; i < s->cdim; ++i) lam[i] = s->lam1[i];
+}
+
+// The eigenvalues of h^RR and H11, their DSYEV infos and the step sizes
+// (eta, mu) of the last iteration (gradient types 1 and 2).
+void orc_vap_get_step(const orc_vap* s, double* eig_hsp, double* eig_H11, int* infos, double* eta_mu) {
+  for (int i = 0; i < s->n && !s->eig_hsp.empty(); ++i) {
+    eig_hsp[i] = s->eig_hsp[i];
+    eig_H11[i] = s->eig_H11[i];
+  }
+  infos[0] = s->info_hsp;
+  infos[1] = s->info_H11;
+  eta_mu[0] = s->eta_used;
+  eta_mu[1] = s->mu_used;
+}
+
+// diagonalize_hsp_and_H11(0) for a state (U, V) of a projection with
+// Mp angles per proton, with multipliers lam of the constraints cHO (cdim
+// operators, the last cpair of them pair operators).
+int orc_diagonalize_hsp_and_H11(const orc_model* m, const double* U, const double* V, int Mp, int cdim, int cpair,
+                                const double* lam, const double* cHO, double factor_delta, double* eig_hsp,
+                                double* eig_H11, int* infos, int nthreads) {
+  orc_vap s;
+  const int n = m->n;
+  const size_t n2 = size_t(n) * n;
+  s.m = m;
+  s.n = n;
+  s.Mp = Mp;
+  s.U0.assign(U, U + n2);
+  s.V0.assign(V, V + n2);
+  s.rhoRR.assign(n2, 0.0);
+  s.kapRR.assign(n2, 0.0);
+  densities_real(U, V, s.rhoRR.data(), s.kapRR.data(), n);
+  s.cdim = cdim;
+  s.cpair = cpair;
+  s.cHO.assign(cHO, cHO + size_t(cdim) * n2);
+  s.lam1.assign(lam, lam + cdim);
+  s.factor_delta = factor_delta;
+  s.nthreads = nthreads;
+  diagonalize_hsp_and_H11(&s);
+  std::copy(s.eig_hsp.begin(), s.eig_hsp.end(), eig_hsp);
+  std::copy(s.eig_H11.begin(), s.eig_H11.end(), eig_H11);
+  infos[0] = s.info_hsp;
+  infos[1] = s.info_H11;
+  return 0;
 }
 
 // Thouless map Z -> (U1, V1) of a state (cholesky_factorization +

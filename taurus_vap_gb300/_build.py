@@ -33,6 +33,7 @@ GPU_SOURCES = [
     "jacobi_cluster.cu",
     "field_blocks.cu",
     "linalg_abi.cu",
+    "diag_hsp_h11.cu",
 ]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -2839,6 +2839,12 @@ int ensure_workspace(tvap_ctx* c, int G) { return ws_ensure(c, G); }
 double* ws_U(tvap_ctx* c) { return c->ws->U; }
 double* ws_V(tvap_ctx* c) { return c->ws->V; }
 double* ws_H20v(tvap_ctx* c) { return c->ws->H20v; }
+// one real product C = alpha op(A) op(B) + beta C in the calling thread's
+// arithmetic (for the other translation units)
+int real_product(int M, int N, int K, View A, View B, double* C, int ldc, double alpha, double beta,
+                 cudaStream_t s) {
+  return real_gemm(M, N, K, A, B, C, ldc, alpha, beta, s);
+}
 // the six projected sums (over, ener, prot, neut, prot2, neut2), then two
 // free complex slots
 double2* ws_sums(tvap_ctx* c) { return c->ws->pscal; }

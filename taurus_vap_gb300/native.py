@@ -105,6 +105,10 @@ def lib():
         L.tvap_iterate.argtypes = [vp, vp, vp, ctypes.POINTER(TvapProjOpts), cd, cd, vp, vp, vp, vp,
                                    ctypes.POINTER(TvapPnp), vp, vp]
         L.tvap_iterate.restype = ci
+        L.tvap_diagonalize_hsp_and_H11.argtypes = [vp, vp, vp, ci, ci, vp, vp, cd, vp, vp, vp]
+        L.tvap_diagonalize_hsp_and_H11.restype = ci
+        L.tvap_gradient_parameters.argtypes = [ci, ci, vp, vp, vp, cd, cd, vp, vp]
+        L.tvap_gradient_parameters.restype = ci
         L.tvap_test_wait_timeout.argtypes = [vp]
         L.tvap_test_wait_timeout.restype = ci
         L.tvap_zskpfa_batched.argtypes = [vp, ci, ctypes.c_int64, vp, vp]
@@ -286,6 +290,22 @@ class Context:
         _check(lib().tvap_evolve(self.h, _p(U), _p(V), _p(Zm), _p(U1), _p(V1)), "tvap_evolve")
         return U1, V1
 
+    # -- diagonalize_hsp_and_H11(0) (module_gradient.f90:158-453) -------------
+    def diagonalize_hsp_and_H11(self, U0, V0, lambdas=None, constraints_HO=None, cpair=0, factor_delta=1.0):
+        """Eigenvalues of h^RR and H11 (with the constraint terms of the
+        multipliers): (eigen_hsp, eigen_H11, (info_hsp, info_H11))."""
+        n = self.n
+        U, V = _f(U0, np.float64), _f(V0, np.float64)
+        cdim = 0 if lambdas is None else len(lambdas)
+        lam = None if cdim == 0 else np.ascontiguousarray(lambdas, dtype=np.float64)
+        C = None if cdim == 0 else np.ascontiguousarray(constraints_HO, dtype=np.float64).reshape(-1)
+        eh = np.zeros(n)
+        e11 = np.zeros(n)
+        info = np.zeros(2, dtype=np.int32)
+        _check(lib().tvap_diagonalize_hsp_and_H11(self.h, _p(U), _p(V), cdim, cpair, _p(lam), _p(C), factor_delta,
+                                                  _p(eh), _p(e11), _p(info)), "tvap_diagonalize_hsp_and_H11")
+        return eh, e11, (int(info[0]), int(info[1]))
+
     # -- one gradient iteration (taurus_vap.f90:86-113), gradient_type 0 -------
     def iterate(self, U0, V0, Zim1, Mphip, Mphin, facpi, valence_Z, valence_N, eta, mu, factor_delta=1.0,
                 seed_occeps=0.0, seed_allemp=0, want_H20v=False):
@@ -357,3 +377,16 @@ class Context:
 
 
 TWO_PI = 2.0 * math.pi
+
+
+def gradient_parameters(gradient_type, eigen_hsp, eigen_H11, info, eta_in, mu_in):
+    """(eta, mu) of calculate_gradient (module_gradient.f90:86-119) for
+    gradient_type 0, 1 or 2 (tvap_gradient_parameters)."""
+    eh = np.ascontiguousarray(eigen_hsp, dtype=np.float64)
+    e11 = np.ascontiguousarray(eigen_H11, dtype=np.float64)
+    inf = np.ascontiguousarray(info, dtype=np.int32)
+    eta = ctypes.c_double()
+    mu = ctypes.c_double()
+    _check(lib().tvap_gradient_parameters(int(gradient_type), eh.size, _p(eh), _p(e11), _p(inf), eta_in, mu_in,
+                                          ctypes.byref(eta), ctypes.byref(mu)), "tvap_gradient_parameters")
+    return eta.value, mu.value

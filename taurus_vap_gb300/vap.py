@@ -15,7 +15,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .native import Context, TvapError
+from .native import Context, TvapError, gradient_parameters
 
 
 def set_operator_qpbasis(part: str, U, V, A):
@@ -63,7 +63,8 @@ class VAP:
     """State and loop of one PNVAP minimisation."""
 
     def __init__(self, ctx: Context, U0, V0, Mphip, Mphin, valence_Z, valence_N, eta, mu, gradient_eps=1e-4,
-                 constraints: Constraints | None = None, facpi=2 * np.pi, factor_delta=1.0, mode=0):
+                 constraints: Constraints | None = None, facpi=2 * np.pi, factor_delta=1.0, mode=0,
+                 gradient_type=0):
         self.ctx = ctx
         self.n = ctx.n
         self.U0 = np.asfortranarray(U0, dtype=np.float64)
@@ -74,6 +75,8 @@ class VAP:
         self.cons = constraints or Constraints()
         self.factor_delta = factor_delta
         self.mode = mode
+        self.gradient_type = gradient_type
+        self.step_sizes = (eta, mu)
         n = self.n
         self.Zi = np.zeros(n * n)
         self.Zim1 = np.zeros(n * n)
@@ -132,9 +135,18 @@ class VAP:
         pnp, H20v = self.ctx.project(self.U0, self.V0, self.Mp, self.Mn, self.facpi, self.Z, self.N,
                                      self.factor_delta, mode=self.mode)
         self.lagrange_multipliers(H20v)
+        eta, mu = self.eta, self.mu
+        if self.gradient_type > 0:
+            # diagonalize_hsp_and_H11(0), then the step sizes of
+            # calculate_gradient (taurus_vap.f90:93; module_gradient.f90:86-119)
+            c = self.cons.dim
+            eh, e11, info = self.ctx.diagonalize_hsp_and_H11(
+                self.U0, self.V0, self.lam1 if c else None, np.stack(self.cons.ops) if c else None,
+                cpair=self.cons.npair, factor_delta=self.factor_delta)
+            eta, mu = gradient_parameters(self.gradient_type, eh, e11, info, self.eta, self.mu)
+        self.step_sizes = (eta, mu)
         self.Zi, gnorm = self.ctx.calculate_gradient(H20v, self.lam1 if self.cons.dim else None,
-                                                     self.C20 if self.cons.dim else None, self.Zim1, self.eta,
-                                                     self.mu)
+                                                     self.C20 if self.cons.dim else None, self.Zim1, eta, mu)
         over = pnp.c("over")
         ener = (pnp.c("ener") / over).real
         prot = (pnp.c("prot") / over).real

@@ -9,10 +9,11 @@ from conftest import golden_table
 import oracle as O
 
 
-def run_oracle(model, U, V, cons, M, eta, mu, iters=3000):
+def run_oracle(model, U, V, cons, M, eta, mu, iters=3000, gradient_type=0):
     om = O.OracleModel(model)
     ops, vals = cons
-    vap = O.OracleVAP(om, U, V, M, M, 2 * np.pi, 4.0, 4.0, eta, mu, 1e-4, np.stack(ops), np.array(vals), nthreads=1)
+    vap = O.OracleVAP(om, U, V, M, M, 2 * np.pi, 4.0, 4.0, eta, mu, 1e-4, np.stack(ops), np.array(vals), nthreads=1,
+                      gradient_type=gradient_type)
     assert vap.initial_adjust() == 0
     for it in range(1, iters + 1):
         st, info = vap.iterate()
@@ -38,6 +39,46 @@ def test_mg24_hfb(usdb_model, mg24_seed, mg24_constraints, eta, mu):
     it, info = run_oracle(usdb_model, *mg24_seed, mg24_constraints, 1, eta, mu)
     assert abs(info[1] - e_ref) < 1e-6
     assert it == it_ref
+
+
+def recipe_rows(name):
+    """The 'Recipe k: Iter = i Ener = e' lines: the automatic step sizes of
+    gradient_type k (examples/gradient_mg24/launch_example.sh runs them with
+    eta = mu = 0)."""
+    import os
+
+    from conftest import GOLDEN
+
+    rows = {}
+    for line in open(os.path.join(GOLDEN, name)):
+        w = line.split()
+        if len(w) >= 8 and w[0] == "Recipe":
+            rows[int(w[1].rstrip(":"))] = (int(w[4]), float(w[7]))
+    return rows
+
+
+@pytest.mark.parametrize("recipe", [1, 2])
+def test_mg24_pnvap_m5_gradient_types(usdb_model, mg24_seed, mg24_constraints, recipe):
+    # diagonalize_hsp_and_H11 + calculate_gradient types 1 and 2: the
+    # reference's iteration counts and energies, exactly
+    it_ref, e_ref = recipe_rows("mg24_results_vap_benchmark")[recipe]
+    it, info = run_oracle(usdb_model, *mg24_seed, mg24_constraints, 5, 0.0, 0.0, gradient_type=recipe)
+    assert abs(info[1] - e_ref) < 1e-6
+    assert it == it_ref
+
+
+@pytest.mark.parametrize("recipe", [1, 2])
+def test_mg24_hfb_gradient_types(usdb_model, mg24_seed, mg24_constraints, recipe):
+    # HFB (M = 1): the energies exactly; the iteration count within two of the
+    # table's.  These runs react to rounding: with the step sizes recomputed
+    # from the spectra every iteration, taking the fields of the real
+    # densities instead of those of the phi = 0 transition densities (equal to
+    # 1e-15) moves the count by one, so the reference's own LAPACK rounding is
+    # not reproducible to the iteration here
+    it_ref, e_ref = recipe_rows("mg24_results_hfb_benchmark")[recipe]
+    it, info = run_oracle(usdb_model, *mg24_seed, mg24_constraints, 1, 0.0, 0.0, gradient_type=recipe)
+    assert abs(info[1] - e_ref) < 1e-6
+    assert abs(it - it_ref) <= 2
 
 
 def minima_table():

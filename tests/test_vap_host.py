@@ -45,6 +45,10 @@ class OracleBackedContext:
         assert st == 0, st
         return U1, V1
 
+    def diagonalize_hsp_and_H11(self, U0, V0, lambdas=None, constraints_HO=None, cpair=0, factor_delta=1.0):
+        return O.diagonalize_hsp_and_H11(self.om, U0, V0, () if lambdas is None else lambdas, constraints_HO,
+                                         cpair=cpair, factor_delta=factor_delta, nthreads=1)
+
 
 @pytest.mark.parametrize("M,table,eta,mu", [(5, "mg24_results_vap_benchmark", 0.05, 0.6),
                                             (1, "mg24_results_hfb_benchmark", 0.025, 0.6)])
@@ -53,6 +57,22 @@ def test_host_loop_reproduces_mg24(usdb_model, mg24_seed, mg24_constraints, M, t
     ops, vals = mg24_constraints
     vap = VAP(OracleBackedContext(usdb_model), *mg24_seed, M, M, 4.0, 4.0, eta, mu,
               constraints=Constraints(ops, vals))
+    it, info = vap.run(iter_max=3000)
+    assert abs(info[1] - e_ref) < 1e-6
+    assert it == it_ref
+
+
+@pytest.mark.parametrize("recipe", [1, 2])
+def test_host_loop_gradient_types(usdb_model, mg24_seed, mg24_constraints, recipe):
+    # vap.VAP with gradient_type 1 / 2: the spectra from the context, the step
+    # sizes from tvap_gradient_parameters (host arithmetic of the library);
+    # the reference's PNVAP recipe rows (M = 5)
+    from test_oracle_golden import recipe_rows
+
+    it_ref, e_ref = recipe_rows("mg24_results_vap_benchmark")[recipe]
+    ops, vals = mg24_constraints
+    vap = VAP(OracleBackedContext(usdb_model), *mg24_seed, 5, 5, 4.0, 4.0, 0.0, 0.0,
+              constraints=Constraints(ops, vals), gradient_type=recipe)
     it, info = vap.run(iter_max=3000)
     assert abs(info[1] - e_ref) < 1e-6
     assert it == it_ref
