@@ -242,6 +242,20 @@ int tvap_diagonalize_hsp_and_H11(tvap_ctx* ctx, const double* U0, const double* 
 int tvap_gradient_parameters(int gradient_type, int n, const double* eigen_hsp, const double* eigen_H11,
                              const int* info, double eta_in, double mu_in, double* eta, double* mu);
 
+/* adjust_constraints (src/module_constraints.f90:270-373): up to 100 Newton
+ * steps that move the Thouless step Zi (n*n reals, updated in place) until
+ * the constraint expectation values of (U1, V1) = evolve(U0, V0, Zi) reach
+ * `values` within eps: Tr(C_m rho) for the first cdim - cpair operators of
+ * constraint_HO, Tr(C_m kappa^T) for the last cpair (pair operators), with
+ * the update Zi += sum_m x_m C20_m, A x = values - <C>, A_ij =
+ * Tr(C20_i^T C20_j) and C20_m the 20 part of C_m at (U1, V1) (f20 / g20 of
+ * set_operator_qpbasis).  Writes U1, V1, C20 (cdim n*n reals, may be NULL)
+ * of the last step and the number of steps; cdim = 0 is one evolution.  All
+ * but the cdim x cdim solve runs on the device; cdim <= 64. */
+int tvap_adjust_constraints(tvap_ctx* ctx, const double* U0, const double* V0, double* Zi, int cdim, int cpair,
+                            const double* constraint_HO, const double* values, double eps, double* U1, double* V1,
+                            double* C20, int* iterations);
+
 /* Test hook, no counterpart in the reference: the next tvap_evolve on this
  * context runs its cooperative launch with one CTA that leaves before the
  * first grid-wide barrier, so that the other CTAs' bounded waits there run

@@ -34,6 +34,7 @@ GPU_SOURCES = [
     "field_blocks.cu",
     "linalg_abi.cu",
     "diag_hsp_h11.cu",
+    "constraints.cu",
 ]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -156,6 +156,24 @@ int evolve_device(tvap_ctx* c, EvolveBuf& b, int n, double* U1, double* V1, bool
 
 }  // namespace
 
+// The Thouless evolution of a device state for the other translation units:
+// U1 = (U0 + V0 Z) L^-T, V1 = (V0 + U0 Z) L^-T, every matrix on the device;
+// work holds 3 n^2 + n doubles.  Runs on the context's stream in the calling
+// thread's arithmetic.
+int evolve_state(tvap_ctx* c, const double* U0, const double* V0, const double* Z, double* U1, double* V1,
+                 double* work) {
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  EvolveBuf b;
+  b.Z = const_cast<double*>(Z);
+  b.U0 = const_cast<double*>(U0);
+  b.V0 = const_cast<double*>(V0);
+  b.A1 = work;
+  b.A2 = work + nn;
+  b.L = work + 2 * nn;
+  return evolve_device(c, b, n, U1, V1, false);
+}
+
 double* ws_U(tvap_ctx* c);
 double* ws_V(tvap_ctx* c);
 double* ws_H20v(tvap_ctx* c);

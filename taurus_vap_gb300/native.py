@@ -109,6 +109,8 @@ def lib():
         L.tvap_diagonalize_hsp_and_H11.restype = ci
         L.tvap_gradient_parameters.argtypes = [ci, ci, vp, vp, vp, cd, cd, vp, vp]
         L.tvap_gradient_parameters.restype = ci
+        L.tvap_adjust_constraints.argtypes = [vp, vp, vp, vp, ci, ci, vp, vp, cd, vp, vp, vp, vp]
+        L.tvap_adjust_constraints.restype = ci
         L.tvap_test_wait_timeout.argtypes = [vp]
         L.tvap_test_wait_timeout.restype = ci
         L.tvap_zskpfa_batched.argtypes = [vp, ci, ctypes.c_int64, vp, vp]
@@ -289,6 +291,24 @@ class Context:
         V1 = np.zeros((n, n), order="F")
         _check(lib().tvap_evolve(self.h, _p(U), _p(V), _p(Zm), _p(U1), _p(V1)), "tvap_evolve")
         return U1, V1
+
+    # -- adjust_constraints (module_constraints.f90:270-373) -------------------
+    def adjust_constraints(self, U0, V0, Zi, constraints_HO, values, cpair=0, eps=1e-6):
+        """The constraint Newton loop on the device: returns (U1, V1, Zi, C20,
+        steps) with Zi the adjusted step."""
+        n = self.n
+        U, V = _f(U0, np.float64), _f(V0, np.float64)
+        Z = np.array(np.reshape(Zi, -1), dtype=np.float64)
+        cdim = len(values)
+        C = None if cdim == 0 else np.ascontiguousarray(constraints_HO, dtype=np.float64).reshape(-1)
+        vals = None if cdim == 0 else np.ascontiguousarray(values, dtype=np.float64)
+        U1 = np.zeros((n, n), order="F")
+        V1 = np.zeros((n, n), order="F")
+        C20 = np.zeros((max(cdim, 1), n * n))
+        it = ctypes.c_int()
+        _check(lib().tvap_adjust_constraints(self.h, _p(U), _p(V), _p(Z), cdim, cpair, _p(C), _p(vals), eps, _p(U1),
+                                             _p(V1), _p(C20), ctypes.byref(it)), "tvap_adjust_constraints")
+        return U1, V1, Z, C20[:cdim], it.value
 
     # -- diagonalize_hsp_and_H11(0) (module_gradient.f90:158-453) -------------
     def diagonalize_hsp_and_H11(self, U0, V0, lambdas=None, constraints_HO=None, cpair=0, factor_delta=1.0):

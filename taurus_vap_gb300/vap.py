@@ -109,8 +109,19 @@ class VAP:
         self.lam0 = self.lam1.copy()
 
     def adjust_constraints(self):
-        """module_constraints.f90:270-373; the Thouless evolution runs on the device."""
+        """module_constraints.f90:270-373.  On a device context the whole
+        Newton loop runs there (tvap_adjust_constraints); otherwise the loop
+        runs here around the context's evolution."""
         c = self.cons.dim
+        if hasattr(self.ctx, "adjust_constraints"):
+            U1, V1, Zi, C20, _ = self.ctx.adjust_constraints(
+                self.U0, self.V0, self.Zi, np.stack(self.cons.ops) if c else None, list(self.cons.values),
+                cpair=self.cons.npair, eps=self.cons.eps)
+            self.Zi = Zi
+            if c:
+                self.C20 = C20
+            self.U0, self.V0 = np.asfortranarray(U1), np.asfortranarray(V1)
+            return
         U1, V1 = self.U0, self.V0
         for _ in range(100):
             U1, V1 = self.ctx.evolve(self.U0, self.V0, self.Zi)
