@@ -412,6 +412,10 @@ def run_ours(args):
     emax6 = None
     if rank == 0 and not args.no_emax6:
         emax6 = emax6_leg(torch, peaks, hbm_peak)
+    seeds = sweep = None
+    if rank == 0 and not args.no_multi:
+        seeds = seeds_leg(args)
+        sweep = sweep_leg(args)
 
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
@@ -428,7 +432,7 @@ def run_ours(args):
         "timeline_ms": {k: [round(a, 3), round(b, 3)] for k, (a, b) in timeline.items() if sections[k][1]},
         "longest_section": longest[0], "canonical_paths": canon_paths, "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
         "final_energy": it.energy, "iterations_from_seed": args.warmup + args.steps,
-        "adjoint": adjoint, "parity": parity, "emax6": emax6,
+        "adjoint": adjoint, "parity": parity, "emax6": emax6, "many_seeds": seeds, "constraint_sweep": sweep,
     }
     if rank == 0:
         print(json.dumps(out))
@@ -506,6 +510,192 @@ def device_parity(ctx, U, V, torch, oracle_energies):
             "E_final_oracle": oracle_energies[-1], "bound": 1e-6, "unit": "MeV",
             "what": "projected energy of each iterated state, device loop against the oracle's loop from the "
                     "workload's seed (same eta, mu, 15x15 angles)"}
+
+
+def seeds_leg(args, steps=3, sd_workers=8, e4_workers=4, parity_iters=3):
+    """Many independent seeds (a minima search): 64 random real Bogoliubov
+    seeds on the sd space (n = 24) and 16 on the emax=4 space (n = 140), half
+    of each with odd proton number (one blocked quasiparticle), 15 x 15 gauge
+    angles, unconstrained gradient iterations.  All 80 states make one
+    iteration per tvap_iterate_many call: the states of one worker context in
+    order, the contexts (8 sd, 4 emax=4) concurrently.  One warm-up call, then
+    `steps` timed calls (host perf_counter around each call: host buffers,
+    copies included).  Parity: three states (an even and an odd sd seed, an
+    odd emax=4 seed) iterated by the oracle for `parity_iters` iterations,
+    projected energy of every iterated state against the device's."""
+    import numpy as np
+
+    from taurus_vap_gb300 import model as M
+    from taurus_vap_gb300.native import Context, iterate_many
+
+    t0 = time.perf_counter()
+    sd = M.sd_model(seed=1)
+    e4 = M.noncore_model(4, seed=1)
+    sd_ctx = [Context(sd.basis, sd.ham) for _ in range(sd_workers)]
+    e4_ctx = [Context(e4.basis, e4.ham) for _ in range(e4_workers)]
+    states, ctxs, opts, etas = [], [], [], []
+    for k in range(64):
+        odd = k % 2 == 1
+        Z = 5 if odd else 4
+        states.append(M.random_bogoliubov(sd.basis, Z, 4, seed=100 + k, block=3 if odd else 0))
+        ctxs.append(sd_ctx[k % sd_workers])
+        opts.append(dict(Mphip=MPHI, Mphin=MPHI, facpi=2 * math.pi, valence_Z=Z, valence_N=4))
+        etas.append(0.02)
+    for k in range(16):
+        odd = k % 2 == 1
+        Z = 9 if odd else 8
+        states.append(M.random_bogoliubov(e4.basis, Z, 8, seed=200 + k, block=3 if odd else 0))
+        ctxs.append(e4_ctx[k % e4_workers])
+        opts.append(dict(Mphip=MPHI, Mphin=MPHI, facpi=2 * math.pi, valence_Z=Z, valence_N=8))
+        etas.append(ETA)
+    ns = len(states)
+    mus = [MU] * ns
+    U = [st[0] for st in states]
+    V = [st[1] for st in states]
+    Zm = [np.zeros(c.n * c.n) for c in ctxs]
+    setup_s = time.perf_counter() - t0
+    energies = [[] for _ in range(ns)]
+
+    def one():
+        res = iterate_many(ctxs, U, V, Zm, opts, etas, mus)
+        for q in range(ns):
+            p, Zi, g, U1, V1 = res[q]
+            energies[q].append((p.c("ener") / p.c("over")).real)
+            U[q], V[q], Zm[q] = U1, V1, Zi
+
+    one()
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        one()
+        times.append(time.perf_counter() - t)
+    ms = 1000.0 * sum(times) / len(times)
+    # parity sample against the oracle's loop from the same seeds
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    par = []
+    for q in (0, 1, 65):
+        mdl = sd if q < 64 else e4
+        o = opts[q]
+        st0 = states[q]
+        om = O.OracleModel(mdl)
+        ov = O.OracleVAP(om, st0[0], st0[1], MPHI, MPHI, 2 * math.pi, o["valence_Z"], o["valence_N"], etas[q], mus[q],
+                         0.0, np.zeros((0, mdl.n * mdl.n)), np.zeros(0))
+        for it in range(min(parity_iters, len(energies[q]))):
+            st, info = ov.iterate()
+            par.append(abs(info[1] - energies[q][it]))
+    return {
+        "workload": "64 sd seeds (n=24) + 16 emax=4 seeds (n=140), half with odd proton number (one blocked "
+                    "quasiparticle), 15x15 angles, unconstrained gradient iterations, FP64",
+        "states": ns, "workers": {"sd": sd_workers, "emax4": e4_workers}, "steps": steps,
+        "ms_per_batch_iteration": ms, "value": ns * 1000.0 / ms, "unit": "state-iterations/s",
+        "timer": "host perf_counter around each tvap_iterate_many call (host buffers)",
+        "setup_s": setup_s, "parity": {"states": [0, 1, 65], "iterations": parity_iters, "dE_max": max(par),
+                                       "bound": 1e-6, "unit": "MeV"},
+        "form": "tvap_iterate_many: states of one context in order, worker contexts concurrently on one GPU",
+    }
+
+
+SWEEP_LIMITS = {2: 25.0, 3: 50.0, 4: 75.0, 6: 100.0}  # fm^2: what Z = N = 10 reaches in each basis
+
+
+def sweep_leg(args, steps=2, per_basis=8, workers_per_basis=2, parity_iters=3):
+    """A quadrupole constraint sweep over uneven bases: 32 points, 8 on each
+    of the emax = 2, 3, 4, 6 bases (n = 40, 80, 140, 336), with Q20 targets
+    evenly spaced within +-25, 50, 75, 100 fm^2 (the deformations each model
+    space reaches with Z = N = 10; within -100..+100 fm^2 overall), Z = N = 10
+    constrained as well (the reference's 'Force constraint N/Z'), 15 x 15
+    angles; each point a full constrained gradient iteration (projection,
+    Lagrange multipliers, gradient, the constraint Newton loop on the
+    device).  Two contexts per basis; each context's points run in order on
+    one host thread, the eight contexts concurrently.  Setup (contexts,
+    seeds, one initial adjustment of every point) is outside the timing; then
+    `steps` timed sweep iterations.  Parity: the first emax=2 point iterated
+    by the oracle's loop for `parity_iters` iterations."""
+    import numpy as np
+
+    from taurus_vap_gb300 import model as M
+    from taurus_vap_gb300.native import Context
+    from taurus_vap_gb300.vap import VAP, Constraints, particle_number_ops
+
+    t0 = time.perf_counter()
+    groups = []  # (context, [VAP ...])
+    first = None
+    k = 0
+    for emax in (2, 3, 4, 6):
+        mdl = M.noncore_model(emax, seed=1, valence_Z=10, valence_N=10)
+        q = mdl.multipoles()
+        q20 = q[1, 0, 0] + q[1, 1, 0]
+        Qz, Qn = particle_number_ops(mdl.n)
+        lim = SWEEP_LIMITS[emax]
+        targets = np.linspace(-lim, lim, per_basis)
+        ctxs = [Context(mdl.basis, mdl.ham) for _ in range(workers_per_basis)]
+        vaps = [[] for _ in ctxs]
+        for j in range(per_basis):
+            U, V = M.random_bogoliubov(mdl.basis, 10, 10, seed=300 + k)
+            cons = ([Qz, Qn, q20], [10.0, 10.0, float(targets[j])])
+            vp = VAP(ctxs[j % workers_per_basis], U, V, MPHI, MPHI, 10.0, 10.0, ETA, MU,
+                     constraints=Constraints(*cons))
+            vp.adjust_constraints()
+            if first is None:
+                first = (mdl, U, V, cons)
+            vaps[j % workers_per_basis].append(vp)
+            k += 1
+        groups += list(zip(ctxs, vaps))
+    setup_s = time.perf_counter() - t0
+
+    def sweep_once():
+        errors = []
+
+        def run(vlist):
+            try:
+                for vp in vlist:
+                    vp.iterate()
+            except Exception as e:  # reported below
+                errors.append(repr(e))
+
+        th = [threading.Thread(target=run, args=(vl,)) for _, vl in groups]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        if errors:
+            raise RuntimeError(errors[0])
+
+    sweep_once()
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        sweep_once()
+        times.append(time.perf_counter() - t)
+    ms = 1000.0 * sum(times) / len(times)
+    n_points = sum(len(vl) for _, vl in groups)
+    # parity: the first point from its seed, device loop against the oracle's
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    mdl, U, V, cons = first
+    dv = VAP(Context(mdl.basis, mdl.ham), U, V, MPHI, MPHI, 10.0, 10.0, ETA, MU, constraints=Constraints(*cons))
+    dv.adjust_constraints()
+    ov = O.OracleVAP(O.OracleModel(mdl), U, V, MPHI, MPHI, 2 * math.pi, 10.0, 10.0, ETA, MU, 0.0,
+                     np.stack(cons[0]), np.array(cons[1]))
+    ov.initial_adjust()
+    dE = []
+    for _ in range(parity_iters):
+        _, info_d = dv.iterate()
+        _, info_o = ov.iterate()
+        dE.append(abs(info_d[1] - info_o[1]))
+    return {
+        "workload": "32 Q20 points over emax=2,3,4,6 (n=40/80/140/336; targets within +-25/50/75/100 fm^2), "
+                    "Z=N=10 and Q20 constrained, 15x15 angles, constrained gradient iterations, FP64",
+        "parity": {"point": "emax=2, Q20 = -25 fm^2", "iterations": parity_iters, "dE_max": max(dE), "bound": 1e-6,
+                   "unit": "MeV"},
+        "points": n_points, "contexts": len(groups), "steps": steps, "ms_per_sweep_iteration": ms,
+        "value": n_points * 1000.0 / ms, "unit": "point-iterations/s", "setup_s": setup_s,
+        "timer": "host perf_counter around each sweep iteration (host buffers)",
+        "form": "vap.VAP per point on shared per-basis contexts, contexts on concurrent host threads",
+    }
 
 
 def emax6_leg(torch, peaks, hbm_peak, steps=3):
@@ -653,6 +843,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip the FP64-pipe comparison run")
     ap.add_argument("--no-emax6", action="store_true", help="skip the emax=6 (n = 336) iteration leg")
+    ap.add_argument("--no-multi", action="store_true", help="skip the many-seeds and constraint-sweep legs")
     ap.add_argument("--gemm-mode", type=int, default=2,
                     help="dense products: 2 emulated with tcgen05 (default), 1 emulated with mma.sync, 0 FP64 pipe")
     args = ap.parse_args()

@@ -256,6 +256,20 @@ int tvap_adjust_constraints(tvap_ctx* ctx, const double* U0, const double* V0, d
                             const double* constraint_HO, const double* values, double eps, double* U1, double* V1,
                             double* C20, int* iterations);
 
+/* Many independent states iterated at once (the seeds of a minima search,
+ * the points of a constraint sweep; no counterpart in the reference, which
+ * runs one state per process): state s makes one tvap_iterate step on
+ * context ctx[s] with U0[s], V0[s], opts[s], eta[s], mu[s], Zim1[s] and
+ * writes Zi[s], U1[s], V1[s], out[s], gradient_norm[s] and status[s].  The
+ * states of one context run in order on one host thread; distinct contexts
+ * (each with its own streams; bases of different sizes allowed) run on
+ * concurrent host threads, so their kernels share the device.  The first
+ * failing state's status is returned. */
+int tvap_iterate_many(int nstates, tvap_ctx* const* ctx, const double* const* U0, const double* const* V0,
+                      const tvap_proj_opts* opts, const double* eta, const double* mu, const double* const* Zim1,
+                      double* const* Zi, double* const* U1, double* const* V1, tvap_pnp* out,
+                      double* gradient_norm, int* status);
+
 /* Test hook, no counterpart in the reference: the next tvap_evolve on this
  * context runs its cooperative launch with one CTA that leaves before the
  * first grid-wide barrier, so that the other CTAs' bounded waits there run

@@ -35,6 +35,7 @@ GPU_SOURCES = [
     "linalg_abi.cu",
     "diag_hsp_h11.cu",
     "constraints.cu",
+    "state_batch.cu",
 ]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

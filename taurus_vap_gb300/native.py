@@ -111,6 +111,9 @@ def lib():
         L.tvap_gradient_parameters.restype = ci
         L.tvap_adjust_constraints.argtypes = [vp, vp, vp, vp, ci, ci, vp, vp, cd, vp, vp, vp, vp]
         L.tvap_adjust_constraints.restype = ci
+        L.tvap_iterate_many.argtypes = [ci, vp, vp, vp, ctypes.POINTER(TvapProjOpts), vp, vp, vp, vp, vp, vp,
+                                        ctypes.POINTER(TvapPnp), vp, vp]
+        L.tvap_iterate_many.restype = ci
         L.tvap_test_wait_timeout.argtypes = [vp]
         L.tvap_test_wait_timeout.restype = ci
         L.tvap_zskpfa_batched.argtypes = [vp, ci, ctypes.c_int64, vp, vp]
@@ -410,3 +413,33 @@ def gradient_parameters(gradient_type, eigen_hsp, eigen_H11, info, eta_in, mu_in
     _check(lib().tvap_gradient_parameters(int(gradient_type), eh.size, _p(eh), _p(e11), _p(inf), eta_in, mu_in,
                                           ctypes.byref(eta), ctypes.byref(mu)), "tvap_gradient_parameters")
     return eta.value, mu.value
+
+
+def iterate_many(contexts, U0s, V0s, Zim1s, opts, etas, mus):
+    """tvap_iterate_many: one gradient iteration for each state s on
+    contexts[s] (states of one context in order, distinct contexts
+    concurrently).  opts[s] is a dict of tvap_proj_opts fields (Mphip, Mphin,
+    facpi, valence_Z, valence_N[, factor_delta, seed_occeps, seed_allemp]).
+    Returns [(pnp, Zi, gradient_norm, U1, V1)] per state."""
+    ns = len(contexts)
+    P = ctypes.c_void_p * ns
+    Us = [_f(u, np.float64) for u in U0s]
+    Vs = [_f(v, np.float64) for v in V0s]
+    Zm = [np.ascontiguousarray(z, dtype=np.float64).reshape(-1) for z in Zim1s]
+    Zi = [np.zeros(c.n * c.n) for c in contexts]
+    U1 = [np.zeros((c.n, c.n), order="F") for c in contexts]
+    V1 = [np.zeros((c.n, c.n), order="F") for c in contexts]
+    O = (TvapProjOpts * ns)()
+    for s, d in enumerate(opts):
+        O[s] = TvapProjOpts(d["Mphip"], d["Mphin"], d["facpi"], d["valence_Z"], d["valence_N"],
+                            d.get("factor_delta", 1.0), d.get("seed_occeps", 0.0), d.get("seed_allemp", 0), 0)
+    outs = (TvapPnp * ns)()
+    eta = np.ascontiguousarray(etas, dtype=np.float64)
+    mu = np.ascontiguousarray(mus, dtype=np.float64)
+    gn = np.zeros(ns)
+    st = np.zeros(ns, dtype=np.int32)
+    ptrs = lambda arrs: P(*[a.ctypes.data for a in arrs])
+    _check(lib().tvap_iterate_many(ns, P(*[c.h.value for c in contexts]), ptrs(Us), ptrs(Vs), O, _p(eta), _p(mu),
+                                   ptrs(Zm), ptrs(Zi), ptrs(U1), ptrs(V1), outs, _p(gn), _p(st)),
+           "tvap_iterate_many")
+    return [(outs[s], Zi[s], float(gn[s]), U1[s], V1[s]) for s in range(ns)]
