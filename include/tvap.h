@@ -123,8 +123,12 @@ int tvap_get_timeline(tvap_ctx* ctx, double* start_ms, double* end_ms, int nsec)
  * basis: [0] FP32 Jacobi + FP64 refinement attempts, [1] of them accepted by
  * the final check, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in
  * total, [4..6] attempts rejected because clusters stayed coupled / the
- * basis was not orthonormal / a cluster of near-degenerate levels was too
- * large.  No reference counterpart. */
+ * basis was not orthonormal / the clusters of near-degenerate levels could
+ * not be diagonalised (more large ones than the list holds, or a block's
+ * Jacobi did not converge), [7] large clusters diagonalised by the FP64
+ * Jacobi of their block, [8] refinements continued by two second-order
+ * steps after a failed check ([4..6] count each failed check).  No
+ * reference counterpart. */
 int tvap_get_counters(tvap_ctx* ctx, long long* out, int nout);
 
 /* One upload of the reduced two-body list and the one-body part:
@@ -269,6 +273,24 @@ int tvap_iterate_many(int nstates, tvap_ctx* const* ctx, const double* const* U0
                       const tvap_proj_opts* opts, const double* eta, const double* mu, const double* const* Zim1,
                       double* const* Zi, double* const* U1, double* const* V1, tvap_pnp* out,
                       double* gradient_norm, int* status);
+
+/* Launch shapes of the projection, chosen by measurement (no counterpart
+ * in the reference).  tvap_autotune times `reps` projections of (U0, V0)
+ * with opts for each candidate -- B' tile policy of the tcgen05 products (0:
+ * the width that pads the output columns less, 1: 64 rows, 2: 48 rows) x the
+ * groups of angles in the Thouless solve (2 staggered on two streams, or 1)
+ * x the cap on the tcgen05 CTAs beside the second group's panels (0: the
+ * SMs the panels leave, 1: half the SMs, 2: none; 2 groups only) -- 12
+ * candidates, CUDA events on the context's stream, and keeps the fastest in
+ * the context.  table_ms (may be NULL) receives the ms per projection of the
+ * first ntable candidates in the order groups 2 (cap 0, 1, 2), then groups
+ * 1, each with bn 0, 1, 2.  Results do not depend on the choice (the same
+ * FP64 emulation; only tile and launch shapes change).  tvap_set_tuning and
+ * tvap_get_tuning (knobs[3] = bn, groups, cap) set and read them. */
+int tvap_autotune(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts, int reps,
+                  double* table_ms, int ntable);
+int tvap_set_tuning(tvap_ctx* ctx, int bn_policy, int solve_groups, int solve_cap);
+int tvap_get_tuning(const tvap_ctx* ctx, int* knobs);
 
 /* Test hook, no counterpart in the reference: the next tvap_evolve on this
  * context runs its cooperative launch with one CTA that leaves before the

@@ -131,6 +131,7 @@ int tvap_adjust_constraints(tvap_ctx* c, const double* U0, const double* V0, dou
     return TVAP_ERR_ARG;
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;

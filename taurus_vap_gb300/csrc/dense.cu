@@ -258,6 +258,7 @@ int pick_tile(int M, int N) {
 
 thread_local int g_gemm_mode = 2;
 thread_local int g_tc_grid_cap = 0;
+thread_local int g_tc_bn_policy = 0;
 thread_local int* g_dev_flags = nullptr;
 thread_local tvap_ctx* g_tc_timing_ctx = nullptr;
 thread_local int g_tc_timing_sec = -1;
@@ -371,6 +372,7 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_kernel(int N, double2* Aa
     int KP;
     double pv;
     block_argmax(best, bi, sv, si, KP, pv);
+    if (KP > K - 1) KP = 1;  // every |a(i, K)| is NaN: IZAMAX returns the first index
     const int KK = K - 1;
     if (pv == 0.0) {
       zero = true;
@@ -630,19 +632,203 @@ __global__ void __launch_bounds__(kPfThreads) pfaffian_smem_kernel(int N, const 
   }
 }
 
+// Blocked Parlett-Reid (the reference's ZLASKTRF form of ZSKTRF for large
+// N, subroutines_pfaffian.f:1015-1400): a panel of up to kPfNb columns from
+// the right is eliminated with delayed updates -- the current value of a
+// column is its stored value plus sum_t (p_t q_t[c] - q_t p_t[c]) over the
+// panel's earlier steps, with p_t = x (the column K above the pivot row) and
+// q_t = y / A(K-1, K) (column K-1) -- and the interchanges act on the stored
+// upper triangle and on the rows of the p and q vectors alike.  The leading
+// block then takes the whole panel at once, A += P Q^T - Q P^T, as one
+// batched product on the tensor cores (pf_trailing in pfaffian_batched).
+// The pivots are those of the unblocked elimination; only the order of the
+// rounding changes.
+constexpr int kPfNb = 32;          // panel width (columns)
+constexpr int kPfNs = kPfNb / 2;   // steps per panel
+
+// One panel of every matrix: columns Kstart, Kstart-1, ..., Kstart-width+1
+// (0-based).  X = [P | Q], Y = [Q | -P] (n x 2 kPfNs per matrix, unused
+// columns zero) for the trailing product X Y^T.  pf[b] = (log|Pf|, 0) and
+// pf[batch + b] = phase accumulate over the panels (first: start them).
+__global__ void __launch_bounds__(kPfThreads) pf_panel_kernel(int N, int Kstart, int width, double2* __restrict__ Aall,
+                                                           double2* __restrict__ Xall, double2* __restrict__ Yall,
+                                                           double2* __restrict__ pf, int batch, int* flags,
+                                                           int first) {
+  __shared__ double sv[kPfThreads];
+  __shared__ int si[kPfThreads];
+  __shared__ double2 ck[512], ckk[512];
+  __shared__ double s_lm;
+  __shared__ double2 s_ph;
+  __shared__ int s_zero;
+  const int b = blockIdx.x;
+  double2* A = Aall + size_t(b) * N * N;
+  const size_t ldx = size_t(N);
+  double2* X = Xall + size_t(b) * N * 2 * kPfNs;
+  double2* Y = Yall + size_t(b) * N * 2 * kPfNs;
+  auto a = [A, N](int i, int j) -> double2& { return A[i + size_t(j) * N]; };
+  auto P = [X, ldx](int i, int t) -> double2& { return X[i + t * ldx]; };
+  auto Q = [X, ldx](int i, int t) -> double2& { return X[i + (kPfNs + t) * ldx]; };
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) {
+    if (first) {
+      s_lm = 0.0;
+      s_ph = make_double2(1.0, 0.0);
+      s_zero = 0;
+    } else {
+      s_lm = pf[b].x;
+      s_ph = pf[batch + b];
+      s_zero = isinf(s_lm) && s_lm < 0.0;
+    }
+  }
+  for (size_t idx = tid; idx < ldx * 2 * kPfNs; idx += nt) X[idx] = make_double2(0.0, 0.0);
+  __syncthreads();
+  if (s_zero) return;  // a zero pivot earlier: Pf = 0
+  const int ns = width / 2;
+  for (int s = 0; s < ns; ++s) {
+    const int K = Kstart - 2 * s, KK = K - 1;
+    // the current column K above the diagonal
+    double best = -1.0;
+    int bi = N + 1;
+    for (int i = tid; i < K; i += nt) {
+      double2 v = a(i, K);
+      for (int t = 0; t < s; ++t) {
+        cfma(v, P(i, t), Q(K, t));
+        cfma(v, cneg(Q(i, t)), P(K, t));
+      }
+      ck[i] = v;
+      const double m = cabs1(v);
+      if (m > best) {
+        best = m;
+        bi = i;
+      }
+    }
+    int KP;
+    double pv;
+    block_argmax(best, bi, sv, si, KP, pv);
+    if (KP >= K) KP = 0;  // every |a(i, K)| is NaN: IZAMAX returns the first index
+    if (pv == 0.0) {
+      if (tid == 0) s_zero = 1;
+      break;  // uniform: every thread holds the same pv
+    }
+    if (KP != KK) {
+      // symmetric interchange KP <-> KK of the leading block in upper storage
+      for (int i = tid; i < KP; i += nt) {
+        const double2 t0 = a(i, KK);
+        a(i, KK) = a(i, KP);
+        a(i, KP) = t0;
+      }
+      for (int j = KP + 1 + tid; j < KK; j += nt) {
+        const double2 t1 = a(j, KK), t2 = a(KP, j);
+        a(j, KK) = cneg(t2);
+        a(KP, j) = cneg(t1);
+      }
+      if (tid == 0) {
+        a(KP, KK) = cneg(a(KP, KK));
+        const double2 t3 = ck[KP];
+        ck[KP] = ck[KK];
+        ck[KK] = t3;
+        s_ph = cneg(s_ph);
+      }
+      for (int t = tid; t < s; t += nt) {
+        double2 u = P(KP, t);
+        P(KP, t) = P(KK, t);
+        P(KK, t) = u;
+        u = Q(KP, t);
+        Q(KP, t) = Q(KK, t);
+        Q(KK, t) = u;
+      }
+      __syncthreads();
+    }
+    const double2 piv = ck[KK];
+    const double2 alpha = crcp(piv);
+    // the current column KK above the diagonal, then p_s and q_s
+    for (int i = tid; i < KK; i += nt) {
+      double2 v = a(i, KK);
+      for (int t = 0; t < s; ++t) {
+        cfma(v, P(i, t), Q(KK, t));
+        cfma(v, cneg(Q(i, t)), P(KK, t));
+      }
+      ckk[i] = v;
+    }
+    __syncthreads();
+    for (int i = tid; i < KK; i += nt) {
+      P(i, s) = ck[i];
+      Q(i, s) = cmul(alpha, ckk[i]);
+    }
+    if (tid == 0) {
+      const double m = hypot(piv.x, piv.y);
+      s_lm += log(m);
+      s_ph = cmul(s_ph, make_double2(piv.x / m, piv.y / m));
+    }
+    __syncthreads();
+  }
+  // Y = [Q | -P]
+  for (size_t idx = tid; idx < ldx * kPfNs; idx += nt) {
+    Y[idx] = X[idx + ldx * kPfNs];
+    Y[idx + ldx * kPfNs] = cneg(X[idx]);
+  }
+  if (tid == 0) {
+    if (s_zero) {
+      pf[b] = make_double2(-INFINITY, 0.0);
+      pf[batch + b] = make_double2(0.0, 0.0);
+      atomicOr(flags, DEV_PFAFF_ZERO);
+    } else {
+      pf[b] = make_double2(s_lm, 0.0);
+      pf[batch + b] = s_ph;
+    }
+  }
+}
+
 }  // namespace
 
 int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s) {
   if (n > 512 || (n & 1)) return TVAP_ERR_ARG;
   const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 4 * size_t(n + 1) + size_t(n));
   if (shm <= jacobi32_smem_limit()) {
+    // the packed upper triangle fits shared memory: the unblocked elimination
     if (int rc = smem_opt_in((const void*)pfaffian_smem_kernel, jacobi32_smem_limit())) return rc;
     pfaffian_smem_kernel<<<batch, kPfThreads, shm, tvap::counted(s)>>>(n, A, pf, batch, flags);
-  } else {
-    pfaffian_kernel<<<batch, kPfThreads, 0, tvap::counted(s)>>>(n, A, pf, batch, flags);
+    TVAP_CUDA(cudaGetLastError());
+    return TVAP_OK;
   }
-  TVAP_CUDA(cudaGetLastError());
-  return TVAP_OK;
+  if (n == 0) return TVAP_ERR_ARG;
+  // blocked: panels of kPfNb columns, the trailing updates on the tensor cores
+  const size_t xy = size_t(batch) * n * 2 * kPfNs;
+  double2* XY = nullptr;
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&XY), sizeof(double2) * 2 * xy, s));
+  double2 *X = XY, *Y = XY + xy;
+  int rc = TVAP_OK;
+  for (int Kstart = n - 1, first = 1; Kstart > 0 && rc == TVAP_OK; first = 0) {
+    const int width = std::min(kPfNb, Kstart + 1);
+    pf_panel_kernel<<<batch, kPfThreads, 0, tvap::counted(s)>>>(n, Kstart, width, A, X, Y, pf, batch, flags, first);
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = TVAP_ERR_CUDA;
+      break;
+    }
+    const int L = Kstart - width + 1;  // the leading block still to eliminate
+    if (L > 1) {
+      // A[0:L, 0:L] += X Y^T (upper triangle read later)
+      GemmArgs g{};
+      g.M = g.N = L;
+      g.K = 2 * kPfNs;
+      g.batch = batch;
+      g.A = View{X, 1, n, (long long)n * 2 * kPfNs};
+      g.B = View{Y, n, 1, (long long)n * 2 * kPfNs};  // B(k, j) = Y(j, k)
+      g.C = A;
+      g.crs = 1;
+      g.ccs = n;
+      g.cbs = (long long)n * n;
+      g.alpha = make_double2(1.0, 0.0);
+      g.beta = make_double2(1.0, 0.0);
+      g.three_m = true;
+      g.upper_only = true;
+      rc = gemm(g, s);
+    }
+    Kstart = L - 1;
+  }
+  cudaFreeAsync(XY, s);
+  if (rc == TVAP_ERR_CUDA) set_last_error("blocked Pfaffian launch failed", __FILE__, __LINE__);
+  return rc;
 }
 
 // ---------------------------------------------------------------------------
@@ -657,7 +843,7 @@ constexpr int kJacThreads = 1024;
 
 template <typename T>
 __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, double* evals, double* work,
-                                                             int* flags, double tolfac) {
+                                                             int* flags, double tolfac, double relrot) {
   extern __shared__ double jsh[];
   const int m = (n + 1) & ~1;  // even count incl. a dummy index
   double* cs = jsh;                                    // m/2 cosines
@@ -666,7 +852,7 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
   int* pp = pairs + m;                                 // m/2 p indices
   int* qq = pp + m / 2;                                // m/2 q indices
   __shared__ double red[kJacThreads];
-  __shared__ int done;
+  __shared__ int done, nrot;
   const int tid = threadIdx.x, nt = blockDim.x;
   auto Ael = [A, n](int i, int j) -> T& { return A[i + size_t(j) * n]; };
   for (size_t idx = tid; idx < size_t(n) * n; idx += nt) W[idx] = ((idx % n) == (idx / n)) ? T(1) : T(0);
@@ -682,6 +868,7 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
   const double fro2 = red[0];
   __syncthreads();
   const double tol2 = fro2 * tolfac;  // converged when off-diagonal^2 <= tolfac ||A||_F^2
+  const double absrot = 0.1 * relrot * sqrt(fro2);
   const int kstep = nt / n;
   const int r0 = (tid < kstep * n) ? tid % n : n;
   const int k0 = (tid < kstep * n) ? tid / n : 0;
@@ -699,9 +886,14 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
       if (tid < s) red[tid] += red[tid + s];
       __syncthreads();
     }
-    if (tid == 0) done = (red[0] <= tol2) ? 1 : 0;
+    // converged: the off-diagonal norm is small, or the last sweep found no
+    // entry above the rounding level of its diagonal pair (the off-diagonal
+    // norm of a large matrix can stay above tol2 at that level)
+    if (tid == 0) done = (red[0] <= tol2 || (sweep > 0 && nrot == 0)) ? 1 : 0;
     __syncthreads();
     if (done) break;
+    if (tid == 0) nrot = 0;
+    __syncthreads();
     for (int round = 0; round < m - 1; ++round) {
       // pairs (pairs[k], pairs[m-1-k]) for k < m/2
       for (int k = tid; k < m / 2; k += nt) {
@@ -721,8 +913,11 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
         T c = T(1), s = T(0);
         if (q < n) {
           const T apq = Ael(p, q);
-          if (apq != T(0)) {
-            const T app = Ael(p, p), aqq = Ael(q, q);
+          const T app = Ael(p, p), aqq = Ael(q, q);
+          // rotate unless apq is at the rounding level of its pair, or below
+          // a tenth of it for the whole matrix
+          if (apq != T(0) && fabs(double(apq)) > fmax(relrot * sqrt(fabs(double(app) * double(aqq))), absrot)) {
+            atomicAdd(&nrot, 1);
             const T theta = (aqq - app) / (T(2) * apq);
             const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
             c = T(1) / sqrt(t * t + T(1));
@@ -792,7 +987,7 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
 int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s) {
   const int m = (n + 1) & ~1;
   const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
-  jacobi_kernel<double><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-30);
+  jacobi_kernel<double><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-30, 1.0e-16);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }
@@ -800,7 +995,7 @@ int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* 
 int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s) {
   const int m = (n + 1) & ~1;
   const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
-  jacobi_kernel<float><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-13);
+  jacobi_kernel<float><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-13, 6.0e-8);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }

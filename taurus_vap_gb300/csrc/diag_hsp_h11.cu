@@ -272,6 +272,7 @@ int tvap_diagonalize_hsp_and_H11(tvap_ctx* c, const double* U0, const double* V0
   if (n > kTdMaxN) return TVAP_ERR_ARG;
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
   g_dev_flags = c->d_flags;
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;

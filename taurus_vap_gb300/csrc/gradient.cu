@@ -262,6 +262,7 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   if (!c || !U0 || !V0 || !Z || !U1 || !V1) return TVAP_ERR_ARG;
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -296,6 +297,7 @@ int tvap_iterate(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -424,6 +426,7 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
   if ((rc = ensure_workspace(c, angle_count(*opts)))) return rc;
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
   g_dev_flags = c->d_flags;
   double* buf = nullptr;
   if ((rc = ctx_scratch(c, 7 * nn + n, &buf))) return rc;

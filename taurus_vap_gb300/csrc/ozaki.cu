@@ -594,7 +594,7 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   // B' tiles of 48 or 64 rows, whichever pads the output columns less (140
   // columns: 144 instead of 192)
   const int pad48 = (xb.xrows + 47) / 48 * 48, pad64 = (xb.xrows + 63) / 64 * 64;
-  const int bn = pad48 < pad64 ? 48 : 64;
+  const int bn = g_tc_bn_policy == 1 ? 64 : g_tc_bn_policy == 2 ? 48 : (pad48 < pad64 ? 48 : 64);
   const int b_rows_pad = bn == 48 ? pad48 : pad64;
   const int nks = (xa.xk + 15) / 16;
   const size_t asz = size_t(a_slots) * (a_rows_pad / oztc::kM) * nks * (oztc::kABytes / 2);

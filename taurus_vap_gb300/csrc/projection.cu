@@ -78,6 +78,11 @@ struct Workspace {
   // overlap chain scratch (runs on the second stream)
   double2 *OW = nullptr, *OX = nullptr, *OY = nullptr;
   int* rflag = nullptr;
+  // canonical-basis clusters: cluster of each refined column (its first
+  // position in the sorted order of the first refinement step), the
+  // columns in cluster order, and (start, size) of the clusters left to
+  // the FP64 Jacobi of their block
+  int *cid = nullptr, *cperm = nullptr, *bigd = nullptr;
   int* piv = nullptr;  // [G][n] row interchanges of the Thouless LU
   // [G][panel][L11^-1, U11^-1] (kPanelMax^2 each) of the Thouless LU
   double2* Tinv = nullptr;
@@ -102,6 +107,7 @@ int dalloc(T** p, size_t count, size_t& total) {
 
 constexpr int kPanelMax = 32;  // columns per panel of the Thouless solve
 constexpr int kSubMax = 64;    // largest degenerate subspace of the canonical basis
+constexpr int kCfBigSlots = 16;  // clusters of the refined basis passed to the FP64 Jacobi per attempt
 
 // double2 entries per angle of Workspace::Tinv
 size_t tinv_stride(int n) { return size_t((n + kPanelMax - 1) / kPanelMax) * 2 * kPanelMax * kPanelMax; }
@@ -113,7 +119,8 @@ void ws_free(Workspace* w) {
                   w->kLR, w->kRL,   w->gam,    w->hsp,   w->dLR,    w->dRL,   w->ephase, w->weight, w->mult,
                   w->obs, w->pf,    w->detR22, w->coefA, w->coefAE, w->pA,    w->pH,     w->pAH,   w->pscal,
                   w->H20v,  w->XB,    w->RS,     w->Br,    w->Mr,     w->lam,   w->rscal,
-                  w->rflag, w->OW,    w->OX,     w->OY,     w->piv, w->Tinv, w->tpart, w->schq};
+                  w->rflag, w->cid,   w->cperm,  w->bigd,   w->OW,  w->OX,   w->OY,    w->piv,   w->Tinv,
+                  w->tpart, w->schq};
   for (void* p : ptrs) cudaFree(p);
   *w = Workspace();
 }
@@ -141,7 +148,8 @@ int ws_ensure(tvap_ctx* c, int G) {
   A_(Rn, nG) A_(K, nG) A_(SZ, nG) A_(rhoL, nG) A_(kLR, nG) A_(kRL, nG) A_(gam, nG) A_(hsp, nG) A_(dLR, nG)
   A_(dRL, nG) A_(ephase, 2 * G) A_(weight, G) A_(mult, G) A_(obs, 8 * G) A_(pf, 2 * G) A_(detR22, 2 * G)
   A_(coefA, G) A_(coefAE, G) A_(pA, nn) A_(pH, nn) A_(pAH, nn) A_(pscal, 8) A_(H20v, nn)
-  A_(XB, 4 * nn) A_(RS, 2 * nn) A_(Br, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 4)
+  A_(XB, 4 * nn) A_(RS, 2 * nn) A_(Br, nn) A_(Mr, nn) A_(lam, n) A_(rscal, 8) A_(rflag, 8)
+  A_(cid, n) A_(cperm, n) A_(bigd, 2 * kCfBigSlots)
   A_(OW, nG) A_(OX, nG) A_(OY, nG) A_(piv, size_t(n) * G)
   A_(Tinv, size_t(G) * tinv_stride(n)) A_(tpart, size_t(G) * 9 * 256) A_(schq, 2 * kSubMax * kSubMax)
 #undef A_
@@ -1002,7 +1010,8 @@ __global__ void __launch_bounds__(kRlThreads)
 
 __global__ void refine_update_kernel(int n, const double* __restrict__ XtX, const double* __restrict__ S,
                                      const double* __restrict__ lam, const double* __restrict__ rscal,
-                                     double* __restrict__ M) {
+                                     const int* __restrict__ cid, double* __restrict__ M,
+                                     double* __restrict__ Fout) {
   const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (e >= size_t(n) * n) return;
   const int i = int(e % n), j = int(e / n);
@@ -1015,12 +1024,20 @@ __global__ void refine_update_kernel(int n, const double* __restrict__ XtX, cons
   const double rb = 0.5 * ((((i == j) ? 1.0 : 0.0) - XtX[e]) + (((i == j) ? 1.0 : 0.0) - XtX[et]));
   const double sb = 0.5 * (S[e] + S[et]);
   const double dl = lam[j] - lam[i];
-  // the rotation only where the gap dominates the coupling; pairs that are
-  // (nearly) degenerate relative to their coupling are only re-orthonormalised
-  // and diagonalised exactly at the end
-  const bool newton = (i != j) && fabs(dl) > 4.0 * fabs(sb) + 1.0e-13 * rscal[1];
+  // the rotation only between columns of different clusters (fixed at the
+  // first step, where the gap dominated the coupling 64-fold); the pairs
+  // within a cluster are only re-orthonormalised and diagonalised exactly
+  // at the end.  Admitting such a pair later, once its coupling looks small
+  // beside the shrinking residual, gives corrections of order one whose
+  // second-order terms undo the orthonormality.
+  const bool newton = (i != j) && cid[i] != cid[j] && fabs(dl) > 2.0 * fabs(sb) + 1.0e-13 * rscal[1];
   const double F = newton ? (sb + 0.5 * (lam[i] + lam[j]) * rb) / dl : 0.0;
+  // M = I + R/2 + F here; the steps that continue a refinement whose check
+  // failed add F^2 / 2 (I + F + F^2/2 is orthogonal to O(F^3) where I + F
+  // loses O(F^2): from an FP32 start, ||R|| ~ 1e-4, on nearly closed shells
+  // that stays above the acceptance test after three steps)
   M[e] = ((i == j) ? 1.0 : 0.0) + 0.5 * rb + F;
+  Fout[e] = F;
 }
 
 // Cyclic Jacobi of one cluster block a (m x m, m <= M) with its rotations
@@ -1089,57 +1106,125 @@ __device__ void cluster_solve(int n, int m, int k0, const double* __restrict__ S
   }
 }
 
-// Sort by eigenvalue, diagonalise clusters of (near-)degenerate eigenvalues
-// exactly with a small Jacobi, verify the off-diagonal coupling between
-// clusters, write D (ascending) and the eigenvalues.  One CTA: the diagonal,
-// the order and the clusters in shared memory, one thread per cluster for
-// the Jacobi, a warp per cluster for the rotation of its columns.
 constexpr int kCfThreads = 512;
 constexpr int kCfMaxN = 512;
-constexpr int kCfQ = 2048;  // rotation entries of all clusters (sum of m^2)
+constexpr int kCfQ = 2048;          // rotation entries of the small clusters (sum of m^2)
+constexpr double kCfGate = 64.0;    // Newton step where |l_j - l_i| > kCfGate |S_ij|
+
+// Clusters of the refined basis, fixed at the first refinement step (Ogita
+// & Aishima's treatment of clustered eigenvalues): columns i, j whose gap
+// is not kCfGate times their coupling, |l_j - l_i| <= kCfGate |S_ij| +
+// 1e-13 ||A||, belong to one cluster, and a cluster is the smallest range
+// of the sorted Rayleigh quotients that contains every such pair.  cid[i] =
+// the first sorted position of column i's cluster.  One CTA.
+__global__ void __launch_bounds__(kCfThreads)
+    cluster_assign_kernel(int n, const double* __restrict__ S, const double* __restrict__ lam,
+                          const double* __restrict__ rscal, int* __restrict__ cid) {
+  __shared__ int pos[kCfMaxN], order[kCfMaxN], reach[kCfMaxN];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < n; i += nt) {
+    const double v = lam[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const double u = lam[j];
+      rank += (u < v || (u == v && j < i)) ? 1 : 0;
+    }
+    pos[i] = rank;
+    order[rank] = i;
+    reach[rank] = rank;
+  }
+  __syncthreads();
+  const double floor = 1.0e-13 * rscal[1];
+  for (size_t e = tid; e < size_t(n) * n; e += nt) {
+    const int i = int(e % n), j = int(e / n);
+    if (i >= j) continue;
+    const double sb = 0.5 * (S[e] + S[j + size_t(i) * n]);
+    if (fabs(lam[j] - lam[i]) <= kCfGate * fabs(sb) + floor) {
+      const int pa = pos[i], pb = pos[j];
+      atomicMax(&reach[min(pa, pb)], max(pa, pb));
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int k = 0;
+    while (k < n) {
+      int j = reach[k];
+      for (int t = k; t <= j; ++t) j = max(j, reach[t]);
+      for (int t = k; t <= j; ++t) cid[order[t]] = k;
+      k = j + 1;
+    }
+  }
+}
+
+// The refined columns ordered by cluster (the order of the first step) and,
+// within a cluster, by Rayleigh quotient; each cluster diagonalised exactly
+// (up to 8 columns: a Jacobi by one thread here; larger ones, or those
+// beyond the rotation buffer: listed in bigd for the FP64 Jacobi of their
+// block, big_cluster_rotate_kernel); the coupling between clusters and the
+// orthonormality verified; D and the eigenvalues written in that order.
+// One CTA: the diagonal, the order and the clusters in shared memory, one
+// thread per small cluster for its Jacobi, a warp per cluster for the
+// rotation of its columns.  rflag[0] = failure bits, rflag[2] = number of
+// clusters in bigd, rflag[3] = 0 (the big clusters' Jacobi status).
 __global__ void __launch_bounds__(kCfThreads)
     cluster_finish_kernel(int n, const double* __restrict__ S, const double* __restrict__ X,
-                          const double* __restrict__ rscal, double* __restrict__ D, double* __restrict__ evals,
-                          int* rflag) {
+                          const double* __restrict__ rscal, const int* __restrict__ cidg, double* __restrict__ D,
+                          double* __restrict__ evals, int* __restrict__ cperm, int* __restrict__ bigd, int* rflag) {
   constexpr int CM = 8;
   __shared__ double sd[kCfMaxN], lsh[kCfMaxN];
   __shared__ int perm[kCfMaxN], cid[kCfMaxN], osh[kCfMaxN], cl_start[kCfMaxN + 1], qoff[kCfMaxN + 1];
   __shared__ double qbuf[kCfQ];
-  __shared__ int ncl, fail;
+  __shared__ int ncl, fail, nbig;
   __shared__ double red[kCfThreads / 32];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  if (tid == 0) fail = 0;
-  for (int i = tid; i < n; i += nt) sd[i] = S[i + size_t(i) * n];
+  if (tid == 0) {
+    fail = 0;
+    nbig = 0;
+  }
+  for (int i = tid; i < n; i += nt) {
+    sd[i] = S[i + size_t(i) * n];
+    cid[i] = cidg[i];
+  }
   __syncthreads();
   for (int i = tid; i < n; i += nt) {
     const double v = sd[i];
+    const int ci = cid[i];
     int rank = 0;
     for (int j = 0; j < n; ++j) {
       const double u = sd[j];
-      rank += (u < v || (u == v && j < i)) ? 1 : 0;
+      const int cj = cid[j];
+      rank += (cj < ci || (cj == ci && (u < v || (u == v && j < i)))) ? 1 : 0;
     }
     perm[rank] = i;
   }
   __syncthreads();
+  for (int k = tid; k < n; k += nt) cperm[k] = perm[k];
   const double nA = rscal[1];
-  const double tau = fmax(rscal[0], 1.0e-13 * nA);
   if (tid == 0) {
     int c = 0;
     cl_start[0] = 0;
-    for (int k = 0; k < n; ++k) {
-      if (k > 0 && sd[perm[k]] - sd[perm[k - 1]] > tau) cl_start[++c] = k;
-      cid[perm[k]] = c;
-    }
+    for (int k = 1; k < n; ++k)
+      if (cid[perm[k]] != cid[perm[k - 1]]) cl_start[++c] = k;
     ncl = c + 1;
     cl_start[ncl] = n;
+    // small clusters take rotation buffer space; the rest go to bigd
+    // (qoff = -1), as many as it holds
     int off = 0;
     for (int q = 0; q < ncl; ++q) {
       const int m = cl_start[q + 1] - cl_start[q];
-      qoff[q] = off;
-      if (m <= CM) off += m * m;
+      if (m <= CM && off + m * m <= kCfQ) {
+        qoff[q] = off;
+        off += m * m;
+      } else if (nbig < kCfBigSlots) {
+        qoff[q] = -1;
+        bigd[2 * nbig] = cl_start[q];
+        bigd[2 * nbig + 1] = m;
+        ++nbig;
+      } else {
+        qoff[q] = -1;
+        fail |= 4;  // more large clusters than the list holds
+      }
     }
-    qoff[ncl] = off;
-    if (off > kCfQ) fail |= 4;
   }
   __syncthreads();
   // coupling between different clusters must be negligible
@@ -1158,33 +1243,29 @@ __global__ void __launch_bounds__(kCfThreads)
     if (m2 > 1.0e-12 * fmax(nA, 1e-300)) fail |= 1;  // clusters still coupled
     if (rscal[3] > 1.0e-12 * sqrt(double(n))) fail |= 2;  // not orthonormal
   }
-  const bool qfit = qoff[ncl] <= kCfQ;
   for (int c = tid; c < ncl; c += nt) {
     const int k0 = cl_start[c], m = cl_start[c + 1] - k0;
-    if (m > CM) {
-      atomicOr(&fail, 4);  // cluster too large
-    } else if (qfit) {
-      double* qb = qbuf + qoff[c];
-      if (m == 1) {
-        osh[k0] = 0;
-        lsh[k0] = sd[perm[k0]];
-        qb[0] = 1.0;
-      } else if (m == 2) {
-        cluster_solve<2>(n, m, k0, S, perm, lsh, osh, qb);
-      } else if (m <= 4) {
-        cluster_solve<4>(n, m, k0, S, perm, lsh, osh, qb);
-      } else {
-        cluster_solve<CM>(n, m, k0, S, perm, lsh, osh, qb);
-      }
+    if (qoff[c] < 0) continue;
+    double* qb = qbuf + qoff[c];
+    if (m == 1) {
+      osh[k0] = 0;
+      lsh[k0] = sd[perm[k0]];
+      qb[0] = 1.0;
+    } else if (m == 2) {
+      cluster_solve<2>(n, m, k0, S, perm, lsh, osh, qb);
+    } else if (m <= 4) {
+      cluster_solve<4>(n, m, k0, S, perm, lsh, osh, qb);
+    } else {
+      cluster_solve<CM>(n, m, k0, S, perm, lsh, osh, qb);
     }
   }
   __syncthreads();
   for (int c = warp; c < ncl; c += nwarp) {
     const int k0 = cl_start[c], m = cl_start[c + 1] - k0;
-    if (m > CM || !qfit) {
-      // too large to diagonalise here (the attempt fails): the refined
-      // columns go to D unrotated, so that D stays an orthonormal basis to
-      // start the next attempt from
+    if (qoff[c] < 0) {
+      // left to the FP64 Jacobi of the block (or the attempt fails): the
+      // refined columns go to D unrotated, so that D stays an orthonormal
+      // basis to start the next attempt from
       for (int r = 0; r < m; ++r) {
         if (lane == 0) evals[k0 + r] = sd[perm[k0 + r]];
         for (int row = lane; row < n; row += 32) D[row + size_t(k0 + r) * n] = X[row + size_t(perm[k0 + r]) * n];
@@ -1203,7 +1284,35 @@ __global__ void __launch_bounds__(kCfThreads)
     }
   }
   __syncthreads();
-  if (tid == 0) rflag[0] = fail;
+  if (tid == 0) {
+    rflag[0] = fail;
+    rflag[2] = nbig;
+    rflag[3] = 0;
+  }
+}
+
+// The block S_cc of one large cluster (columns cperm[k0 .. k0+m-1] of the
+// refined basis), column-major m x m, for the FP64 Jacobi.
+__global__ void big_cluster_extract_kernel(int n, int m, const double* __restrict__ S, const int* __restrict__ cp,
+                                           double* __restrict__ Sc) {
+  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (e >= size_t(m) * m) return;
+  const int a = int(e % m), b = int(e / m);
+  Sc[e] = S[cp[a] + size_t(cp[b]) * n];
+}
+
+// D(:, k0 + r) = sum_t X(:, cperm[k0 + t]) W(t, r) and the eigenvalues of
+// the cluster (ascending, from the FP64 Jacobi of its block).
+__global__ void big_cluster_rotate_kernel(int n, int m, const double* __restrict__ X, const int* __restrict__ cp,
+                                          const double* __restrict__ W, const double* __restrict__ ev,
+                                          double* __restrict__ Dk, double* __restrict__ evk) {
+  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (e >= size_t(n) * m) return;
+  const int row = int(e % n), r = int(e / n);
+  double v = 0.0;
+  for (int t = 0; t < m; ++t) v = fma(X[row + size_t(cp[t]) * n], W[t + size_t(r) * m], v);
+  Dk[row + size_t(r) * n] = v;
+  if (row == 0) evk[r] = ev[r];
 }
 
 // ---------------------------------------------------------------------------
@@ -2153,11 +2262,11 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     // factorisation runs beside the other half's products.  The products
     // leave SMs for it (their CTAs are capped at the SMs the other half's
     // panels do not hold: a panel CTA and a product CTA do not fit one SM).
-    const bool split = c->streamM2 && G >= 32;
+    const bool split = c->streamM2 && G >= 32 && c->tune_groups != 1;
     if (!split) return gj_solve_range(c, 0, G, nb, s, nullptr);
     const int sms = device_sms();
     const int G1 = (G + 1) / 2, G2 = G - G1;
-    TcGridCap cap(std::max(sms - G1, sms / 2));
+    TcGridCap cap(c->tune_cap == 2 ? 0 : c->tune_cap == 1 ? sms / 2 : std::max(sms - G1, sms / 2));
     if ((rc = gj_solve_range(c, 0, G1, nb, s, c->ev_stagger))) return rc;
     TVAP_CUDA(cudaStreamWaitEvent(c->streamM2, c->ev_stagger, 0));
     if ((rc = gj_solve_range(c, G1, G2, nb, c->streamM2, nullptr))) return rc;
@@ -2247,10 +2356,13 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
 // shared-memory stage.
 namespace {
 
-// Refinement steps from the approximate eigenvectors in *X (Xn scratch), the
+// Refinement steps from the approximate eigenvectors in X (Xn scratch), the
 // exact treatment of near-degenerate clusters and the final check; *fail is
-// the check's verdict (read back on the host).
-int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, cudaStream_t s) {
+// the check's verdict (read back on the host) and *Xout the buffer holding
+// the refined columns.  assign: fix the clusters at the first step (else
+// keep those of the previous call); second_order: add F^2/2 to each step.
+int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, cudaStream_t s, bool assign,
+                     bool second_order, double** Xout) {
   Workspace* w = c->ws;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -2267,21 +2379,57 @@ int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, c
     const View Xv = view_cm(X, n, 0);
     if ((rc = gram(X))) return rc;
     refine_lambda_kernel<<<1, kRlThreads, 0, tvap::counted(s)>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
-    refine_update_kernel<<<nblk(nn, 256), 256, 0, tvap::counted(s)>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->Mr);
+    if (step == 0 && assign)
+      cluster_assign_kernel<<<1, kCfThreads, 0, tvap::counted(s)>>>(n, w->Sr, w->lam, w->rscal, w->cid);
+    refine_update_kernel<<<nblk(nn, 256), 256, 0, tvap::counted(s)>>>(n, w->Rr, w->Sr, w->lam, w->rscal, w->cid,
+                                                                      w->Mr, w->Br);
+    if (second_order) {
+      const View Fv = view_cm(w->Br, n, 0);
+      if ((rc = real_gemm(n, n, n, Fv, Fv, w->Mr, n, 0.5, 1.0, s))) return rc;  // M += F^2 / 2
+    }
     if ((rc = real_gemm(n, n, n, Xv, view_cm(w->Mr, n, 0), Xn, n, 1.0, 0.0, s))) return rc;
     std::swap(X, Xn);
   }
   if ((rc = gram(X))) return rc;
   refine_lambda_kernel<<<1, kRlThreads, 0, tvap::counted(s)>>>(n, w->Rr, w->Sr, w->rho, w->lam, w->rscal);
-  cluster_finish_kernel<<<1, kCfThreads, 0, tvap::counted(s)>>>(n, w->Sr, X, w->rscal, w->D, w->evals, w->rflag);
+  cluster_finish_kernel<<<1, kCfThreads, 0, tvap::counted(s)>>>(n, w->Sr, X, w->rscal, w->cid, w->D, w->evals,
+                                                                 w->cperm, w->bigd, w->rflag);
   TVAP_CUDA(cudaGetLastError());
-  int hr[2] = {1, 0};
+  int hr[3] = {1, 0, 0};
+  int bd[2 * kCfBigSlots];
   TVAP_CUDA(cudaMemcpyAsync(hr, w->rflag, sizeof(hr), cudaMemcpyDeviceToHost, s));
+  TVAP_CUDA(cudaMemcpyAsync(bd, w->bigd, sizeof(bd), cudaMemcpyDeviceToHost, s));
   TVAP_CUDA(cudaStreamSynchronize(s));
   *fail = hr[0];
   c->canon_attempts[3] += hr[1];
+  if (hr[0] == 0 && hr[2] > 0) {
+    // the large clusters: the FP64 Jacobi of each block (it starts close to
+    // diagonal: the coupling inside a cluster is that left by the FP32
+    // stage), its eigenvectors rotate the cluster's columns.  w->jac, w->Mr,
+    // w->lam and w->jwork are free here.
+    int nb = 0;
+    for (int b = 0; b < hr[2] && b < kCfBigSlots; ++b, ++nb) {
+      const int k0 = bd[2 * b], m = bd[2 * b + 1];
+      if (k0 < 0 || m < 1 || k0 + m > n) {
+        *fail = 4;  // not a cluster of this basis: the attempt fails
+        break;
+      }
+      big_cluster_extract_kernel<<<nblk(size_t(m) * m, 256), 256, 0, tvap::counted(s)>>>(n, m, w->Sr, w->cperm + k0,
+                                                                                      w->jac);
+      if ((rc = jacobi_eigen(m, w->jac, w->Mr, w->lam, w->jwork, w->rflag + 3, s))) return rc;
+      big_cluster_rotate_kernel<<<nblk(size_t(n) * m, 256), 256, 0, tvap::counted(s)>>>(
+          n, m, X, w->cperm + k0, w->Mr, w->lam, w->D + size_t(k0) * n, w->evals + k0);
+      TVAP_CUDA(cudaGetLastError());
+    }
+    c->canon_attempts[7] += nb;
+    int jf = 0;
+    TVAP_CUDA(cudaMemcpyAsync(&jf, w->rflag + 3, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TVAP_CUDA(cudaStreamSynchronize(s));
+    if (jf) *fail = 4;  // a block's Jacobi did not converge
+  }
   for (int b = 0; b < 3; ++b)
-    if (hr[0] & (1 << b)) ++c->canon_attempts[4 + b];
+    if (*fail & (1 << b)) ++c->canon_attempts[4 + b];
+  *Xout = X;
   return TVAP_OK;
 }
 
@@ -2340,7 +2488,16 @@ int eigen_canonical(tvap_ctx* c, cudaStream_t s) {
         return rc;
       }
       ++c->canon_attempts[0];
-      if ((rc = refine_canonical(c, X, Xn, 3, &fail, s))) return rc;
+      double* Xf = X;
+      if ((rc = refine_canonical(c, X, Xn, 3, &fail, s, true, false, &Xf))) return rc;
+      if (fail && !(fail & 4)) {
+        // not yet orthonormal or decoupled (nearly closed shells: an FP32
+        // start with ||I - X^T X|| ~ 1e-4 and clusters of levels it could not
+        // separate): two second-order steps more from the refined basis,
+        // with the same clusters, before anything is recomputed
+        ++c->canon_attempts[8];
+        if ((rc = refine_canonical(c, Xf, Xf == X ? Xn : X, 2, &fail, s, false, true, &Xf))) return rc;
+      }
     }
     if (!fail) {
       ++c->canon_attempts[1];

@@ -226,7 +226,7 @@ int tvap_get_timeline(tvap_ctx* c, double* t0, double* t1, int nsec) {
 
 int tvap_get_counters(tvap_ctx* c, long long* out, int nout) {
   if (!c || !out) return TVAP_ERR_ARG;
-  for (int i = 0; i < nout && i < 7; ++i) out[i] = c->canon_attempts[i];
+  for (int i = 0; i < nout && i < 9; ++i) out[i] = c->canon_attempts[i];
   return TVAP_OK;
 }
 
@@ -397,6 +397,7 @@ int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, cons
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n, tot = nn * ncol;
@@ -444,6 +445,7 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -464,6 +466,67 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
     if (!is_device_pointer(H20v)) TVAP_CUDA(cudaStreamSynchronize(c->stream));
   }
   return TVAP_OK;
+}
+
+int tvap_set_tuning(tvap_ctx* c, int bn_policy, int solve_groups, int solve_cap) {
+  if (!c || bn_policy < 0 || bn_policy > 2 || solve_groups < 1 || solve_groups > 2 || solve_cap < 0 || solve_cap > 2)
+    return TVAP_ERR_ARG;
+  c->tune_bn = bn_policy;
+  c->tune_groups = solve_groups;
+  c->tune_cap = solve_cap;
+  return TVAP_OK;
+}
+
+int tvap_get_tuning(const tvap_ctx* c, int* knobs) {
+  if (!c || !knobs) return TVAP_ERR_ARG;
+  knobs[0] = c->tune_bn;
+  knobs[1] = c->tune_groups;
+  knobs[2] = c->tune_cap;
+  return TVAP_OK;
+}
+
+int tvap_autotune(tvap_ctx* c, const double* U0, const double* V0, const tvap_proj_opts* opts, int reps,
+                  double* table_ms, int ntable) {
+  if (!c || !U0 || !V0 || !opts || reps < 1) return TVAP_ERR_ARG;
+  if (!c->have_ham) return TVAP_ERR_NOT_READY;
+  struct Cand {
+    int bn, groups, cap;
+  };
+  std::vector<Cand> cands;
+  for (int groups = 2; groups >= 1; --groups)
+    for (int cap = 0; cap < (groups == 2 ? 3 : 1); ++cap)
+      for (int bn = 0; bn < 3; ++bn) cands.push_back({bn, groups, cap});
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  TVAP_CUDA(cudaEventCreate(&e0));
+  TVAP_CUDA(cudaEventCreate(&e1));
+  int rc = TVAP_OK;
+  double best = 1e300;
+  Cand chosen = {c->tune_bn, c->tune_groups, c->tune_cap};
+  tvap_pnp out{};
+  for (size_t k = 0; k < cands.size() && rc == TVAP_OK; ++k) {
+    c->tune_bn = cands[k].bn;
+    c->tune_groups = cands[k].groups;
+    c->tune_cap = cands[k].cap;
+    if ((rc = tvap_project(c, U0, V0, opts, &out, nullptr))) break;  // warm-up (scratch, tables)
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && rc == TVAP_OK; ++r) rc = tvap_project(c, U0, V0, opts, &out, nullptr);
+    cudaEventRecord(e1, c->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = TVAP_ERR_CUDA;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per = double(ms) / reps;
+    if (table_ms && int(k) < ntable) table_ms[k] = per;
+    if (per < best) {
+      best = per;
+      chosen = cands[k];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->tune_bn = chosen.bn;
+  c->tune_groups = chosen.groups;
+  c->tune_cap = chosen.cap;
+  return rc;
 }
 
 int tvap_project_batched(tvap_ctx* c, int nstates, const double* U0s, const double* V0s, const tvap_proj_opts* opts,

@@ -154,6 +154,10 @@ extern thread_local int g_gemm_mode;
 // upper bound on the CTAs of a tcgen05 product (0: one per SM), set while
 // two streams share the SMs with kernels that need their own
 extern thread_local int g_tc_grid_cap;
+// width of the tcgen05 products' B' tiles: 0 the one that pads the output
+// columns less, 1 always 64 rows, 2 always 48 (set by every entry point from
+// its context's tuning)
+extern thread_local int g_tc_bn_policy;
 struct TcGridCap {
   int saved;
   explicit TcGridCap(int cap) : saved(g_tc_grid_cap) { g_tc_grid_cap = cap; }
@@ -278,10 +282,17 @@ struct tvap_ctx {
   size_t scratch_count = 0;
   // canonical bases: [0] FP32 Jacobi + refinement attempts, [1] of them
   // accepted, [2] exact FP64 Jacobi runs, [3] FP32 Jacobi sweeps in total
-  long long canon_attempts[7] = {0, 0, 0, 0, 0, 0, 0};
+  long long canon_attempts[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   // test hook (tvap_test_wait_timeout): the next cooperative evolution has
   // its last CTA leave before the first grid barrier; one-shot
   bool test_skip_arrival = false;
+  // launch shapes chosen by tvap_autotune: B' tile policy (g_tc_bn_policy),
+  // groups of angles in the Thouless solve (2 staggered or 1), and the cap
+  // on the tcgen05 CTAs while the second group's panels run (0: the SMs the
+  // panels leave, 1: half of the SMs, 2: none)
+  int tune_bn = 0;
+  int tune_groups = 2;
+  int tune_cap = 0;
 };
 
 namespace tvap {

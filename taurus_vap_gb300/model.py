@@ -227,7 +227,8 @@ def read_wavefunction_text(path: str, n: int):
 
 
 def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: int,
-                      block: int = 0, mix_isospin: bool = True, zero_pair: int | None = None):
+                      block: int = 0, mix_isospin: bool = True, zero_pair: int | None = None,
+                      v2: np.ndarray | None = None):
     """Random real Bogoliubov seed in the spirit of seed_type 0
     (module_wavefunctions.f90:134-204,250-354,442-547): BCS occupations drawn
     until the particle numbers are reached, then two random orthogonal
@@ -241,7 +242,10 @@ def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: in
     the two columns stay zero: the result is not a Bogoliubov transformation
     (U_phi has two zero rows at every gauge angle), while rho and kappa are
     those of a valid state with that pair empty -- an input for the
-    singular-U_phi failure path.  The random stream is NumPy's, not the Fortran processor's."""
+    singular-U_phi failure path.  ``v2`` (n/2 values: the proton pairs in the
+    basis order, then the neutron pairs) replaces the drawn occupations, e.g.
+    for nearly closed shells.  The random stream is NumPy's, not the Fortran
+    processor's."""
     rng = np.random.default_rng(seed)
     n = basis.n
     v2c = np.zeros(n // 2)
@@ -256,8 +260,11 @@ def random_bogoliubov(basis: Basis, valence_Z: float, valence_N: float, seed: in
         if num > target and target > 0:
             v2c[lo:hi] /= num / target
 
-    fill(0, n // 4, valence_Z)
-    fill(n // 4, n // 2, valence_N)
+    if v2 is None:
+        fill(0, n // 4, valence_Z)
+        fill(n // 4, n // 2, valence_N)
+    else:
+        v2c[:] = np.asarray(v2, dtype=np.float64)
     U = np.zeros((n, n))
     V = np.zeros((n, n))
     ipos = 0

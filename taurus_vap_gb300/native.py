@@ -114,6 +114,12 @@ def lib():
         L.tvap_iterate_many.argtypes = [ci, vp, vp, vp, ctypes.POINTER(TvapProjOpts), vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(TvapPnp), vp, vp]
         L.tvap_iterate_many.restype = ci
+        L.tvap_autotune.argtypes = [vp, vp, vp, ctypes.POINTER(TvapProjOpts), ci, vp, ci]
+        L.tvap_autotune.restype = ci
+        L.tvap_set_tuning.argtypes = [vp, ci, ci, ci]
+        L.tvap_set_tuning.restype = ci
+        L.tvap_get_tuning.argtypes = [vp, vp]
+        L.tvap_get_tuning.restype = ci
         L.tvap_test_wait_timeout.argtypes = [vp]
         L.tvap_test_wait_timeout.restype = ci
         L.tvap_zskpfa_batched.argtypes = [vp, ci, ctypes.c_int64, vp, vp]
@@ -193,10 +199,12 @@ class Context:
     def canonical_paths(self):
         """Canonical-basis counters since the last set_timing: (FP32 Jacobi +
         refinement attempts, accepted, exact FP64 Jacobi runs, FP32 sweeps,
-        rejections for coupled clusters, for lost orthonormality, for too
-        large clusters)."""
-        out = np.zeros(7, dtype=np.int64)
-        _check(lib().tvap_get_counters(self.h, _p(out), 7), "tvap_get_counters")
+        rejections for coupled clusters, for lost orthonormality, for
+        clusters that could not be diagonalised (each failed check counts),
+        large clusters diagonalised by the FP64 Jacobi of their block,
+        refinements continued by two second-order steps)."""
+        out = np.zeros(9, dtype=np.int64)
+        _check(lib().tvap_get_counters(self.h, _p(out), 9), "tvap_get_counters")
         return tuple(int(v) for v in out)
 
     GEMM_FP64, GEMM_MMA_SYNC, GEMM_TCGEN05 = 0, 1, 2
@@ -294,6 +302,27 @@ class Context:
         V1 = np.zeros((n, n), order="F")
         _check(lib().tvap_evolve(self.h, _p(U), _p(V), _p(Zm), _p(U1), _p(V1)), "tvap_evolve")
         return U1, V1
+
+    # -- launch shapes by measurement ------------------------------------------
+    TUNE_CANDIDATES = [(bn, g, cap) for g in (2, 1) for cap in ((0, 1, 2) if g == 2 else (0,)) for bn in (0, 1, 2)]
+
+    def autotune(self, U0, V0, Mphip, Mphin, facpi, valence_Z, valence_N, reps=3):
+        """tvap_autotune: times the projection for every candidate launch
+        shape and keeps the fastest; returns {(bn, groups, cap): ms}."""
+        U, V = _f(U0, np.float64), _f(V0, np.float64)
+        o = TvapProjOpts(Mphip, Mphin, facpi, valence_Z, valence_N, 1.0, 0.0, 0, 0)
+        table = np.zeros(len(self.TUNE_CANDIDATES))
+        _check(lib().tvap_autotune(self.h, _p(U), _p(V), ctypes.byref(o), reps, _p(table), table.size),
+               "tvap_autotune")
+        return dict(zip(self.TUNE_CANDIDATES, table.tolist()))
+
+    def tuning(self):
+        k = np.zeros(3, dtype=np.int32)
+        _check(lib().tvap_get_tuning(self.h, _p(k)), "tvap_get_tuning")
+        return tuple(int(x) for x in k)
+
+    def set_tuning(self, bn_policy, solve_groups, solve_cap):
+        _check(lib().tvap_set_tuning(self.h, bn_policy, solve_groups, solve_cap), "tvap_set_tuning")
 
     # -- adjust_constraints (module_constraints.f90:270-373) -------------------
     def adjust_constraints(self, U0, V0, Zi, constraints_HO, values, cpair=0, eps=1e-6):

@@ -86,6 +86,7 @@ class VAP:
         self._ops = [np.reshape(o, (n, n), order="F") for o in self.cons.ops]
         self.control_NZ = [0] * 5
         self.history = []
+        self.adjust_steps = 0  # evolutions made by the last adjust_constraints (100: the targets were not met)
 
     def _part(self, i):
         return "f20" if i < self.cons.dim - self.cons.npair else "g20"
@@ -114,7 +115,7 @@ class VAP:
         runs here around the context's evolution."""
         c = self.cons.dim
         if hasattr(self.ctx, "adjust_constraints"):
-            U1, V1, Zi, C20, _ = self.ctx.adjust_constraints(
+            U1, V1, Zi, C20, self.adjust_steps = self.ctx.adjust_constraints(
                 self.U0, self.V0, self.Zi, np.stack(self.cons.ops) if c else None, list(self.cons.values),
                 cpair=self.cons.npair, eps=self.cons.eps)
             self.Zi = Zi
@@ -123,8 +124,10 @@ class VAP:
             self.U0, self.V0 = np.asfortranarray(U1), np.asfortranarray(V1)
             return
         U1, V1 = self.U0, self.V0
+        self.adjust_steps = 0
         for _ in range(100):
             U1, V1 = self.ctx.evolve(self.U0, self.V0, self.Zi)
+            self.adjust_steps += 1
             rho = V1 @ V1.T
             kap = V1 @ U1.T
             expec = np.array([expectval_obo(rho, A) if i < c - self.cons.npair else expectval_pair(kap, A)

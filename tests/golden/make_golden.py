@@ -24,7 +24,9 @@ FILES = {
 }
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference project root>")
+    ref = sys.argv[1]
     for src, dst in FILES.items():
         shutil.copyfile(os.path.join(ref, src), os.path.join(HERE, dst))
         print("wrote", dst)

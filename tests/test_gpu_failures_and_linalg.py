@@ -188,13 +188,14 @@ def test_zskpfa_matches_oracle(sd, m):
         assert abs(got[q] ** 2 / (sign * np.exp(logdet)) - 1.0) < 1e-9
 
 
-def test_zskpfa_identities(sd):
+@pytest.mark.parametrize("m", [40, 200])  # the unblocked and the blocked form
+def test_zskpfa_identities(sd, m):
     mdl, _, _ = sd
     ctx = Context(mdl.basis)
     rng = np.random.default_rng(5)
-    A = _skew(rng, 40) / math.sqrt(40)
+    A = _skew(rng, m) / math.sqrt(m)
     # a row/column exchange flips the sign
-    P = np.eye(40)
+    P = np.eye(m)
     P[[3, 29]] = P[[29, 3]]
     B = P @ A @ P.T
     # a zero column (and row): Pf = 0 from the zero pivot, status OK
@@ -202,10 +203,10 @@ def test_zskpfa_identities(sd):
     Z[:, 17] = 0
     Z[17, :] = 0
     # Pf(C A C^T) = det(C) Pf(A)
-    C = np.eye(40) + 0.1 * (rng.normal(size=(40, 40)) + 1j * rng.normal(size=(40, 40)))
+    C = np.eye(m) + (0.1 / math.sqrt(m / 40)) * (rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m)))
     D = C @ A @ C.T
     pa, pb, pz, pd = ctx.zskpfa_batched(np.stack([A, B, Z, D]))
-    assert abs(pb + pa) < 1e-12 * abs(pa)
+    assert abs(pb + pa) < 1e-11 * abs(pa)
     assert pz == 0
     assert abs(pd - np.linalg.det(C) * pa) < 1e-10 * abs(pd)
     # odd order: 0 (A not referenced); order 0: 1
