@@ -843,7 +843,8 @@ constexpr int kJacThreads = 1024;
 
 template <typename T>
 __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, double* evals, double* work,
-                                                             int* flags, double tolfac, double relrot) {
+                                                             int* flags, double tolfac, double relrot,
+                                                             const double* __restrict__ scale) {
   extern __shared__ double jsh[];
   const int m = (n + 1) & ~1;  // even count incl. a dummy index
   double* cs = jsh;                                    // m/2 cosines
@@ -868,7 +869,9 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
   const double fro2 = red[0];
   __syncthreads();
   const double tol2 = fro2 * tolfac;  // converged when off-diagonal^2 <= tolfac ||A||_F^2
-  const double absrot = 0.1 * relrot * sqrt(fro2);
+  // a block of a larger matrix (scale = that matrix's norm) needs no more
+  // than the larger matrix's rounding level
+  const double absrot = fmax(0.1 * relrot * sqrt(fro2), scale ? relrot * *scale : 0.0);
   const int kstep = nt / n;
   const int r0 = (tid < kstep * n) ? tid % n : n;
   const int k0 = (tid < kstep * n) ? tid / n : 0;
@@ -984,10 +987,12 @@ __global__ void __launch_bounds__(kJacThreads) jacobi_kernel(int n, T* A, T* W, 
 
 }  // namespace
 
-int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s) {
+int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s,
+                 const double* scale) {
   const int m = (n + 1) & ~1;
   const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
-  jacobi_kernel<double><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-30, 1.0e-16);
+  jacobi_kernel<double><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-30, 1.0e-16,
+                                                                    scale);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }
@@ -995,7 +1000,7 @@ int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* 
 int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s) {
   const int m = (n + 1) & ~1;
   const size_t shm = sizeof(double) * m + sizeof(int) * 2 * m + 64;
-  jacobi_kernel<float><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-13, 6.0e-8);
+  jacobi_kernel<float><<<1, kJacThreads, shm, tvap::counted(s)>>>(n, A, W, evals, work, flags, 1.0e-13, 6.0e-8, nullptr);
   TVAP_CUDA(cudaGetLastError());
   return TVAP_OK;
 }

@@ -2416,7 +2416,8 @@ int refine_canonical(tvap_ctx* c, double* X, double* Xn, int steps, int* fail, c
       }
       big_cluster_extract_kernel<<<nblk(size_t(m) * m, 256), 256, 0, tvap::counted(s)>>>(n, m, w->Sr, w->cperm + k0,
                                                                                       w->jac);
-      if ((rc = jacobi_eigen(m, w->jac, w->Mr, w->lam, w->jwork, w->rflag + 3, s))) return rc;
+      // ||rho||_F (rscal[1] of the last Gram step) sets the rounding level
+      if ((rc = jacobi_eigen(m, w->jac, w->Mr, w->lam, w->jwork, w->rflag + 3, s, w->rscal + 1))) return rc;
       big_cluster_rotate_kernel<<<nblk(size_t(n) * m, 256), 256, 0, tvap::counted(s)>>>(
           n, m, X, w->cperm + k0, w->Mr, w->lam, w->D + size_t(k0) * n, w->evals + k0);
       TVAP_CUDA(cudaGetLastError());

@@ -342,7 +342,10 @@ int fields_batched(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
 // blocks, stride n*n), Parlett-Reid with the reference's pivoting.
 int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s);
 // symmetric eigen-decomposition by cyclic Jacobi (one matrix), ascending order
-int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s);
+// scale (device, may be null): the norm of the matrix A is a block of; the
+// sweeps stop at that matrix's rounding level
+int jacobi_eigen(int n, double* A, double* W, double* evals, double* work, int* flags, cudaStream_t s,
+                 const double* scale = nullptr);
 // same in FP32 (cold start of the refinement); tolerance ~1e-6.5 ||A||
 int jacobi_eigen_f32(int n, float* A, float* W, double* evals, double* work, int* flags, cudaStream_t s);
 // FP32 Jacobi with A and W in shared memory (n <= 160); W64 gets the unsorted
