@@ -73,6 +73,21 @@ typedef struct {
   int nocc, nemp;
 } tvap_pnp;
 
+/* Gauge sums of project_wavefunction with iopt = 1 (the observables that
+ * print_results prints, src/module_projection.f90:990-1322): the pnp_*
+ * accumulators of sum_gauge (src/module_projection.f90:425-458), complex, not
+ * divided by the overlap.  ener is the projected energy (the reference leaves
+ * rot_ener unset in this mode and prints the sum of ecomp and H0, equal to it
+ * up to rounding); pari = sum of weight x <Phi| P R(phi) |Phi> (rot_pari,
+ * :279-283); ecomp = calculate_decompo_energy's components
+ * (src/module_hamiltonian.f90:1134-1260): 1-body p, n; 2-body PH pp, pn, np,
+ * nn; PP pp, pn, np, nn; energy p, n. */
+typedef struct {
+  double over[2], ener[2], prot[2], neut[2], prot2[2], neut2[2], pari[2];
+  double ecomp[12][2];
+  int nocc, nemp;
+} tvap_pnp_obs;
+
 /* Options of the projection that the reference reads from module globals. */
 typedef struct {
   int Mphip, Mphin;      /* proj_Mphip, proj_Mphin */
@@ -273,6 +288,30 @@ int tvap_iterate_many(int nstates, tvap_ctx* const* ctx, const double* const* U0
                       const tvap_proj_opts* opts, const double* eta, const double* mu, const double* const* Zim1,
                       double* const* Zi, double* const* U1, double* const* V1, tvap_pnp* out,
                       double* gradient_norm, int* status);
+
+/* project_wavefunction(1, 0, Mphip, Mphin, ndim) as print_results calls it
+ * (src/module_projection.f90:1059, the branch :279-354): per gauge angle the
+ * transition densities and fields, then the traces the printed observables
+ * need, summed over the angles with weight x overlap.
+ *   obo:   nobo complex n x n one-body operators B_k (column-major, as the
+ *          reference passes its vectorised tables: Jx, i Jy, Jz, the
+ *          spin-orbit term, the Q_lm, r^2); obo_sum[k] = (proton, neutron)
+ *          sums of Tr(B_k rho^LR) over those rows (calculate_expectval_obo_
+ *          cplx, src/module_operators.f90:146-164), 2 x nobo complex;
+ *   sq:    nsq pairs (O_k, O2_k) of complex n x n matrices, one after the
+ *          other; sq_sum[k] = the sum of <O_k^2> (calculate_expectval_obos_
+ *          cplx, src/module_operators.f90:227-257), nsq complex;
+ *   sp_parity: (-1)^l of each state (host; NULL: no parity overlap, pari 0);
+ *   shell_size: 2j+1 of each of the nshell shells (host); occnum = the
+ *          (proton, neutron) occupations of the shells (calculate_occupation_
+ *          number, src/module_particlenumber.f90:157-176), 2 x nshell complex;
+ *   rho:   pnp_rho, n x n complex (host or device; may be NULL).
+ * All Mphip x Mphin angles are computed (no conjugate folding).  obo and sq
+ * may be host or device arrays; the sums are host arrays. */
+int tvap_project_observables(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts,
+                             int nobo, const double* obo, int nsq, const double* sq, const int32_t* sp_parity,
+                             int nshell, const int32_t* shell_size, tvap_pnp_obs* out, double* obo_sum,
+                             double* sq_sum, double* occnum, double* rho);
 
 /* Launch shapes of the projection, chosen by measurement (no counterpart
  * in the reference).  tvap_autotune times `reps` projections of (U0, V0)

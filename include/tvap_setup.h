@@ -13,6 +13,10 @@
  *   tvs_write_red/     write_/read_hamiltonian_reduced
  *   tvs_read_red       (src/module_hamiltonian.f90:533-627)
  *   tvs_multipoles     set_multipoles (src/module_multipoles.f90:43-128)
+ *   tvs_observable_ops set_angular_momentum (src/module_angularmomentum.f90:33-120),
+ *                      set_radius (src/module_radius.f90:30-63) and the
+ *                      single-particle parities of generate_rotation_parity
+ *                      (src/module_projection.f90:607-625)
  *
  * All index arrays use the reference's values (1-based sp indices in abcd,
  * sp_sh and sp_tr).  Matrices are column-major; complex numbers are pairs of
@@ -47,6 +51,9 @@ void tvs_get_shells(const tvs_model* m, int* sh_na);
 void tvs_get_hamiltonian(const tvs_model* m, double* H0, double* H1, int16_t* abcd, float* h2, int8_t* trperm);
 void tvs_multipoles(const tvs_model* m, double* q);
 void tvs_coeff_betalm(const tvs_model* m, double* out);
+/* ops: 9 * n * n doubles (Jx, Jy, Jz, Jx^2, Jy^2, Jz^2, spin-orbit, r^2 of
+ * protons, r^2 of neutrons; vectorised as the reference's tables); parity: n. */
+void tvs_observable_ops(const tvs_model* m, double* ops, int* parity);
 int tvs_write_red(const tvs_model* m, const char* path);
 int tvs_read_red(tvs_model* m, const char* path);
 double tvs_clebsch(int j1, int j2, int j3, int m1, int m2, int m3);

@@ -74,6 +74,9 @@ def lib():
         L.orc_canonical.restype = ci
         L.orc_project.argtypes = [vp, vp, vp, ci, ci, cd, cd, cd, cd, cd, ci, vp, vp, vp, vp, vp, vp, ci]
         L.orc_project.restype = ci
+        L.orc_project_observables.argtypes = [vp, vp, vp, ci, ci, cd, cd, cd, cd, cd, ci, ci, vp, ci, vp, vp, ci, vp,
+                                              vp, vp, vp, vp, vp, ci]
+        L.orc_project_observables.restype = ci
         L.orc_angle_densities.argtypes = [vp, vp, vp, cd, cd, vp, vp, vp, vp]
         L.orc_angle_densities.restype = ci
         L.orc_overlap.argtypes = [vp, vp, ci, cd, cd, cd, ci, vp]
@@ -161,6 +164,30 @@ class OracleModel:
         if want_angles:
             res["angles"] = angles
         return res
+
+    def project_observables(self, U, V, Mp, Mn, facpi, Z, N, ops, factor_delta=1.0, occeps=0.0, allemp=0,
+                            nthreads=0, with_parity=True):
+        """project_wavefunction with iopt = 1 and its gauge sums: the scalars
+        (over, ener, prot, neut, prot2, neut2, pari, ecomp[12]), the one-body
+        traces (nobo x (p, n)), the <O^2> of the pairs, the occupation
+        numbers (nshell x (p, n)) and pnp_rho.  ops: the dictionary of
+        taurus_vap_gb300.model.Model.observable_operators()."""
+        n = self.n
+        U, V = _cf(U, np.float64), _cf(V, np.float64)
+        obo = np.ascontiguousarray(np.stack([np.asfortranarray(b).ravel(order="F") for b in ops["obo"]]))
+        sq = np.ascontiguousarray(np.stack([np.asfortranarray(b).ravel(order="F") for pr in ops["sq"] for b in pr]))
+        par = np.ascontiguousarray(ops["parity"], dtype=np.int32)
+        shells = np.ascontiguousarray(ops["shell_size"], dtype=np.int32)
+        nobo, nsq, nsh = len(ops["obo"]), len(ops["sq"]), len(shells)
+        scal = np.zeros(19, dtype=np.complex128)
+        bs = np.zeros((nobo, 2), dtype=np.complex128)
+        ss = np.zeros(nsq, dtype=np.complex128)
+        oc = np.zeros((nsh, 2), dtype=np.complex128)
+        rho = np.zeros((n, n), dtype=np.complex128, order="F")
+        st = lib().orc_project_observables(self.h, _p(U), _p(V), Mp, Mn, facpi, Z, N, factor_delta, occeps, allemp,
+                                           nobo, _p(obo), nsq, _p(sq), _p(par) if with_parity else None, nsh,
+                                           _p(shells), _p(scal), _p(bs), _p(ss), _p(oc), _p(rho), nthreads)
+        return {"status": st, "scal": scal, "obo": bs, "sq": ss, "occnum": oc, "rho": rho}
 
 
 def pfaffian(A):

@@ -895,6 +895,188 @@ int orc_project(const orc_model* m, const double* U0, const double* V0, int Mp, 
   return status;
 }
 
+// calculate_decompo_energy (module_hamiltonian.f90:1134-1260): ecomp[0..11] =
+// 1-body p, n; 2-body PH pp, pn, np, nn; PP pp, pn, np, nn; energy p, n
+static void calculate_decompo_energy(const orc_model* m, const Mat& rho, const Mat& kRL, const Mat& gam,
+                                     const Mat& dLR, cplx* ecomp) {
+  const int n = rho.n, h = n / 2;
+  auto blk = [h](const Mat& X, int bi, int bj) {
+    Mat B(h);
+    for (int j = 0; j < h; ++j)
+      for (int i = 0; i < h; ++i) B(i, j) = X(i + bi * h, j + bj * h);
+    return B;
+  };
+  auto tr = [](const Mat& A) {
+    cplx t = 0;
+    for (int i = 0; i < A.n; ++i) t += A(i, i);
+    return t;
+  };
+  Mat A(h);
+  const int pr[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};  // pp, pn, np, nn
+  for (int q = 0; q < 4; ++q) {
+    const int bi = pr[q][0], bj = pr[q][1];
+    // APH_xy = gamma_xy rho_yx; APP_xy = delta_xy kappaRL_xy^T
+    const Mat g = blk(gam, bi, bj), r = blk(rho, bj, bi), d = blk(dLR, bi, bj), k = blk(kRL, bi, bj);
+    zgemm('n', 'n', h, h, h, zone, g.p(), h, r.p(), h, zzero, A.p(), h);
+    ecomp[2 + q] = 0.5 * tr(A);
+    zgemm('n', 't', h, h, h, zone, d.p(), h, k.p(), h, zzero, A.p(), h);
+    ecomp[6 + q] = 0.5 * tr(A);
+  }
+  Mat A1(n), A2(n), A3(n);
+  zgemm('n', 'n', n, n, n, zone, m->H1.p(), n, rho.p(), n, zzero, A1.p(), n);
+  zgemm('n', 'n', n, n, n, zone, gam.p(), n, rho.p(), n, zzero, A2.p(), n);
+  zgemm('n', 't', n, n, n, zone, dLR.p(), n, kRL.p(), n, zzero, A3.p(), n);
+  cplx e1p = 0, e1n = 0, php = 0, phn = 0, ppp = 0, ppn = 0;
+  for (int i = 0; i < h; ++i) {
+    e1p += A1(i, i);
+    e1n += A1(i + h, i + h);
+    php += 0.5 * A2(i, i);
+    phn += 0.5 * A2(i + h, i + h);
+    ppp += 0.5 * A3(i, i);
+    ppn += 0.5 * A3(i + h, i + h);
+  }
+  ecomp[0] = e1p;
+  ecomp[1] = e1n;
+  ecomp[10] = e1p + php + ppp;
+  ecomp[11] = e1n + phn + ppn;
+}
+
+// calculate_expectval_obo_cplx (module_operators.f90:146-164): Tr(B rho) over
+// the proton and the neutron rows of B rho
+static void expectval_obo_cplx(const Mat& rho, const Mat& B, cplx& ep, cplx& en) {
+  const int n = rho.n;
+  Mat A1(n);
+  zgemm('n', 'n', n, n, n, zone, B.p(), n, rho.p(), n, zzero, A1.p(), n);
+  ep = en = zzero;
+  for (int i = 0; i < n / 2; ++i) {
+    ep += A1(i, i);
+    en += A1(i + n / 2, i + n / 2);
+  }
+}
+
+// calculate_expectval_obos_cplx (module_operators.f90:227-257): <O^2>
+static cplx expectval_obos_cplx(const Mat& rho, const Mat& kLR, const Mat& kRL, const Mat& O, const Mat& O2) {
+  const int n = rho.n;
+  Mat A1(n), A2(n), A3(n), A4(n), A5(n), A6(n);
+  zgemm('n', 'n', n, n, n, zone, O.p(), n, rho.p(), n, zzero, A1.p(), n);
+  zgemm('n', 'n', n, n, n, zone, O2.p(), n, rho.p(), n, zzero, A2.p(), n);
+  zgemm('t', 't', n, n, n, zone, O.p(), n, kRL.p(), n, zzero, A3.p(), n);
+  zgemm('n', 'n', n, n, n, zone, O.p(), n, kLR.p(), n, zzero, A4.p(), n);
+  zgemm('n', 'n', n, n, n, zone, A1.p(), n, A1.p(), n, zzero, A5.p(), n);
+  zgemm('n', 'n', n, n, n, zone, A3.p(), n, A4.p(), n, zzero, A6.p(), n);
+  cplx t1 = 0, t2 = 0, t5 = 0, t6 = 0;
+  for (int i = 0; i < n; ++i) {
+    t1 += A1(i, i);
+    t2 += A2(i, i);
+    t5 += A5(i, i);
+    t6 += A6(i, i);
+  }
+  return t1 * t1 + t2 - t5 + t6;
+}
+
+// project_wavefunction with iopt = 1 (module_projection.f90:201-373, the
+// branch :298-354) and sum_gauge with iopt = 1 (:425-458): the gauge sums of
+// the printed observables.  Angles as assign_angles gives them, unfolded.
+// scal (complex): over, ener (the energy of the components: the reference
+// leaves rot_ener stale in this mode and prints the components), prot, neut,
+// prot2, neut2, pari (sum of weight * rot_pari, the overlap with the parity-
+// rotated state, generate_rotation_parity :607-625), ecomp[12]; obo_sum
+// (nobo x 2 complex: protons, neutrons); sq_sum (nsq complex); occnum
+// (nshell x 2 complex, calculate_occupation_number, module_particlenumber.f90:
+// 157-176); rho (n x n complex, pnp_rho).  parity may be null (pari = 0).
+int orc_project_observables(const orc_model* m, const double* U0, const double* V0, int Mp, int Mn, double facpi,
+                            double Z, double N, double factor_delta, double occeps, int allemp, int nobo,
+                            const double* obo, int nsq, const double* sq, const int* parity, int nshell,
+                            const int* shell_size, double* scal, double* obo_sum, double* sq_sum, double* occnum,
+                            double* rho_sum, int nthreads) {
+  const int n = m->n, h = n / 2;
+  const size_t nn = size_t(n) * n;
+  Canon cb;
+  construct_canonical_basis(U0, V0, n, occeps, allemp, cb);
+  if (n - cb.nocc - cb.nemp == 0) cb.ovac = 0.0;
+  voveru_from_canon(cb, n);
+  ProjWork w(n);
+  for (size_t i = 0; i < nn; ++i) {
+    w.zU.v[i] = U0[i] * zone;
+    w.zV.v[i] = V0[i] * zone;
+  }
+  auto mat = [n, nn](const double* p) {
+    Mat M(n);
+    std::memcpy(M.p(), p, sizeof(cplx) * nn);
+    return M;
+  };
+  std::vector<Mat> B, O, O2;
+  for (int k = 0; k < nobo; ++k) B.push_back(mat(obo + 2 * nn * k));
+  for (int k = 0; k < nsq; ++k) {
+    O.push_back(mat(sq + 2 * nn * (2 * k)));
+    O2.push_back(mat(sq + 2 * nn * (2 * k + 1)));
+  }
+  Angles an = assign_angles(Mp, Mn, facpi, Z, N);
+  std::vector<cplx> S(19, zzero), bs(2 * size_t(nobo), zzero), ss(nsq, zzero), oc(2 * size_t(nshell), zzero),
+      rs(nn, zzero);
+  int status = 0;
+  for (size_t g = 0; g < an.php.size(); ++g) {
+    rotation_gauge(an.php[g], an.phn[g], n, w.ROTG);
+    Mat Rc(n);
+    for (size_t i = 0; i < nn; ++i) Rc.v[i] = std::conj(w.ROTG.v[i]);
+    zgemm('n', 'n', n, n, n, zone, w.ROTG.p(), n, w.zU.p(), n, zzero, w.Ubar.p(), n);
+    zgemm('n', 'n', n, n, n, zone, Rc.p(), n, w.zV.p(), n, zzero, w.Vbar.p(), n);
+    cplx rot_over = zone, rot_pari = zzero;
+    if (std::max(Mp, Mn) > 1) {
+      const int st = calculate_overlap(cb, cb, w.ROTG.p(), n, &rot_over);
+      if (st) return st;
+    }
+    const int st = calculate_thouless(w.zU, w.zV, w.Ubar, w.Vbar, w.A, w.Utl, w.Vtl);
+    if (st) status = st;
+    calculate_densities_lr(w.zU, w.zV, w.Utl, w.Vtl, w.rho, w.kLR, w.kRL);
+    if (std::max(Mp, Mn) > 1)
+      calculate_fields(m, w.rho.p(), w.kLR.p(), w.kRL.p(), w.gam.p(), w.hsp.p(), w.dLR.p(), w.dRL.p(), nthreads);
+    else
+      calculate_fields_diag(m, w.rho.p(), w.kLR.p(), w.gam.p(), w.hsp.p(), w.dLR.p(), w.dRL.p(), nthreads);
+    if (parity) {
+      // the parity-rotated gauge rotation P R (module_projection.f90:279-283)
+      Mat RP(n);
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) RP(i, j) = double(parity[i]) * w.ROTG(i, j);
+      const int stp = calculate_overlap(cb, cb, RP.p(), n, &rot_pari);
+      if (stp) return stp;
+    }
+    cplx prot, neut, prot2, neut2;
+    calculate_particle_number(w.rho, w.kLR, w.kRL, prot, neut, prot2, neut2);
+    cplx ec[12];
+    calculate_decompo_energy(m, w.rho, w.kRL, w.gam, w.dLR, ec);
+    const cplx weight = an.wp[g] * an.wn[g];
+    const cplx f1 = weight * rot_over;
+    S[0] += f1;
+    S[1] += (m->H0 + ec[10] + ec[11]) * f1;
+    S[2] += prot * f1;
+    S[3] += neut * f1;
+    S[4] += prot2 * f1;
+    S[5] += neut2 * f1;
+    S[6] += rot_pari * weight;
+    for (int q = 0; q < 12; ++q) S[7 + q] += ec[q] * f1;
+    for (int k = 0; k < nobo; ++k) {
+      cplx ep, en;
+      expectval_obo_cplx(w.rho, B[k], ep, en);
+      bs[2 * k] += ep * f1;
+      bs[2 * k + 1] += en * f1;
+    }
+    for (int k = 0; k < nsq; ++k) ss[k] += expectval_obos_cplx(w.rho, w.kLR, w.kRL, O[k], O2[k]) * f1;
+    for (int t = 0, k = 0; t < nshell; ++t)
+      for (int j = 0; j < shell_size[t]; ++j, ++k) {
+        oc[2 * t] += w.rho(k, k) * f1;
+        oc[2 * t + 1] += w.rho(k + h, k + h) * f1;
+      }
+    for (size_t i = 0; i < nn; ++i) rs[i] += w.rho.v[i] * f1;
+  }
+  std::memcpy(scal, S.data(), sizeof(cplx) * S.size());
+  if (obo_sum) std::memcpy(obo_sum, bs.data(), sizeof(cplx) * bs.size());
+  if (sq_sum) std::memcpy(sq_sum, ss.data(), sizeof(cplx) * ss.size());
+  if (occnum) std::memcpy(occnum, oc.data(), sizeof(cplx) * oc.size());
+  if (rho_sum) std::memcpy(rho_sum, rs.data(), sizeof(cplx) * nn);
+  return status;
+}
+
 // One gauge angle's transition densities (rotation + Thouless + densities),
 // for component parity tests of the field kernel and the density kernels.
 int orc_angle_densities(const orc_model* m, const double* U0, const double* V0, double php, double phn, double* rho,

@@ -143,7 +143,7 @@ int ws_ensure(tvap_ctx* c, int G) {
 #define A_(p, cnt) \
   if ((rc = dalloc(&w->p, (cnt), t)) != TVAP_OK) return rc;
   A_(VU, 2 * nn) A_(rho, nn) A_(kap, nn) A_(jac, nn) A_(D, nn) A_(evals, n) A_(jwork, 2 * n + 2)
-  A_(rhoc, nn) A_(kapc, nn) A_(tmp, nn + n) A_(blocks, 10 * nn) A_(canon_i, 8) A_(canon_d, 8 + n)
+  A_(rhoc, nn) A_(kapc, nn) A_(tmp, nn + n) A_(blocks, 12 * nn) A_(canon_i, 8) A_(canon_d, 8 + n)
   A_(Uphi, nG) A_(Vphi, nG) A_(W, 2 * nG) A_(A, nG) A_(Ut, nG) A_(Vt, nG) A_(X, nG) A_(Y, nG) A_(T, nG)
   A_(Rn, nG) A_(K, nG) A_(SZ, nG) A_(rhoL, nG) A_(kLR, nG) A_(kRL, nG) A_(gam, nG) A_(hsp, nG) A_(dLR, nG)
   A_(dRL, nG) A_(ephase, 2 * G) A_(weight, G) A_(mult, G) A_(obs, 8 * G) A_(pf, 2 * G) A_(detR22, 2 * G)
@@ -2593,14 +2593,18 @@ int prepare_canonical(tvap_ctx* c, double occeps, double allemp_d, int* host_can
 // Overlap chain of angles [0, G) on stream s2 (needs the canonical basis):
 // R_n, Z = R22^{-1} R21 and det R22, the Schur complement S, K = A1^{-1} +
 // S^T C0 S and its Pfaffian.
-int angles_overlap(tvap_ctx* c, int G, const double2* d_ephase, int nocc, int nemp, cudaStream_t s2) {
+// blk: the angle-independent blocks (blocks 8, 9 of it: D_t^T D_t; the
+// parity overlap passes blocks 10, 11 as 8, 9, D_t^T Pi D_t)
+int angles_overlap(tvap_ctx* c, int G, const double2* d_ephase, int nocc, int nemp, cudaStream_t s2,
+                   const double* blk = nullptr) {
   Workspace* w = c->ws;
   const int n = c->n;
   const int tb = 256;
   int rc;
   const int n2 = n - nemp, nb = n2 - nocc;
   sec_begin_on(c, SEC_OVERLAP, s2);
-  build_rn_kernel<<<nblk(size_t(n2) * n2 * G, tb), tb, 0, tvap::counted(s2)>>>(n, n2, G, w->blocks, d_ephase, w->Rn);
+  build_rn_kernel<<<nblk(size_t(n2) * n2 * G, tb), tb, 0, tvap::counted(s2)>>>(n, n2, G, blk ? blk : w->blocks,
+                                                                               d_ephase, w->Rn);
   const double2* S = w->Rn;
   int ldS = n2;
   long long bsS = (long long)n2 * n2;
@@ -2992,6 +2996,374 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out, bool syn
   }
   return check_flags(c);
 }
+
+// ---------------------------------------------------------------------------
+// Observables of the projected state: project_wavefunction with iopt = 1
+// (module_projection.f90:201-373, the branch :279-354) and sum_gauge with
+// iopt = 1 (:425-458).  Per angle: traces of one-body operators with rho^LR
+// over the proton and the neutron rows (calculate_expectval_obo_cplx,
+// module_operators.f90:146-164), the isospin blocks of the energy
+// decomposition (calculate_decompo_energy, module_hamiltonian.f90:1134-1260),
+// <O^2> (calculate_expectval_obos_cplx, module_operators.f90:227-257), the
+// shell occupations (module_particlenumber.f90:157-176), the overlap with the
+// parity-rotated state (generate_rotation_parity, :607-625), and rho^LR;
+// summed with weight x overlap (the parity overlap with the weight alone).
+// All angles are computed (no conjugate folding: an operator need not be
+// real).  FP64 throughout except the <O^2> products (the context's GEMM
+// arithmetic).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kObsRows = 8;       // rows per CTA of the trace kernels
+constexpr int kObsThreads = 128;  // threads over the angles
+
+// part[((ch * nops + k) * 2 + t) * G + b] = sum over the rows i of chunk ch
+// of isospin t of (B_k rho_b)(i, i) = sum_j B_k(i, j) rho_b(j, i)
+__global__ void __launch_bounds__(kObsThreads)
+    obs_trace_kernel(int n, int G, const double2* __restrict__ ops, const double2* __restrict__ rho,
+                     double2* __restrict__ part) {
+  const int k = blockIdx.x, nops = gridDim.x, ch = blockIdx.y, h = n / 2;
+  const double2* B = ops + size_t(k) * n * n;
+  const int b = blockIdx.z * blockDim.x + threadIdx.x;
+  if (b >= G) return;
+  double2 sp = make_double2(0.0, 0.0), sn = make_double2(0.0, 0.0);
+  for (int r = 0; r < kObsRows; ++r) {
+    const int i = ch * kObsRows + r;
+    if (i >= n) break;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int j = 0; j < n; ++j) cfma(acc, B[i + size_t(j) * n], rho[(size_t(j) + size_t(i) * n) * G + b]);
+    if (i < h)
+      sp = cadd(sp, acc);
+    else
+      sn = cadd(sn, acc);
+  }
+  part[((size_t(ch) * nops + k) * 2 + 0) * G + b] = sp;
+  part[((size_t(ch) * nops + k) * 2 + 1) * G + b] = sn;
+}
+
+// part[(ch * 10 + q) * G + b] for the rows i of chunk ch: q = 0..3 PH pp, pn,
+// np, nn = 0.5 sum gamma(i, j) rho(j, i); q = 4..7 PP = 0.5 sum delta(i, j)
+// kappaRL(i, j) (i, j in the blocks' isospins); q = 8, 9 the <O^2> terms
+// sum_j X(i, j) X(j, i) and sum_j Y1(i, j) Y2(i, j) when X is given
+__global__ void __launch_bounds__(kObsThreads)
+    obs_blocks_kernel(int n, int G, const double2* __restrict__ rho, const double2* __restrict__ kRL,
+                      const double2* __restrict__ gam, const double2* __restrict__ dLR,
+                      const double2* __restrict__ X, const double2* __restrict__ Y1, const double2* __restrict__ Y2,
+                      double2* __restrict__ part) {
+  const int ch = blockIdx.x, h = n / 2;
+  const int b = blockIdx.y * blockDim.x + threadIdx.x;
+  if (b >= G) return;
+  auto at = [G, n, b](const double2* A, int i, int j) { return A[(size_t(i) + size_t(j) * n) * G + b]; };
+  double2 a[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) a[q] = make_double2(0.0, 0.0);
+  for (int r = 0; r < kObsRows; ++r) {
+    const int i = ch * kObsRows + r;
+    if (i >= n) break;
+    const int ti = i >= h ? 2 : 0;
+    for (int j = 0; j < n; ++j) {
+      const int q = ti + (j >= h ? 1 : 0);
+      if (gam) {
+        cfma(a[q], at(gam, i, j), at(rho, j, i));
+        cfma(a[4 + q], at(dLR, i, j), at(kRL, i, j));
+      }
+      if (X) {
+        cfma(a[8], at(X, i, j), at(X, j, i));
+        cfma(a[9], at(Y1, i, j), at(Y2, i, j));
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 10; ++q) part[(size_t(ch) * 10 + q) * G + b] = (q < 8) ? cscale(a[q], 0.5) : a[q];
+}
+
+// Q[q * G + b] = sum over the chunks of part[(ch * nq + q) * G + b], in order
+__global__ void obs_chunks_kernel(int G, int nq, int nch, const double2* __restrict__ part, double2* __restrict__ Q) {
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= size_t(nq) * G) return;
+  const int q = int(idx / G), b = int(idx % G);
+  double2 s = make_double2(0.0, 0.0);
+  for (int ch = 0; ch < nch; ++ch) s = cadd(s, part[(size_t(ch) * nq + q) * G + b]);
+  Q[idx] = s;
+}
+
+// the occupation numbers of the shells, Q[(s * 2 + t) * G + b] (shell s holds
+// the states off[s] .. off[s+1]-1 of each isospin)
+__global__ void obs_occ_kernel(int n, int G, int nshell, const int* __restrict__ off, const double2* __restrict__ rho,
+                               double2* __restrict__ Q) {
+  const size_t idx = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (idx >= size_t(nshell) * G) return;
+  const int sh = int(idx / G), b = int(idx % G), h = n / 2;
+  double2 sp = make_double2(0.0, 0.0), sn = make_double2(0.0, 0.0);
+  for (int k = off[sh]; k < off[sh + 1]; ++k) {
+    sp = cadd(sp, rho[(size_t(k) + size_t(k) * n) * G + b]);
+    sn = cadd(sn, rho[(size_t(k + h) + size_t(k + h) * n) * G + b]);
+  }
+  Q[(size_t(sh) * 2 + 0) * G + b] = sp;
+  Q[(size_t(sh) * 2 + 1) * G + b] = sn;
+}
+
+// <O^2> per angle: tr1^2 + tr2 - tr5 + tr6 (tr1, tr2 = the traces of O and
+// O^2 with rho over both isospins; tr5, tr6 from obs_blocks_kernel)
+__global__ void obs_sq_kernel(int G, const double2* __restrict__ t1p, const double2* __restrict__ t2p,
+                              const double2* __restrict__ t56, double2* __restrict__ out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= G) return;
+  const double2 t1 = cadd(t1p[b], t1p[G + b]), t2 = cadd(t2p[b], t2p[G + b]);
+  double2 v = cmul(t1, t1);
+  v = cadd(v, t2);
+  v = cadd(v, cneg(t56[b]));
+  out[b] = cadd(v, t56[G + b]);
+}
+
+// out[q] = sum_b f[b] Q[q * G + b], one warp per q, a fixed-order reduction
+__global__ void obs_sum_kernel(int G, int nq, const double2* __restrict__ Q, const double2* __restrict__ f,
+                               double2* __restrict__ out) {
+  const int q = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int b = lane; b < G; b += 32) cfma(s, f[b], Q[size_t(q) * G + b]);
+  for (int o = 16; o > 0; o >>= 1) {
+    s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+  }
+  if (lane == 0) out[q] = s;
+}
+
+// sum_b weight[b] ov[8 b], one warp, a fixed-order reduction
+__global__ void obs_pari_kernel(int G, const double2* __restrict__ ov, const double2* __restrict__ weight,
+                                double2* __restrict__ out) {
+  const int lane = threadIdx.x;
+  double2 s = make_double2(0.0, 0.0);
+  for (int b = lane; b < G; b += 32) cfma(s, weight[b], ov[8 * size_t(b)]);
+  for (int o = 16; o > 0; o >>= 1) {
+    s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+  }
+  if (lane == 0) *out = s;
+}
+
+// pnp_rho: R(i, j) = sum_b f[b] rho_b(i, j)
+__global__ void obs_rho_kernel(int n, int G, const double2* __restrict__ rho, const double2* __restrict__ f,
+                               double2* __restrict__ R) {
+  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (e >= size_t(n) * n) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int b = 0; b < G; ++b) cfma(s, f[b], rho[e * G + b]);
+  R[e] = s;
+}
+
+// D with its rows scaled by the parities
+__global__ void scale_rows_kernel(int n, const int* __restrict__ par, const double* __restrict__ D,
+                                  double* __restrict__ PD) {
+  const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (e >= size_t(n) * n) return;
+  PD[e] = double(par[e % n]) * D[e];
+}
+
+}  // namespace
+
+// scal: over, ener, prot, neut, prot2, neut2, pari, ecomp[12]; obo_out
+// (nobo x (p, n)), sq_out (nsq), occ_out (nshell x (p, n)): host arrays;
+// rho_out (n x n complex): host or device, may be null.  obo, sq: host or
+// device; parity (may be null), shell_size: host.
+int project_observables_device(tvap_ctx* c, const tvap_proj_opts& o, int nobo, const double* obo, int nsq,
+                               const double* sq, const int* parity, int nshell, const int* shell_size,
+                               double2* scal, double2* obo_out, double2* sq_out, double2* occ_out, double* rho_out,
+                               int* nocc_nemp) {
+  const int n = c->n, h = n / 2;
+  const size_t nn = size_t(n) * n;
+  cudaStream_t s = c->stream;
+  Workspace* w = c->ws;
+  const bool have_overlap = std::max(o.Mphip, o.Mphin) > 1;
+  const AngleTable& t = make_angles(o, false);
+  const int G = int(t.php.size());
+  if (!w || w->G < G) return TVAP_ERR_ARG;
+  int rc;
+  {
+    std::vector<double2> eph(2 * G), wt(G);
+    for (int b = 0; b < G; ++b) {
+      const std::complex<double> I(0.0, 1.0);
+      const std::complex<double> ep = std::exp(I * t.php[b]), en = std::exp(I * t.phn[b]);
+      eph[2 * b] = make_double2(ep.real(), ep.imag());
+      eph[2 * b + 1] = make_double2(en.real(), en.imag());
+      wt[b] = make_double2(t.w[b].real(), t.w[b].imag());
+    }
+    TVAP_CUDA(cudaMemcpyAsync(w->ephase, eph.data(), sizeof(double2) * 2 * G, cudaMemcpyHostToDevice, s));
+    TVAP_CUDA(cudaMemcpyAsync(w->weight, wt.data(), sizeof(double2) * G, cudaMemcpyHostToDevice, s));
+    TVAP_CUDA(cudaMemcpyAsync(w->mult, t.mult.data(), sizeof(double) * G, cudaMemcpyHostToDevice, s));
+    TVAP_CUDA(cudaStreamSynchronize(s));  // the host tables go out of scope
+    w->angles_valid = false;              // the next projection uploads its own
+  }
+  // the trace operators: obo, H1, then O_k and O2_k of the pairs
+  const int ntr = nobo + 1 + 2 * nsq;
+  const int nch = (n + kObsRows - 1) / kObsRows;
+  // Q: 8 energy blocks, 2 per trace operator, nsq <O^2>, 2 per shell
+  const int nq = 8 + 2 * ntr + nsq + 2 * nshell;
+  const size_t part_elems = size_t(nch) * std::max(2 * ntr, 10) * G;
+  double2 *ops = nullptr, *part = nullptr, *Q = nullptr, *sums = nullptr, *obs2 = nullptr, *rsum = nullptr;
+  int *dpar = nullptr, *doff = nullptr;
+  const size_t obs2_elems = 10 * size_t(G);
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&ops), sizeof(double2) * nn * ntr, s));
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&part), sizeof(double2) * part_elems, s));
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&Q), sizeof(double2) * size_t(nq) * G, s));
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sums), sizeof(double2) * (nq + 1), s));
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&obs2), sizeof(double2) * obs2_elems, s));
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&rsum), sizeof(double2) * nn, s));
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dpar), sizeof(int) * n, s));
+  TVAP_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&doff), sizeof(int) * (nshell + 1), s));
+  auto release = [&]() {
+    void* bufs[] = {ops, part, Q, sums, obs2, rsum, dpar, doff};
+    for (void* p : bufs)
+      if (p) cudaFreeAsync(p, s);
+  };
+  auto run = [&]() -> int {
+    int r;
+    for (int k = 0; k < nobo; ++k)
+      if ((r = upload_matrix(obo + 2 * nn * k, ops + nn * k, sizeof(double2) * nn, s))) return r;
+    TVAP_CUDA(cudaMemcpyAsync(ops + nn * nobo, c->d_H1, sizeof(double2) * nn, cudaMemcpyDeviceToDevice, s));
+    for (int k = 0; k < 2 * nsq; ++k)
+      if ((r = upload_matrix(sq + 2 * nn * k, ops + nn * (nobo + 1 + k), sizeof(double2) * nn, s))) return r;
+    std::vector<int> off(nshell + 1, 0);
+    for (int k = 0; k < nshell; ++k) off[k + 1] = off[k] + shell_size[k];
+    if (off[nshell] > h) return TVAP_ERR_ARG;
+    TVAP_CUDA(cudaMemcpyAsync(doff, off.data(), sizeof(int) * (nshell + 1), cudaMemcpyHostToDevice, s));
+    if (parity) TVAP_CUDA(cudaMemcpyAsync(dpar, parity, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    TVAP_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+    // the projection itself (densities, fields, overlaps, traces, sums) on
+    // one stream, then the parity-rotated overlaps
+    int canon[3] = {0, 0, 0};
+    sec_mark(c, s);
+    if ((r = prepare_uv_blocks(c, s))) return r;
+    if ((r = prepare_canonical(c, o.seed_occeps, o.seed_allemp, canon, s))) return r;
+    if (canon[2]) {
+      set_last_error("canonical basis: a degenerate subspace larger than 64 or not reducible to 2 x 2 blocks",
+                     __FILE__, __LINE__);
+      return TVAP_ERR_CANONICAL;
+    }
+    if ((r = angles_thouless(c, G, w->ephase, o.factor_delta, s))) return r;
+    if (have_overlap && (r = angles_overlap(c, G, w->ephase, canon[0], canon[1], s))) return r;
+    if ((r = angles_sums(c, G, w->weight, w->mult, have_overlap, 0, s))) return r;
+    nocc_nemp[0] = canon[0];
+    nocc_nemp[1] = canon[1];
+    const int tb = 256;
+    // Q: the energy blocks (and, per pair, the <O^2> terms)
+    const dim3 gblk(nch, (G + kObsThreads - 1) / kObsThreads);
+    obs_blocks_kernel<<<gblk, kObsThreads, 0, tvap::counted(s)>>>(n, G, w->rhoL, w->kRL, w->gam, w->dLR, nullptr,
+                                                                   nullptr, nullptr, part);
+    obs_chunks_kernel<<<nblk(size_t(10) * G, tb), tb, 0, tvap::counted(s)>>>(G, 10, nch, part, obs2);
+    TVAP_CUDA(cudaMemcpyAsync(Q, obs2, sizeof(double2) * 8 * G, cudaMemcpyDeviceToDevice, s));
+    // the traces of the operators
+    const dim3 gtr(ntr, nch, (G + kObsThreads - 1) / kObsThreads);
+    obs_trace_kernel<<<gtr, kObsThreads, 0, tvap::counted(s)>>>(n, G, ops, w->rhoL, part);
+    obs_chunks_kernel<<<nblk(size_t(2 * ntr) * G, tb), tb, 0, tvap::counted(s)>>>(G, 2 * ntr, nch, part,
+                                                                                   Q + size_t(8) * G);
+    TVAP_CUDA(cudaGetLastError());
+    // <O^2>: X = O rho, Y1 = kappaRL O, Y2 = O kappaLR per angle (angle-innermost)
+    for (int k = 0; k < nsq; ++k) {
+      const double2* Op = ops + nn * (nobo + 1 + 2 * k);
+      const View Ov{Op, 1, n, 0};
+      const View rhoV{w->rhoL, (long long)G, (long long)n * G, 1};
+      GemmArgs g{};
+      g.M = g.N = g.K = n;
+      g.batch = G;
+      g.crs = G;
+      g.ccs = (long long)n * G;
+      g.cbs = 1;
+      g.alpha = make_double2(1.0, 0.0);
+      g.beta = make_double2(0.0, 0.0);
+      g.A = Ov;
+      g.B = rhoV;
+      g.C = w->X;
+      if ((r = gemm(g, s))) return r;
+      g.A = View{w->kRL, (long long)G, (long long)n * G, 1};
+      g.B = Ov;
+      g.C = w->Y;
+      if ((r = gemm(g, s))) return r;
+      g.A = Ov;
+      g.B = View{w->kLR, (long long)G, (long long)n * G, 1};
+      g.C = w->T;
+      if ((r = gemm(g, s))) return r;
+      obs_blocks_kernel<<<gblk, kObsThreads, 0, tvap::counted(s)>>>(n, G, w->rhoL, w->kRL, nullptr, nullptr, w->X,
+                                                                     w->Y, w->T, part);
+      obs_chunks_kernel<<<nblk(size_t(10) * G, tb), tb, 0, tvap::counted(s)>>>(G, 10, nch, part, obs2);
+      const double2* tr = Q + size_t(8) * G;
+      obs_sq_kernel<<<nblk(G, tb), tb, 0, tvap::counted(s)>>>(G, tr + size_t(2 * (nobo + 1 + 2 * k)) * G,
+                                                              tr + size_t(2 * (nobo + 2 + 2 * k)) * G,
+                                                              obs2 + size_t(8) * G,
+                                                              Q + size_t(8 + 2 * ntr + k) * G);
+      TVAP_CUDA(cudaGetLastError());
+    }
+    if (nshell > 0)
+      obs_occ_kernel<<<nblk(size_t(nshell) * G, tb), tb, 0, tvap::counted(s)>>>(
+          n, G, nshell, doff, w->rhoL, Q + size_t(8 + 2 * ntr + nsq) * G);
+    // sums with weight x overlap (coefA of angles_sums), and pnp_rho
+    obs_sum_kernel<<<(nq + 3) / 4, 128, 0, tvap::counted(s)>>>(G, nq, Q, w->coefA, sums);
+    obs_rho_kernel<<<nblk(nn, tb), tb, 0, tvap::counted(s)>>>(n, G, w->rhoL, w->coefA, rsum);
+    TVAP_CUDA(cudaGetLastError());
+    // the overlaps with the parity-rotated state: R_n from the blocks
+    // D_t^T Pi D_t (10, 11), then the overlap chain once more
+    double2 pari = make_double2(0.0, 0.0);
+    if (parity) {
+      scale_rows_kernel<<<nblk(nn, tb), tb, 0, tvap::counted(s)>>>(n, dpar, w->D, w->tmp);
+      GemmArgs g{};
+      g.M = g.N = n;
+      g.K = h;
+      g.batch = 2;
+      g.A = View{w->D, n, 1, h};
+      g.B = View{w->tmp, 1, n, h};
+      g.C = w->blocks + 10 * nn;
+      g.crs = 1;
+      g.ccs = n;
+      g.cbs = (long long)nn;
+      g.alpha = make_double2(1.0, 0.0);
+      g.beta = make_double2(0.0, 0.0);
+      g.a_real = g.b_real = g.c_real = true;
+      if ((r = gemm(g, s))) return r;
+      if ((r = angles_overlap(c, G, w->ephase, canon[0], canon[1], s, w->blocks + 2 * nn))) return r;
+      // the overlap formula into obs2 (8 G), its coefficients into scratch
+      double2* o2 = obs2;
+      TVAP_CUDA(cudaMemsetAsync(o2, 0, sizeof(double2) * 8 * G, s));
+      overlap_finish_kernel<<<nblk(G, tb), tb, 0, tvap::counted(s)>>>(n, G, 1, w->canon_i, w->canon_d, w->pf,
+                                                                     w->detR22, w->weight, w->mult, o2, part,
+                                                                     part + G);
+      // sum_b weight_b rot_pari_b (the overlaps sit at stride 8 in o2)
+      obs_pari_kernel<<<1, 32, 0, tvap::counted(s)>>>(G, o2, w->weight, sums + nq);
+      TVAP_CUDA(cudaGetLastError());
+    }
+    // results
+    std::vector<double2> hs(nq + 1);
+    TVAP_CUDA(cudaMemcpyAsync(hs.data(), sums, sizeof(double2) * (nq + 1), cudaMemcpyDeviceToHost, s));
+    double2 sc6[6];
+    TVAP_CUDA(cudaMemcpyAsync(sc6, w->pscal, sizeof(double2) * 6, cudaMemcpyDeviceToHost, s));
+    if (rho_out && (r = download_matrix(rsum, rho_out, sizeof(double2) * nn, s))) return r;
+    if ((r = check_flags(c))) return r;  // synchronises the stream
+    if (parity) pari = hs[nq];
+    for (int q = 0; q < 6; ++q) scal[q] = sc6[q];
+    scal[6] = pari;
+    const double2* tr = hs.data() + 8;
+    const double2 e1p = tr[2 * nobo], e1n = tr[2 * nobo + 1];
+    scal[7] = e1p;
+    scal[8] = e1n;
+    for (int q = 0; q < 8; ++q) scal[9 + q] = hs[q];
+    // energy_p = 1b_p + PH_pp + PH_pn + PP_pp + PP_pn (and n)
+    scal[17] = cadd(cadd(e1p, cadd(hs[0], hs[1])), cadd(hs[4], hs[5]));
+    scal[18] = cadd(cadd(e1n, cadd(hs[2], hs[3])), cadd(hs[6], hs[7]));
+    for (int k = 0; k < nobo; ++k) {
+      obo_out[2 * k] = tr[2 * k];
+      obo_out[2 * k + 1] = tr[2 * k + 1];
+    }
+    for (int k = 0; k < nsq; ++k) sq_out[k] = hs[8 + 2 * ntr + k];
+    for (int k = 0; k < 2 * nshell; ++k) occ_out[k] = hs[8 + 2 * ntr + nsq + k];
+    return TVAP_OK;
+  };
+  rc = run();
+  release();
+  if (rc == TVAP_OK) TVAP_CUDA(cudaStreamSynchronize(s));
+  return rc;
+}
+
+int observables_angle_count(const tvap_proj_opts& o) { return int(make_angles(o, false).php.size()); }
 
 int ensure_workspace(tvap_ctx* c, int G) { return ws_ensure(c, G); }
 double* ws_U(tvap_ctx* c) { return c->ws->U; }

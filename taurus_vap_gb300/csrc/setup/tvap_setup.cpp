@@ -555,6 +555,33 @@ void tvs_get_hamiltonian(const tvs_model* m, double* H0, double* H1, int16_t* ab
   std::memcpy(trperm, m->trperm.data(), sizeof(int8_t) * m->trperm.size());
 }
 
+// <a| r^lam |b> of the HO radial functions (radial_integral_even,
+// module_basis.f90:374-410: Suhonen's closed form).  For la = lb it equals
+// the Gauss-Laguerre quadrature of radial_integral (module_basis.f90:329-372),
+// which is exact for this polynomial integrand.
+static double radial_integral_even(const tvs_model* m, int ia, int ib, int lam) {
+  const int na = m->sp_n[ia], nb = m->sp_n[ib], la = m->sp_l[ia], lb = m->sp_l[ib];
+  double integral = 0.0;
+  if (((la + lb + lam) % 2) == 0) {
+    const int taua = (lb - la + lam) / 2, taub = (la - lb + lam) / 2;
+    if (taua >= 0 && taub >= 0) {
+      const double pre = (((na + nb) & 1) ? -1.0 : 1.0) *
+                         std::sqrt((factorial_d(na) * factorial_d(nb)) /
+                                   (std::tgamma(na + la + 1.5) * std::tgamma(nb + lb + 1.5))) *
+                         factorial_d(taua) * factorial_d(taub);
+      const int smin = std::max(0, std::max(na - taua, nb - taub));
+      const int smax = std::min(na, nb);
+      double s = 0.0;
+      for (int sg = smin; sg <= smax; ++sg)
+        s += std::tgamma((la + lb + lam) / 2.0 + sg + 1.5) /
+             (factorial_d(sg) * factorial_d(na - sg) * factorial_d(nb - sg) * factorial_d(sg + taua - na) *
+              factorial_d(sg + taub - nb));
+      integral = s * pre * std::pow(m->b, lam);
+    }
+  }
+  return integral;
+}
+
 // Q_lm HO matrix elements for lambda = 1..4 (set_multipoles,
 // module_multipoles.f90:43-128).  Output layout: q[((lam-1)*2 + t)*5 + mq][incr]
 // with incr = ia*n + ib (the reference's vectorised operator, 0-based),
@@ -564,28 +591,7 @@ void tvs_multipoles(const tvs_model* m, double* q) {
   const int n = m->n;
   const size_t n2 = size_t(n) * n;
   std::memset(q, 0, sizeof(double) * 40 * n2);
-  auto radial_even = [&](int ia, int ib, int lam) {
-    const int na = m->sp_n[ia], nb = m->sp_n[ib], la = m->sp_l[ia], lb = m->sp_l[ib];
-    double integral = 0.0;
-    if (((la + lb + lam) % 2) == 0) {
-      const int taua = (lb - la + lam) / 2, taub = (la - lb + lam) / 2;
-      if (taua >= 0 && taub >= 0) {
-        const double pre = (((na + nb) & 1) ? -1.0 : 1.0) *
-                           std::sqrt((factorial_d(na) * factorial_d(nb)) /
-                                     (std::tgamma(na + la + 1.5) * std::tgamma(nb + lb + 1.5))) *
-                           factorial_d(taua) * factorial_d(taub);
-        const int smin = std::max(0, std::max(na - taua, nb - taub));
-        const int smax = std::min(na, nb);
-        double s = 0.0;
-        for (int sg = smin; sg <= smax; ++sg)
-          s += std::tgamma((la + lb + lam) / 2.0 + sg + 1.5) /
-               (factorial_d(sg) * factorial_d(na - sg) * factorial_d(nb - sg) * factorial_d(sg + taua - na) *
-                factorial_d(sg + taub - nb));
-        integral = s * pre * std::pow(m->b, lam);
-      }
-    }
-    return integral;
-  };
+  auto radial_even = [&](int ia, int ib, int lam) { return radial_integral_even(m, ia, ib, lam); };
   size_t incr = 0;
   for (int ia = 0; ia < n; ++ia) {
     const int la = m->sp_l[ia] * 2, ja = m->sp_2j[ia], mja = m->sp_2mj[ia], mta = m->sp_2mt[ia];
@@ -631,6 +637,52 @@ void tvs_coeff_betalm(const tvs_model* m, double* out) {
       const double c2 = 1.0 / (kRadiusR0 * std::pow(np, 1.0 / 3.0));
       out[(i - 1) * 4 + (j - 1)] = c1 * std::pow(c2, j);
     }
+}
+
+// The one-body operators of the printed observables, each n*n in the
+// reference's vectorised layout (incr = ia*n + ib, 0-based):
+//   ops[0..5]  Jx, Jy, Jz, Jx^2, Jy^2, Jz^2 (set_angular_momentum,
+//              module_angularmomentum.f90:33-103: Jy is stored real, the
+//              operator being i Jy);
+//   ops[6]     the spin-orbit l.s factor on the diagonal (:106-119);
+//   ops[7..8]  r^2 for protons, neutrons (set_radius, module_radius.f90:30-63).
+// parity[i] = (-1)^l_i (generate_rotation_parity, module_projection.f90:607-625).
+void tvs_observable_ops(const tvs_model* m, double* ops, int* parity) {
+  const int n = m->n;
+  const size_t n2 = size_t(n) * n;
+  std::memset(ops, 0, sizeof(double) * 9 * n2);
+  size_t incr = 0;
+  for (int ia = 0; ia < n; ++ia) {
+    const int ina = m->sp_n[ia], ila = m->sp_l[ia], ija = m->sp_2j[ia], ima = m->sp_2mj[ia], ita = m->sp_2mt[ia];
+    for (int ib = 0; ib < n; ++ib, ++incr) {
+      const int inb = m->sp_n[ib], ilb = m->sp_l[ib], ijb = m->sp_2j[ib], imb = m->sp_2mj[ib], itb = m->sp_2mt[ib];
+      const double rjb = ijb / 2.0, rmb = imb / 2.0;
+      const double fp1 = rjb * (rjb + 1.0) - rmb * (rmb + 1.0);
+      const double fm1 = rjb * (rjb + 1.0) - rmb * (rmb - 1.0);
+      const double fp1p2 = rjb * (rjb + 1.0) - (rmb + 1.0) * (rmb + 2.0);
+      const double fm1m2 = rjb * (rjb + 1.0) - (rmb - 1.0) * (rmb - 2.0);
+      const double f02 = rjb * (rjb + 1.0) - rmb * rmb;
+      if (ina == inb && ila == ilb && ija == ijb && ita == itb) {
+        const double dp2 = (ima == imb + 4), dp1 = (ima == imb + 2), d0 = (ima == imb), dm1 = (ima == imb - 2),
+                     dm2 = (ima == imb - 4);
+        ops[0 * n2 + incr] = 0.5 * (std::sqrt(fp1) * dp1 + std::sqrt(fm1) * dm1);
+        ops[1 * n2 + incr] = 0.5 * (std::sqrt(fp1) * dp1 - std::sqrt(fm1) * dm1);
+        ops[2 * n2 + incr] = rmb * d0;
+        ops[3 * n2 + incr] = 0.25 * (std::sqrt(fp1 * fp1p2) * dp2 + std::sqrt(fm1 * fm1m2) * dm2 + 2 * f02 * d0);
+        ops[4 * n2 + incr] = 0.25 * (std::sqrt(fp1 * fp1p2) * dp2 + std::sqrt(fm1 * fm1m2) * dm2 - 2 * f02 * d0);
+        ops[5 * n2 + incr] = (rmb * d0) * (rmb * d0);
+      }
+      if (ia == ib) {
+        const double xja = ija / 2.0;
+        ops[6 * n2 + incr] = xja * (xja + 1) - ila * (ila + 1) - 0.75;
+      }
+      if (ija == ijb && ima == imb && ita == itb && ila == ilb) {
+        const int t = (ita + 3) / 2 - 1;
+        ops[size_t(7 + t) * n2 + incr] = radial_integral_even(m, ib, ia, 2);
+      }
+    }
+    parity[ia] = (ila & 1) ? -1 : 1;
+  }
 }
 
 // .red stream file (module_hamiltonian.f90:533-627): name (100 chars),

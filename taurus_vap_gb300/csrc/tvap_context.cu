@@ -66,6 +66,11 @@ int project_device(tvap_ctx* c, const tvap_proj_opts& o, tvap_pnp* out, bool syn
 int ensure_workspace(tvap_ctx* c, int G);
 void destroy_workspace(tvap_ctx* c);
 int angle_count(const tvap_proj_opts& o);
+int observables_angle_count(const tvap_proj_opts& o);
+int project_observables_device(tvap_ctx* c, const tvap_proj_opts& o, int nobo, const double* obo, int nsq,
+                               const double* sq, const int* parity, int nshell, const int* shell_size,
+                               double2* scal, double2* obo_out, double2* sq_out, double2* occ_out, double* rho_out,
+                               int* nocc_nemp);
 int check_flags(tvap_ctx* c);
 double* ws_U(tvap_ctx* c);
 double* ws_V(tvap_ctx* c);
@@ -465,6 +470,59 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
     // a host one is complete on return
     if (!is_device_pointer(H20v)) TVAP_CUDA(cudaStreamSynchronize(c->stream));
   }
+  return TVAP_OK;
+}
+
+int tvap_project_observables(tvap_ctx* c, const double* U0, const double* V0, const tvap_proj_opts* opts, int nobo,
+                             const double* obo, int nsq, const double* sq, const int32_t* sp_parity, int nshell,
+                             const int32_t* shell_size, tvap_pnp_obs* out, double* obo_sum, double* sq_sum,
+                             double* occnum, double* rho) {
+  if (!c || !U0 || !V0 || !opts || !out || opts->Mphip < 1 || opts->Mphin < 1 || nobo < 0 || nsq < 0 ||
+      nshell < 0 || (nobo > 0 && (!obo || !obo_sum)) || (nsq > 0 && (!sq || !sq_sum)) ||
+      (nshell > 0 && (!shell_size || !occnum)))
+    return TVAP_ERR_ARG;
+  if (sp_parity && is_device_pointer(sp_parity)) return TVAP_ERR_ARG;
+  if (shell_size && is_device_pointer(shell_size)) return TVAP_ERR_ARG;
+  for (int k = 0; k < nshell; ++k)
+    if (shell_size[k] < 0) return TVAP_ERR_ARG;
+  if (sp_parity)
+    for (int i = 0; i < c->n; ++i)
+      if (sp_parity[i] != 1 && sp_parity[i] != -1) return TVAP_ERR_ARG;
+  if (!c->have_ham) return TVAP_ERR_NOT_READY;
+  LaunchTally tally(c);
+  g_gemm_mode = c->gemm_mode;
+  g_tc_bn_policy = c->tune_bn;
+  g_dev_flags = c->d_flags;
+  const int n = c->n;
+  const size_t nn = size_t(n) * n;
+  int rc;
+  {
+    const double* mats[2] = {U0, V0};
+    const char* names[2] = {"U0", "V0"};
+    if ((rc = check_finite(c, mats, names, 2, nn))) return rc;
+  }
+  if ((rc = ensure_workspace(c, observables_angle_count(*opts)))) return rc;
+  if ((rc = upload_matrix(U0, ws_U(c), sizeof(double) * nn, c->stream))) return rc;
+  if ((rc = upload_matrix(V0, ws_V(c), sizeof(double) * nn, c->stream))) return rc;
+  std::vector<double2> scal(19), bo(2 * size_t(nobo)), so(static_cast<size_t>(nsq)), oc(2 * size_t(nshell));
+  int nn2[2] = {0, 0};
+  if ((rc = project_observables_device(c, *opts, nobo, obo, nsq, sq, sp_parity, nshell, shell_size, scal.data(),
+                                       bo.data(), so.data(), oc.data(), rho, nn2)))
+    return rc;
+  double* dst[7] = {out->over, out->ener, out->prot, out->neut, out->prot2, out->neut2, out->pari};
+  for (int q = 0; q < 7; ++q) {
+    dst[q][0] = scal[q].x;
+    dst[q][1] = scal[q].y;
+  }
+  for (int q = 0; q < 12; ++q) {
+    out->ecomp[q][0] = scal[7 + q].x;
+    out->ecomp[q][1] = scal[7 + q].y;
+  }
+  out->nocc = nn2[0];
+  out->nemp = nn2[1];
+  if (nobo > 0) std::memcpy(obo_sum, bo.data(), sizeof(double2) * bo.size());
+  if (nsq > 0) std::memcpy(sq_sum, so.data(), sizeof(double2) * so.size());
+  if (nshell > 0) std::memcpy(occnum, oc.data(), sizeof(double2) * oc.size());
   return TVAP_OK;
 }
 

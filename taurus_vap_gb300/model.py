@@ -52,6 +52,7 @@ def _setup_lib():
         L.tvs_get_hamiltonian.argtypes = [vp] * 6
         L.tvs_multipoles.argtypes = [vp, vp]
         L.tvs_coeff_betalm.argtypes = [vp, vp]
+        L.tvs_observable_ops.argtypes = [vp, vp, vp]
         L.tvs_write_red.argtypes = [vp, ctypes.c_char_p]
         L.tvs_write_red.restype = ctypes.c_int
         L.tvs_read_red.argtypes = [vp, ctypes.c_char_p]
@@ -122,6 +123,32 @@ class Model:
         q = np.zeros((4, 2, 5, n * n), dtype=np.float64)
         _setup_lib().tvs_multipoles(self._handle, _ptr(q))
         return q
+
+    def observable_operators(self) -> dict:
+        """The operators whose projected expectation values print_results
+        reports (project_wavefunction with iopt = 1, module_projection.f90:
+        298-354), as complex n x n matrices used the way the reference uses
+        its vectorised tables: ``obo`` (one-body: Jx, i Jy, Jz, spin-orbit,
+        Q_lm for l = 1..4 and m = 0..l with both isospins, r^2), ``sq`` (the
+        pairs (O, O^2) of <J_i^2>: (Jx, Jx^2), (-i Jy, -Jy^2), (Jz, Jz^2)),
+        ``parity`` ((-1)^l per state) and ``shell_size`` (2j + 1 per shell,
+        for the occupation numbers)."""
+        n = self.n
+        ops = np.zeros((9, n * n), dtype=np.float64)
+        par = np.zeros(n, dtype=np.int32)
+        _setup_lib().tvs_observable_ops(self._handle, _ptr(ops), _ptr(par))
+        mat = lambda v: np.reshape(v, (n, n), order="F").astype(np.complex128)
+        q = self.multipoles()
+        names, obo = ["Jx", "Jy", "Jz", "so"], [mat(ops[0]), 1j * mat(ops[1]), mat(ops[2]), mat(ops[6])]
+        for lam in range(1, 5):
+            for mu in range(lam + 1):
+                names.append(f"Q{lam}{mu}")
+                obo.append(mat(q[lam - 1, 0, mu] + q[lam - 1, 1, mu]))
+        names.append("r2")
+        obo.append(mat(ops[7] + ops[8]))
+        sq = [(mat(ops[0]), mat(ops[3])), (-1j * mat(ops[1]), -mat(ops[4])), (mat(ops[2]), mat(ops[5]))]
+        return {"obo_names": names, "obo": np.array(obo), "sq_names": ["Jx2", "Jy2", "Jz2"], "sq": np.array(sq),
+                "parity": par, "shell_size": np.array([s % 100 + 1 for s in self.basis.shells], dtype=np.int32)}
 
     def coeff_betalm(self) -> np.ndarray:
         c = np.zeros((4, 4), dtype=np.float64)

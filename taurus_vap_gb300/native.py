@@ -48,6 +48,15 @@ class TvapPnp(ctypes.Structure):
         return complex(v[0], v[1])
 
 
+class TvapPnpObs(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double * 2) for k in ("over", "ener", "prot", "neut", "prot2", "neut2", "pari")] + [
+        ("ecomp", (ctypes.c_double * 2) * 12), ("nocc", ctypes.c_int), ("nemp", ctypes.c_int)]
+
+    def c(self, k: str) -> complex:
+        v = getattr(self, k)
+        return complex(v[0], v[1])
+
+
 class TvapProjOpts(ctypes.Structure):
     _fields_ = [("Mphip", ctypes.c_int), ("Mphin", ctypes.c_int), ("facpi", ctypes.c_double),
                 ("valence_Z", ctypes.c_double), ("valence_N", ctypes.c_double),
@@ -114,6 +123,9 @@ def lib():
         L.tvap_iterate_many.argtypes = [ci, vp, vp, vp, ctypes.POINTER(TvapProjOpts), vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(TvapPnp), vp, vp]
         L.tvap_iterate_many.restype = ci
+        L.tvap_project_observables.argtypes = [vp, vp, vp, ctypes.POINTER(TvapProjOpts), ci, vp, ci, vp, vp, ci, vp,
+                                               ctypes.POINTER(TvapPnpObs), vp, vp, vp, vp]
+        L.tvap_project_observables.restype = ci
         L.tvap_autotune.argtypes = [vp, vp, vp, ctypes.POINTER(TvapProjOpts), ci, vp, ci]
         L.tvap_autotune.restype = ci
         L.tvap_set_tuning.argtypes = [vp, ci, ci, ci]
@@ -261,6 +273,33 @@ class Context:
         _check(lib().tvap_project(self.h, _p(U), _p(V), ctypes.byref(o), ctypes.byref(out), _p(H20v)),
                "tvap_project")
         return out, H20v
+
+    def project_observables(self, U0, V0, Mphip, Mphin, facpi, valence_Z, valence_N, ops, factor_delta=1.0,
+                            seed_occeps=0.0, seed_allemp=0, with_parity=True):
+        """tvap_project_observables (project_wavefunction with iopt = 1):
+        returns a dict with 'scal' (over, ener, prot, neut, prot2, neut2,
+        pari, ecomp[12]: the complex gauge sums), 'obo' (nobo x (p, n)), 'sq'
+        (nsq), 'occnum' (nshell x (p, n)), 'rho' (pnp_rho, n x n), 'nocc',
+        'nemp'.  ops: taurus_vap_gb300.model.Model.observable_operators()."""
+        n = self.n
+        U, V = _f(U0, np.float64), _f(V0, np.float64)
+        o = TvapProjOpts(Mphip, Mphin, facpi, valence_Z, valence_N, factor_delta, seed_occeps, seed_allemp, 0)
+        obo = np.ascontiguousarray(np.stack([np.asfortranarray(b).ravel(order="F") for b in ops["obo"]]))
+        sq = np.ascontiguousarray(np.stack([np.asfortranarray(b).ravel(order="F") for pr in ops["sq"] for b in pr]))
+        par = np.ascontiguousarray(ops["parity"], dtype=np.int32)
+        shells = np.ascontiguousarray(ops["shell_size"], dtype=np.int32)
+        nobo, nsq, nsh = len(ops["obo"]), len(ops["sq"]), len(shells)
+        out = TvapPnpObs()
+        bs = np.zeros((nobo, 2), dtype=np.complex128)
+        ss = np.zeros(nsq, dtype=np.complex128)
+        oc = np.zeros((nsh, 2), dtype=np.complex128)
+        rho = np.zeros((n, n), dtype=np.complex128, order="F")
+        _check(lib().tvap_project_observables(self.h, _p(U), _p(V), ctypes.byref(o), nobo, _p(obo), nsq, _p(sq),
+                                              _p(par) if with_parity else None, nsh, _p(shells), ctypes.byref(out),
+                                              _p(bs), _p(ss), _p(oc), _p(rho)), "tvap_project_observables")
+        scal = np.array([out.c(k) for k in ("over", "ener", "prot", "neut", "prot2", "neut2", "pari")] +
+                        [complex(out.ecomp[q][0], out.ecomp[q][1]) for q in range(12)])
+        return {"scal": scal, "obo": bs, "sq": ss, "occnum": oc, "rho": rho, "nocc": out.nocc, "nemp": out.nemp}
 
     def project_batched(self, U0s, V0s, opts):
         """tvap_project_batched: states U0s[s], V0s[s] (n x n each) with

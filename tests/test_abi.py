@@ -73,8 +73,8 @@ def test_context_without_a_device_raises():
 
 def test_struct_layouts_match_the_header(tmp_path):
     """The ctypes structures of the binding have the sizes and field offsets
-    of the header's tvap_pnp and tvap_proj_opts (compiled with the host C
-    compiler)."""
+    of the header's tvap_pnp, tvap_pnp_obs and tvap_proj_opts (compiled with
+    the host C compiler)."""
     import shutil
     import subprocess
 
@@ -85,12 +85,15 @@ def test_struct_layouts_match_the_header(tmp_path):
         pytest.skip("no C compiler")
     pnp = [f[0] for f in native.TvapPnp._fields_]
     opts = [f[0] for f in native.TvapProjOpts._fields_]
+    obs = [f[0] for f in native.TvapPnpObs._fields_]
     src = tmp_path / "layout.c"
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tvap.h"', "int main(void) {"]
     lines.append('  printf("pnp %zu\\n", sizeof(tvap_pnp));')
     lines += [f'  printf("pnp.{k} %zu\\n", offsetof(tvap_pnp, {k}));' for k in pnp]
     lines.append('  printf("opts %zu\\n", sizeof(tvap_proj_opts));')
     lines += [f'  printf("opts.{k} %zu\\n", offsetof(tvap_proj_opts, {k}));' for k in opts]
+    lines.append('  printf("obs %zu\\n", sizeof(tvap_pnp_obs));')
+    lines += [f'  printf("obs.{k} %zu\\n", offsetof(tvap_pnp_obs, {k}));' for k in obs]
     lines += ["  return 0;", "}"]
     src.write_text("\n".join(lines) + "\n")
     exe = tmp_path / "layout"
@@ -103,3 +106,6 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert int(got[f"pnp.{k}"]) == getattr(native.TvapPnp, k).offset, k
     for k in opts:
         assert int(got[f"opts.{k}"]) == getattr(native.TvapProjOpts, k).offset, k
+    assert int(got["obs"]) == ctypes.sizeof(native.TvapPnpObs)
+    for k in obs:
+        assert int(got[f"obs.{k}"]) == getattr(native.TvapPnpObs, k).offset, k

@@ -111,3 +111,71 @@ def test_adjoint_formula_against_finite_differences():
     h = 1e-5
     fd = (E(Z + h * D)[0] - E(Z - h * D)[0]) / (2 * h)
     assert abs(fd - (G * D).sum()) < 1e-6 * max(1.0, abs(fd))
+
+
+# ---------------------------------------------------------------------------
+# project_wavefunction with iopt = 1 (the printed observables)
+# ---------------------------------------------------------------------------
+def _obs_state(emax, Z, N, seed):
+    mdl = M.noncore_model(emax, seed=1, valence_Z=Z, valence_N=N)
+    U, V = M.random_bogoliubov(mdl.basis, Z, N, seed=seed)
+    return mdl, U, V
+
+
+def test_observables_unprojected_are_plain_traces():
+    # M = 1: rho^LR = V V^T, the sums are the expectation values; |<P>| is
+    # the Onishi overlap of the state with its parity image (U, V) -> (P U, P V)
+    mdl, U, V = _obs_state(2, 4, 4, seed=3)
+    ops = mdl.observable_operators()
+    om = O.OracleModel(mdl)
+    r = om.project_observables(U, V, 1, 1, 2 * np.pi, 4, 4, ops)
+    assert r["status"] == 0
+    n, h = mdl.n, mdl.n // 2
+    rho = V @ V.T
+    for k, B in enumerate(ops["obo"]):
+        A = B @ rho
+        assert abs(r["obo"][k, 0] - np.trace(A[:h, :h])) < 1e-12 * (1 + np.abs(A).max())
+        assert abs(r["obo"][k, 1] - np.trace(A[h:, h:])) < 1e-12 * (1 + np.abs(A).max())
+    P = np.diag(ops["parity"].astype(float))
+    onishi = np.sqrt(abs(np.linalg.det(U.T @ P @ U + V.T @ P @ V)))
+    assert abs(abs(r["scal"][6]) - onishi) < 1e-10
+    occ = r["occnum"]
+    assert abs(occ[:, 0].sum() - np.trace(rho[:h, :h])) < 1e-12
+    # <J^2> = sum of its components is j-weighted: positive and at least <J>^2
+    J2 = r["sq"].sum().real
+    Jv = r["obo"][:3].sum(axis=1)
+    assert J2 > 0 and J2 >= np.sum(np.abs(Jv) ** 2) - 1e-9
+
+
+@pytest.mark.parametrize("emax,M_", [(0, 5), (2, 5)])
+def test_observables_projected_identities(emax, M_):
+    # the energy of the components equals the projection's energy (two code
+    # paths over the same densities and fields), the shell occupations and
+    # the trace of pnp_rho add up to the proton number, and with only even-l
+    # states (the sd space) the parity-rotated overlaps are the overlaps
+    if emax == 0:
+        mdl = M.sd_model(seed=2)
+        U, V = M.random_bogoliubov(mdl.basis, 4, 4, seed=5)
+        Z = N = 4
+    else:
+        mdl, U, V = _obs_state(emax, 4, 4, seed=3)
+        Z = N = 4
+    ops = mdl.observable_operators()
+    om = O.OracleModel(mdl)
+    r = om.project_observables(U, V, M_, M_, 2 * np.pi, Z, N, ops)
+    ref = om.project(U, V, M_, M_, 2 * np.pi, Z, N)
+    assert r["status"] == 0 and ref["status"] == 0
+    p = ref["pnp"]
+    over = p.c("over")
+    s = r["scal"]
+    assert abs(s[0] - over) < 1e-12 * abs(over)
+    assert abs(s[1] / s[0] - p.c("ener") / over) < 1e-9
+    assert abs(s[2] / s[0] - p.c("prot") / over) < 1e-10
+    h = mdl.n // 2
+    assert abs(r["occnum"][:, 0].sum() - s[2]) < 1e-10 * abs(s[0])
+    assert abs(np.trace(r["rho"][:h, :h]) - s[2]) < 1e-10 * abs(s[0])
+    if np.all(ops["parity"] == 1):
+        assert abs(s[6] - s[0]) < 1e-10 * abs(s[0])
+    # the components: energy_p + energy_n = 1b + PH + PP over the blocks
+    e = s[7:] / s[0]
+    assert abs(e[10] + e[11] - (e[0] + e[1] + e[2:6].sum() + e[6:10].sum())) < 1e-9
