@@ -247,8 +247,9 @@ def run_ours(args):
     autotune = None
     if not args.no_autotune:
         tune_table = ctx.autotune(U, V, MPHI, MPHI, 2 * math.pi, ZV, NV, reps=3)
-        autotune = {"chosen": dict(zip(("bn_policy", "solve_groups", "solve_cap"), ctx.tuning())),
-                    "ms_per_projection": {f"bn{b}_g{g}_cap{c}": round(v, 4) for (b, g, c), v in tune_table.items()}}
+        autotune = {"chosen": dict(zip(("bn_policy", "solve_groups", "solve_cap", "lookahead"), ctx.tuning())),
+                    "ms_per_projection": {f"bn{b}_g{g}_cap{c}_la{a}": round(v, 4)
+                                          for (b, g, c, a), v in tune_table.items()}}
 
     # ---- device-resident value (batched form)
     it = DeviceIteration(ctx, U, V, 0, torch)
@@ -341,6 +342,9 @@ def run_ours(args):
     # ---- the adjoint of E(Z) (tvap_energy_adjoint) at the workload's seed
     # and a random skew Thouless matrix with entries ~ N(0, 0.1)
     adjoint = adjoint_timing(ctx, U, V, torch, stream)
+
+    # ---- the observables of print_results (tvap_project_observables)
+    observables = observables_leg(ctx, mdl, U, V, args) if rank == 0 else None
 
     # ---- roofline of the dominant kernel, from the live section timings.
     # The dominant kernel (launch list in profiles/) is the tcgen05 product
@@ -440,7 +444,8 @@ def run_ours(args):
         "timeline_ms": {k: [round(a, 3), round(b, 3)] for k, (a, b) in timeline.items() if sections[k][1]},
         "longest_section": longest[0], "canonical_paths": canon_paths, "plain_gpu": plain, "fp64_pipe_gemm": fp64_pipe, "cpu_baseline": cpu,
         "final_energy": it.energy, "iterations_from_seed": args.warmup + args.steps,
-        "adjoint": adjoint, "parity": parity, "emax6": emax6, "many_seeds": seeds, "constraint_sweep": sweep,
+        "adjoint": adjoint, "parity": parity, "observables": observables, "emax6": emax6, "many_seeds": seeds,
+        "constraint_sweep": sweep,
         "autotune": autotune,
     }
     if rank == 0:
@@ -768,6 +773,39 @@ def emax6_leg(torch, peaks, hbm_peak, steps=3):
     }
     ctx.close()
     return res
+
+
+def observables_leg(ctx, mdl, U, V, args, calls=3):
+    """tvap_project_observables at the workload (project_wavefunction with
+    iopt = 1, all 225 angle pairs: energy decomposition, J, J^2, spin-orbit,
+    Q_lm, r^2, shell occupations, parity overlap, pnp_rho), host perf_counter
+    around `calls` calls after one warm-up (host operator tables, host
+    results); parity: the oracle's restatement of the same branch, every sum
+    divided by the overlap."""
+    import numpy as np
+
+    ops = mdl.observable_operators()
+    args_p = (MPHI, MPHI, 2 * math.pi, ZV, NV, ops)
+    ctx.project_observables(U, V, *args_p)
+    t = time.perf_counter()
+    for _ in range(calls):
+        got = ctx.project_observables(U, V, *args_p)
+    ms = 1000.0 * (time.perf_counter() - t) / calls
+    out = {"ms_per_call": ms, "calls": calls, "angle_pairs": MPHI * MPHI,
+           "operators": {"one_body": len(ops["obo"]), "squared": len(ops["sq"]), "shells": len(ops["shell_size"])},
+           "timer": "host perf_counter around each call (host buffers)"}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        ref = O.OracleModel(mdl).project_observables(U, V, *args_p)
+        og, orr = got["scal"][0], ref["scal"][0]
+        dev = 0.0
+        for k in ("scal", "obo", "sq", "occnum"):
+            x, y = np.asarray(got[k]) / og, np.asarray(ref[k]) / orr
+            dev = max(dev, float(np.max(np.abs(x - y) / (1.0 + np.abs(y)))))
+        out["parity"] = {"max_rel_dev": dev, "what": "every gauge sum divided by the overlap, against the oracle"}
+    return out
 
 
 def adjoint_timing(ctx, U, V, torch, stream, calls=5):

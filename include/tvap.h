@@ -319,17 +319,24 @@ int tvap_project_observables(tvap_ctx* ctx, const double* U0, const double* V0, 
  * the width that pads the output columns less, 1: 64 rows, 2: 48 rows) x the
  * groups of angles in the Thouless solve (2 staggered on two streams, or 1)
  * x the cap on the tcgen05 CTAs beside the second group's panels (0: the
- * SMs the panels leave, 1: half the SMs, 2: none; 2 groups only) -- 12
+ * SMs the panels leave, 1: half the SMs, 2: none; 2 groups only) x the
+ * look-ahead of the solve's panels (the bulk of each elimination product on
+ * a stream of its own while the next panel is factored: on, off) -- 24
  * candidates, CUDA events on the context's stream, and keeps the fastest in
  * the context.  table_ms (may be NULL) receives the ms per projection of the
- * first ntable candidates in the order groups 2 (cap 0, 1, 2), then groups
- * 1, each with bn 0, 1, 2.  Results do not depend on the choice (the same
- * FP64 emulation; only tile and launch shapes change).  tvap_set_tuning and
- * tvap_get_tuning (knobs[3] = bn, groups, cap) set and read them. */
+ * first ntable candidates in the order look-ahead on, then off, each with
+ * groups 2 (cap 0, 1, 2), then groups 1, each with bn 0, 1, 2.  Results do
+ * not depend on the choice (the same FP64 emulation and the same arithmetic
+ * in every product; only tile and launch shapes and their order change).
+ * tvap_set_tuning and tvap_get_tuning (knobs[3] = bn, groups, cap),
+ * tvap_set_lookahead and tvap_get_lookahead (1 on, 0 off; off unless set
+ * or chosen by the tuner) set and read them. */
 int tvap_autotune(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts, int reps,
                   double* table_ms, int ntable);
 int tvap_set_tuning(tvap_ctx* ctx, int bn_policy, int solve_groups, int solve_cap);
 int tvap_get_tuning(const tvap_ctx* ctx, int* knobs);
+int tvap_set_lookahead(tvap_ctx* ctx, int on);
+int tvap_get_lookahead(const tvap_ctx* ctx);
 
 /* Test hook, no counterpart in the reference: the next tvap_evolve on this
  * context runs its cooperative launch with one CTA that leaves before the

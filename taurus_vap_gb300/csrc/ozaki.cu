@@ -452,7 +452,7 @@ struct OzScratch {
   int* counter = nullptr;  // tile counter of the tcgen05 kernel
   LeftSlice left;          // what buf / ex hold at their start
 };
-constexpr int kMaxScratch = 128;  // streams with scratch at once (five per context)
+constexpr int kMaxScratch = 192;  // streams with scratch at once (seven per context)
 OzScratch g_oz[kMaxScratch];
 std::mutex g_oz_mutex;
 

@@ -2122,7 +2122,14 @@ int real_gemm(int M, int N, int K, View A, View B, double* C, int ldc, double al
 // Gauss-Jordan solve of angles [g0, g0 + gc) on stream s (panels of nb
 // columns); ev_first, when given, is recorded after the first panel's
 // factorisation.  build_augmented_kernel has filled W.
-int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEvent_t ev_first) {
+// sb (may be null): a stream for the look-ahead -- the elimination product
+// of panel k splits into the next panel's columns (on s, so that panel k+1 is
+// factored right after them) and the rest (on sb, beside that factorisation;
+// ev_ready / ev_bulk order the two streams), and the row interchanges of
+// panel k+1 wait for the rest.  Panel k+1 writes only its own columns, the
+// rest only the columns right of them.
+int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEvent_t ev_first,
+                   cudaStream_t sb = nullptr, cudaEvent_t ev_ready = nullptr, cudaEvent_t ev_bulk = nullptr) {
   Workspace* w = c->ws;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -2153,6 +2160,9 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
         return TVAP_ERR_ARG;
     }
     if (j0 == 0 && ev_first) TVAP_CUDA(cudaEventRecord(ev_first, s));
+    // the bulk of the previous elimination product must be done before the
+    // interchanges touch its columns
+    if (sb && j0 > 0) TVAP_CUDA(cudaStreamWaitEvent(s, ev_bulk, 0));
     if (j1 < 2 * n) {
       if (n - j0 <= kPermMaxRows) {
         dim3 gp((2 * n - j1 + kPermCols - 1) / kPermCols, gc);
@@ -2196,6 +2206,19 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
     g.alpha = make_double2(-1.0, 0.0);
     g.beta = make_double2(1.0, 0.0);
     g.three_m = true;
+    const int j2 = j1 + std::min(nb, n - j1);  // the next panel's columns end
+    if (sb && j1 < n) {
+      // look-ahead: columns j2 .. 2n-1 on sb, then j1 .. j2-1 on s
+      TVAP_CUDA(cudaEventRecord(ev_ready, s));
+      TVAP_CUDA(cudaStreamWaitEvent(sb, ev_ready, 0));
+      GemmArgs gb = g;
+      gb.N = 2 * n - j2;
+      gb.B = View{W + j0 + size_t(j2) * n, 1, n, bsW};
+      gb.C = W + size_t(j2) * n;
+      if ((rc = gemm(gb, sb))) return rc;
+      TVAP_CUDA(cudaEventRecord(ev_bulk, sb));
+      g.N = j2 - j1;
+    }
     if ((rc = gemm(g, s))) return rc;
   }
   const size_t tot = nn * gc;
@@ -2263,13 +2286,19 @@ int blocked_thouless_solve(tvap_ctx* c, int G, cudaStream_t s) {
     // leave SMs for it (their CTAs are capped at the SMs the other half's
     // panels do not hold: a panel CTA and a product CTA do not fit one SM).
     const bool split = c->streamM2 && G >= 32 && c->tune_groups != 1;
-    if (!split) return gj_solve_range(c, 0, G, nb, s, nullptr);
+    const bool la = c->tune_lookahead != 0;
+    if (!split)
+      return gj_solve_range(c, 0, G, nb, s, nullptr, la ? c->streamB[0] : nullptr, c->ev_la[0][0], c->ev_la[0][1]);
     const int sms = device_sms();
     const int G1 = (G + 1) / 2, G2 = G - G1;
     TcGridCap cap(c->tune_cap == 2 ? 0 : c->tune_cap == 1 ? sms / 2 : std::max(sms - G1, sms / 2));
-    if ((rc = gj_solve_range(c, 0, G1, nb, s, c->ev_stagger))) return rc;
+    if ((rc = gj_solve_range(c, 0, G1, nb, s, c->ev_stagger, la ? c->streamB[0] : nullptr, c->ev_la[0][0],
+                             c->ev_la[0][1])))
+      return rc;
     TVAP_CUDA(cudaStreamWaitEvent(c->streamM2, c->ev_stagger, 0));
-    if ((rc = gj_solve_range(c, G1, G2, nb, c->streamM2, nullptr))) return rc;
+    if ((rc = gj_solve_range(c, G1, G2, nb, c->streamM2, nullptr, la ? c->streamB[1] : nullptr, c->ev_la[1][0],
+                             c->ev_la[1][1])))
+      return rc;
     TVAP_CUDA(cudaEventRecord(c->ev_join2, c->streamM2));
     TVAP_CUDA(cudaStreamWaitEvent(s, c->ev_join2, 0));
     return TVAP_OK;

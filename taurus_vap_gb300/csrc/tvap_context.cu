@@ -283,6 +283,12 @@ int tvap_init(tvap_ctx** ctx, int64_t n, const int32_t* sp_2mj, const int32_t* s
     return fail(e);
   if ((e = cudaStreamCreateWithPriority(&c->streamM2, cudaStreamNonBlocking, prio_mid)) != cudaSuccess)
     return fail(e);
+  for (int q = 0; q < 2; ++q) {
+    if ((e = cudaStreamCreateWithPriority(&c->streamB[q], cudaStreamNonBlocking, prio_lo)) != cudaSuccess)
+      return fail(e);
+    for (int r = 0; r < 2; ++r)
+      if ((e = cudaEventCreateWithFlags(&c->ev_la[q][r], cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  }
   if ((e = cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&c->ev_stagger, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaMallocHost(&c->h_pin, kPinnedBytes)) != cudaSuccess) return fail(e);
@@ -313,6 +319,8 @@ void tvap_destroy(tvap_ctx* c) {
   if (c->stream3) cudaStreamSynchronize(c->stream3);
   if (c->streamM) cudaStreamSynchronize(c->streamM);
   if (c->streamM2) cudaStreamSynchronize(c->streamM2);
+  for (auto sb : c->streamB)
+    if (sb) cudaStreamSynchronize(sb);
   cudaFree(c->scratch);
   destroy_workspace(c);
   free_field_csr(c->csr);
@@ -335,6 +343,14 @@ void tvap_destroy(tvap_ctx* c) {
   if (c->stream3) oz_release(c->stream3);
   if (c->streamM) oz_release(c->streamM);
   if (c->streamM2) oz_release(c->streamM2);
+  for (auto sb : c->streamB)
+    if (sb) {
+      oz_release(sb);
+      cudaStreamDestroy(sb);
+    }
+  for (auto& q : c->ev_la)
+    for (auto ev : q)
+      if (ev) cudaEventDestroy(ev);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->stream3) cudaStreamDestroy(c->stream3);
@@ -535,6 +551,14 @@ int tvap_set_tuning(tvap_ctx* c, int bn_policy, int solve_groups, int solve_cap)
   return TVAP_OK;
 }
 
+int tvap_set_lookahead(tvap_ctx* c, int on) {
+  if (!c || on < 0 || on > 1) return TVAP_ERR_ARG;
+  c->tune_lookahead = on;
+  return TVAP_OK;
+}
+
+int tvap_get_lookahead(const tvap_ctx* c) { return c ? c->tune_lookahead : -1; }
+
 int tvap_get_tuning(const tvap_ctx* c, int* knobs) {
   if (!c || !knobs) return TVAP_ERR_ARG;
   knobs[0] = c->tune_bn;
@@ -548,23 +572,25 @@ int tvap_autotune(tvap_ctx* c, const double* U0, const double* V0, const tvap_pr
   if (!c || !U0 || !V0 || !opts || reps < 1) return TVAP_ERR_ARG;
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   struct Cand {
-    int bn, groups, cap;
+    int bn, groups, cap, la;
   };
   std::vector<Cand> cands;
-  for (int groups = 2; groups >= 1; --groups)
-    for (int cap = 0; cap < (groups == 2 ? 3 : 1); ++cap)
-      for (int bn = 0; bn < 3; ++bn) cands.push_back({bn, groups, cap});
+  for (int la = 1; la >= 0; --la)
+    for (int groups = 2; groups >= 1; --groups)
+      for (int cap = 0; cap < (groups == 2 ? 3 : 1); ++cap)
+        for (int bn = 0; bn < 3; ++bn) cands.push_back({bn, groups, cap, la});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   TVAP_CUDA(cudaEventCreate(&e0));
   TVAP_CUDA(cudaEventCreate(&e1));
   int rc = TVAP_OK;
   double best = 1e300;
-  Cand chosen = {c->tune_bn, c->tune_groups, c->tune_cap};
+  Cand chosen = {c->tune_bn, c->tune_groups, c->tune_cap, c->tune_lookahead};
   tvap_pnp out{};
   for (size_t k = 0; k < cands.size() && rc == TVAP_OK; ++k) {
     c->tune_bn = cands[k].bn;
     c->tune_groups = cands[k].groups;
     c->tune_cap = cands[k].cap;
+    c->tune_lookahead = cands[k].la;
     if ((rc = tvap_project(c, U0, V0, opts, &out, nullptr))) break;  // warm-up (scratch, tables)
     cudaEventRecord(e0, c->stream);
     for (int r = 0; r < reps && rc == TVAP_OK; ++r) rc = tvap_project(c, U0, V0, opts, &out, nullptr);
@@ -584,6 +610,7 @@ int tvap_autotune(tvap_ctx* c, const double* U0, const double* V0, const tvap_pr
   c->tune_bn = chosen.bn;
   c->tune_groups = chosen.groups;
   c->tune_cap = chosen.cap;
+  c->tune_lookahead = chosen.la;
   return rc;
 }
 

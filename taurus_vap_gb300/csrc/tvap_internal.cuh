@@ -262,6 +262,11 @@ struct tvap_ctx {
   cudaStream_t streamM2 = nullptr;  // second half of the angles in the Thouless solve (same priority)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_canon = nullptr, ev_main = nullptr;
   cudaEvent_t ev_stagger = nullptr, ev_join2 = nullptr;  // the two halves of the Thouless solve
+  // look-ahead of the Thouless solve, per half: the bulk of each elimination
+  // product on its own stream (lowest priority) while the next panel is
+  // factored; ev_la[h][0] = the block row is ready, [1] = the bulk is done
+  cudaStream_t streamB[2] = {nullptr, nullptr};
+  cudaEvent_t ev_la[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   void* h_pin = nullptr;  // pinned host buffer (kPinnedBytes) for the status word and small results
   tvap::Workspace* ws = nullptr;
   int* d_flags = nullptr;  // device status word
@@ -293,6 +298,7 @@ struct tvap_ctx {
   int tune_bn = 0;
   int tune_groups = 2;
   int tune_cap = 0;
+  int tune_lookahead = 0;  // look-ahead of the Thouless solve's panels (streamB)
 };
 
 namespace tvap {
