@@ -55,6 +55,20 @@ def test_calculate_fields(case, request):
         assert relerr(g, r) < FIELD_TOL, name
 
 
+@pytest.mark.parametrize("case", ["sd", "emax2", "emax4"])
+def test_calculate_fields_of_a_real_state_is_fields_diag(case, request):
+    # calculate_fields_diag (module_fields.f90:204-317) is the L = R case:
+    # the device's general contraction with kappa^RL = kappa^LR = V U^T and
+    # rho = V V^T against the oracle's restatement of calculate_fields_diag
+    mdl, U, V = request.getfixturevalue(case)
+    rho = (V @ V.T).astype(complex)
+    kap = (V @ U.T).astype(complex)
+    ref = O.OracleModel(mdl).calculate_fields_diag(rho, kap, nthreads=1)
+    got = Context(mdl.basis, mdl.ham).calculate_fields(rho, kap, kap)
+    for g, r, name in zip(got, ref, ("gamma", "h", "deltaLR", "deltaRL")):
+        assert relerr(g, r) < FIELD_TOL, name
+
+
 def test_calculate_fields_edge_cases(sd):
     mdl, U, V = sd
     ctx = Context(mdl.basis, mdl.ham)

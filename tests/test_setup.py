@@ -91,3 +91,49 @@ def test_multipoles_symmetric(usdb_model):
         for t in range(2):
             Q = q[lam, t, 0].reshape(n, n)
             assert np.allclose(Q, Q.T, atol=1e-12)
+
+
+def test_synthetic_emax4_is_hermitian():
+    # the same field check on the emax=4 list of the benchmark (n = 140)
+    mdl = M.noncore_model(4, seed=1)
+    n = mdl.n
+    import oracle as O
+    om = O.OracleModel(mdl)
+    rng = np.random.default_rng(1)
+    A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    rho = A + A.conj().T
+    K = rng.normal(size=(n, n)); K = K - K.T
+    g, h, dl, dr = om.calculate_fields(rho, K, K)
+    assert np.allclose(g, g.conj().T, atol=1e-12 * abs(g).max())
+
+
+@pytest.mark.parametrize("emax", [2, 4])
+def test_synthetic_interaction_is_rotation_and_isospin_invariant(emax):
+    # the JT-coupled synthetic interaction is a scalar in angular momentum and
+    # isospin: the HFB energy (M = 1) of a state equals that of the state
+    # rotated about y, c' = exp(beta Jy) c with the real antisymmetric table
+    # of i Jy (set_angular_momentum), and that of the state with protons and
+    # neutrons exchanged
+    from scipy.linalg import expm
+
+    import oracle as O
+    mdl = M.noncore_model(emax, seed=1, valence_Z=4, valence_N=4)
+    n, h = mdl.n, mdl.n // 2
+    U, V = M.random_bogoliubov(mdl.basis, 4, 4, seed=7)
+    om = O.OracleModel(mdl)
+
+    def energy(U_, V_):
+        r = om.project(U_, V_, 1, 1, 2 * np.pi, 4, 4)
+        assert r["status"] == 0
+        p = r["pnp"]
+        return (p.c("ener") / p.c("over")).real
+
+    e0 = energy(U, V)
+    Jy = np.imag(mdl.observable_operators()["obo"][1])  # the real table: the operator is i Jy
+    D = expm(0.7 * Jy)
+    assert np.allclose(D.T @ D, np.eye(n), atol=1e-12)
+    assert abs(energy(D @ U, D @ V) - e0) < 1e-9 * (1 + abs(e0))
+    P = np.zeros((n, n))
+    P[np.arange(h), np.arange(h) + h] = 1.0
+    P[np.arange(h) + h, np.arange(h)] = 1.0
+    assert abs(energy(P @ U, P @ V) - e0) < 1e-9 * (1 + abs(e0))
