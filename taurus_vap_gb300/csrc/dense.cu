@@ -1455,8 +1455,9 @@ __device__ bool coop_factor_diag_warp(int n, double* S, double* rd, int j0, int 
 __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, double* S, const double* A,
                                                                        long long a_stride, double* X,
                                                                        long long x_stride, unsigned* bar,
-                                                                       int* flags, int skip_cta) {
-  extern __shared__ double coop_smem[];  // the panel rows; then L (n x n) and 1 / L_jj in the solve phase
+                                                                       int* flags, int skip_cta, int l_smem) {
+  // the panel rows; then, in the solve phase, L (n x n, when l_smem) and 1 / L_jj
+  extern __shared__ double coop_smem[];
   __shared__ double L11[kCoopNb][kCoopNb + 1];
   __shared__ double rdiag[kCoopNb];
   __shared__ unsigned gen_s;
@@ -1552,10 +1553,14 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
   const int warps = blockDim.x >> 5, warp = t >> 5, lane = t & 31;
   const int rows = 2 * n;
   if (cta >= rows) return;
+  // L from shared memory when it fits (n <= 168), else from L2 (S is
+  // written by this grid before the last barrier: read through L2, not L1)
   double* Ls = coop_smem;
-  double* dinv = Ls + size_t(n) * n;
+  double* dinv = l_smem ? Ls + size_t(n) * n : coop_smem;
+  if (l_smem) {
 #pragma unroll 8
-  for (int idx = t; idx < n * n; idx += blockDim.x) Ls[idx] = __ldcg(&S[idx]);
+    for (int idx = t; idx < n * n; idx += blockDim.x) Ls[idx] = __ldcg(&S[idx]);
+  }
   __syncthreads();
   for (int j = t; j < n; j += blockDim.x) dinv[j] = __ldcg(&rd[j]);
   __syncthreads();
@@ -1582,11 +1587,20 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
         for (int q = 0; q < kMaxPerLane; ++q)
           if (q == qj) v[q] = xj;
       }
-      const double* lc = Ls + size_t(j) * n;
+      if (l_smem) {
+        const double* lc = Ls + size_t(j) * n;
 #pragma unroll
-      for (int q = 0; q < kMaxPerLane; ++q) {
-        const int jj = lane + 32 * q;
-        if (32 * q + 31 > j && 32 * q < n && jj > j && jj < n) v[q] = fma(-xj, lc[jj], v[q]);
+        for (int q = 0; q < kMaxPerLane; ++q) {
+          const int jj = lane + 32 * q;
+          if (32 * q + 31 > j && 32 * q < n && jj > j && jj < n) v[q] = fma(-xj, lc[jj], v[q]);
+        }
+      } else {
+        const double* lc = S + size_t(j) * n;
+#pragma unroll
+        for (int q = 0; q < kMaxPerLane; ++q) {
+          const int jj = lane + 32 * q;
+          if (32 * q + 31 > j && 32 * q < n && jj > j && jj < n) v[q] = fma(-xj, __ldcg(&lc[jj]), v[q]);
+        }
       }
     }
 #pragma unroll
@@ -1601,7 +1615,11 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
 
 int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, double* X, long long x_stride,
                          unsigned* bar, int* flags, cudaStream_t s, int skip_cta) {
-  const size_t shm = sizeof(double) * (size_t(n) * n + n);
+  // L in shared memory for the solves when it fits; else the panel rows
+  // ((n - 1) x kCoopNb) and 1 / L_jj only, L read from L2
+  const size_t shm_full = sizeof(double) * (size_t(n) * n + n);
+  const int l_smem = shm_full <= jacobi32_smem_limit() ? 1 : 0;
+  const size_t shm = l_smem ? shm_full : sizeof(double) * (size_t(n) * kCoopNb + n);
   if (n > 384 || shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
   // the co-resident grid for this shared-memory size, found once per device
   static std::mutex m;
@@ -1626,7 +1644,7 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
   // the hook names the grid's last CTA (never CTA 0, which factors the
   // diagonal blocks); -1 leaves every CTA in
   int skip = (skip_cta >= 0 && grid > 1) ? grid - 1 : -1;
-  void* args[] = {&n, &S, &A, &a_stride, &X, &x_stride, &bar, &flags, &skip};
+  void* args[] = {&n, &S, &A, &a_stride, &X, &x_stride, &bar, &flags, &skip, const_cast<int*>(&l_smem)};
   ++g_launch_count;
   TVAP_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_evolve_kernel, dim3(grid), dim3(kCoopThreads), args,
                                         shm, s));
