@@ -247,9 +247,10 @@ def run_ours(args):
     autotune = None
     if not args.no_autotune:
         tune_table = ctx.autotune(U, V, MPHI, MPHI, 2 * math.pi, ZV, NV, reps=3)
-        autotune = {"chosen": dict(zip(("bn_policy", "solve_groups", "solve_cap", "lookahead"), ctx.tuning())),
-                    "ms_per_projection": {f"bn{b}_g{g}_cap{c}_la{a}": round(v, 4)
-                                          for (b, g, c, a), v in tune_table.items()}}
+        autotune = {"chosen": dict(zip(("bn_policy", "solve_groups", "solve_cap", "lookahead", "pfaffian_blocked"),
+                                       ctx.tuning())),
+                    "ms_per_projection": {f"bn{b}_g{g}_cap{c}_la{a}_pf{f}": round(v, 4)
+                                          for (b, g, c, a, f), v in tune_table.items()}}
 
     # ---- device-resident value (batched form)
     it = DeviceIteration(ctx, U, V, 0, torch)

@@ -321,22 +321,27 @@ int tvap_project_observables(tvap_ctx* ctx, const double* U0, const double* V0, 
  * x the cap on the tcgen05 CTAs beside the second group's panels (0: the
  * SMs the panels leave, 1: half the SMs, 2: none; 2 groups only) x the
  * look-ahead of the solve's panels (the bulk of each elimination product on
- * a stream of its own while the next panel is factored: on, off) -- 24
+ * a stream of its own while the next panel is factored: on, off) x the form
+ * of the overlap's Pfaffian (the shared-memory elimination where it fits, or
+ * always the blocked one: the same pivots, another summation order) -- 48
  * candidates, CUDA events on the context's stream, and keeps the fastest in
  * the context.  table_ms (may be NULL) receives the ms per projection of the
- * first ntable candidates in the order look-ahead on, then off, each with
- * groups 2 (cap 0, 1, 2), then groups 1, each with bn 0, 1, 2.  Results do
- * not depend on the choice (the same FP64 emulation and the same arithmetic
- * in every product; only tile and launch shapes and their order change).
- * tvap_set_tuning and tvap_get_tuning (knobs[3] = bn, groups, cap),
- * tvap_set_lookahead and tvap_get_lookahead (1 on, 0 off; off unless set
- * or chosen by the tuner) set and read them. */
+ * first ntable candidates in the order Pfaffian form 0, then 1, each with
+ * look-ahead on, then off, each with groups 2 (cap 0, 1, 2), then groups 1,
+ * each with bn 0, 1, 2.  Results do not depend on the tile and launch
+ * shapes (the same FP64 emulation in every product); the Pfaffian form
+ * changes the order of its rounding.  tvap_set_tuning and tvap_get_tuning
+ * (knobs[3] = bn, groups, cap), tvap_set_option and tvap_get_option (the
+ * look-ahead and the Pfaffian form, 0 or 1; 0 unless set or chosen by the
+ * tuner; tvap_get_option returns -1 for an unknown option) set and read
+ * them. */
 int tvap_autotune(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_proj_opts* opts, int reps,
                   double* table_ms, int ntable);
 int tvap_set_tuning(tvap_ctx* ctx, int bn_policy, int solve_groups, int solve_cap);
 int tvap_get_tuning(const tvap_ctx* ctx, int* knobs);
-int tvap_set_lookahead(tvap_ctx* ctx, int on);
-int tvap_get_lookahead(const tvap_ctx* ctx);
+enum { TVAP_OPT_SOLVE_LOOKAHEAD = 1, TVAP_OPT_PFAFFIAN_BLOCKED = 2 };
+int tvap_set_option(tvap_ctx* ctx, int option, int value);
+int tvap_get_option(const tvap_ctx* ctx, int option);
 
 /* Test hook, no counterpart in the reference: the next tvap_evolve on this
  * context runs its cooperative launch with one CTA that leaves before the

@@ -781,10 +781,13 @@ __global__ void __launch_bounds__(kPfThreads) pf_panel_kernel(int N, int Kstart,
 
 }  // namespace
 
-int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s) {
+// blocked: the blocked form also where the packed triangle fits shared
+// memory (its CTAs hold 22 KB instead of up to 227 KB, so that products of
+// other streams share their SMs)
+int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s, bool blocked) {
   if (n > 512 || (n & 1)) return TVAP_ERR_ARG;
   const size_t shm = sizeof(double2) * (size_t(n) * (n + 1) / 2 + 4 * size_t(n + 1) + size_t(n));
-  if (shm <= jacobi32_smem_limit()) {
+  if (shm <= jacobi32_smem_limit() && !(blocked && n >= 2)) {
     // the packed upper triangle fits shared memory: the unblocked elimination
     if (int rc = smem_opt_in((const void*)pfaffian_smem_kernel, jacobi32_smem_limit())) return rc;
     pfaffian_smem_kernel<<<batch, kPfThreads, shm, tvap::counted(s)>>>(n, A, pf, batch, flags);

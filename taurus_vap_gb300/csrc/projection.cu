@@ -2674,7 +2674,7 @@ int angles_overlap(tvap_ctx* c, int G, const double2* d_ephase, int nocc, int ne
     if ((rc = gemm(g, s2))) return rc;
     sec_end_on(c, SEC_OVERLAP, s2);
     sec_begin_on(c, SEC_PFAFFIAN, s2);
-    if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s2))) return rc;
+    if ((rc = pfaffian_batched(nb, G, w->K, w->pf, c->d_flags, s2, c->tune_pf_blocked != 0))) return rc;
     sec_end_on(c, SEC_PFAFFIAN, s2);
   } else {
     fill_det_one_kernel<<<nblk(G, tb), tb, 0, tvap::counted(s2)>>>(G, w->pf);

@@ -551,13 +551,23 @@ int tvap_set_tuning(tvap_ctx* c, int bn_policy, int solve_groups, int solve_cap)
   return TVAP_OK;
 }
 
-int tvap_set_lookahead(tvap_ctx* c, int on) {
-  if (!c || on < 0 || on > 1) return TVAP_ERR_ARG;
-  c->tune_lookahead = on;
-  return TVAP_OK;
+int tvap_set_option(tvap_ctx* c, int option, int value) {
+  if (!c || value < 0 || value > 1) return TVAP_ERR_ARG;
+  switch (option) {
+    case TVAP_OPT_SOLVE_LOOKAHEAD: c->tune_lookahead = value; return TVAP_OK;
+    case TVAP_OPT_PFAFFIAN_BLOCKED: c->tune_pf_blocked = value; return TVAP_OK;
+    default: return TVAP_ERR_ARG;
+  }
 }
 
-int tvap_get_lookahead(const tvap_ctx* c) { return c ? c->tune_lookahead : -1; }
+int tvap_get_option(const tvap_ctx* c, int option) {
+  if (!c) return -1;
+  switch (option) {
+    case TVAP_OPT_SOLVE_LOOKAHEAD: return c->tune_lookahead;
+    case TVAP_OPT_PFAFFIAN_BLOCKED: return c->tune_pf_blocked;
+    default: return -1;
+  }
+}
 
 int tvap_get_tuning(const tvap_ctx* c, int* knobs) {
   if (!c || !knobs) return TVAP_ERR_ARG;
@@ -572,25 +582,27 @@ int tvap_autotune(tvap_ctx* c, const double* U0, const double* V0, const tvap_pr
   if (!c || !U0 || !V0 || !opts || reps < 1) return TVAP_ERR_ARG;
   if (!c->have_ham) return TVAP_ERR_NOT_READY;
   struct Cand {
-    int bn, groups, cap, la;
+    int bn, groups, cap, la, pf;
   };
   std::vector<Cand> cands;
-  for (int la = 1; la >= 0; --la)
-    for (int groups = 2; groups >= 1; --groups)
-      for (int cap = 0; cap < (groups == 2 ? 3 : 1); ++cap)
-        for (int bn = 0; bn < 3; ++bn) cands.push_back({bn, groups, cap, la});
+  for (int pf = 0; pf <= 1; ++pf)
+    for (int la = 1; la >= 0; --la)
+      for (int groups = 2; groups >= 1; --groups)
+        for (int cap = 0; cap < (groups == 2 ? 3 : 1); ++cap)
+          for (int bn = 0; bn < 3; ++bn) cands.push_back({bn, groups, cap, la, pf});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   TVAP_CUDA(cudaEventCreate(&e0));
   TVAP_CUDA(cudaEventCreate(&e1));
   int rc = TVAP_OK;
   double best = 1e300;
-  Cand chosen = {c->tune_bn, c->tune_groups, c->tune_cap, c->tune_lookahead};
+  Cand chosen = {c->tune_bn, c->tune_groups, c->tune_cap, c->tune_lookahead, c->tune_pf_blocked};
   tvap_pnp out{};
   for (size_t k = 0; k < cands.size() && rc == TVAP_OK; ++k) {
     c->tune_bn = cands[k].bn;
     c->tune_groups = cands[k].groups;
     c->tune_cap = cands[k].cap;
     c->tune_lookahead = cands[k].la;
+    c->tune_pf_blocked = cands[k].pf;
     if ((rc = tvap_project(c, U0, V0, opts, &out, nullptr))) break;  // warm-up (scratch, tables)
     cudaEventRecord(e0, c->stream);
     for (int r = 0; r < reps && rc == TVAP_OK; ++r) rc = tvap_project(c, U0, V0, opts, &out, nullptr);
@@ -611,6 +623,7 @@ int tvap_autotune(tvap_ctx* c, const double* U0, const double* V0, const tvap_pr
   c->tune_groups = chosen.groups;
   c->tune_cap = chosen.cap;
   c->tune_lookahead = chosen.la;
+  c->tune_pf_blocked = chosen.pf;
   return rc;
 }
 

@@ -299,6 +299,7 @@ struct tvap_ctx {
   int tune_groups = 2;
   int tune_cap = 0;
   int tune_lookahead = 0;  // look-ahead of the Thouless solve's panels (streamB)
+  int tune_pf_blocked = 0;  // the blocked Pfaffian also where the shared-memory one fits
 };
 
 namespace tvap {
@@ -346,7 +347,7 @@ int fields_batched(tvap_ctx* c, int ncol, int ldc, const double2* rho, const dou
 // ---------------------------------------------------------------------------
 // Pfaffian of `batch` skew matrices (upper triangle of column-major n x n
 // blocks, stride n*n), Parlett-Reid with the reference's pivoting.
-int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s);
+int pfaffian_batched(int n, int batch, double2* A, double2* pf, int* flags, cudaStream_t s, bool blocked = false);
 // symmetric eigen-decomposition by cyclic Jacobi (one matrix), ascending order
 // scale (device, may be null): the norm of the matrix A is a block of; the
 // sweeps stop at that matrix's rounding level

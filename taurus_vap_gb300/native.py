@@ -132,10 +132,10 @@ def lib():
         L.tvap_set_tuning.restype = ci
         L.tvap_get_tuning.argtypes = [vp, vp]
         L.tvap_get_tuning.restype = ci
-        L.tvap_set_lookahead.argtypes = [vp, ci]
-        L.tvap_set_lookahead.restype = ci
-        L.tvap_get_lookahead.argtypes = [vp]
-        L.tvap_get_lookahead.restype = ci
+        L.tvap_set_option.argtypes = [vp, ci, ci]
+        L.tvap_set_option.restype = ci
+        L.tvap_get_option.argtypes = [vp, ci]
+        L.tvap_get_option.restype = ci
         L.tvap_test_wait_timeout.argtypes = [vp]
         L.tvap_test_wait_timeout.restype = ci
         L.tvap_zskpfa_batched.argtypes = [vp, ci, ctypes.c_int64, vp, vp]
@@ -347,12 +347,14 @@ class Context:
         return U1, V1
 
     # -- launch shapes by measurement ------------------------------------------
-    TUNE_CANDIDATES = [(bn, g, cap, la) for la in (1, 0) for g in (2, 1) for cap in ((0, 1, 2) if g == 2 else (0,))
-                       for bn in (0, 1, 2)]
+    OPT_SOLVE_LOOKAHEAD, OPT_PFAFFIAN_BLOCKED = 1, 2
+    TUNE_CANDIDATES = [(bn, g, cap, la, pf) for pf in (0, 1) for la in (1, 0) for g in (2, 1)
+                       for cap in ((0, 1, 2) if g == 2 else (0,)) for bn in (0, 1, 2)]
 
     def autotune(self, U0, V0, Mphip, Mphin, facpi, valence_Z, valence_N, reps=3):
         """tvap_autotune: times the projection for every candidate launch
-        shape and keeps the fastest; returns {(bn, groups, cap, lookahead): ms}."""
+        shape and keeps the fastest; returns {(bn, groups, cap, lookahead,
+        pfaffian_blocked): ms}."""
         U, V = _f(U0, np.float64), _f(V0, np.float64)
         o = TvapProjOpts(Mphip, Mphin, facpi, valence_Z, valence_N, 1.0, 0.0, 0, 0)
         table = np.zeros(len(self.TUNE_CANDIDATES))
@@ -361,14 +363,16 @@ class Context:
         return dict(zip(self.TUNE_CANDIDATES, table.tolist()))
 
     def tuning(self):
-        """(bn, groups, cap, lookahead) of the context."""
+        """(bn, groups, cap, lookahead, pfaffian_blocked) of the context."""
         k = np.zeros(3, dtype=np.int32)
         _check(lib().tvap_get_tuning(self.h, _p(k)), "tvap_get_tuning")
-        return tuple(int(x) for x in k) + (int(lib().tvap_get_lookahead(self.h)),)
+        return tuple(int(x) for x in k) + (int(lib().tvap_get_option(self.h, self.OPT_SOLVE_LOOKAHEAD)),
+                                           int(lib().tvap_get_option(self.h, self.OPT_PFAFFIAN_BLOCKED)))
 
-    def set_tuning(self, bn_policy, solve_groups, solve_cap, lookahead=1):
+    def set_tuning(self, bn_policy, solve_groups, solve_cap, lookahead=0, pfaffian_blocked=0):
         _check(lib().tvap_set_tuning(self.h, bn_policy, solve_groups, solve_cap), "tvap_set_tuning")
-        _check(lib().tvap_set_lookahead(self.h, lookahead), "tvap_set_lookahead")
+        _check(lib().tvap_set_option(self.h, self.OPT_SOLVE_LOOKAHEAD, lookahead), "tvap_set_option")
+        _check(lib().tvap_set_option(self.h, self.OPT_PFAFFIAN_BLOCKED, pfaffian_blocked), "tvap_set_option")
 
     # -- adjust_constraints (module_constraints.f90:270-373) -------------------
     def adjust_constraints(self, U0, V0, Zi, constraints_HO, values, cpair=0, eps=1e-6):

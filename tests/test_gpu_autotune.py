@@ -1,7 +1,7 @@
 """tvap_autotune: the launch-shape candidates of the projection (B' tile
 policy of the tcgen05 products, staggered groups of the Thouless solve, the
 CTA cap beside the panel factorisations, the look-ahead of the solve's
-panels) give the same results -- the
+panels, the form of the Pfaffian) give the same results -- the
 emulated products sum exact integers whatever the tiling -- and the tuner
 keeps the fastest one.  Workload: emax=4 (n = 140), 15 x 15 angles."""
 
@@ -22,11 +22,14 @@ def test_autotune_candidates_agree_and_fastest_is_kept():
     ctx = Context(mdl.basis, mdl.ham)
     args = (15, 15, 2 * math.pi, 8, 8)
     ref, Href = ctx.project(U, V, *args)
-    for bn, groups, cap, la in Context.TUNE_CANDIDATES:
-        ctx.set_tuning(bn, groups, cap, la)
+    for bn, groups, cap, la, pf in Context.TUNE_CANDIDATES:
+        ctx.set_tuning(bn, groups, cap, la, pf)
         p, H = ctx.project(U, V, *args)
-        assert abs(p.c("ener") - ref.c("ener")) <= 1e-13 * abs(ref.c("ener")), (bn, groups, cap, la)
-        assert np.abs(H - Href).max() <= 1e-13 * np.abs(Href).max(), (bn, groups, cap, la)
+        # the shapes give the same sums to rounding; the blocked Pfaffian
+        # only another order of the overlap's rounding
+        tol = 1e-13 if pf == 0 else 1e-11
+        assert abs(p.c("ener") - ref.c("ener")) <= tol * abs(ref.c("ener")), (bn, groups, cap, la, pf)
+        assert np.abs(H - Href).max() <= tol * np.abs(Href).max(), (bn, groups, cap, la, pf)
     table = ctx.autotune(U, V, *args, reps=2)
-    assert len(table) == 24 and all(v > 0 for v in table.values())
+    assert len(table) == 48 and all(v > 0 for v in table.values())
     assert ctx.tuning() == min(table, key=table.get)
