@@ -752,6 +752,7 @@ def emax6_leg(torch, peaks, hbm_peak, steps=3):
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / steps
     sec = ctx.get_timing()
+    tl = ctx.get_timeline()
     ctx.set_timing(False)
     n, S = mdl.n, mdl.ham.S
     G = (MPHI * MPHI + 1) // 2
@@ -764,6 +765,7 @@ def emax6_leg(torch, peaks, hbm_peak, steps=3):
         "n": n, "elements": S, "ms_per_step": ms, "value": 1000.0 / ms, "unit": "iters/s", "steps": steps,
         "setup_s": setup_s, "energy": it.energy,
         "sections_ms_per_step": {k: round(v[0] / steps, 4) for k, v in sec.items()},
+        "timeline_ms": {k: [round(v[0], 3), round(v[1], 3)] for k, v in tl.items() if sec[k][1]},
         "roofline_fields": {
             "algorithmic_bytes": fld_bytes, "element_list_bytes": list_bytes, "ms_per_step": fld_ms,
             "achieved_gbs": fld_bytes / (fld_ms / 1000.0) / 1e9,

@@ -1689,7 +1689,7 @@ __device__ __forceinline__ float2 fcmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
-constexpr int kGjMaxSlots = 6;  // panels of up to 192 rows
+constexpr int kGjMaxSlots = 12;  // panels of up to 384 rows
 constexpr int kGjEntries = (kPanelMax * kPanelMax + kFactorThreads - 1) / kFactorThreads;  // block entries per thread
 
 template <int SLOTS>
@@ -1806,29 +1806,29 @@ __global__ void __launch_bounds__(kFactorThreads)
     }
   }
   // the original rows in the pivoted order: the block to shared memory, the
-  // rows below back to the panel (the block rows as zeros)
-  double2 raw[kQ][SLOTS];
-#pragma unroll
-  for (int q = 0; q < kQ; ++q) {
-    const int c = warp + 8 * q;
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-      const int r = lane + 32 * s;
-      raw[q][s] = (c < nbp && r < m) ? W[(j0 + srow[r]) + size_t(j0 + c) * n] : make_double2(0.0, 0.0);
-      if (c < nbp && r < nbp) A11[r + c * kP] = raw[q][s];
-    }
-  }
-  __syncthreads();
+  // rows below back to the panel (the block rows as zeros).  A column
+  // belongs to one warp, so the permutation in place needs only that warp's
+  // reads before its writes (one column of rows in registers at a time).
+  __syncthreads();  // srow is complete
 #pragma unroll
   for (int q = 0; q < kQ; ++q) {
     const int c = warp + 8 * q;
     if (c >= nbp) continue;
+    double2 raw[SLOTS];
 #pragma unroll
     for (int s = 0; s < SLOTS; ++s) {
       const int r = lane + 32 * s;
-      if (r < m) W[(j0 + r) + size_t(j0 + c) * n] = (r < nbp) ? make_double2(0.0, 0.0) : raw[q][s];
+      raw[s] = (r < m) ? W[(j0 + srow[r]) + size_t(j0 + c) * n] : make_double2(0.0, 0.0);
+      if (r < nbp) A11[r + c * kP] = raw[s];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+      const int r = lane + 32 * s;
+      if (r < m) W[(j0 + r) + size_t(j0 + c) * n] = (r < nbp) ? make_double2(0.0, 0.0) : raw[s];
     }
   }
+  __syncthreads();
   if (s_sing && tid == 0) atomicOr(flags, DEV_SINGULAR_UPHI);
   // Gauss-Jordan inverse of the block in place: step k with the reciprocal
   // of the pivot (formed by the owner of that entry at the end of the step
@@ -2155,6 +2155,12 @@ int gj_solve_range(tvap_ctx* c, int g0, int gc, int nb, cudaStream_t s, cudaEven
       TVAP_PANEL_GJ(4)
       TVAP_PANEL_GJ(5)
       TVAP_PANEL_GJ(6)
+      TVAP_PANEL_GJ(7)
+      TVAP_PANEL_GJ(8)
+      TVAP_PANEL_GJ(9)
+      TVAP_PANEL_GJ(10)
+      TVAP_PANEL_GJ(11)
+      TVAP_PANEL_GJ(12)
 #undef TVAP_PANEL_GJ
       default:
         return TVAP_ERR_ARG;
