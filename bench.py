@@ -50,8 +50,14 @@ def build_workload():
 # clocks sampled during the timed region
 # --------------------------------------------------------------------------
 class ClockSampler:
-    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """nvidia-smi clock samples every 25 ms, each with its timestamp; stop()
+    keeps those inside the wall-clock window it is given (the timed region),
+    so that the sampler can start before the warm-up (nvidia-smi takes about
+    0.1 s to print its first line, as long as a short timed region)."""
+
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
         self.device = device
@@ -62,7 +68,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "25"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
@@ -72,7 +78,11 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """t0, t1: time.time() at the start and the end of the timed region
+        (None: every sample)."""
+        import datetime
+
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -84,19 +94,24 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.lines:
             w = [x.strip() for x in line.split(",")]
-            if len(w) < 6:
+            if len(w) < 7:
                 continue
             try:
-                sm.append(float(w[0]))
-                mx = float(w[1])
+                ts = datetime.datetime.strptime(w[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                sm_v, mx_v = float(w[1]), float(w[2])
             except ValueError:
                 continue
+            if t0 is not None and not (t0 <= ts <= t1):
+                continue
+            sm.append(sm_v)
+            mx = mx_v
             for k, name in enumerate(names):
-                if w[2 + k].lower().startswith("active"):
+                if w[3 + k].lower().startswith("active"):
                     reasons.add(name)
         sm.sort()
         med = sm[len(sm) // 2] if sm else None
-        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "interval_ms": 25, "window": "the timed region" if t0 is not None else "the whole run"}
 
 
 # --------------------------------------------------------------------------
@@ -252,7 +267,10 @@ def run_ours(args):
                     "ms_per_projection": {f"bn{b}_g{g}_cap{c}_la{a}_pf{f}": round(v, 4)
                                           for (b, g, c, a, f), v in tune_table.items()}}
 
-    # ---- device-resident value (batched form)
+    # ---- device-resident value (batched form).  The clock sampler starts
+    # before the warm-up; its samples inside the timed region are kept.
+    clocks = ClockSampler(local)
+    clocks.start()
     it = DeviceIteration(ctx, U, V, 0, torch)
     for _ in range(args.warmup):
         it.step()
@@ -263,18 +281,18 @@ def run_ours(args):
     # step, no synchronisation)
     ctx.set_timing(True)
     it.launches = 0
-    clocks = ClockSampler(local)
-    clocks.start()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    w0 = time.time()
     t0.record(stream)
     for _ in range(args.steps):
         it.step()
     t1.record(stream)
     torch.cuda.synchronize()
+    w1 = time.time()
     barrier()
-    clk = clocks.stop()
+    clk = clocks.stop(w0, w1)
     ms = t0.elapsed_time(t1)
     launches = it.launches
     sections = ctx.get_timing()
@@ -318,7 +336,10 @@ def run_ours(args):
         torch.cuda.synchronize()
         pms = a.elapsed_time(b) / args.plain_steps
         plain = {"value": 1000.0 / pms, "unit": "iters/s", "ms_per_step": pms, "steps": args.plain_steps,
-                 "batched_over_plain": (1000.0 / ms_per_step) / (1000.0 / pms)}
+                 "batched_over_plain": (1000.0 / ms_per_step) / (1000.0 / pms),
+                 "angle_pairs": MPHI * MPHI, "angle_pairs_batched": (MPHI * MPHI + 1) // 2,
+                 "note": "the plain form computes every angle pair; the batched form folds conjugate pairs "
+                         "(about 2x of the ratio) and batches all angles into each launch"}
 
     # ---- end to end through the C ABI with host buffers
     state = (np.asfortranarray(U), np.asfortranarray(V), np.zeros(n * n))
