@@ -66,7 +66,7 @@ def build_setup(force: bool = False) -> str:
     src = os.path.join(CSRC, "setup", "tvap_setup.cpp")
     hdr = os.path.join(INCLUDE, "tvap_setup.h")
     if force or _stale(SETUP_LIB, [src, hdr]):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", SETUP_LIB, src])
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-o", SETUP_LIB, src])
     return SETUP_LIB
 
 

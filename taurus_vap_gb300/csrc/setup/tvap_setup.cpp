@@ -28,6 +28,9 @@
 #include <random>
 #include <sstream>
 #include <string>
+#include <algorithm>
+#include <atomic>
+#include <thread>
 #include <vector>
 
 #include "../../../include/tvap_setup.h"
@@ -262,17 +265,47 @@ double uncouple_jt(const tvs_model* m, CgCache& cg, int a, int b, int c, int d) 
   return sum;
 }
 
+// Runs body(i, w) for i in [0, count) on up to `threads` host threads (w =
+// the worker, 0 .. threads-1; worker 0 is the calling thread), the indices
+// taken in order from a shared counter.
+template <class F>
+void parallel_for(int count, int threads, F body) {
+  std::atomic<int> next{0};
+  auto work = [&](int w) {
+    for (int i; (i = next.fetch_add(1)) < count;) body(i, w);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+}
+
+int host_threads() {
+  const unsigned hc = std::thread::hardware_concurrency();
+  return int(std::max(1u, std::min(hc, 32u)));
+}
+
 // m-scheme enumeration (module_hamiltonian.f90:321-378) and the time-reversal
-// permutation codes (reconstruct_2body_timerev, :970-1018).
+// permutation codes (reconstruct_2body_timerev, :970-1018).  The elements of
+// each first index a are found on the host threads (each with its own
+// Clebsch-Gordan cache) and joined in the order of a: the list is the serial
+// one, element for element.
 void enumerate_mscheme(tvs_model* m) {
   const int n = m->n;
   int jmax = 0;
   for (int i = 0; i < m->nsh; ++i) jmax = std::max(jmax, m->sh_2j[i]);
-  CgCache cg(std::max(jmax, 2));
   m->abcd.clear();
   m->h2.clear();
   const double Vcut = 1.0e-16;
-  for (int a = 0; a < n; ++a) {
+  std::vector<std::vector<int16_t>> abcd_a(n);
+  std::vector<std::vector<float>> h2_a(n);
+  const int threads = host_threads();
+  std::vector<CgCache*> caches(threads, nullptr);
+  parallel_for(n, threads, [&](int a, int w) {
+    if (!caches[w]) caches[w] = new CgCache(std::max(jmax, 2));
+    CgCache& cg = *caches[w];
+    auto& out_abcd = abcd_a[a];
+    auto& out_h2 = h2_a[a];
     const int la = m->sp_l[a], ma = m->sp_2mj[a], ta = m->sp_2mt[a];
     for (int b = a + 1; b < n; ++b) {
       const int lb = m->sp_l[b], mb = m->sp_2mj[b], tb = m->sp_2mt[b];
@@ -288,19 +321,32 @@ void enumerate_mscheme(tvs_model* m) {
           double V = uncouple_jt(m, cg, a, b, c, d);
           V = V * m->scaling_2b;
           if (std::fabs(V) > Vcut) {
-            m->abcd.push_back(int16_t(a + 1));
-            m->abcd.push_back(int16_t(b + 1));
-            m->abcd.push_back(int16_t(c + 1));
-            m->abcd.push_back(int16_t(d + 1));
-            m->h2.push_back(float(V));
+            out_abcd.push_back(int16_t(a + 1));
+            out_abcd.push_back(int16_t(b + 1));
+            out_abcd.push_back(int16_t(c + 1));
+            out_abcd.push_back(int16_t(d + 1));
+            out_h2.push_back(float(V));
           }
         }
       }
     }
+  });
+  for (CgCache* cgp : caches) delete cgp;
+  size_t total = 0;
+  for (int a = 0; a < n; ++a) total += h2_a[a].size();
+  m->abcd.reserve(4 * total);
+  m->h2.reserve(total);
+  for (int a = 0; a < n; ++a) {
+    m->abcd.insert(m->abcd.end(), abcd_a[a].begin(), abcd_a[a].end());
+    m->h2.insert(m->h2.end(), h2_a[a].begin(), h2_a[a].end());
+    std::vector<int16_t>().swap(abcd_a[a]);
+    std::vector<float>().swap(h2_a[a]);
   }
   const size_t S = m->h2.size();
   m->trperm.assign(S, 0);
-  for (size_t kk = 0; kk < S; ++kk) {
+  const int chunks = 64 * threads;
+  parallel_for(chunks, threads, [&](int ch, int) {
+  for (size_t kk = S * ch / chunks; kk < S * (ch + 1) / chunks; ++kk) {
     const int ia = m->abcd[4 * kk] - 1, ib = m->abcd[4 * kk + 1] - 1;
     const int ic = m->abcd[4 * kk + 2] - 1, id = m->abcd[4 * kk + 3] - 1;
     const int e = (m->sp_2j[ia] + m->sp_2j[ib] + m->sp_2j[ic] + m->sp_2j[id]) / 2;
@@ -321,6 +367,7 @@ void enumerate_mscheme(tvs_model* m) {
     if (phase < 0.0) code -= 8;
     m->trperm[kk] = int8_t(code);
   }
+  });
 }
 
 // Token reader for list-directed Fortran input.
