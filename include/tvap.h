@@ -339,7 +339,14 @@ int tvap_autotune(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_
                   double* table_ms, int ntable);
 int tvap_set_tuning(tvap_ctx* ctx, int bn_policy, int solve_groups, int solve_cap);
 int tvap_get_tuning(const tvap_ctx* ctx, int* knobs);
-enum { TVAP_OPT_SOLVE_LOOKAHEAD = 1, TVAP_OPT_PFAFFIAN_BLOCKED = 2 };
+/* TVAP_OPT_COMPLEX_PAIRS = k >= 0: the complex x complex products on the
+ * tensor cores whose contraction length is at least k take the paired form
+ * (real and imaginary rows interleaved in both operands, the four real
+ * products of each element combined on the exact integer accumulators:
+ * half the digit planes of the left operand, twice the tiles of half the
+ * k-steps), the others the real representation [[Re, -Im], [Im, Re]] x
+ * [Re, Im]; 0: none.  Both forms give the same bits. */
+enum { TVAP_OPT_SOLVE_LOOKAHEAD = 1, TVAP_OPT_PFAFFIAN_BLOCKED = 2, TVAP_OPT_COMPLEX_PAIRS = 3 };
 int tvap_set_option(tvap_ctx* ctx, int option, int value);
 int tvap_get_option(const tvap_ctx* ctx, int option);
 

@@ -132,6 +132,7 @@ int tvap_adjust_constraints(tvap_ctx* c, const double* U0, const double* V0, dou
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;

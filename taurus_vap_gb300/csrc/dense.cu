@@ -259,6 +259,7 @@ int pick_tile(int M, int N) {
 thread_local int g_gemm_mode = 2;
 thread_local int g_tc_grid_cap = 0;
 thread_local int g_tc_bn_policy = 0;
+thread_local int g_tc_pairs_min_k = 0;
 thread_local int* g_dev_flags = nullptr;
 thread_local tvap_ctx* g_tc_timing_ctx = nullptr;
 thread_local int g_tc_timing_sec = -1;

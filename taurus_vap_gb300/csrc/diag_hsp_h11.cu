@@ -273,6 +273,7 @@ int tvap_diagonalize_hsp_and_H11(tvap_ctx* c, const double* U0, const double* V0
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   const size_t nn = size_t(n) * n;
   cudaStream_t s = c->stream;

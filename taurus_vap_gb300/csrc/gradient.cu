@@ -263,6 +263,7 @@ int tvap_evolve(tvap_ctx* c, const double* U0, const double* V0, const double* Z
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -298,6 +299,7 @@ int tvap_iterate(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -427,6 +429,7 @@ int tvap_energy_adjoint(tvap_ctx* c, const double* U0, const double* V0, const d
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   double* buf = nullptr;
   if ((rc = ctx_scratch(c, 7 * nn + n, &buf))) return rc;

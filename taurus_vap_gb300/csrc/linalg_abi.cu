@@ -58,6 +58,7 @@ int gemm_abi(tvap_ctx* c, bool cplx, char transa, char transb, int m, int n, int
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   cudaStream_t s = c->stream;
   const size_t w = cplx ? 2 : 1;  // doubles per element
@@ -181,6 +182,7 @@ int tvap_zskpfa_batched(tvap_ctx* c, int batch, int64_t n, const double* A, doub
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;  // the blocked form (n > 164) updates with the context's products
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   cudaStream_t s = c->stream;
   const size_t nn = size_t(n) * n;

@@ -163,9 +163,15 @@ int launch_ozaki_mma(int M, int N, int mpad, int npad, int kpad, const __nv_bflo
 //   1  complex, planes stacked:     X' = [Re X; Im X]                       (2 rows x K)
 //   2  complex, real representation X' = [[Re X, -Im X], [Im X, Re X]]      (2 rows x 2 kp)
 //   3  complex, planes side by side X' = [Re X, Im X]                       (rows x 2 kp)
+//   4  complex, rows interleaved:   X'(2r, k) = Re X(r, k), X'(2r+1, k) = Im X(r, k)
+//                                                                           (2 rows x K)
 // so that A' B'^T of (2, 3) holds [Re C; Im C] of a complex x complex
-// product, of (1, 0) [Re C; Im C] and of (0, 1) [Re C, Im C].  In forms 2 and
-// 3 each column block is padded with zeros from K to kp (a multiple of 16).
+// product, of (1, 0) [Re C; Im C] and of (0, 1) [Re C, Im C]; of (4, 4) the
+// four real products Re/Im A x Re/Im B in 2 x 2 blocks, which the epilogue
+// combines.  In forms 2 and 3 each column block is padded with zeros from K
+// to kp (a multiple of 16).  Forms 2, 3 and 4 give the real and imaginary part
+// of a row one exponent (so that the digits of form 4 are those of forms 2
+// and 3); forms 0 and 1 give each part its own.
 // nstack > 1 stacks the rows of nstack batch entries (X' row b xrows + r).
 struct TcSrc {
   const void* p;
@@ -186,7 +192,8 @@ struct TcSrc {
 // one warp per row takes the exponents, then every thread converts 8
 // consecutive k of one part (real or imaginary) of one row to 8 digits and
 // stores one 16-byte core-matrix row per digit at each place of X' that
-// holds them (twice in form 2: the imaginary block negated by its sign bits).
+// holds them (twice in form 2: the imaginary block negated by its sign bits;
+// once in form 4, whose left operand is half the size of form 2's).
 constexpr int kSliceThreads = 256;
 __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int tile_rows, int rows_pad, int nks,
                                                                   __nv_bfloat16* __restrict__ out,
@@ -248,7 +255,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int ti
       er = max(er, __shfl_xor_sync(0xffffffffu, er, off));
       ei = max(ei, __shfl_xor_sync(0xffffffffu, ei, off));
     }
-    if (form >= 2) er = ei = max(er, ei);  // one exponent for the whole X' row
+    if (form >= 2) er = ei = max(er, ei);  // one exponent for the real and imaginary part
     if (er == oz::kExpZero) er = 0;
     if (ei == oz::kExpZero) ei = 0;
     if (lane == 0) {
@@ -257,16 +264,17 @@ __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int ti
       if (sq0 + w < nsrc) {
         int b, i;
         src_row(w, b, i);
-        const size_t qtop = size_t(x.nstack > 1 ? b * x.xrows : 0) + i;
+        const size_t qtop = size_t(x.nstack > 1 ? b * x.xrows : 0) + (form == 4 ? 2 * i : i);
         ex[size_t(slot) * rows_pad + qtop] = er;
         if (form == 1 || form == 2) ex[size_t(slot) * rows_pad + qtop + x.rows] = ei;
+        if (form == 4) ex[size_t(slot) * rows_pad + qtop + 1] = ei;
       }
     }
   }
   __syncthreads();
   // work items: (row, chunk of 8 k, part), rows fastest so that a half-warp
   // writes whole 256-byte core-matrix row groups
-  const int nchunk = form >= 2 ? x.kp / 8 : nks * 2;
+  const int nchunk = (form == 2 || form == 3) ? x.kp / 8 : nks * 2;
   const int nparts = cplx ? 2 : 1;
   const int tiles = rows_pad / tile_rows;
   const size_t tile_elems = size_t(tile_rows) * 16;
@@ -276,7 +284,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int ti
     if (sq0 + row >= nsrc) continue;
     int b, i;
     src_row(row, b, i);
-    const int qtop = (x.nstack > 1 ? b * x.xrows : 0) + i;
+    const int qtop = (x.nstack > 1 ? b * x.xrows : 0) + (form == 4 ? 2 * i : i);
     const int emax = e_s[row][part];
     const int k0 = 8 * c;
     uint32_t w[kDigits][4];
@@ -311,14 +319,17 @@ __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int ti
           put(qtop, x.kp + k0, 0x80008000u);
         }
         break;
-      default: put(qtop, part ? x.kp + k0 : k0, 0u); break;
+      case 3: put(qtop, part ? x.kp + k0 : k0, 0u); break;
+      default: put(qtop + part, k0, 0u); break;
     }
   }
 }
 
 // Output mapping of the tensor-memory product: row q of A' (slot z) and row
 // col of B' hold component comp = (r >= a_split) + (col >= b_split) of
-// C(i, j) of batch entry b; alpha and beta are real.
+// C(i, j) of batch entry b; alpha and beta are real.  In the paired form
+// (both operands sliced in form 4) rows 2i, 2i + 1 of A' and 2j, 2j + 1 of B'
+// are the real and imaginary parts of row i of op(A) and column j of op(B).
 struct TcOut {
   void* C;
   long long crs, ccs, cbs;
@@ -330,8 +341,15 @@ struct TcOut {
 // Persistent CTAs over the (128 x 64 tile of A' B'^T, slot) tiles, claimed in
 // order from *counter; tile numbers run over the N tiles fastest, then the M
 // tiles, then the slots, so that the CTAs working at one time share their A
-// and B tiles through L2.
-template <bool UNIT, int BN>
+// and B tiles through L2.  PAIRS: the paired form, whose 2 x 2 blocks
+// P(2i .. 2i+1, 2j .. 2j+1) give Re C(i, j) = P(2i, 2j) - P(2i+1, 2j+1) and
+// Im C(i, j) = P(2i+1, 2j) + P(2i, 2j+1): the two rows of a block are adjacent
+// TMEM lanes (one shuffle per column pair), its two columns adjacent
+// accumulator columns of one thread.  The four products of a block share one
+// exponent (rows and columns: one per real/imaginary pair), so the
+// combination is exact on the integer accumulators and the result is, bit
+// for bit, that of the real representation [[Re, -Im], [Im, Re]] x [Re, Im].
+template <bool UNIT, int BN, bool PAIRS>
 __global__ void __launch_bounds__(oztc::kThreads, 1)
     ozaki_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ ea, int a_rows_pad,
                     const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ eb, int b_rows_pad, int b_shared,
@@ -356,18 +374,24 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
     const int mt = rest % a_tiles, z = rest / a_tiles;
     const int bz = b_shared ? 0 : z;
     const int q = mt * oztc::kM + 32 * (warp & 3) + lane;
-    if (q >= o.nstack * o.a_rows) return;
     if constexpr (BN < 64) {
       if (16 * (warp >> 2) >= BN) return;  // these warps' columns belong to the next tile
     }
+    // a row pair lies within the rows of A' or beyond them (a_rows is even):
+    // the paired form returns after its shuffles, which the whole warp takes
+    const bool row_ok = q < o.nstack * o.a_rows;
+    if (!PAIRS && !row_ok) return;
     const int b = o.nstack > 1 ? q / o.a_rows : z;
     int i = o.nstack > 1 ? q - b * o.a_rows : q;
     int comp_a = 0;
-    if (i >= o.a_split) {
+    if (PAIRS) {
+      comp_a = i & 1;
+      i >>= 1;
+    } else if (i >= o.a_split) {
       i -= o.a_split;
       comp_a = 1;
     }
-    const int eai = ea[size_t(z) * a_rows_pad + q] - 57;
+    const int eai = (row_ok ? ea[size_t(z) * a_rows_pad + q] : 0) - 57;
     double* __restrict__ C = static_cast<double*>(o.C);
     const int cw = o.c_real ? 1 : 2;  // doubles per element
     const int col0 = nt * BN + 16 * (warp >> 2);
@@ -384,12 +408,48 @@ __global__ void __launch_bounds__(oztc::kThreads, 1)
       if (col >= o.b_rows || (comp > 0 && o.c_real)) return -1;
       return (i * o.crs + j * o.ccs + b * o.cbs) * cw + comp;
     };
-    // alpha = +-1 (nearly every product) is a sign of the integer
-    // conversion; any other alpha one product more
     // UNIT: alpha = +-1 (every product of the path), a sign of the integer
     // conversion; otherwise one product more (a separate instantiation, so
     // that no FP64 multiply is predicated into the common case)
     const bool neg = o.alpha < 0.0;
+    if constexpr (PAIRS) {
+      // even lane (real row): P(2i, 2j) - P(2i+1, 2j+1); odd lane (imaginary
+      // row): P(2i+1, 2j) + P(2i, 2j+1).  Both take the partner's odd column.
+      long long hs[8], ls[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const long long th = __shfl_xor_sync(0xffffffffu, acc.h[2 * c + 1], 1);
+        const long long tl = __shfl_xor_sync(0xffffffffu, acc.l[2 * c + 1], 1);
+        hs[c] = comp_a ? acc.h[2 * c] + th : acc.h[2 * c] - th;
+        ls[c] = comp_a ? acc.l[2 * c] + tl : acc.l[2 * c] - tl;
+      }
+      if (!row_ok || (comp_a && o.c_real)) return;
+      const int j0 = col0 >> 1;
+      double w[8];
+      long long k[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const bool in = col0 + 2 * c < o.b_rows;
+        const int e = in ? ebz[col0 + 2 * c] : 0;
+        double x;
+        if (oztc::scaled(hs[c], ls[c], eai + e, UNIT && neg, x))
+          w[c] = UNIT ? x : x * o.alpha;
+        else
+          w[c] = fma(double(hs[c]), 0x1p28, double(ls[c])) * (o.alpha * oz::pow2(eai + e));
+        k[c] = in ? (i * o.crs + (j0 + c) * o.ccs + b * o.cbs) * cw + comp_a : -1;
+      }
+      if (o.beta != 0.0) {
+        double old[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) old[c] = k[c] >= 0 ? C[k[c]] : 0.0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) w[c] = fma(o.beta, old[c], w[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (k[c] >= 0) C[k[c]] = w[c];
+      return;
+    }
     double v[16];
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
@@ -569,7 +629,16 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
            scale_left ? 1.0 : g.s2};
   TcOut o{};
   o.a_split = o.b_split = INT_MAX;
-  if (!L.real && !R.real) {
+  // complex x complex: the paired form (rows interleaved on both sides, the
+  // 2 x 2 blocks combined by the epilogue; half the left operand's digit
+  // planes, twice the tiles of half the k-steps, so that it pays where the
+  // contraction is long) or the real representation
+  const bool pairs = !L.real && !R.real && g_tc_pairs_min_k > 0 && K >= g_tc_pairs_min_k;
+  if (pairs) {
+    xa.form = xb.form = 4;
+    xa.xrows = 2 * L.rows;
+    xb.xrows = 2 * R.rows;
+  } else if (!L.real && !R.real) {
     xa.form = 2;
     xa.xrows = 2 * L.rows;
     xa.xk = 2 * kp;
@@ -601,8 +670,11 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const size_t bsz = size_t(b_slots) * (b_rows_pad / bn) * nks * (oztc::b_bytes(bn) / 2);
   // products of few tiles (the single small products of the canonical basis
   // and the evolution) are latency-bound: the 32 x 32 mma.sync tiles spread
-  // them over more SMs
-  if (size_t(a_rows_pad / oztc::kM) * (b_rows_pad / bn) * a_slots < size_t(kTcMinTiles)) return TVAP_ERR_ARG;
+  // them over more SMs.  The paired form has twice the tiles of half the
+  // k-steps; it is counted in tiles of the real representation, so that both
+  // forms route the same products here.
+  if (size_t(a_rows_pad / oztc::kM) * (b_rows_pad / bn) * a_slots / (pairs ? 2 : 1) < size_t(kTcMinTiles))
+    return TVAP_ERR_ARG;
   int rc;
   OzScratch* sc = nullptr;
   if ((rc = oz_reserve(s, sizeof(__nv_bfloat16) * (asz + bsz), size_t(a_slots) * a_rows_pad +
@@ -661,10 +733,12 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const long long ntiles = (long long)(a_rows_pad / oztc::kM) * (b_rows_pad / bn) * a_slots;
   const int grid = int(std::min<long long>(ntiles, g_tc_grid_cap > 0 ? std::min(sms, g_tc_grid_cap) : sms));
   // the instantiation: alpha = +-1 (a sign in the integer conversion) or
-  // general, and the B' tile width
+  // general, the B' tile width and the paired form
   const bool unit_alpha = g_alpha_unit(o.alpha);
-  auto kern = unit_alpha ? (bn == 48 ? ozaki_tc_kernel<true, 48> : ozaki_tc_kernel<true, 64>)
-                         : (bn == 48 ? ozaki_tc_kernel<false, 48> : ozaki_tc_kernel<false, 64>);
+  auto kern = pairs ? (unit_alpha ? (bn == 48 ? ozaki_tc_kernel<true, 48, true> : ozaki_tc_kernel<true, 64, true>)
+                                  : (bn == 48 ? ozaki_tc_kernel<false, 48, true> : ozaki_tc_kernel<false, 64, true>))
+                    : (unit_alpha ? (bn == 48 ? ozaki_tc_kernel<true, 48, false> : ozaki_tc_kernel<true, 64, false>)
+                                  : (bn == 48 ? ozaki_tc_kernel<false, 48, false> : ozaki_tc_kernel<false, 64, false>));
   if ((rc = smem_opt_in((const void*)kern, oztc::kSmemBytes))) return rc;
   TVAP_CUDA(cudaMemsetAsync(sc->counter, 0, sizeof(int), s));
   if (g_tc_timing_ctx) sec_begin_on(g_tc_timing_ctx, g_tc_timing_sec, s);

@@ -350,10 +350,13 @@ __device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char*
       wait_parity(&ctl.mma_done, 0u, nullptr, false);
     }
   } else {
+    // the epilogue warps decide as whole warps (a lane that gives up takes its
+    // warp with it): the accumulator loads are warp-wide (.sync.aligned) and
+    // the paired store shuffles between lanes
     long long fc = 0;
     for (int tt = 0; ok; ++tt) {
       const int slot = tt % kRing;
-      if (!wait_parity(&ctl.tile_full[slot], uint32_t((tt / kRing) & 1), abort, true)) {
+      if (!__all_sync(0xffffffffu, wait_parity(&ctl.tile_full[slot], uint32_t((tt / kRing) & 1), abort, true))) {
         ok = false;
         break;
       }
@@ -365,7 +368,7 @@ __device__ bool run_tiles(int* counter, int ntiles, NksOf nks_of, unsigned char*
 #pragma unroll
       for (int c = 0; c < 16; ++c) o.h[c] = o.l[c] = 0;
       for (int f = 0; f < nfold; ++f, ++fc) {
-        if (!wait_parity(&ctl.acc_full, uint32_t(fc & 1), abort, true)) {
+        if (!__all_sync(0xffffffffu, wait_parity(&ctl.acc_full, uint32_t(fc & 1), abort, true))) {
           ok = false;
           break;
         }

@@ -419,6 +419,7 @@ int tvap_calculate_fields_batched(tvap_ctx* c, int ncol, const double* rho, cons
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n, tot = nn * ncol;
@@ -467,6 +468,7 @@ int tvap_project(tvap_ctx* c, const double* U0, const double* V0, const tvap_pro
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -508,6 +510,7 @@ int tvap_project_observables(tvap_ctx* c, const double* U0, const double* V0, co
   LaunchTally tally(c);
   g_gemm_mode = c->gemm_mode;
   g_tc_bn_policy = c->tune_bn;
+  g_tc_pairs_min_k = c->tune_pairs_k;
   g_dev_flags = c->d_flags;
   const int n = c->n;
   const size_t nn = size_t(n) * n;
@@ -552,7 +555,12 @@ int tvap_set_tuning(tvap_ctx* c, int bn_policy, int solve_groups, int solve_cap)
 }
 
 int tvap_set_option(tvap_ctx* c, int option, int value) {
-  if (!c || value < 0 || value > 1) return TVAP_ERR_ARG;
+  if (!c || value < 0) return TVAP_ERR_ARG;
+  if (option == TVAP_OPT_COMPLEX_PAIRS) {
+    c->tune_pairs_k = value;
+    return TVAP_OK;
+  }
+  if (value > 1) return TVAP_ERR_ARG;
   switch (option) {
     case TVAP_OPT_SOLVE_LOOKAHEAD: c->tune_lookahead = value; return TVAP_OK;
     case TVAP_OPT_PFAFFIAN_BLOCKED: c->tune_pf_blocked = value; return TVAP_OK;
@@ -565,6 +573,7 @@ int tvap_get_option(const tvap_ctx* c, int option) {
   switch (option) {
     case TVAP_OPT_SOLVE_LOOKAHEAD: return c->tune_lookahead;
     case TVAP_OPT_PFAFFIAN_BLOCKED: return c->tune_pf_blocked;
+    case TVAP_OPT_COMPLEX_PAIRS: return c->tune_pairs_k;
     default: return -1;
   }
 }

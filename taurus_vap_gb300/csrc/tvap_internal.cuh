@@ -158,6 +158,11 @@ extern thread_local int g_tc_grid_cap;
 // columns less, 1 always 64 rows, 2 always 48 (set by every entry point from
 // its context's tuning)
 extern thread_local int g_tc_bn_policy;
+// the tcgen05 complex x complex products of contraction length >= this take
+// the paired form (real and imaginary rows interleaved on both sides), the
+// others the real representation [[Re, -Im], [Im, Re]] x [Re, Im]; 0: none
+// (set by every entry point from its context)
+extern thread_local int g_tc_pairs_min_k;
 struct TcGridCap {
   int saved;
   explicit TcGridCap(int cap) : saved(g_tc_grid_cap) { g_tc_grid_cap = cap; }
@@ -300,6 +305,7 @@ struct tvap_ctx {
   int tune_cap = 0;
   int tune_lookahead = 0;  // look-ahead of the Thouless solve's panels (streamB)
   int tune_pf_blocked = 0;  // the blocked Pfaffian also where the shared-memory one fits
+  int tune_pairs_k = 0;     // complex x complex tcgen05 products in the paired form from K = this on (0: none)
 };
 
 namespace tvap {

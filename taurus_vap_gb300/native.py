@@ -347,7 +347,7 @@ class Context:
         return U1, V1
 
     # -- launch shapes by measurement ------------------------------------------
-    OPT_SOLVE_LOOKAHEAD, OPT_PFAFFIAN_BLOCKED = 1, 2
+    OPT_SOLVE_LOOKAHEAD, OPT_PFAFFIAN_BLOCKED, OPT_COMPLEX_PAIRS = 1, 2, 3
     TUNE_CANDIDATES = [(bn, g, cap, la, pf) for pf in (0, 1) for la in (1, 0) for g in (2, 1)
                        for cap in ((0, 1, 2) if g == 2 else (0,)) for bn in (0, 1, 2)]
 
@@ -368,6 +368,14 @@ class Context:
         _check(lib().tvap_get_tuning(self.h, _p(k)), "tvap_get_tuning")
         return tuple(int(x) for x in k) + (int(lib().tvap_get_option(self.h, self.OPT_SOLVE_LOOKAHEAD)),
                                            int(lib().tvap_get_option(self.h, self.OPT_PFAFFIAN_BLOCKED)))
+
+    def set_option(self, option, value):
+        """tvap_set_option (OPT_SOLVE_LOOKAHEAD, OPT_PFAFFIAN_BLOCKED,
+        OPT_COMPLEX_PAIRS; 0 or 1)."""
+        _check(lib().tvap_set_option(self.h, option, value), "tvap_set_option")
+
+    def option(self, option):
+        return int(lib().tvap_get_option(self.h, option))
 
     def set_tuning(self, bn_policy, solve_groups, solve_cap, lookahead=0, pfaffian_blocked=0):
         _check(lib().tvap_set_tuning(self.h, bn_policy, solve_groups, solve_cap), "tvap_set_tuning")

@@ -226,12 +226,13 @@ def _wide_rows(rng, m, k, cplx):
     return X
 
 
-@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("cplx,pairs", [(False, 0), (True, 0), (True, 1)])
 @pytest.mark.parametrize("gemm_mode", [1, 2])
-def test_emulated_product_bound(sd, cplx, gemm_mode):
+def test_emulated_product_bound(sd, cplx, pairs, gemm_mode):
     mdl, _, _ = sd
     ctx = Context(mdl.basis)
     ctx.set_gemm_mode(gemm_mode)
+    ctx.set_option(Context.OPT_COMPLEX_PAIRS, pairs)
     rng = np.random.default_rng(17 + gemm_mode)
     m, n, k = 2048, 2048, 256  # 512 output tiles: the tcgen05 kernel in mode 2
     A = _wide_rows(rng, m, k, cplx)
@@ -250,3 +251,36 @@ def test_emulated_product_bound(sd, cplx, gemm_mode):
     ctx.set_gemm_mode(0)
     C0 = ctx.gemm(A, B)
     assert np.all(np.abs(C0 - ref) <= 2.0 ** -49 * k * (np.abs(A) @ np.abs(B)) + 1e-300)
+
+
+@pytest.mark.parametrize("shape,ta,tb,alpha,beta", [((1533, 1037, 141), "C", "T", -1.0, 0.5),
+                                                    ((999, 1501, 77), "N", "C", 0.75, -2.0),
+                                                    ((1200, 640, 300), "T", "N", 1.0, 1.0)])
+def test_complex_product_forms(sd, shape, ta, tb, alpha, beta):
+    # odd sizes, transposed and conjugated operands, alpha = -1 (the sign in the
+    # integer conversion), a general alpha and beta (each product > 152
+    # tiles): the paired form of the complex x complex tcgen05 products gives
+    # the bits of the real representation, within the bound
+    mdl, _, _ = sd
+    ctx = Context(mdl.basis)
+    rng = np.random.default_rng(41)
+    m, n, k = shape
+    A = _wide_rows(rng, m, k, True)
+    B = _wide_rows(rng, n, k, True).T.copy()
+    # op(Ain) = A, op(Bin) = B
+    Ain = {"N": A, "T": A.T.copy(), "C": A.conj().T.copy()}[ta]
+    Bin = {"N": B, "T": B.T.copy(), "C": B.conj().T.copy()}[tb]
+    C0 = rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n))
+    got = []
+    for min_k in (0, 1, k, k + 1):  # none, every product, this K, above this K
+        ctx.set_option(Context.OPT_COMPLEX_PAIRS, min_k)
+        assert ctx.option(Context.OPT_COMPLEX_PAIRS) == min_k
+        got.append(ctx.gemm(Ain, Bin, ta, tb, alpha, beta, C0))
+    for C in got[1:]:
+        assert np.array_equal(C, got[0])
+    ref = alpha * (A @ B) + beta * C0
+    part = lambda X: np.maximum(np.abs(X.real), np.abs(X.imag))
+    bound = abs(alpha) * 2.0 ** -46 * k * np.outer(part(A).max(axis=1), part(B).max(axis=0))
+    slack = 2.0 ** -50 * k * abs(alpha) * (np.abs(A) @ np.abs(B)) + 2.0 ** -51 * (np.abs(ref) + abs(beta * C0))
+    err = np.abs(got[0] - ref)
+    assert np.all(err <= bound + slack), float((err / (bound + slack)).max())

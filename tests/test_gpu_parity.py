@@ -124,12 +124,14 @@ def test_calculate_fields_dense_blocks(case, ncol, request):
             assert relerr(got[q][c], gathered[q][c]) < FIELD_TOL, (c, q)
 
 
-def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0, gemm_mode=2):
+def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0, gemm_mode=2, pairs=None):
     om = O.OracleModel(mdl)
     ref = om.project(U, V, Mp, Mn, 2 * np.pi, Z, N, nthreads=nthreads)
     assert ref["status"] == 0
     ctx = Context(mdl.basis, mdl.ham)
     ctx.set_gemm_mode(gemm_mode)
+    if pairs is not None:
+        ctx.set_option(Context.OPT_COMPLEX_PAIRS, pairs)
     pnp, H20v = ctx.project(U, V, Mp, Mn, 2 * np.pi, Z, N, mode=mode)
     rp = ref["pnp"]
     e_ref = (rp.c("ener") / rp.c("over")).real
@@ -147,6 +149,13 @@ def check_projection(mdl, U, V, Mp, Mn, Z, N, mode, nthreads=0, gemm_mode=2):
 def test_project_sd(sd, mode, gemm_mode):
     mdl, U, V = sd
     check_projection(mdl, U, V, 9, 9, 4, 4, mode, gemm_mode=gemm_mode)
+
+
+@pytest.mark.parametrize("pairs", [0, 1])
+def test_project_sd_complex_forms(sd, pairs):
+    # both forms of the complex x complex tcgen05 products
+    mdl, U, V = sd
+    check_projection(mdl, U, V, 9, 9, 4, 4, 0, pairs=pairs)
 
 
 @pytest.mark.parametrize("gemm_mode", [0, 1, 2])
@@ -172,12 +181,13 @@ def test_project_emax4_small_grid(emax4, gemm_mode):
     check_projection(mdl, U, V, 3, 3, 8, 8, 0, gemm_mode=gemm_mode)
 
 
-def test_project_emax4_full_grid(emax4):
+@pytest.mark.parametrize("pairs", [0, 1])
+def test_project_emax4_full_grid(emax4, pairs):
     # the benchmark's workload (n = 140, 15 x 15 angles, 113 folded pairs): the
     # staggered groups of the solve, the reused digit planes and the traces
-    # beside H20 all run here
+    # beside H20 all run here, with both forms of the complex products
     mdl, U, V = emax4
-    check_projection(mdl, U, V, 15, 15, 8, 8, 0)
+    check_projection(mdl, U, V, 15, 15, 8, 8, 0, pairs=pairs)
 
 
 def test_emulated_gemm_matches_fp64_pipe(emax4):
@@ -185,8 +195,9 @@ def test_emulated_gemm_matches_fp64_pipe(emax4):
     mdl, U, V = emax4
     ctx = Context(mdl.basis, mdl.ham)
     res = []
-    for gm in (0, 1, 2):
+    for gm, pairs in ((0, 0), (1, 0), (2, 0), (2, 1)):
         ctx.set_gemm_mode(gm)
+        ctx.set_option(Context.OPT_COMPLEX_PAIRS, pairs)
         res.append(ctx.project(U, V, 5, 5, 2 * np.pi, 8, 8))
     p0, h0 = res[0]
     e0 = (p0.c("ener") / p0.c("over")).real
