@@ -198,10 +198,14 @@ constexpr int kSliceThreads = 256;
 __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int tile_rows, int rows_pad, int nks,
                                                                   __nv_bfloat16* __restrict__ out,
                                                                   int* __restrict__ ex) {
-  extern __shared__ double2 xs[];  // 8 rows x K (real sources use .x)
+  // 8 rows of ldk = K | 1 elements (real sources use .x): an odd row stride,
+  // so that the 8 rows read by 8 consecutive threads (one 16-byte element
+  // each) fall in 8 different groups of 4 banks
+  extern __shared__ double2 xs[];
   __shared__ int e_s[8][2];        // exponent of the real / imaginary part
   const int t = threadIdx.x;
   const int K = x.K, form = x.form;
+  const int ldk = K | 1;
   const bool cplx = form != 0;
   const int sq0 = blockIdx.x * 8;
   const int slot = blockIdx.y;
@@ -240,14 +244,14 @@ __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int ti
         v.y *= x.scale2;
       }
     }
-    xs[row * K + k] = v;
+    xs[row * ldk + k] = v;
   }
   __syncthreads();
   {
     const int w = t >> 5, lane = t & 31;
     int er = oz::kExpZero, ei = oz::kExpZero;
     for (int k = lane; k < K; k += 32) {
-      const double2 v = xs[w * K + k];
+      const double2 v = xs[w * ldk + k];
       if (v.x != 0.0) er = max(er, oz::dexp(v.x));
       if (v.y != 0.0) ei = max(ei, oz::dexp(v.y));
     }
@@ -291,8 +295,8 @@ __global__ void __launch_bounds__(kSliceThreads) slice_tc_kernel(TcSrc x, int ti
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
       int d0[kDigits], d1[kDigits];
-      const double2 v0 = (k0 + j < K) ? xs[row * K + k0 + j] : make_double2(0.0, 0.0);
-      const double2 v1 = (k0 + j + 1 < K) ? xs[row * K + k0 + j + 1] : make_double2(0.0, 0.0);
+      const double2 v0 = (k0 + j < K) ? xs[row * ldk + k0 + j] : make_double2(0.0, 0.0);
+      const double2 v1 = (k0 + j + 1 < K) ? xs[row * ldk + k0 + j + 1] : make_double2(0.0, 0.0);
       oz::to_digits(oz::to_fixed(part ? v0.y : v0.x, emax), d0);
       oz::to_digits(oz::to_fixed(part ? v1.y : v1.x, emax), d1);
 #pragma unroll
@@ -684,7 +688,7 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
   __nv_bfloat16* Bs = sc->buf + asz;
   int* ea = sc->ex;
   int* eb = sc->ex + size_t(a_slots) * a_rows_pad;
-  const size_t slice_shm = sizeof(double2) * 8 * size_t(K);
+  const size_t slice_shm = sizeof(double2) * 8 * size_t(K | 1);  // slice_tc_kernel's padded rows
   if (slice_shm > 48 * 1024) {
     if (slice_shm > size_t(227) * 1024) return TVAP_ERR_ARG;
     if ((rc = smem_opt_in((const void*)slice_tc_kernel, slice_shm))) return rc;
