@@ -87,6 +87,7 @@ class VAP:
         self.control_NZ = [0] * 5
         self.history = []
         self.adjust_steps = 0  # evolutions made by the last adjust_constraints (100: the targets were not met)
+        self._c20_of = None  # the (U, V) arrays C20 belongs to (replaced, not modified in place)
 
     def _part(self, i):
         return "f20" if i < self.cons.dim - self.cons.npair else "g20"
@@ -94,6 +95,10 @@ class VAP:
     def update_constraints_qpbasis(self, U, V):
         for i, A in enumerate(self._ops):
             self.C20[i] = set_operator_qpbasis(self._part(i), U, V, A).reshape(-1, order="F")
+        self._c20_of = (U, V)
+
+    def _c20_current(self):
+        return self._c20_of is not None and self._c20_of[0] is self.U0 and self._c20_of[1] is self.V0
 
     def lagrange_multipliers(self, H20v):
         c = self.cons.dim
@@ -119,9 +124,11 @@ class VAP:
                 self.U0, self.V0, self.Zi, np.stack(self.cons.ops) if c else None, list(self.cons.values),
                 cpair=self.cons.npair, eps=self.cons.eps)
             self.Zi = Zi
-            if c:
-                self.C20 = C20
             self.U0, self.V0 = np.asfortranarray(U1), np.asfortranarray(V1)
+            if c:
+                # the device loop ends with C20 of the state it returns
+                self.C20 = C20
+                self._c20_of = (self.U0, self.V0)
             return
         U1, V1 = self.U0, self.V0
         self.adjust_steps = 0
@@ -141,11 +148,16 @@ class VAP:
             B = np.linalg.solve(A, B)
             self.Zi = self.Zi + B @ self.C20
         self.U0, self.V0 = np.asfortranarray(U1), np.asfortranarray(V1)
+        if self.adjust_steps:
+            self._c20_of = (self.U0, self.V0)  # the loop's last update was of (U1, V1)
 
     def iterate(self):
         """One gradient iteration.  Returns (status, info) with status 0
         continue, 1 converged; info = gradient norm, E, <Z>, Var Z, <N>, Var N."""
-        self.update_constraints_qpbasis(self.U0, self.V0)
+        # C20 of the current state: the constraint loop that produced it
+        # leaves it behind (module_constraints.f90:381-397 on the same state)
+        if not self._c20_current():
+            self.update_constraints_qpbasis(self.U0, self.V0)
         pnp, H20v = self.ctx.project(self.U0, self.V0, self.Mp, self.Mn, self.facpi, self.Z, self.N,
                                      self.factor_delta, mode=self.mode)
         self.lagrange_multipliers(H20v)
