@@ -340,7 +340,8 @@ int tvap_autotune(tvap_ctx* ctx, const double* U0, const double* V0, const tvap_
 int tvap_set_tuning(tvap_ctx* ctx, int bn_policy, int solve_groups, int solve_cap);
 int tvap_get_tuning(const tvap_ctx* ctx, int* knobs);
 /* TVAP_OPT_COMPLEX_PAIRS = k >= 0: the complex x complex products on the
- * tensor cores whose contraction length is at least k take the paired form
+ * tensor cores whose contraction length is at least k (and whose batch
+ * entries share no operand) take the paired form
  * (real and imaginary rows interleaved in both operands, the four real
  * products of each element combined on the exact integer accumulators:
  * half the digit planes of the left operand, twice the tiles of half the

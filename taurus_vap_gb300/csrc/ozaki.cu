@@ -633,11 +633,13 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
            scale_left ? 1.0 : g.s2};
   TcOut o{};
   o.a_split = o.b_split = INT_MAX;
+  const bool stack = g.batch > 1 && (a_sh || b_sh);
   // complex x complex: the paired form (rows interleaved on both sides, the
   // 2 x 2 blocks combined by the epilogue; half the left operand's digit
   // planes, twice the tiles of half the k-steps, so that it pays where the
-  // contraction is long) or the real representation
-  const bool pairs = !L.real && !R.real && g_tc_pairs_min_k > 0 && K >= g_tc_pairs_min_k;
+  // contraction is long; batches with a shared operand keep the real
+  // representation) or the real representation
+  const bool pairs = !L.real && !R.real && !stack && g_tc_pairs_min_k > 0 && K >= g_tc_pairs_min_k;
   if (pairs) {
     xa.form = xb.form = 4;
     xa.xrows = 2 * L.rows;
@@ -660,7 +662,6 @@ int gemm_tc(const GemmArgs& g, cudaStream_t s) {
     xb.xrows = 2 * R.rows;
     o.b_split = R.rows;
   }
-  const bool stack = g.batch > 1 && (a_sh || b_sh);
   xa.nstack = stack ? g.batch : 1;
   const int a_slots = stack ? 1 : g.batch, b_slots = stack ? 1 : g.batch;
   const int a_rows_pad = (xa.nstack * xa.xrows + oztc::kM - 1) / oztc::kM * oztc::kM;
