@@ -148,3 +148,48 @@ def test_autograd_function_on_the_cpu():
     Em = projected_energy(torch.tensor(Z0 - h * D), ctx, U, V, 5, 5, 4, 4).item()
     fd = 3.0 * (Ep - Em) / (2 * h)
     assert abs(fd - float((Z.grad.numpy() * D).sum())) < 1e-6 * max(1.0, abs(fd))
+
+
+
+def test_c20_follows_the_state(usdb_model, mg24_seed, mg24_constraints):
+    """The loop takes C20 from the constraint loop that produced the state and
+    recomputes it (update_constraints_qpbasis, module_constraints.f90:381-397)
+    only for a state set from outside: after every iteration C20 is that of
+    the current state (set_operator_qpbasis, module_operators.f90:49-97)."""
+    from taurus_vap_gb300.vap import set_operator_qpbasis
+
+    ops, vals = mg24_constraints
+    vap = VAP(OracleBackedContext(usdb_model), *mg24_seed, 5, 5, 4.0, 4.0, 0.05, 0.6,
+              constraints=Constraints(ops, vals))
+    n = usdb_model.n
+    calls = []  # the U of every C20 update
+    update = vap.update_constraints_qpbasis
+
+    def recording_update(U, V):
+        calls.append(U)
+        update(U, V)
+
+    vap.update_constraints_qpbasis = recording_update
+
+    def c20_is_of_state():
+        for i, op in enumerate(ops):
+            want = set_operator_qpbasis(vap._part(i), vap.U0, vap.V0, np.reshape(op, (n, n), order="F"))
+            assert np.allclose(vap.C20[i].reshape((n, n), order="F"), want, rtol=0, atol=1e-13)
+
+    seed = vap.U0
+    vap.iterate()
+    assert calls[0] is seed  # the seed's C20, before the first projection
+    c20_is_of_state()
+    state, n_calls = vap.U0, len(calls)
+    vap.iterate()
+    # no recompute for the constraint loop's own state: the next update is of
+    # the loop's first evolved state
+    assert len(calls) > n_calls and calls[n_calls] is not state
+    c20_is_of_state()
+    # a state set from outside is recomputed before it is used
+    outside = np.asfortranarray(mg24_seed[0])
+    vap.U0, vap.V0 = outside, np.asfortranarray(mg24_seed[1])
+    n_calls = len(calls)
+    vap.iterate()
+    assert calls[n_calls] is outside
+    c20_is_of_state()
