@@ -1416,47 +1416,53 @@ __device__ __forceinline__ double rsqrt_newton(double d) {
   return y;
 }
 
-// Unblocked Cholesky of the nb x nb diagonal block at (j0, j0) of S by one
-// warp: lane i holds row i of the block in registers, each pivot is one
-// lane's value broadcast by a shuffle, the column is scaled by the pivot's
-// reciprocal (as DPBTF2 does).  The reciprocals go to rd[j0 ..] for the
-// solves.  An FP64 warp instruction occupies the SM's FP64 pipe for about 16
-// cycles on this part, so the block stays in one warp (no CTA barriers, no
-// redundant arithmetic).  Elements written by other CTAs are read through L2.
-__device__ bool coop_factor_diag_warp(int n, double* S, double* rd, int j0, int nb) {
-  const int lane = threadIdx.x & 31;
-  double li[kCoopNb];
-#pragma unroll
-  for (int j = 0; j < kCoopNb; ++j)
-    li[j] = (lane < nb && j <= lane && j < nb) ? __ldcg(&S[(j0 + lane) + size_t(j0 + j) * n]) : 0.0;
-  bool ok = true;
-#pragma unroll
-  for (int k = 0; k < kCoopNb; ++k) {
-    if (k >= nb) break;
-    const double d = __shfl_sync(0xffffffffu, li[k], k);
-    if (!(d > 0.0)) {
-      ok = false;  // uniform: every lane holds the same pivot
-      break;
+// Unblocked Cholesky of the nb x nb diagonal block at (j0, j0) of S by the
+// whole CTA (kCoopThreads >= kCoopNb^2 threads, one entry of the block each,
+// the block in B): per step the pivot's thread forms 1 / sqrt(d), the column
+// is scaled by it (as DPBTF2 does) and the trailing entries take
+// A_ij -= L_ik L_jk, each entry in the same order as an unblocked
+// elimination.  An FP64 warp instruction holds the FP64 unit of its SM
+// sub-partition for about 64 cycles on this part: with the block's entries
+// spread over all the CTA's warps, a step's update is one instruction on
+// every sub-partition instead of up to 15 on one.  The reciprocals go to
+// rd[j0 ..] for the solves; sc (2 doubles of shared memory) carries the
+// pivot's reciprocal and the failure flag.  Elements written by other CTAs
+// are read through L2.  Every thread of the CTA calls it; the result is
+// uniform.
+__device__ bool coop_factor_diag(int n, double* S, double* rd, int j0, int nb, double (*B)[kCoopNb + 1],
+                                 double* sc) {
+  static_assert(kCoopThreads >= kCoopNb * kCoopNb, "one thread per entry of the diagonal block");
+  const int t = threadIdx.x;
+  const int i = t % kCoopNb, j = t / kCoopNb;
+  const bool mine = t < kCoopNb * kCoopNb && i < nb && j < nb && i >= j;
+  if (mine) B[i][j] = __ldcg(&S[(j0 + i) + size_t(j0 + j) * n]);
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (t == k * kCoopNb + k) {  // the pivot's thread
+      const double d = B[k][k];
+      if (d > 0.0) {
+        const double y = rsqrt_newton(d);
+        B[k][k] = d * y;
+        rd[j0 + k] = y;
+        sc[0] = y;
+        sc[1] = 0.0;
+      } else {
+        sc[1] = 1.0;
+      }
     }
-    const double y = rsqrt_newton(d);
-    if (lane == k) li[k] = d * y;
-    if (lane > k) li[k] *= y;
-    if (lane == 0) rd[j0 + k] = y;
-#pragma unroll
-    for (int j = k + 1; j < kCoopNb; ++j) {
-      if (j >= nb) break;
-      const double ljk = __shfl_sync(0xffffffffu, li[k], j);
-      if (lane >= j) li[j] = fma(-li[k], ljk, li[j]);
-    }
+    __syncthreads();
+    if (sc[1] != 0.0) return false;  // uniform: read by every thread after the barrier
+    if (mine && j == k && i > k) B[i][k] *= sc[0];
+    __syncthreads();
+    if (mine && j > k) B[i][j] = fma(-B[i][k], B[j][k], B[i][j]);
+    __syncthreads();
   }
-  if (!ok) return false;
-#pragma unroll
-  for (int j = 0; j < kCoopNb; ++j)
-    if (lane < nb && j <= lane && j < nb) S[(j0 + lane) + size_t(j0 + j) * n] = li[j];
+  if (mine) S[(j0 + i) + size_t(j0 + j) * n] = B[i][j];
   return true;
 }
 
-__global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, double* S, const double* A,
+template <int SLOTS>
+__global__ void __launch_bounds__(kCoopThreads, 1) cholesky_evolve_kernel(int n, double* S, const double* A,
                                                                        long long a_stride, double* X,
                                                                        long long x_stride, unsigned* bar,
                                                                        int* flags, int skip_cta, int l_smem) {
@@ -1470,11 +1476,9 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
   __syncthreads();
   unsigned gen = gen_s;  // every thread keeps its own copy of the generation
   double* rd = S + size_t(n) * n;  // 1 / L_jj
-  if (cta == 0 && t < 32 && !coop_factor_diag_warp(n, S, rd, 0, min(kCoopNb, n))) {
-    if (t == 0) {
-      atomicOr(flags, DEV_CHOLESKY);
-      atomicExch(&bar[2], 1u);
-    }
+  if (cta == 0 && !coop_factor_diag(n, S, rd, 0, min(kCoopNb, n), L11, rdiag) && t == 0) {
+    atomicOr(flags, DEV_CHOLESKY);
+    atomicExch(&bar[2], 1u);
   }
   // test hook: this CTA leaves without arriving, so that the others' bounded
   // waits at the first barrier run out (status DEV_WAIT_TIMEOUT, abort)
@@ -1531,7 +1535,8 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
         S[(j1 + i) + size_t(j1 + j) * n] = v;
       }
       __syncthreads();
-      if (t < 32 && !coop_factor_diag_warp(n, S, rd, j1, nb2) && t == 0) {
+      // (L11 and rdiag are free until the barrier: every CTA reloads them)
+      if (!coop_factor_diag(n, S, rd, j1, nb2, L11, rdiag) && t == 0) {
         atomicOr(flags, DEV_CHOLESKY);
         atomicExch(&bar[2], 1u);
       }
@@ -1562,13 +1567,23 @@ __global__ void __launch_bounds__(kCoopThreads) cholesky_evolve_kernel(int n, do
   double* Ls = coop_smem;
   double* dinv = l_smem ? Ls + size_t(n) * n : coop_smem;
   if (l_smem) {
-#pragma unroll 8
-    for (int idx = t; idx < n * n; idx += blockDim.x) Ls[idx] = __ldcg(&S[idx]);
+    if ((reinterpret_cast<uintptr_t>(S) & 15) == 0) {
+      // 16-byte loads, many in flight
+      const int nn2 = (n * n) / 2;
+      const double2* S2 = reinterpret_cast<const double2*>(S);
+      double2* L2 = reinterpret_cast<double2*>(Ls);
+#pragma unroll 16
+      for (int idx = t; idx < nn2; idx += blockDim.x) L2[idx] = __ldcg(&S2[idx]);
+      if (((n * n) & 1) && t == 0) Ls[n * n - 1] = __ldcg(&S[n * n - 1]);
+    } else {
+#pragma unroll 16
+      for (int idx = t; idx < n * n; idx += blockDim.x) Ls[idx] = __ldcg(&S[idx]);
+    }
   }
   __syncthreads();
   for (int j = t; j < n; j += blockDim.x) dinv[j] = __ldcg(&rd[j]);
   __syncthreads();
-  constexpr int kMaxPerLane = 12;  // n <= 384
+  constexpr int kMaxPerLane = SLOTS;
   for (int r = cta + G * warp; r < rows; r += G * warps) {
     const int mat = r >= n ? 1 : 0, row = r - mat * n;
     const double* a = A + mat * a_stride;
@@ -1625,6 +1640,14 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
   const int l_smem = shm_full <= jacobi32_smem_limit() ? 1 : 0;
   const size_t shm = l_smem ? shm_full : sizeof(double) * (size_t(n) * kCoopNb + n);
   if (n > 384 || shm > jacobi32_smem_limit()) return TVAP_ERR_ARG;
+  const int slots = (n + 31) / 32;
+  const void* kern = slots <= 2    ? (const void*)cholesky_evolve_kernel<2>
+                     : slots <= 4  ? (const void*)cholesky_evolve_kernel<4>
+                     : slots <= 5  ? (const void*)cholesky_evolve_kernel<5>
+                     : slots <= 6  ? (const void*)cholesky_evolve_kernel<6>
+                     : slots <= 8  ? (const void*)cholesky_evolve_kernel<8>
+                     : slots <= 11 ? (const void*)cholesky_evolve_kernel<11>
+                                   : (const void*)cholesky_evolve_kernel<12>;
   // the co-resident grid for this shared-memory size, found once per device
   static std::mutex m;
   static std::vector<std::pair<std::pair<int, size_t>, int>> grids;  // ((device, bytes), grid)
@@ -1636,9 +1659,9 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
     for (const auto& e : grids)
       if (e.first.first == dev && e.first.second == shm) grid = e.second;
     if (grid == 0) {
-      if (int rc = smem_opt_in((const void*)cholesky_evolve_kernel, shm)) return rc;
+      if (int rc = smem_opt_in(kern, shm)) return rc;
       int per_sm = 0;
-      TVAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cholesky_evolve_kernel, kCoopThreads, shm));
+      TVAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCoopThreads, shm));
       grid = std::min(per_sm * device_sms(), 128);
       if (grid >= 1) grids.push_back({{dev, shm}, grid});
     }
@@ -1650,7 +1673,7 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
   int skip = (skip_cta >= 0 && grid > 1) ? grid - 1 : -1;
   void* args[] = {&n, &S, &A, &a_stride, &X, &x_stride, &bar, &flags, &skip, const_cast<int*>(&l_smem)};
   ++g_launch_count;
-  TVAP_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_evolve_kernel, dim3(grid), dim3(kCoopThreads), args,
+  TVAP_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kCoopThreads), args,
                                         shm, s));
   return TVAP_OK;
 }
