@@ -32,6 +32,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 EMAX, ZV, NV, MPHI = 4, 8.0, 8.0, 15
+# a new context's launch shapes: (B' width policy, solve groups, cap, look-ahead, blocked Pfaffian)
+DEFAULT_TUNING = (0, 2, 0, 0, 0)
 ETA, MU = 0.005, 0.3
 METRIC = "PNVAP gradient iters/s, emax=4, 15 gauge angles: batched+adjoint vs plain GPU (FP64)"
 WORKLOAD = ("PNVAP gradient iteration, emax=4 no-core SHO basis (n=140), Z=N=8, 15x15 gauge angles, "
@@ -262,9 +264,38 @@ def run_ours(args):
     autotune = None
     if not args.no_autotune:
         tune_table = ctx.autotune(U, V, MPHI, MPHI, 2 * math.pi, ZV, NV, reps=3)
-        autotune = {"chosen": dict(zip(("bn_policy", "solve_groups", "solve_cap", "lookahead", "pfaffian_blocked"),
-                                       ctx.tuning())),
-                    "ms_per_projection": {f"bn{b}_g{g}_cap{c}_la{a}_pf{f}": round(v, 4)
+        key = lambda b, g, c, a, f: f"bn{b}_g{g}_cap{c}_la{a}_pf{f}"
+        names = ("bn_policy", "solve_groups", "solve_cap", "lookahead", "pfaffian_blocked")
+        proposed = ctx.tuning()
+        # the tuner ranks projections, whose best shapes lie within about 1 %
+        # of each other; the timed step also evolves the state and reads its
+        # results back.  Its three best and the context's defaults are timed
+        # again on whole iterations (3 alternating rounds of 8) and the
+        # fastest is kept.
+        cands = [k for k, _ in sorted(tune_table.items(), key=lambda kv: kv[1])[:3]]
+        if DEFAULT_TUNING not in cands:
+            cands.append(DEFAULT_TUNING)
+        it_ms = {cnd: [] for cnd in cands}
+        itc = DeviceIteration(ctx, U, V, 0, torch)
+        ea = torch.cuda.Event(enable_timing=True)
+        eb = torch.cuda.Event(enable_timing=True)
+        for _ in range(3):
+            for cnd in cands:
+                ctx.set_tuning(*cnd)
+                for _ in range(2):
+                    itc.step()
+                torch.cuda.synchronize()
+                ea.record(stream)
+                for _ in range(8):
+                    itc.step()
+                eb.record(stream)
+                torch.cuda.synchronize()
+                it_ms[cnd].append(ea.elapsed_time(eb) / 8)
+        best = min(cands, key=lambda cnd: min(it_ms[cnd]))
+        ctx.set_tuning(*best)
+        autotune = {"chosen": dict(zip(names, ctx.tuning())), "proposed_by_tuner": dict(zip(names, proposed)),
+                    "ms_per_iteration_check": {key(*cnd): round(min(v), 4) for cnd, v in it_ms.items()},
+                    "ms_per_projection": {key(b, g, c, a, f): round(v, 4)
                                           for (b, g, c, a, f), v in tune_table.items()}}
 
     # ---- device-resident value (batched form).  The clock sampler starts
