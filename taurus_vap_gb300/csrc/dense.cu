@@ -1401,16 +1401,17 @@ __device__ bool coop_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, int
   return ok_s != 0;
 }
 
-// 1 / sqrt(d) for a positive normal d: an FP32 seed refined by two
-// Newton-Raphson steps for the reciprocal square root, y <- y (3 - d y^2) / 2
-// (each step doubles the correct bits: 2^-22 -> 2^-44 -> FP64 rounding).
-// About 8 instructions on the FP64 pipe, against several times that for an
-// FP64 square root followed by a division; outside the FP32 exponent range
-// the library routines are used.
+// 1 / sqrt(d) for a positive normal d: an FP32 seed (of d's value with the
+// mantissa truncated to 23 bits) refined by two Newton-Raphson steps for the
+// reciprocal square root, y <- y (3 - d y^2) / 2 (each step doubles the
+// correct bits: 2^-22 -> 2^-44 -> FP64 rounding).  The range test, the seed's
+// conversions and d / 2 (an exponent decrement) run on the integer pipe, so
+// the 6 Newton instructions are all that occupy the FP64 pipe; outside the
+// range of seed_range the library routines are used.
 __device__ __forceinline__ double rsqrt_newton(double d) {
-  if (!(d > 1.0e-30 && d < 1.0e30)) return 1.0 / sqrt(d);
-  double y = double(rsqrtf(float(d)));
-  const double h = 0.5 * d;
+  if (!seed_range(d)) return 1.0 / sqrt(d);
+  double y = seed_f64(rsqrtf(seed_f32(d)));
+  const double h = __longlong_as_double(__double_as_longlong(d) - (1LL << 52));  // d / 2, exact
   y = y * fma(-h, y * y, 1.5);
   y = y * fma(-h, y * y, 1.5);
   return y;

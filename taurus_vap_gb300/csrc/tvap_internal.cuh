@@ -43,13 +43,35 @@ __host__ __device__ __forceinline__ double2 crcp(double2 z) {
 }
 __host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) { return cmul(a, crcp(b)); }
 #ifdef __CUDACC__
+// Helpers of the Newton seeds on the integer pipe (an FP64 instruction, a
+// compare or a conversion included, holds its SM sub-partition's FP64 unit
+// for about 64 cycles on this part, and the seeds sit on dependent chains):
+// d > 0 with 2^-99 <= d < 2^100 (normal, within the FP32 exponent range
+// with room), its float value with the mantissa truncated to 23 bits, and
+// the double of a positive normal float, all from the bits.
+__device__ __forceinline__ bool seed_range(double d) {
+  const long long b = __double_as_longlong(d);
+  const int e = int((b >> 52) & 0x7ff);  // biased exponent; sign bit set: b < 0
+  return b > 0 && e >= 1023 - 99 && e <= 1023 + 99;
+}
+__device__ __forceinline__ float seed_f32(double d) {
+  const long long b = __double_as_longlong(d);
+  const unsigned e = unsigned(int((b >> 52) & 0x7ff) - 1023 + 127);
+  return __uint_as_float((e << 23) | unsigned((b >> 29) & 0x7fffff));
+}
+__device__ __forceinline__ double seed_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const long long e = (long long)((u >> 23) & 0xff) - 127 + 1023;
+  return __longlong_as_double((e << 52) | ((long long)(u & 0x7fffff) << 29));
+}
 // 1/z = conj(z) / |z|^2 with |z|^2 inverted by two Newton steps from the
-// single-precision reciprocal (relative error a few units of the last
-// place); outside the safe range the scaled division (crcp)
+// single-precision reciprocal of its truncated value (22 bits or more, 88
+// after the steps: relative error a few units of the last place); outside
+// the range of seed_range the scaled division (crcp)
 __device__ __forceinline__ double2 crcp_newton(double2 z) {
   const double d = fma(z.x, z.x, z.y * z.y);
-  if (!(d > 1.0e-30 && d < 1.0e30)) return crcp(z);
-  double y = double(__frcp_rn(float(d)));
+  if (!seed_range(d)) return crcp(z);
+  double y = seed_f64(__frcp_rn(seed_f32(d)));
   double e = fma(-d, y, 1.0);
   y = fma(y, e, y);
   e = fma(-d, y, 1.0);
