@@ -109,3 +109,14 @@ def test_struct_layouts_match_the_header(tmp_path):
     assert int(got["obs"]) == ctypes.sizeof(native.TvapPnpObs)
     for k in obs:
         assert int(got[f"obs.{k}"]) == getattr(native.TvapPnpObs, k).offset, k
+
+
+def test_option_numbers_match_the_header():
+    # the binding's OPT_* constants are the header's TVAP_OPT_* enumerators
+    from taurus_vap_gb300.native import Context
+
+    text = open(os.path.join(ROOT, "include", "tvap.h")).read()
+    enum = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"TVAP_OPT_([A-Z_]+)\s*=\s*(\d+)", text))
+    assert enum, "no TVAP_OPT_* enumerators in tvap.h"
+    for name, value in enum.items():
+        assert getattr(Context, "OPT_" + name) == value, name
