@@ -1649,22 +1649,28 @@ int cholesky_evolve_coop(int n, double* S, const double* A, long long a_stride, 
                      : slots <= 8  ? (const void*)cholesky_evolve_kernel<8>
                      : slots <= 11 ? (const void*)cholesky_evolve_kernel<11>
                                    : (const void*)cholesky_evolve_kernel<12>;
-  // the co-resident grid for this shared-memory size, found once per device
+  // the co-resident grid of this instantiation and shared-memory size, found
+  // once per device
+  struct GridKey {
+    int dev;
+    const void* kern;
+    size_t shm;
+  };
   static std::mutex m;
-  static std::vector<std::pair<std::pair<int, size_t>, int>> grids;  // ((device, bytes), grid)
+  static std::vector<std::pair<GridKey, int>> grids;
   int dev = 0;
   TVAP_CUDA(cudaGetDevice(&dev));
   int grid = 0;
   {
     std::lock_guard<std::mutex> lock(m);
     for (const auto& e : grids)
-      if (e.first.first == dev && e.first.second == shm) grid = e.second;
+      if (e.first.dev == dev && e.first.kern == kern && e.first.shm == shm) grid = e.second;
     if (grid == 0) {
       if (int rc = smem_opt_in(kern, shm)) return rc;
       int per_sm = 0;
       TVAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCoopThreads, shm));
       grid = std::min(per_sm * device_sms(), 128);
-      if (grid >= 1) grids.push_back({{dev, shm}, grid});
+      if (grid >= 1) grids.push_back({GridKey{dev, kern, shm}, grid});
     }
   }
   if (grid < 1) return TVAP_ERR_ARG;
