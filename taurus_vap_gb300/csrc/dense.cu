@@ -1595,31 +1595,28 @@ __global__ void __launch_bounds__(kCoopThreads, 1) cholesky_evolve_kernel(int n,
       const int j = lane + 32 * q;
       v[q] = (j < n) ? a[row + size_t(j) * n] : 0.0;
     }
-    for (int j = 0; j < n; ++j) {
-      const int owner = j & 31, qj = j >> 5;
-      double vj = v[0];
+    // columns j in slot qj (a compile-time index once unrolled): the slots
+    // below qj are finished, the slots above take every lane, slot qj the
+    // lanes above j -- only those FMAs are issued (each an FP64 instruction
+    // of about 64 cycles on this part), in the order of an unblocked solve
 #pragma unroll
-      for (int q = 1; q < kMaxPerLane; ++q)
-        if (q == qj) vj = v[q];
-      const double xj = __shfl_sync(0xffffffffu, vj, owner) * dinv[j];
-      if (lane == owner) {
-#pragma unroll
-        for (int q = 0; q < kMaxPerLane; ++q)
-          if (q == qj) v[q] = xj;
-      }
-      if (l_smem) {
-        const double* lc = Ls + size_t(j) * n;
-#pragma unroll
-        for (int q = 0; q < kMaxPerLane; ++q) {
-          const int jj = lane + 32 * q;
-          if (32 * q + 31 > j && 32 * q < n && jj > j && jj < n) v[q] = fma(-xj, lc[jj], v[q]);
+    for (int qj = 0; qj < kMaxPerLane; ++qj) {
+      if (32 * qj >= n) break;
+      const int jend = min(32 * qj + 32, n);
+      for (int j = 32 * qj; j < jend; ++j) {
+        const int owner = j & 31;
+        const double xj = __shfl_sync(0xffffffffu, v[qj], owner) * dinv[j];
+        if (lane == owner) v[qj] = xj;
+        const double* lc = (l_smem ? Ls : S) + size_t(j) * n;
+        {
+          const int jj = lane + 32 * qj;
+          if (jj > j && jj < n) v[qj] = fma(-xj, l_smem ? lc[jj] : __ldcg(&lc[jj]), v[qj]);
         }
-      } else {
-        const double* lc = S + size_t(j) * n;
 #pragma unroll
-        for (int q = 0; q < kMaxPerLane; ++q) {
+        for (int q = qj + 1; q < kMaxPerLane; ++q) {
+          if (32 * q >= n) break;
           const int jj = lane + 32 * q;
-          if (32 * q + 31 > j && 32 * q < n && jj > j && jj < n) v[q] = fma(-xj, __ldcg(&lc[jj]), v[q]);
+          if (jj < n) v[q] = fma(-xj, l_smem ? lc[jj] : __ldcg(&lc[jj]), v[q]);
         }
       }
     }
